@@ -1,0 +1,132 @@
+"""Geometry descriptors of the MLEM hot path.
+
+``MeasurementSetup`` mirrors the reference's ``DefaultMeasurementSetup<T>``
+(MeasurementSetup.hpp:124-164; constructor argument order
+pos0x, pos1x, na, n0z, n0y, n1z, n1y, da, segx, segy, segz) and ``VoxelGrid``
+mirrors ``DefaultVoxelGrid<T>`` (VoxelGrid.hpp:88-200; origin, pitch, count
+per axis).  Units are metres and degrees, as in the reference's compiled
+defaults (real_measurementsetup_defines.h, voxelgrid_defines.h).
+
+The reference bakes one geometry into ``__constant__`` memory per process
+(device_constant_memory.hpp:14-26); here a ``Problem`` is a value passed to
+every call, so several geometries can live side by side (batched form).
+"""
+from __future__ import annotations
+
+from dataclasses import dataclass, field, replace
+
+import numpy as np
+
+
+@dataclass(frozen=True)
+class MeasurementSetup:
+    """Two planar heads rotating about y (MeasurementSetup.hpp:124-164)."""
+    pos0x: float
+    pos1x: float
+    na: int
+    n0z: int
+    n0y: int
+    n1z: int
+    n1y: int
+    da: float
+    segx: float
+    segy: float
+    segz: float
+
+    @property
+    def nchannels(self) -> int:
+        return self.na * self.n0z * self.n0y * self.n1z * self.n1y
+
+    def channel_id(self, ida, id0z, id0y, id1z, id1y):
+        """Linear channel id (MeasurementSetupLinIndex.hpp:39-44): angle
+        slowest, id1y fastest."""
+        return (((ida * self.n0z + id0z) * self.n0y + id0y) * self.n1z + id1z) * self.n1y + id1y
+
+    def channel_indices(self, cnl):
+        """Inverse of :meth:`channel_id` (MeasurementSetupLinIndex.hpp:58-165)."""
+        cnl = np.asarray(cnl)
+        id1y = cnl % self.n1y
+        t = cnl // self.n1y
+        id1z = t % self.n1z
+        t = t // self.n1z
+        id0y = t % self.n0y
+        t = t // self.n0y
+        id0z = t % self.n0z
+        ida = t // self.n0z
+        return ida, id0z, id0y, id1z, id1y
+
+
+@dataclass(frozen=True)
+class VoxelGrid:
+    """Axis-aligned grid (VoxelGrid.hpp:88-200); voxel id = ix*(ny*nz) +
+    iy*nz + iz (VoxelGridLinIndex.hpp:33-35)."""
+    origin: tuple
+    pitch: tuple
+    n: tuple
+
+    @property
+    def nvoxels(self) -> int:
+        return int(self.n[0]) * int(self.n[1]) * int(self.n[2])
+
+    def voxel_id(self, ix, iy, iz):
+        return (ix * self.n[1] + iy) * self.n[2] + iz
+
+    def voxel_indices(self, vxl):
+        vxl = np.asarray(vxl)
+        iz = vxl % self.n[2]
+        t = vxl // self.n[2]
+        return t // self.n[1], t % self.n[1], iz
+
+    def centres(self, axis: int) -> np.ndarray:
+        """Voxel centre coordinates along an axis, float32 as the reference
+        forms them (o + (i + 0.5) * d)."""
+        o = np.float32(self.origin[axis])
+        d = np.float32(self.pitch[axis])
+        i = np.arange(self.n[axis], dtype=np.float32)
+        return (o + (i + np.float32(0.5)) * d).astype(np.float32)
+
+
+@dataclass(frozen=True)
+class Problem:
+    """One reconstruction geometry plus its Monte-Carlo ray settings."""
+    setup: MeasurementSetup
+    grid: VoxelGrid
+    nrays: int
+    seed: int = 1251  # RANDOM_SEED (getSystemMatrixFromWorkqueue.cu:22)
+
+    @property
+    def nchannels(self) -> int:
+        return self.setup.nchannels
+
+    @property
+    def nvoxels(self) -> int:
+        return self.grid.nvoxels
+
+    def with_seed(self, seed: int) -> "Problem":
+        return replace(self, seed=seed)
+
+
+def two_head_setup(na: int, da: float, pos: float = 0.25, n: int = 13,
+                   seg=(0.020, 0.004, 0.004)) -> MeasurementSetup:
+    """Two opposing heads of n x n crystals of seg (x, y, z) metres, centres
+    at x = -pos and +pos, na angular steps of da degrees about y."""
+    return MeasurementSetup(-pos, pos, na, n, n, n, n, da, *seg)
+
+
+def centred_grid(n: int, pitch: float = 0.002) -> VoxelGrid:
+    half = n * pitch / 2
+    return VoxelGrid((-half,) * 3, (pitch,) * 3, (n,) * 3)
+
+
+# Workloads.  "small" is the CPU-runnable case; "full" is the headline
+# single-GPU case (52^3 voxels x 5,140,980 channels, 100 rays, 20 iterations).
+CONFIGS = {
+    "small": dict(problem=Problem(two_head_setup(8, 22.5), centred_grid(32), 10),
+                  iterations=5, counts=1e6),
+    "full": dict(problem=Problem(two_head_setup(180, 2.0), centred_grid(52), 100),
+                 iterations=20, counts=5e8),
+}
+
+
+def config(name: str) -> dict:
+    return dict(CONFIGS[name])
