@@ -1,0 +1,355 @@
+"""Benchmark of the MLEM hot path on the full workload (one JSON line).
+
+Workload ("full"): two 13x13-crystal heads 500 mm apart, 180 angles in 2
+degree steps (5,140,980 channels), 52^3 voxels of 2 mm, 100 Monte-Carlo rays
+per channel, 20 MLEM iterations; seeded synthetic phantom (cylinder + 3 hot
+spheres) forward-projected with an independent ray seed, Poisson noise at
+5e8 counts; measured rows = channels with counts > 0.
+
+A step is one complete reconstruction through the library: the system
+matrix of the measured rows built on the fly (rays -> walks -> CSR), its
+column-major copy, and 20 MLEM iterations (forward product, ratio,
+transpose product, update, normalisation).  The metric is MLEM iterations
+per second of that step: 20 / step time, the matrix build included.  The
+sensitivity image and the measurement are inputs (the reference reads them
+from files).
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+
+With torchrun (N > 1) every rank reconstructs its own copy of the workload
+(replicas; the path has no cross-GPU exchange in this form), the step time
+is the max over ranks and the value counts all ranks' iterations.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "MLEM it/s (52^3 vox, 5.1M ch)"
+UNIT = "it/s"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--config", default="full", choices=["full", "small"])
+    ap.add_argument("--cpu-sample", type=int, default=48,
+                    help="channels in the CPU-baseline sample")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    return ap.parse_args()
+
+
+# --------------------------------------------------------------- clocks
+
+class ClockSampler:
+    """nvidia-smi clocks/throttle reasons during the timed region."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.path = os.path.join(ROOT, "gpurun_out", f"clocks_rank{index}.csv")
+
+    def start(self):
+        try:
+            os.makedirs(os.path.dirname(self.path), exist_ok=True)
+            self.fh = open(self.path, "w")
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.Q}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=self.fh, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.fh.close()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax.append(float(f[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm.sort()
+        return {"sm_mhz": sm[len(sm) // 2], "sm_max_mhz": max(smax), "samples": len(sm),
+                "reasons": sorted(reasons)}
+
+
+# ------------------------------------------------------------ CPU baseline
+
+def cpu_baseline(cfg_name: str, sample: int, seed: int = 0):
+    """The oracle (plain C restatement of the reference's per-iteration work,
+    OpenMP over host cores): for a seeded sample of channels, the reference's
+    dense candidate scan over all voxels, the nrays-ray values of every
+    candidate, and the forward/transpose products of those rows.  Scaled by
+    the number of measured channels (estimated from the sample); the
+    reference rebuilds the matrix in every iteration (reco.cu:216-254)."""
+    import numpy as np
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    from pyoracle import Oracle
+    from epetreco_gb300.phantom import phantom_image
+    from epetreco_gb300.problem import config
+    cfg = config(cfg_name)
+    p = cfg["problem"]
+    o = Oracle()
+    rng = np.random.default_rng(seed)
+    rows = np.sort(rng.choice(p.nchannels, sample, replace=False)).astype(np.int32)
+    rnd = rng.random((sample, p.nrays, 6)).astype(np.float32)
+    rnd[rnd == 0] = 1.0
+    x_true = phantom_image(p, 1)
+    t0 = time.perf_counter()
+    rp, col, val = o.sm_build_csr(p, rows, p.nrays, rnd, exact=False)
+    yb = o.csrmv(0, rp, col, val, x_true, p.nvoxels)
+    e = np.where(yb > 0, 1.0 / np.maximum(yb, 1e-30), 0).astype(np.float32)
+    o.csrmv(1, rp, col, val, e, p.nvoxels)
+    dt = time.perf_counter() - t0
+    measured_frac = max(float((yb > 0).mean()), 1.0 / sample)
+    m_est = measured_frac * p.nchannels
+    t_iter = dt / sample * m_est
+    cores = int(os.environ.get("OMP_NUM_THREADS", os.cpu_count() or 1))
+    return {"value": 1.0 / t_iter, "unit": UNIT, "cores": cores, "kind": "port",
+            "sample": (f"{sample} seeded channels of the {cfg_name} workload through candidate "
+                       f"scan + {p.nrays}-ray values + forward/transpose products "
+                       f"({dt:.1f} s), scaled to {m_est:.0f} measured rows per iteration"),
+            "sample_seconds": dt}
+
+
+def reference_arm(args):
+    """--impl reference: the reference's CPU work for the path (oracle port;
+    the reference's own sources do not exist on the GPU machine)."""
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    per = []
+    for _ in range(args.warmup if args.warmup < 1 else 1):
+        cpu_baseline(args.config, max(4, args.cpu_sample // 4), seed=99)
+    info = None
+    for k in range(args.steps):
+        info = cpu_baseline(args.config, args.cpu_sample, seed=k)
+        per.append(info["value"])
+    v = sorted(per)[len(per) // 2]
+    out = {"metric": METRIC, "value": v, "unit": UNIT, "impl": "reference",
+           "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+           "ms_per_step": 1000.0 * 20 / v if v else None, "higher_is_better": True,
+           "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+           "config": {"workload": "full: 52^3 voxels x 5,140,980 channels, 100 rays, "
+                                  "20 iterations (matrix rebuilt every iteration)"},
+           "cpu_baseline": {"value": v, "unit": UNIT, "cores": info["cores"],
+                            "kind": info["kind"], "sample": info["sample"]},
+           "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(out), flush=True)
+
+
+# ------------------------------------------------------------------ GB300
+
+def gb300_arm(args):
+    import numpy as np
+    import torch
+
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+
+    from epetreco_gb300 import api, build, phantom
+    from epetreco_gb300._lib import lib
+    from epetreco_gb300.problem import config
+    build.build()
+    cfg = config(args.config)
+    p, nit, counts = cfg["problem"], cfg["iterations"], cfg["counts"]
+    L = lib()
+
+    # ---- inputs (not timed): measurement and sensitivity
+    rows, y, _ = phantom.measurement(p, counts)
+    s = api.sensitivity(p)
+    torch.cuda.synchronize()
+    m = rows.numel()
+    rows_h = rows.cpu().pin_memory()
+    y_h = y.cpu().pin_memory()
+    s_h = s.cpu().pin_memory()
+    x_h = torch.empty(p.nvoxels, dtype=torch.float32).pin_memory()
+    st = torch.cuda.current_stream()
+
+    def step(r, yy, ss):
+        R = api.Mlem(p, r, yy, ss, use_graph=True)
+        R.iterate(nit)
+        return R
+
+    def barrier():
+        if dist is not None:
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    for _ in range(args.warmup):
+        R = step(rows, y, s)
+        R.close()
+    barrier()
+
+    # ---- timed: device-resident inputs
+    clk = ClockSampler(local)
+    clk.start()
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    n0 = L.epet_launch_count()
+    barrier()
+    ev0.record(st)
+    for _ in range(args.steps):
+        R = step(rows, y, s)
+        R.close()
+    ev1.record(st)
+    barrier()
+    launches = (L.epet_launch_count() - n0) // args.steps
+    t_step = ev0.elapsed_time(ev1) / 1000.0 / args.steps
+    clocks = clk.stop()
+
+    # ---- e2e: host buffers through the public API
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    barrier()
+    e0.record(st)
+    for _ in range(args.steps):
+        r_d = rows_h.to("cuda", non_blocking=True)
+        y_d = y_h.to("cuda", non_blocking=True)
+        s_d = s_h.to("cuda", non_blocking=True)
+        R = step(r_d, y_d, s_d)
+        x_h.copy_(R.image(), non_blocking=True)
+        R.close()
+    e1.record(st)
+    barrier()
+    t_e2e = e0.elapsed_time(e1) / 1000.0 / args.steps
+
+    # ---- breakdown and roofline of the dominant kernels (not timed above)
+    R = api.Mlem(p, rows, y, s, use_graph=False)
+    stats = R.stats()
+    nnz = stats["nnz"]
+    A = api.systemMatrixCalculation(p, rows, cap=nnz)
+    torch.cuda.synchronize()
+
+    def timeit(fn, reps=3):
+        a = torch.cuda.Event(enable_timing=True)
+        b = torch.cuda.Event(enable_timing=True)
+        fn()
+        torch.cuda.synchronize()
+        a.record(st)
+        for _ in range(reps):
+            fn()
+        b.record(st)
+        torch.cuda.synchronize()
+        return a.elapsed_time(b) / 1000.0 / reps
+
+    t_build = timeit(lambda: api.systemMatrixCalculation(p, rows, cap=nnz), reps=1)
+    t_csc = timeit(lambda: api.csr_to_csc(A), reps=1)
+    At = api.csr_to_csc(A)
+    x = torch.full((p.nvoxels,), 1.0 / p.nvoxels, device="cuda")
+    e = torch.rand(m, device="cuda")
+    t_fwd = timeit(lambda: api.CSRmv(0, A, x), reps=5)
+    t_bwd = timeit(lambda: api.CSRmv(1, A, e, At=At), reps=5)
+    t_iter = timeit(lambda: R.iterate(1), reps=5)
+    R.close()
+    peaks = {}
+    try:
+        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except Exception:
+        pass
+    peak = peaks.get("hbm_gbs", 6800.0)
+    peak_src = "measured" if "hbm_gbs" in peaks else "fallback"
+    fwd_bytes = 8 * nnz + 8 * (m + 1) + 4 * p.nvoxels + 4 * m
+    bwd_bytes = 8 * nnz + 8 * (p.nvoxels + 1) + 4 * m + 4 * p.nvoxels
+    dominant = "spmv_transpose" if t_bwd >= t_fwd else "spmv_forward"
+    d_bytes, d_t = (bwd_bytes, t_bwd) if t_bwd >= t_fwd else (fwd_bytes, t_fwd)
+    achieved = d_bytes / d_t / 1e9
+    traffic = None
+    tp = os.path.join(ROOT, "profiles", "traffic_full.json")
+    if os.path.exists(tp):
+        try:
+            traffic = json.load(open(tp)).get(dominant)
+        except Exception:
+            traffic = None
+
+    # ---- aggregate over ranks
+    vals = torch.tensor([t_step, t_e2e], device="cuda", dtype=torch.float64)
+    if dist is not None:
+        dist.all_reduce(vals, op=dist.ReduceOp.MAX)
+    t_step, t_e2e = float(vals[0]), float(vals[1])
+    if rank != 0:
+        if dist is not None:
+            dist.destroy_process_group()
+        return
+    value = world * nit / t_step
+    cpu = None
+    if not args.no_cpu_baseline and world == 1:
+        cpu = cpu_baseline(args.config, args.cpu_sample)
+        cpu.pop("sample_seconds", None)
+    h2d = rows_h.numel() * 4 + y_h.numel() * 4 + s_h.numel() * 4
+    d2h = x_h.numel() * 4
+    out = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": 1000.0 * t_step, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": (f"{args.config}: {p.grid.n[0]}^3 voxels x {p.nchannels} "
+                                f"channels, {p.nrays} rays, {nit} iterations per step, "
+                                f"matrix built once per step"),
+                   "measured_rows": m, "nnz": nnz, "parallelism": f"replicas{world}",
+                   "l2": "inputs larger than L2 (matrix streams of GBs per pass)"},
+        "e2e": {"value": world * nit / t_e2e, "unit": UNIT, "h2d_bytes_per_step": h2d,
+                "d2h_bytes_per_step": d2h},
+        "gpu_launches": int(launches),
+        "clocks": clocks,
+        "roofline": {"bound": "hbm", "kernel": dominant, "achieved": achieved, "peak": peak,
+                     "unit": "GB/s", "frac": achieved / peak, "traffic": traffic,
+                     "peak_source": peak_src, "algorithmic_bytes": d_bytes},
+        "breakdown_ms": {"sm_build": 1000 * t_build, "csc": 1000 * t_csc,
+                         "spmv_forward": 1000 * t_fwd, "spmv_transpose": 1000 * t_bwd,
+                         "iteration": 1000 * t_iter},
+        "sm_build_nnz_per_s": nnz / t_build,
+        "spmv_gbs": {"forward": fwd_bytes / t_fwd / 1e9, "transpose": bwd_bytes / t_bwd / 1e9},
+    }
+    if cpu is not None:
+        out["cpu_baseline"] = cpu
+    print(json.dumps(out), flush=True)
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        reference_arm(args)
+    else:
+        gb300_arm(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,355 @@
+"""Host-side mirror of the reference's operator surface for the MLEM hot path.
+
+Names, argument meaning and order follow the reference headers so drivers
+read like ``reco.cu`` / ``backprojection.cu``; buffers are torch CUDA tensors
+(device memory and streams only -- every computation runs in
+``libepet_gb300.so``).  Errors raise ``EpetError`` (the reference throws
+``cudaException`` from ``HANDLE_ERROR``, CUDA_HandleError.hpp:17-31).
+
+  reference (file:line)                         here
+  systemMatrixCalculation (wrappers.hpp:166-247)  systemMatrixCalculation
+  getWorkqueue (getWorkqueue.hpp:187-223)         getWorkqueue
+  getSystemMatrixFromWorkqueue (...Workqueue.cu)   getSystemMatrixFromWorkqueue
+  cooSort (cooSort.hpp:53-71)                     cooSort
+  convertCoo2Csr (cusparseWrapper.hpp:38-45)      convertCoo2Csr
+  convertCsr2Ecsr (convertCsr2Ecsr.hpp:34-47)     convertCsr2Ecsr
+  CSRmv<float> (csrmv.hpp:25-36)                  CSRmv
+  divides/dividesMultiplies/scales/sum            same names
+  (mlemOperations.hpp:22-139)
+  nInChunk/chunkPtr/nChunks (wrappers.hpp:410-446) same names
+"""
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass
+
+import torch
+
+from . import _lib
+from ._lib import CscC, CsrC, MlemOptions, check, lib, problem_struct
+
+NON_TRANSPOSE = 0
+TRANSPOSE = 1
+
+
+def _ptr(t: torch.Tensor | None):
+    if t is None:
+        return None
+    if not t.is_cuda:
+        raise ValueError("expected a CUDA tensor")
+    if not t.is_contiguous():
+        raise ValueError("expected a contiguous tensor")
+    return C.c_void_p(t.data_ptr())
+
+
+def _stream(stream=None):
+    s = stream if stream is not None else torch.cuda.current_stream()
+    return C.c_void_p(s.cuda_stream)
+
+
+def _i32(t):
+    return t.to(torch.int32).contiguous()
+
+
+@dataclass
+class Csr:
+    """CSR over a measurement list (the reference's ECSR)."""
+    row_ptr: torch.Tensor  # int64 [m+1]
+    col: torch.Tensor      # int32 [nnz]
+    val: torch.Tensor      # float32 [nnz]
+    n: int                 # columns (voxels)
+
+    @property
+    def m(self) -> int:
+        return self.row_ptr.numel() - 1
+
+    @property
+    def nnz(self) -> int:
+        return self.col.numel()
+
+    def cstruct(self) -> CsrC:
+        return CsrC(self.m, self.n, self.nnz, self.row_ptr.data_ptr(),
+                    self.col.data_ptr() if self.nnz else None,
+                    self.val.data_ptr() if self.nnz else None)
+
+
+@dataclass
+class Csc:
+    col_ptr: torch.Tensor
+    row: torch.Tensor
+    val: torch.Tensor
+    m: int
+
+    @property
+    def n(self) -> int:
+        return self.col_ptr.numel() - 1
+
+    @property
+    def nnz(self) -> int:
+        return self.row.numel()
+
+    def cstruct(self) -> CscC:
+        return CscC(self.m, self.n, self.nnz, self.col_ptr.data_ptr(),
+                    self.row.data_ptr() if self.nnz else None,
+                    self.val.data_ptr() if self.nnz else None)
+
+
+# ---------------------------------------------------------------- geometry
+
+def trig_table(p) -> torch.Tensor:
+    out = torch.empty(2 * p.setup.na, dtype=torch.float32, device="cuda")
+    check(lib().epet_trig_table(C.byref(problem_struct(p)), _ptr(out), _stream()))
+    return out
+
+
+def dump_uniforms(p, rows: torch.Tensor) -> torch.Tensor:
+    rows = _i32(rows)
+    out = torch.empty((rows.numel(), p.nrays, 6), dtype=torch.float32, device="cuda")
+    check(lib().epet_dump_uniforms(C.byref(problem_struct(p)), _ptr(rows), rows.numel(),
+                                   _ptr(out), _stream()))
+    return out
+
+
+def rays(p, rows: torch.Tensor) -> torch.Tensor:
+    rows = _i32(rows)
+    out = torch.empty((rows.numel(), p.nrays, 6), dtype=torch.float32, device="cuda")
+    check(lib().epet_rays(C.byref(problem_struct(p)), _ptr(rows), rows.numel(), _ptr(out),
+                          _stream()))
+    return out
+
+
+# --------------------------------------------------------- system matrix
+
+def getWorkqueue(p, rows: torch.Tensor):
+    """All candidate (channel, voxel) pairs of the listed channels, list-major
+    and voxel-minor.  Returns (cnl int32, vxl int32, row_ptr int64)."""
+    rows = _i32(rows)
+    m = rows.numel()
+    cnt = torch.empty(m + 1, dtype=torch.int64, device="cuda")
+    total = C.c_int64(0)
+    PS = C.byref(problem_struct(p))
+    check(lib().epet_workqueue_count(PS, _ptr(rows), m, _ptr(cnt), C.byref(total), _stream()))
+    off = torch.zeros(m + 1, dtype=torch.int64, device="cuda")
+    off[1:] = torch.cumsum(cnt[:m], 0)
+    n = total.value
+    cnl = torch.empty(max(n, 1), dtype=torch.int32, device="cuda")
+    vxl = torch.empty(max(n, 1), dtype=torch.int32, device="cuda")
+    check(lib().epet_workqueue_fill(PS, _ptr(rows), m, _ptr(off), _ptr(cnl), _ptr(vxl),
+                                    _stream()))
+    return cnl[:n], vxl[:n], off
+
+
+def getSystemMatrixFromWorkqueue(p, rows: torch.Tensor, row_ptr: torch.Tensor,
+                                 vxl: torch.Tensor) -> torch.Tensor:
+    """Element values for a row-grouped workqueue, bit-identical to the
+    reference's per-channel-seeded kernel."""
+    rows = _i32(rows)
+    val = torch.empty(max(vxl.numel(), 1), dtype=torch.float32, device="cuda")
+    check(lib().epet_sm_values(C.byref(problem_struct(p)), _ptr(rows), rows.numel(),
+                               _ptr(row_ptr.contiguous()), _ptr(_i32(vxl)), _ptr(val), None, 0,
+                               _stream()))
+    return val[:vxl.numel()]
+
+
+def systemMatrixCalculation(p, rows: torch.Tensor, max_row_nnz: int = 0,
+                            cap: int | None = None) -> Csr:
+    """Fused build of the system matrix rows of the listed channels (CSR,
+    columns ascending, zero values dropped).  Synchronous."""
+    rows = _i32(rows)
+    m = rows.numel()
+    PS = C.byref(problem_struct(p))
+    row_ptr = torch.empty(m + 1, dtype=torch.int64, device="cuda")
+    nnz = C.c_int64(0)
+    if cap is None:
+        # first pass sizes the output
+        cs = CsrC(m, p.nvoxels, 0, row_ptr.data_ptr(), None, None)
+        st = lib().epet_sm_build(PS, _ptr(rows), m, C.byref(cs), 0, C.byref(nnz),
+                                 int(max_row_nnz), None, 0, _stream())
+        if st not in (_lib.EPET_OK, 2):
+            check(st)
+        cap = nnz.value
+    col = torch.empty(max(cap, 1), dtype=torch.int32, device="cuda")
+    val = torch.empty(max(cap, 1), dtype=torch.float32, device="cuda")
+    cs = CsrC(m, p.nvoxels, 0, row_ptr.data_ptr(), col.data_ptr(), val.data_ptr())
+    check(lib().epet_sm_build(PS, _ptr(rows), m, C.byref(cs), cap, C.byref(nnz),
+                              int(max_row_nnz), None, 0, _stream()))
+    n = nnz.value
+    return Csr(row_ptr, col[:n], val[:n], p.nvoxels)
+
+
+def project_forward(p, rows, x, max_row_nnz: int = 0) -> torch.Tensor:
+    """Matrix-free y = A x (chords recomputed, nothing stored)."""
+    rows = _i32(rows)
+    y = torch.empty(rows.numel(), dtype=torch.float32, device="cuda")
+    check(lib().epet_project_forward(C.byref(problem_struct(p)), _ptr(rows), rows.numel(),
+                                     _ptr(x.contiguous()), _ptr(y), int(max_row_nnz), None, 0,
+                                     _stream()))
+    return y
+
+
+def project_back(p, rows, e, c=None, max_row_nnz: int = 0) -> torch.Tensor:
+    """Matrix-free c += A^T e."""
+    rows = _i32(rows)
+    if c is None:
+        c = torch.zeros(p.nvoxels, dtype=torch.float32, device="cuda")
+    check(lib().epet_project_back(C.byref(problem_struct(p)), _ptr(rows), rows.numel(),
+                                  _ptr(e.contiguous()), _ptr(c), int(max_row_nnz), None, 0,
+                                  _stream()))
+    return c
+
+
+def sensitivity(p, rows=None, max_row_nnz: int = 0, return_f64: bool = False):
+    """s = column sums of A over the listed channels (all channels by
+    default), fp64 accumulation, normalised to sum 1."""
+    if rows is None:
+        rows = torch.arange(p.nchannels, dtype=torch.int32, device="cuda")
+    rows = _i32(rows)
+    s = torch.empty(p.nvoxels, dtype=torch.float32, device="cuda")
+    s64 = torch.empty(p.nvoxels, dtype=torch.float64, device="cuda")
+    check(lib().epet_sensitivity(C.byref(problem_struct(p)), _ptr(rows), rows.numel(), _ptr(s),
+                                 _ptr(s64), int(max_row_nnz), None, 0, _stream()))
+    return (s, s64) if return_f64 else s
+
+
+# ------------------------------------------------------------ sparse formats
+
+def cooSort(val: torch.Tensor, row: torch.Tensor, col: torch.Tensor) -> None:
+    """In-place stable sort of COO triples by (row, col)."""
+    for t, dt in ((val, torch.float32), (row, torch.int32), (col, torch.int32)):
+        if t.dtype != dt or not t.is_contiguous():
+            raise ValueError("cooSort expects contiguous float32 val, int32 row/col")
+    check(lib().epet_coo_sort(_ptr(val), _ptr(row), _ptr(col), val.numel(), None, 0, _stream()))
+
+
+def convertCoo2Csr(row: torch.Tensor, nnz: int, m: int) -> torch.Tensor:
+    csr = torch.empty(m + 1, dtype=torch.int64, device="cuda")
+    check(lib().epet_coo2csr(_ptr(_i32(row)), int(nnz), int(m), _ptr(csr), _stream()))
+    return csr
+
+
+def convertCsr2Ecsr(yRowId: torch.Tensor, nnzr: int, csr: torch.Tensor, m: int) -> torch.Tensor:
+    ecsr = torch.empty(nnzr + 1, dtype=torch.int64, device="cuda")
+    check(lib().epet_csr2ecsr(_ptr(ecsr), _ptr(_i32(yRowId)), int(nnzr),
+                              _ptr(csr.to(torch.int64).contiguous()), int(m), _stream()))
+    return ecsr
+
+
+def csr_to_csc(a: Csr) -> Csc:
+    col_ptr = torch.empty(a.n + 1, dtype=torch.int64, device="cuda")
+    row = torch.empty(max(a.nnz, 1), dtype=torch.int32, device="cuda")
+    val = torch.empty(max(a.nnz, 1), dtype=torch.float32, device="cuda")
+    cc = CscC(a.m, a.n, a.nnz, col_ptr.data_ptr(), row.data_ptr(), val.data_ptr())
+    ca = a.cstruct()
+    check(lib().epet_csr_to_csc(C.byref(ca), C.byref(cc), None, 0, _stream()))
+    return Csc(col_ptr, row[:a.nnz], val[:a.nnz], a.m)
+
+
+# ---------------------------------------------------------------------- SpMV
+
+def CSRmv(transA: int, A: Csr, x: torch.Tensor, alpha: float = 1.0, beta: float = 0.0,
+          y: torch.Tensor | None = None, At: Csc | None = None) -> torch.Tensor:
+    """y = alpha*op(A)*x + beta*y.  The transpose uses the column-major copy
+    when given (scatter-free), else fp32 atomics."""
+    out_len = A.n if transA else A.m
+    if y is None:
+        y = torch.zeros(out_len, dtype=torch.float32, device="cuda")
+    ca = A.cstruct()
+    cc = At.cstruct() if At is not None else None
+    check(lib().epet_csrmv(int(transA), C.byref(ca), C.byref(cc) if cc else None, float(alpha),
+                           _ptr(x.contiguous()), float(beta), _ptr(y), _stream()))
+    return y
+
+
+# ---------------------------------------------------------- MLEM operations
+
+def divides(result, dividend, divisor, n: int | None = None) -> None:
+    n = dividend.numel() if n is None else n
+    check(lib().epet_divides(_ptr(result), _ptr(dividend), _ptr(divisor), n, _stream()))
+
+
+def dividesMultiplies(result, a, b, c, n: int | None = None) -> None:
+    n = a.numel() if n is None else n
+    check(lib().epet_divides_multiplies(_ptr(result), _ptr(a), _ptr(b), _ptr(c), n, _stream()))
+
+
+def scales(x, alpha: float, n: int | None = None) -> None:
+    n = x.numel() if n is None else n
+    check(lib().epet_scales(_ptr(x), float(alpha), n, _stream()))
+
+
+def sum(x, n: int | None = None) -> float:  # noqa: A001 - reference name
+    """Sum in fp64 on the device; returns a host value (synchronising), as the
+    reference's thrust::reduce does."""
+    n = x.numel() if n is None else n
+    out = torch.empty(1, dtype=torch.float64, device="cuda")
+    check(lib().epet_sum_f64(_ptr(x), n, _ptr(out), _stream()))
+    return float(out.item())
+
+
+# ------------------------------------------------------------ chunk helpers
+
+def nInChunk(idChunk: int, nAll: int, nFullChunk: int) -> int:
+    if idChunk < (nAll + nFullChunk - 1) // nFullChunk:
+        if idChunk < nAll // nFullChunk:
+            return nFullChunk
+        return nAll % nFullChunk
+    return 0
+
+
+def chunkPtr(chunkId: int, nFullChunk: int) -> int:
+    return chunkId * nFullChunk
+
+
+def nChunks(maxNnz: int, maxNChunk: int) -> int:
+    return (maxNnz + maxNChunk - 1) // maxNChunk
+
+
+# --------------------------------------------------------------- MLEM driver
+
+class Mlem:
+    """One reconstruction on the device (reco.cu's loop): the system matrix
+    of the measured rows is built once at construction."""
+
+    def __init__(self, p, rows, y, s, use_graph: bool = True, max_row_nnz: int = 0,
+                 value_format: int = 0):
+        self.p = p
+        rows = _i32(rows)
+        y = y.to(torch.float32).contiguous()
+        s = s.to(torch.float32).contiguous()
+        self._h = C.c_void_p()
+        opt = MlemOptions(int(max_row_nnz), 1 if use_graph else 0, int(value_format), 0)
+        check(lib().epet_mlem_create(C.byref(problem_struct(p)), _ptr(rows), _ptr(y),
+                                     rows.numel(), _ptr(s), C.byref(opt), C.byref(self._h),
+                                     _stream()))
+
+    def iterate(self, nit: int, loglik: bool = False):
+        ll = C.c_double(0.0)
+        check(lib().epet_mlem_iterate(self._h, int(nit), C.byref(ll) if loglik else None,
+                                      _stream()))
+        return ll.value if loglik else None
+
+    def image(self) -> torch.Tensor:
+        """A copy of the current image (float32, V)."""
+        out = torch.empty(self.p.nvoxels, dtype=torch.float32, device="cuda")
+        check(lib().epet_mlem_get_image(self._h, _ptr(out), _stream()))
+        return out
+
+    def set_image(self, x: torch.Tensor) -> None:
+        check(lib().epet_mlem_set_image(self._h, _ptr(x.to(torch.float32).contiguous()),
+                                        _stream()))
+
+    def stats(self):
+        nnz, b = C.c_int64(0), C.c_int64(0)
+        check(lib().epet_mlem_stats(self._h, C.byref(nnz), C.byref(b)))
+        return {"nnz": nnz.value, "bytes_per_iteration": b.value}
+
+    def close(self):
+        if self._h:
+            lib().epet_mlem_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -1,0 +1,125 @@
+// geometry.cu -- per-angle trig table, cuRAND uniforms and world rays.
+//
+// Rays follow RandRayGen with the per-channel seeding of the workqueue
+// kernel: curand_init(seed, channel, 0) and six curand_uniform draws per ray,
+// the first three placing the start point in crystal 0 and the last three
+// the end point in crystal 1 (getSystemMatrixFromWorkqueue.cu:189-230).
+#include <curand_kernel.h>
+
+#include "common.cuh"
+#include "internal.h"
+
+namespace epet {
+
+__global__ void k_trig(epet_setup s, float* sc) {
+  int a = blockIdx.x * blockDim.x + threadIdx.x;
+  if (a < s.na) angle_sincos(s, a, &sc[2 * a], &sc[2 * a + 1]);
+}
+
+// One thread per channel: the cuRAND stream of a channel is sequential, so a
+// channel's 6*nrays draws stay on one thread; channels spread over threads.
+template <bool kUniformsOnly>
+__global__ void __launch_bounds__(128) k_rays(Geo G, const int32_t* __restrict__ rows,
+                                              int64_t m, float* __restrict__ out) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= m) return;
+  const int cnl = rows[i];
+  int id[5];
+  channel_decode(G.p.setup, cnl, id);
+  float sn, cs;
+  angle_sincos(G.p.setup, id[0], &sn, &cs);
+  const CrystalMat m0 = crystal_matrix(G.p.setup, sn, cs, 0, id[1], id[2]);
+  const CrystalMat m1 = crystal_matrix(G.p.setup, sn, cs, 1, id[3], id[4]);
+  curandState st;
+  curand_init(G.p.seed, (unsigned long long)cnl, 0ull, &st);
+  float2* o = reinterpret_cast<float2*>(out + i * (int64_t)G.p.nrays * 6);
+  for (int r = 0; r < G.p.nrays; r++) {
+    float u[6];
+#pragma unroll
+    for (int k = 0; k < 6; k++) u[k] = curand_uniform(&st);
+    if (kUniformsOnly) {
+      o[3 * r + 0] = make_float2(u[0], u[1]);
+      o[3 * r + 1] = make_float2(u[2], u[3]);
+      o[3 * r + 2] = make_float2(u[4], u[5]);
+    } else {
+      float p0[3], p1[3];
+      crystal_apply(m0, u[0], u[1], u[2], p0);
+      crystal_apply(m1, u[3], u[4], u[5], p1);
+      o[3 * r + 0] = make_float2(p0[0], p0[1]);
+      o[3 * r + 1] = make_float2(p0[2], p1[0]);
+      o[3 * r + 2] = make_float2(p1[1], p1[2]);
+    }
+  }
+}
+
+Geo make_geo(const epet_problem& p) {
+  Geo G;
+  G.p = p;
+  // 0.5*(absolute(vxlEdges)+absolute(pxlEdges)) with absolute = sqrtf of the
+  // left-to-right sum of squares (getSystemMatrixDeviceOnly.cu:55-58); this
+  // file is compiled with host contraction disabled.
+  volatile float a0 = p.grid.d[0] * p.grid.d[0];
+  volatile float a1 = p.grid.d[1] * p.grid.d[1];
+  volatile float a2 = p.grid.d[2] * p.grid.d[2];
+  volatile float av = sqrtf((a0 + a1) + a2);
+  volatile float b0 = p.setup.segx * p.setup.segx;
+  volatile float b1 = p.setup.segy * p.setup.segy;
+  volatile float b2 = p.setup.segz * p.setup.segz;
+  volatile float bv = sqrtf((b0 + b1) + b2);
+  volatile float sr = av + bv;
+  G.sum_radii = 0.5f * sr;
+  G.V = p.grid.n[0] * p.grid.n[1] * p.grid.n[2];
+  G.nyz = p.grid.n[1] * p.grid.n[2];
+  // Fixed-point scale for exact chord sums: nrays chords of at most the
+  // voxel diagonal must stay below 2^62.
+  double maxsum = (double)p.nrays * (double)av * 1.01 + 1e-30;
+  int s = (int)floor(log2(4.611686018427388e18 / maxsum));
+  if (s > 100) s = 100;
+  G.fx_scale = ldexpf(1.0f, s);
+  G.fx_inv = ldexpf(1.0f, -s);
+  return G;
+}
+
+epet_status launch_rays(const Geo& G, const int32_t* rows, int64_t m, float* out,
+                        bool uniforms_only, cudaStream_t st) {
+  if (m == 0) return EPET_OK;
+  const int T = 128;
+  const int nb = ceil_div(m, T);
+  if (uniforms_only) k_rays<true><<<nb, T, 0, st>>>(G, rows, m, out);
+  else k_rays<false><<<nb, T, 0, st>>>(G, rows, m, out);
+  EPET_LAUNCHED();
+  return EPET_OK;
+}
+
+}  // namespace epet
+
+using namespace epet;
+
+extern "C" {
+
+epet_status epet_trig_table(const epet_problem* p, float* sc_d,
+                            epet_stream_t stream) {
+  EPET_CHECK(epet_problem_validate(p));
+  if (!sc_d) return set_error(EPET_ERR_INVALID, "sc_d is NULL");
+  k_trig<<<ceil_div(p->setup.na, 128), 128, 0, (cudaStream_t)stream>>>(p->setup, sc_d);
+  EPET_LAUNCHED();
+  return EPET_OK;
+}
+
+epet_status epet_dump_uniforms(const epet_problem* p, const int32_t* rows_d,
+                               int64_t m, float* out_d, epet_stream_t stream) {
+  EPET_CHECK(epet_problem_validate(p));
+  if (m < 0 || (m > 0 && (!rows_d || !out_d)))
+    return set_error(EPET_ERR_INVALID, "bad rows/out");
+  return launch_rays(make_geo(*p), rows_d, m, out_d, true, (cudaStream_t)stream);
+}
+
+epet_status epet_rays(const epet_problem* p, const int32_t* rows_d, int64_t m,
+                      float* out_d, epet_stream_t stream) {
+  EPET_CHECK(epet_problem_validate(p));
+  if (m < 0 || (m > 0 && (!rows_d || !out_d)))
+    return set_error(EPET_ERR_INVALID, "bad rows/out");
+  return launch_rays(make_geo(*p), rows_d, m, out_d, false, (cudaStream_t)stream);
+}
+
+}  // extern "C"

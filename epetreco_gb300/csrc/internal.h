@@ -1,0 +1,46 @@
+// internal.h -- host-side declarations shared between the library's units.
+#pragma once
+#include "common.cuh"
+
+namespace epet {
+
+Geo make_geo(const epet_problem& p);
+epet_status launch_rays(const Geo& G, const int32_t* rows, int64_t m,
+                        float* out, bool uniforms_only, cudaStream_t st);
+
+// Exclusive scan of int64 counts (n entries) into out[n+1]; out[n] = total.
+// tmp must hold scan_tmp_elems(n) int64.
+size_t scan_tmp_elems(int64_t n);
+epet_status exclusive_scan_i64(const int64_t* in, int64_t* out, int64_t n,
+                               int64_t* tmp, cudaStream_t st);
+
+// Stable LSD radix sort of (uint64 key, uint64 value) pairs on the low `bits`
+// bits of the key.  keys/vals are sorted in place; alt_* are same-sized
+// buffers; hist holds radix_hist_elems(n) uint32.
+size_t radix_hist_elems(int64_t n);
+epet_status radix_sort_pairs(uint64_t* keys, uint64_t* vals, uint64_t* alt_keys,
+                             uint64_t* alt_vals, int64_t n, int bits,
+                             uint32_t* hist, int64_t* scan_tmp, cudaStream_t st);
+
+// Row walk configuration chosen for a problem (per-row accumulator size).
+int auto_row_capacity(const epet_problem& p);
+int64_t exact_rows_total();
+
+// Candidate compaction and per-candidate values (workqueue.cu).
+epet_status launch_workqueue_count(const Geo& G, const int32_t* rows, int64_t m,
+                                   int64_t* row_count, cudaStream_t st);
+epet_status launch_workqueue_fill(const Geo& G, const int32_t* rows, int64_t m,
+                                  const int64_t* row_off, int32_t* cnl, int32_t* vxl,
+                                  cudaStream_t st);
+epet_status launch_values(const Geo& G, const float* rays, int64_t m,
+                          const int64_t* row_ptr, const int32_t* col, float* val,
+                          cudaStream_t st);
+epet_status exact_rows_apply(const Geo& G, const int32_t* rows, const int32_t* ex_rows,
+                             int64_t n_ex, int mode, int64_t stride, int32_t* stage_col,
+                             float* stage_val, int32_t* row_len, const float* x, float* y,
+                             const float* e, float* c, double* s64, cudaStream_t st);
+epet_status column_sums(const epet_problem* p, const int32_t* rows_d, int64_t m,
+                        double* s64, int32_t max_row_nnz, void* ws, size_t ws_bytes,
+                        cudaStream_t st);
+
+}  // namespace epet

@@ -1,0 +1,251 @@
+// mlem.cu -- the reconstruction driver (reco.cu:32-332 without MPI/HDF5).
+//
+// One epet_mlem holds a reconstruction on the device: the measured rows and
+// their counts, the system matrix built once by the fused kernel (it is
+// deterministic, so the reference's rebuild in every iteration is not
+// needed), its column-major copy, the normalised sensitivity and the image.
+// An iteration is four kernels: forward product fused with e = y/(Ax) and
+// the log-likelihood terms; transpose product fused with x*c/s and the image
+// sum; the fixed-order sum; the normalisation.  With use_graph the four are
+// captured once in a CUDA graph and replayed.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+
+#include "common.cuh"
+#include "internal.h"
+#include "spmv.cuh"
+
+struct epet_mlem {
+  epet_problem p;
+  epet_mlem_options opt;
+  int64_t m = 0, V = 0;
+  int32_t* rows = nullptr;
+  float *y = nullptr, *s = nullptr, *x = nullptr, *xnew = nullptr, *e = nullptr;
+  epet_csr A{};
+  epet_csc At{};
+  int64_t capA = 0;
+  double *part_ll = nullptr, *part_x = nullptr, *sums = nullptr;
+  int64_t nb_fwd = 0, nb_bwd = 0;
+  int g_fwd = 32, g_bwd = 32;
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+};
+
+namespace epet {
+epet_status build_csr_growable(const epet_problem* p, const int32_t* rows, int64_t m,
+                               epet_csr* out, int64_t* cap, int32_t max_row_nnz,
+                               cudaStream_t st);
+}
+
+using namespace epet;
+
+static void mlem_free(epet_mlem* h) {
+  if (!h) return;
+  if (h->exec) cudaGraphExecDestroy(h->exec);
+  if (h->graph) cudaGraphDestroy(h->graph);
+  void* bufs[] = {h->rows, h->y, h->s, h->x, h->xnew, h->e, h->A.row_ptr, h->A.col, h->A.val,
+                  h->At.col_ptr, h->At.row, h->At.val, h->part_ll, h->part_x, h->sums};
+  for (void* b : bufs)
+    if (b) cudaFree(b);
+  delete h;
+}
+
+static epet_status mlem_iteration(epet_mlem* h, cudaStream_t st) {
+  EPET_CHECK(launch_rows(h->g_fwd, h->A.row_ptr, h->A.col, h->A.val, h->x, h->m,
+                         EpiMlemForward{h->y, h->e, nullptr}, h->part_ll, st, nullptr));
+  EPET_CHECK(launch_rows(h->g_bwd, h->At.col_ptr, h->At.row, h->At.val, h->e, h->V,
+                         EpiMlemUpdate{h->x, h->s, h->xnew, nullptr}, h->part_x, st, nullptr));
+  EPET_CHECK(launch_sum_partials(h->part_x, h->nb_bwd, h->sums + 1, st));
+  EPET_CHECK(launch_sum_partials(h->part_ll, h->nb_fwd, h->sums + 0, st));
+  EPET_CHECK(launch_normalise(h->xnew, h->sums + 1, h->V, h->x, st));
+  return EPET_OK;
+}
+
+__global__ void k_fill(float* x, int64_t n, float v) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) x[i] = v;
+}
+
+__global__ void k_f64_to_f32(const double* a, int64_t n, float* b) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) b[i] = (float)a[i];
+}
+
+extern "C" {
+
+epet_status epet_mlem_create(const epet_problem* p, const int32_t* rows_d, const float* y_d,
+                             int64_t m, const float* s_d, const epet_mlem_options* opt,
+                             epet_mlem** out, epet_stream_t stream) {
+  EPET_CHECK(epet_problem_validate(p));
+  if (!out || m < 0 || (m > 0 && (!rows_d || !y_d)) || !s_d)
+    return set_error(EPET_ERR_INVALID, "bad arguments");
+  epet_mlem_options o{};
+  if (opt) o = *opt;
+  if (o.value_format != 0)
+    return set_error(EPET_ERR_UNSUPPORTED, "value_format %d not supported by this driver",
+                     o.value_format);
+  cudaStream_t st = (cudaStream_t)stream;
+  epet_mlem* h = new epet_mlem();
+  h->p = *p;
+  h->opt = o;
+  h->m = m;
+  h->V = (int64_t)p->grid.n[0] * p->grid.n[1] * p->grid.n[2];
+  const int64_t V = h->V;
+  auto fail = [&](epet_status rc) {
+    mlem_free(h);
+    return rc;
+  };
+#define ALLOC(ptr, bytes)                                                    \
+  do {                                                                       \
+    cudaError_t e_ = cudaMalloc((void**)&(ptr), std::max<size_t>(bytes, 8)); \
+    if (e_ != cudaSuccess) return fail(cuda_status(e_, "cudaMalloc " #ptr)); \
+  } while (0)
+  ALLOC(h->rows, m * 4);
+  ALLOC(h->y, m * 4);
+  ALLOC(h->e, m * 4);
+  ALLOC(h->s, V * 4);
+  ALLOC(h->x, V * 4);
+  ALLOC(h->xnew, V * 4);
+  ALLOC(h->sums, 64);
+  if (m > 0) {
+    cudaMemcpyAsync(h->rows, rows_d, m * 4, cudaMemcpyDeviceToDevice, st);
+    cudaMemcpyAsync(h->y, y_d, m * 4, cudaMemcpyDeviceToDevice, st);
+  }
+  cudaMemcpyAsync(h->s, s_d, V * 4, cudaMemcpyDeviceToDevice, st);
+  // sensitivity normalised to sum 1 (reco.cu:181-183)
+  {
+    const int nb = (int)std::max<int64_t>(1, std::min<int64_t>(ceil_div(V, 256), 1024));
+    double* part = nullptr;
+    ALLOC(part, nb * 8);
+    epet_status rc = sum_f64(h->s, V, part, nb, h->sums + 2, st);
+    if (rc == EPET_OK) rc = launch_normalise(h->s, h->sums + 2, V, h->s, st);
+    cudaFree(part);
+    if (rc != EPET_OK) return fail(rc);
+  }
+  // x = ones / sum(ones) (reco.cu:126-136)
+  k_fill<<<ceil_div(V, 256), 256, 0, st>>>(h->x, V, (float)(1.0 / (double)(float)V));
+  note_launch();
+  if (cudaGetLastError() != cudaSuccess) return fail(set_error(EPET_ERR_CUDA, "fill"));
+
+  // system matrix (rows in list order) and its column-major copy
+  epet_status rc = build_csr_growable(p, h->rows, m, &h->A, &h->capA, o.max_row_nnz, st);
+  if (rc != EPET_OK) return fail(rc);
+  const int64_t nnz = h->A.nnz;
+  ALLOC(h->At.col_ptr, (V + 1) * 8);
+  ALLOC(h->At.row, nnz * 4);
+  ALLOC(h->At.val, nnz * 4);
+  rc = epet_csr_to_csc(&h->A, &h->At, nullptr, 0, stream);
+  if (rc != EPET_OK) return fail(rc);
+  h->g_fwd = pick_group(m ? (double)nnz / m : 0.0);
+  h->g_bwd = pick_group(V ? (double)nnz / V : 0.0);
+  h->nb_fwd = (m + kSpmvThreads / h->g_fwd - 1) / (kSpmvThreads / h->g_fwd);
+  h->nb_bwd = (V + kSpmvThreads / h->g_bwd - 1) / (kSpmvThreads / h->g_bwd);
+  ALLOC(h->part_ll, std::max<int64_t>(h->nb_fwd, 1) * 8);
+  ALLOC(h->part_x, std::max<int64_t>(h->nb_bwd, 1) * 8);
+  cudaMemsetAsync(h->part_ll, 0, std::max<int64_t>(h->nb_fwd, 1) * 8, st);
+#undef ALLOC
+  cudaError_t e = cudaStreamSynchronize(st);
+  if (e != cudaSuccess) return fail(cuda_status(e, "mlem create"));
+  *out = h;
+  return EPET_OK;
+}
+
+epet_status epet_mlem_destroy(epet_mlem* h) {
+  if (h) cudaDeviceSynchronize();
+  mlem_free(h);
+  return EPET_OK;
+}
+
+epet_status epet_mlem_iterate(epet_mlem* h, int32_t nit, double* loglik_h,
+                              epet_stream_t stream) {
+  if (!h || nit < 0) return set_error(EPET_ERR_INVALID, "bad arguments");
+  cudaStream_t st = (cudaStream_t)stream;
+  if (h->opt.use_graph) {
+    if (!h->exec) {
+      cudaStream_t cap = nullptr;
+      EPET_CUDA(cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking));
+      epet_status rc = EPET_OK;
+      cudaError_t e = cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal);
+      if (e == cudaSuccess) rc = mlem_iteration(h, cap);
+      cudaError_t e2 = cudaStreamEndCapture(cap, &h->graph);
+      cudaStreamDestroy(cap);
+      if (e != cudaSuccess) return cuda_status(e, "begin capture");
+      if (rc != EPET_OK) return rc;
+      if (e2 != cudaSuccess) return cuda_status(e2, "end capture");
+      EPET_CUDA(cudaGraphInstantiate(&h->exec, h->graph, 0));
+    }
+    for (int it = 0; it < nit; it++) {
+      EPET_CUDA(cudaGraphLaunch(h->exec, st));
+      note_launch(5);  // the captured iteration holds five kernels
+    }
+  } else {
+    for (int it = 0; it < nit; it++) EPET_CHECK(mlem_iteration(h, st));
+  }
+  if (loglik_h) {
+    double s[2];
+    EPET_CUDA(cudaMemcpyAsync(s, h->sums, 16, cudaMemcpyDeviceToHost, st));
+    EPET_CUDA(cudaStreamSynchronize(st));
+    *loglik_h = s[0];
+  }
+  return EPET_OK;
+}
+
+float* epet_mlem_image(epet_mlem* h) { return h ? h->x : nullptr; }
+
+epet_status epet_mlem_get_image(const epet_mlem* h, float* x_d, epet_stream_t stream) {
+  if (!h || !x_d) return set_error(EPET_ERR_INVALID, "bad arguments");
+  EPET_CUDA(cudaMemcpyAsync(x_d, h->x, h->V * 4, cudaMemcpyDeviceToDevice,
+                            (cudaStream_t)stream));
+  return EPET_OK;
+}
+
+epet_status epet_mlem_set_image(epet_mlem* h, const float* x_d, epet_stream_t stream) {
+  if (!h || !x_d) return set_error(EPET_ERR_INVALID, "bad arguments");
+  EPET_CUDA(cudaMemcpyAsync(h->x, x_d, h->V * 4, cudaMemcpyDeviceToDevice,
+                            (cudaStream_t)stream));
+  return EPET_OK;
+}
+
+epet_status epet_mlem_stats(const epet_mlem* h, int64_t* nnz_h, int64_t* bytes_h) {
+  if (!h) return set_error(EPET_ERR_INVALID, "bad arguments");
+  if (nnz_h) *nnz_h = h->A.nnz;
+  if (bytes_h) {
+    // forward: values+columns, row pointers, y, x (once), e written;
+    // transpose: values+rows, column pointers, e (once), x, s, xnew written;
+    // sum/normalise: xnew read, x written.
+    const int64_t nnz = h->A.nnz, m = h->m, V = h->V;
+    *bytes_h = 8 * nnz + 8 * (m + 1) + 4 * m + 4 * V + 4 * m +
+               8 * nnz + 8 * (V + 1) + 4 * m + 4 * V + 4 * V + 4 * V +
+               4 * V + 4 * V;
+  }
+  return EPET_OK;
+}
+
+epet_status epet_sensitivity(const epet_problem* p, const int32_t* rows_d, int64_t m,
+                             float* s_d, double* s64_d, int32_t max_row_nnz, void* ws,
+                             size_t ws_bytes, epet_stream_t stream) {
+  EPET_CHECK(epet_problem_validate(p));
+  if (!s_d || m < 0 || (m > 0 && !rows_d)) return set_error(EPET_ERR_INVALID, "bad arguments");
+  cudaStream_t st = (cudaStream_t)stream;
+  const int64_t V = (int64_t)p->grid.n[0] * p->grid.n[1] * p->grid.n[2];
+  double* s64 = s64_d;
+  if (!s64) EPET_CUDA(cudaMallocAsync((void**)&s64, V * 8, st));
+  EPET_CUDA(cudaMemsetAsync(s64, 0, V * 8, st));
+  epet_status rc = column_sums(p, rows_d, m, s64, max_row_nnz, ws, ws_bytes, st);
+  if (rc == EPET_OK) {
+    k_f64_to_f32<<<ceil_div(V, 256), 256, 0, st>>>(s64, V, s_d);
+    note_launch();
+    // normalised to sum 1 as backprojection.cu:157-161
+    const int nb = (int)std::max<int64_t>(1, std::min<int64_t>(ceil_div(V, 256), 1024));
+    double* part = nullptr;
+    cudaMallocAsync((void**)&part, (nb + 1) * 8, st);
+    rc = sum_f64(s_d, V, part, nb, part + nb, st);
+    if (rc == EPET_OK) rc = launch_normalise(s_d, part + nb, V, s_d, st);
+    cudaFreeAsync(part, st);
+  }
+  if (!s64_d) cudaFreeAsync(s64, st);
+  return rc;
+}
+
+}  // extern "C"

@@ -1,0 +1,104 @@
+// runtime.cu -- error reporting, scratch memory, problem validation.
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <atomic>
+
+#include "common.cuh"
+
+namespace epet {
+
+static thread_local char g_err[512] = "";
+
+epet_status set_error(epet_status st, const char* fmt, ...) {
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(g_err, sizeof(g_err), fmt, ap);
+  va_end(ap);
+  return st;
+}
+
+epet_status cuda_status(cudaError_t e, const char* what) {
+  return set_error(EPET_ERR_CUDA, "%s: %s", what, cudaGetErrorString(e));
+}
+
+epet_status Scratch::init(void* ws, size_t ws_bytes, size_t need,
+                          cudaStream_t s) {
+  stream = s;
+  size = need;
+  used = 0;
+  if (need == 0) return EPET_OK;
+  if (ws) {
+    if (ws_bytes < need)
+      return set_error(EPET_ERR_CAPACITY,
+                       "workspace too small: %zu bytes given, %zu needed",
+                       ws_bytes, need);
+    if (reinterpret_cast<uintptr_t>(ws) & 255)
+      return set_error(EPET_ERR_INVALID, "workspace must be 256-byte aligned");
+    base = static_cast<char*>(ws);
+    owned = false;
+    return EPET_OK;
+  }
+  cudaError_t e = cudaMallocAsync(reinterpret_cast<void**>(&base), need, s);
+  if (e != cudaSuccess) {
+    base = nullptr;
+    return cuda_status(e, "cudaMallocAsync(workspace)");
+  }
+  owned = true;
+  return EPET_OK;
+}
+
+Scratch::~Scratch() {
+  if (owned && base) cudaFreeAsync(base, stream);
+}
+
+static std::atomic<long long> g_launches{0};
+void note_launch(int n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
+long long launches() { return g_launches.load(); }
+
+int num_sms() {
+  static int n = 0;
+  if (n == 0) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+    if (n <= 0) n = 1;
+  }
+  return n;
+}
+
+}  // namespace epet
+
+extern "C" {
+
+const char* epet_last_error(void) { return epet::g_err; }
+
+const char* epet_version(void) { return "epet_gb300 1.0 (sm_103a)"; }
+
+long long epet_launch_count(void) { return epet::launches(); }
+
+epet_status epet_problem_validate(const epet_problem* p) {
+  using epet::set_error;
+  if (!p) return set_error(EPET_ERR_INVALID, "problem is NULL");
+  const epet_setup& s = p->setup;
+  const epet_grid& g = p->grid;
+  if (p->nrays < 1) return set_error(EPET_ERR_INVALID, "nrays must be >= 1");
+  if (s.na < 1 || s.n0z < 1 || s.n0y < 1 || s.n1z < 1 || s.n1y < 1)
+    return set_error(EPET_ERR_INVALID, "detector counts must be >= 1");
+  double nch = (double)s.na * s.n0z * s.n0y * s.n1z * s.n1y;
+  if (nch > 2147483647.0)
+    return set_error(EPET_ERR_UNSUPPORTED, "channel count exceeds int32");
+  for (int d = 0; d < 3; d++) {
+    if (g.n[d] < 1) return set_error(EPET_ERR_INVALID, "grid counts must be >= 1");
+    if (!(g.d[d] > 0.f)) return set_error(EPET_ERR_INVALID, "grid pitch must be > 0");
+  }
+  double V = (double)g.n[0] * g.n[1] * g.n[2];
+  if (V > 2147483647.0)
+    return set_error(EPET_ERR_UNSUPPORTED, "voxel count exceeds int32");
+  if (!(s.segx > 0.f && s.segy > 0.f && s.segz > 0.f))
+    return set_error(EPET_ERR_INVALID, "crystal edges must be > 0");
+  return EPET_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,808 @@
+// sm_build.cu -- fused on-the-fly system matrix: ray walks -> exact per-voxel
+// sums -> candidate filter -> CSR rows in voxel order.
+//
+// Semantics (what the reference computes, getSystemMatrixFromWorkqueue.cu:
+// 96-261 over the candidates of getSystemMatrixDeviceOnly.cu:25-77):
+//   A[c,v] = (1/nrays) * sum_r len_r(v)  for candidate voxels v of channel c,
+// len_r(v) the slab chord length of ray r in voxel v (:24-69).  Entries with
+// A[c,v] == 0 are not stored (the reference stores them).
+//
+// GB300 design:
+//  * one CTA per channel; its rays come from a thread-per-channel cuRAND
+//    kernel (geometry.cu), so the sequential XORWOW stream of a channel is
+//    drawn once instead of once per candidate voxel;
+//  * each thread walks a ray voxel by voxel (Siddon order).  The entry/exit
+//    parameters are the reference's own correctly rounded quotients
+//    (plane - r0)/(r1 - r0), shared between neighbouring voxels, so each
+//    chord length is bit-identical to intersectionLength(); a voxel is never
+//    evaluated more than once per ray;
+//  * chords accumulate in a dense shared-memory window covering the ray
+//    bundle slab by slab along x (bounded by the 64 crystal-corner lines, an
+//    exact convex-hull bound), as 64-bit fixed-point integers: the sum is
+//    exact and independent of the order of the atomic adds, so results are
+//    deterministic; it is rounded once to float.  Versus the reference's
+//    sequential fp32 sum the difference is below (nrays-1)*2^-24 relative;
+//  * window cells are ordered by voxel id (x slabs ascending, then y, z), so
+//    extraction is an ordered compaction: no sort;
+//  * candidates are tested with an exact threshold on |ab x ap|^2 that
+//    reproduces the reference's float test bit for bit (common.cuh).
+#include <curand_kernel.h>
+
+#include <algorithm>
+#include <vector>
+
+#include "common.cuh"
+#include "internal.h"
+
+namespace epet {
+
+constexpr int kWalkThreads = 128;
+constexpr int kMaxSlabs = 1024;  // nx limit of the walk kernel
+
+enum WalkMode { kModeCsr = 0, kModeForward = 1, kModeBack = 2, kModeColSum = 3,
+                kModeWindow = 4 };
+
+struct WalkArgs {
+  Geo G;
+  const int32_t* rows;  // this launch's rows
+  int64_t m;
+  const float* rays;    // [m][nrays][6]
+  int cap_cells;        // window capacity (cells) of this launch
+  // CSR staging (row i writes stage_col/val[i*stride ...], row_len[i])
+  int64_t stride;
+  int32_t* stage_col;
+  float* stage_val;
+  int32_t* row_len;
+  // projections
+  const float* x;  // forward input (voxels)
+  float* y;        // forward output (rows)
+  const float* e;  // back-projection input (rows)
+  float* c;        // back-projection output (voxels)
+  double* s64;     // column sums
+  // window sizes (kModeWindow) and overflow reporting
+  int32_t* win_cells;      // per row window cells
+  int32_t* overflow_rows;  // list of rows whose window exceeded cap_cells
+  int32_t* overflow_count;
+  int32_t* hit_outside;    // count of hits outside the window (must stay 0)
+  int32_t* exact_rows;     // rows left to the per-candidate path
+  int32_t* exact_count;
+};
+
+// Slab metadata in shared memory.
+struct Slab {
+  int off;  // first cell
+  int y0, wy;
+  int z0, wz;
+};
+
+__device__ __forceinline__ int clampi(int v, int lo, int hi) {
+  return v < lo ? lo : (v > hi ? hi : v);
+}
+
+// Block-wide exclusive scan of one int per thread (kWalkThreads threads).
+__device__ __forceinline__ int block_excl_scan(int v, int* warp_tot, int* total) {
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  int inc = warp_incl_scan(v);
+  if (lane == 31) warp_tot[w] = inc;
+  __syncthreads();
+  if (w == 0) {
+    int t = lane < (kWalkThreads / 32) ? warp_tot[lane] : 0;
+    int ti = warp_incl_scan(t);
+    if (lane < (kWalkThreads / 32)) warp_tot[lane] = ti - t;
+    if (lane == (kWalkThreads / 32) - 1) *total = ti;
+  }
+  __syncthreads();
+  int r = warp_tot[w] + inc - v;
+  __syncthreads();
+  return r;
+}
+
+// Window of slab ix: y/z index range covered by the convex hull of the two
+// crystal boxes inside x in [X0, X1], padded by one index each side.
+__device__ void slab_window(const Geo& G, const float (*c0)[3],
+                            const float (*c1)[3], int ix, Slab* out) {
+  const epet_grid& g = G.p.grid;
+  const float X0 = voxel_plane(g, 0, ix), X1 = voxel_plane(g, 0, ix + 1);
+  float ymin = 3.4e38f, ymax = -3.4e38f, zmin = 3.4e38f, zmax = -3.4e38f;
+  bool any = false;
+  auto add = [&](float y, float z) {
+    ymin = fminf(ymin, y); ymax = fmaxf(ymax, y);
+    zmin = fminf(zmin, z); zmax = fmaxf(zmax, z);
+    any = true;
+  };
+  // hull vertices inside the slab
+  for (int k = 0; k < 8; k++) {
+    if (c0[k][0] >= X0 && c0[k][0] <= X1) add(c0[k][1], c0[k][2]);
+    if (c1[k][0] >= X0 && c1[k][0] <= X1) add(c1[k][1], c1[k][2]);
+  }
+  // crossings of the corner-pair segments with the two slab planes
+  for (int a = 0; a < 8; a++) {
+    for (int b = 0; b < 8; b++) {
+      const float dx = c1[b][0] - c0[a][0];
+      if (dx == 0.f) continue;
+      const float dy = c1[b][1] - c0[a][1], dz = c1[b][2] - c0[a][2];
+      const float tA = (X0 - c0[a][0]) / dx, tB = (X1 - c0[a][0]) / dx;
+      if (tA >= 0.f && tA <= 1.f) add(c0[a][1] + tA * dy, c0[a][2] + tA * dz);
+      if (tB >= 0.f && tB <= 1.f) add(c0[a][1] + tB * dy, c0[a][2] + tB * dz);
+    }
+  }
+  if (!any) {
+    out->y0 = out->z0 = 0;
+    out->wy = out->wz = 0;
+    return;
+  }
+  const int ny = g.n[1], nz = g.n[2];
+  int j0 = (int)floorf((ymin - g.o[1]) / g.d[1]) - 1;
+  int j1 = (int)floorf((ymax - g.o[1]) / g.d[1]) + 1;
+  int i0 = (int)floorf((zmin - g.o[2]) / g.d[2]) - 1;
+  int i1 = (int)floorf((zmax - g.o[2]) / g.d[2]) + 1;
+  if (j1 < 0 || j0 > ny - 1 || i1 < 0 || i0 > nz - 1) {
+    out->y0 = out->z0 = 0;
+    out->wy = out->wz = 0;
+    return;
+  }
+  j0 = clampi(j0, 0, ny - 1); j1 = clampi(j1, 0, ny - 1);
+  i0 = clampi(i0, 0, nz - 1); i1 = clampi(i1, 0, nz - 1);
+  out->y0 = j0; out->wy = j1 - j0 + 1;
+  out->z0 = i0; out->wz = i1 - i0 + 1;
+}
+
+// Add `units` to voxel (ix,iy,iz) of the window; flags hits outside it.
+__device__ __forceinline__ void win_add(unsigned long long* win, const Slab* slabs,
+                                        int ix, int iy, int iz,
+                                        unsigned long long units, int* outside) {
+  const Slab s = slabs[ix];
+  const unsigned jy = (unsigned)(iy - s.y0), jz = (unsigned)(iz - s.z0);
+  if (jy < (unsigned)s.wy && jz < (unsigned)s.wz) {
+    atomicAdd(&win[s.off + (int)jy * s.wz + (int)jz], units);
+  } else {
+    atomicAdd(outside, 1);
+  }
+}
+
+__device__ __forceinline__ unsigned long long to_units(float len, float scale) {
+  unsigned long long u = __float2ull_rn(fmul(len, scale));
+  return (u == 0ull && len > 0.f) ? 1ull : u;
+}
+
+// Walk one ray through the grid and add its chord lengths to the window.
+// Parameters along the ray are the reference's quotients
+// (plane - r0)/(r1 - r0) per axis; voxel interval = [max lo, min hi];
+// length = (aMax - aMin)*|r1 - r0| (getSystemMatrixFromWorkqueue.cu:24-69).
+__device__ void walk_ray(const Geo& G, const float* ray, unsigned long long* win,
+                         const Slab* slabs, int* outside, int* needs_exact) {
+  const epet_grid& g = G.p.grid;
+  float r0[3] = {ray[0], ray[1], ray[2]};
+  float dr[3] = {fsub(ray[3], ray[0]), fsub(ray[4], ray[1]), fsub(ray[5], ray[2])};
+  const bool act[3] = {ray[0] != ray[3], ray[1] != ray[4], ray[2] != ray[5]};
+  if (!(act[0] || act[1] || act[2])) return;
+  if (!(act[0] && act[1] && act[2])) {
+    // A ray with equal coordinates on an axis: the reference leaves that
+    // axis out of its slab test, so the chord reaches every candidate along
+    // it, possibly beyond the bundle window.  Such (rare) rows are redone by
+    // the per-candidate path.
+    *needs_exact = 1;
+    return;
+  }
+  const float L = norm3(dr[0], dr[1], dr[2]);
+  auto A = [&](int d, int k) { return fdiv(fsub(voxel_plane(g, d, k), r0[d]), dr[d]); };
+
+  // Grid parameter range over the active axes.
+  float a_in = -3.4e38f, a_out = 3.4e38f;
+  for (int d = 0; d < 3; d++) {
+    if (!act[d]) continue;
+    float p0 = A(d, 0), p1 = A(d, g.n[d]);
+    a_in = fmaxf(a_in, fminf(p0, p1));
+    a_out = fminf(a_out, fmaxf(p0, p1));
+  }
+  if (!(a_in < a_out)) return;
+
+  // Entry cell per active axis: lo <= a_in < hi.
+  int idx[3] = {0, 0, 0}, step[3] = {1, 1, 1};
+  float lo[3] = {-3.4e38f, -3.4e38f, -3.4e38f}, hi[3] = {3.4e38f, 3.4e38f, 3.4e38f};
+  for (int d = 0; d < 3; d++) {
+    if (!act[d]) continue;
+    const int n = g.n[d];
+    step[d] = dr[d] > 0.f ? 1 : -1;
+    // estimate from the position at a_in, then correct with exact parameters
+    float pos = r0[d] + a_in * dr[d];
+    int i = clampi((int)floorf((pos - g.o[d]) / g.d[d]), 0, n - 1);
+    if (step[d] > 0) {  // interval of cell i: [A(i), A(i+1)]
+      while (i > 0 && A(d, i) > a_in) i--;
+      while (i < n - 1 && A(d, i + 1) <= a_in) i++;
+      lo[d] = A(d, i); hi[d] = A(d, i + 1);
+    } else {            // interval of cell i: [A(i+1), A(i)]
+      while (i < n - 1 && A(d, i + 1) > a_in) i++;
+      while (i > 0 && A(d, i) <= a_in) i--;
+      lo[d] = A(d, i + 1); hi[d] = A(d, i);
+    }
+    idx[d] = i;
+  }
+  for (int guard = 0; guard < g.n[0] + g.n[1] + g.n[2] + 3; guard++) {
+    const float amin = fmaxf(fmaxf(lo[0], lo[1]), lo[2]);
+    // exit axis: smallest hi (ties: lowest axis)
+    int mdim = 0;
+    float amax = hi[0];
+    if (hi[1] < amax) { amax = hi[1]; mdim = 1; }
+    if (hi[2] < amax) { amax = hi[2]; mdim = 2; }
+    if (amin < amax) {
+      const float len = fmul(fsub(amax, amin), L);
+      win_add(win, slabs, idx[0], idx[1], idx[2], to_units(len, G.fx_scale), outside);
+    }
+    // advance across the exit plane
+    const int ni = idx[mdim] + step[mdim];
+    if (ni < 0 || ni >= g.n[mdim]) break;
+    idx[mdim] = ni;
+    lo[mdim] = hi[mdim];
+    hi[mdim] = step[mdim] > 0 ? A(mdim, ni + 1) : A(mdim, ni);
+  }
+}
+
+template <int kMode>
+__global__ void __launch_bounds__(kWalkThreads)
+k_walk(WalkArgs args) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  const Geo& G = args.G;
+  const epet_grid& g = G.p.grid;
+  const int nx = g.n[0];
+  Slab* slabs = reinterpret_cast<Slab*>(smem);
+  unsigned long long* win =
+      reinterpret_cast<unsigned long long*>(smem + align256(sizeof(Slab) * nx));
+  __shared__ float c0[8][3], c1[8][3];
+  __shared__ ChannelLine line;
+  __shared__ int warp_tot[kWalkThreads / 32];
+  __shared__ int s_total, s_outside, s_exact;
+  __shared__ double red_d[kWalkThreads / 32];
+  __shared__ float red_f[kWalkThreads / 32];
+
+  const int64_t row = blockIdx.x;
+  if (row >= args.m) return;
+  const int cnl = args.rows[row];
+
+  // ---- channel line, crystal corners
+  if (threadIdx.x == 0) {
+    CrystalMat m0, m1;
+    ChannelLine L;
+    channel_line(G, cnl, &L, nullptr, &m0, &m1);
+    line = L;
+    for (int k = 0; k < 8; k++) {
+      crystal_apply(m0, (float)(k & 1), (float)((k >> 1) & 1), (float)(k >> 2), c0[k]);
+      crystal_apply(m1, (float)(k & 1), (float)((k >> 1) & 1), (float)(k >> 2), c1[k]);
+    }
+    s_outside = 0;
+    s_exact = 0;
+  }
+  __syncthreads();
+
+  // ---- per-slab windows and their offsets
+  int my_cells = 0;
+  const int per = (nx + kWalkThreads - 1) / kWalkThreads;
+  const int sbeg = threadIdx.x * per, send = min(nx, sbeg + per);
+  for (int ix = sbeg; ix < send; ix++) {
+    Slab s;
+    slab_window(G, c0, c1, ix, &s);
+    slabs[ix] = s;
+    my_cells += s.wy * s.wz;
+  }
+  const int excl = block_excl_scan(my_cells, warp_tot, &s_total);
+  {
+    int o = excl;
+    for (int ix = sbeg; ix < send; ix++) {
+      slabs[ix].off = o;
+      o += slabs[ix].wy * slabs[ix].wz;
+    }
+  }
+  __syncthreads();
+  const int W = s_total;
+  if (kMode == kModeWindow) {
+    if (threadIdx.x == 0) args.win_cells[row] = W;
+    return;
+  }
+  if (W > args.cap_cells) {
+    if (threadIdx.x == 0) {
+      int k = atomicAdd(args.overflow_count, 1);
+      args.overflow_rows[k] = (int32_t)row;
+      if (kMode == kModeCsr) args.row_len[row] = -1;
+    }
+    return;
+  }
+
+  // ---- zero the window, walk the rays
+  for (int i = threadIdx.x; i < W; i += kWalkThreads) win[i] = 0ull;
+  __syncthreads();
+  const int R = G.p.nrays;
+  const float* rays = args.rays + row * (int64_t)R * 6;
+  for (int r = threadIdx.x; r < R; r += kWalkThreads) {
+    float ray[6];
+    const float2* rp = reinterpret_cast<const float2*>(rays + 6 * r);
+    float2 a = rp[0], b = rp[1], c = rp[2];
+    ray[0] = a.x; ray[1] = a.y; ray[2] = b.x; ray[3] = b.y; ray[4] = c.x; ray[5] = c.y;
+    walk_ray(G, ray, win, slabs, &s_outside, &s_exact);
+  }
+  __syncthreads();
+  if (threadIdx.x == 0 && s_outside) atomicAdd(args.hit_outside, s_outside);
+  if (s_exact) {  // uniform across the block
+    if (threadIdx.x == 0) {
+      int k = atomicAdd(args.exact_count, 1);
+      args.exact_rows[k] = (int32_t)row;
+      if (kMode == kModeCsr) args.row_len[row] = 0;
+    }
+    return;
+  }
+
+  // ---- ordered extraction: thread t owns cells [t*cpt, (t+1)*cpt)
+  const int cpt = (W + kWalkThreads - 1) / kWalkThreads;
+  const int cbeg = min(W, (int)threadIdx.x * cpt), cend = min(W, cbeg + cpt);
+  // locate the slab of cbeg
+  int ix = 0;
+  {
+    int lo_s = 0, hi_s = nx - 1;
+    while (lo_s < hi_s) {  // last slab with off <= cbeg
+      int mid = (lo_s + hi_s + 1) >> 1;
+      if (slabs[mid].off <= cbeg) lo_s = mid;
+      else hi_s = mid - 1;
+    }
+    ix = lo_s;
+  }
+  const ChannelLine L = line;
+  const float invR = (float)R;
+  // pass 1: count passing non-zero cells
+  int cnt = 0;
+  float fsum = 0.f;
+  {
+    int sx = ix;
+    for (int cidx = cbeg; cidx < cend; cidx++) {
+      while (cidx >= slabs[sx].off + slabs[sx].wy * slabs[sx].wz) sx++;
+      const unsigned long long u = win[cidx];
+      if (u == 0ull) continue;
+      const Slab s = slabs[sx];
+      const int k = cidx - s.off;
+      const int iy = s.y0 + k / s.wz, iz = s.z0 + k % s.wz;
+      if (!is_candidate(G, L, sx, iy, iz)) {
+        win[cidx] = 0ull;  // not a candidate of this channel: drop
+        continue;
+      }
+      const float v = fdiv(fmul(__ull2float_rn(u), G.fx_inv), invR);
+      const int vox = sx * G.nyz + iy * g.n[2] + iz;
+      cnt++;
+      if (kMode == kModeForward) fsum = fadd(fsum, fmul(v, args.x[vox]));
+      if (kMode == kModeBack) {
+        const float ev = args.e[row];
+        if (ev != 0.f) atomicAdd(&args.c[vox], fmul(v, ev));
+      }
+      if (kMode == kModeColSum) atomicAdd(&args.s64[vox], (double)v);
+    }
+  }
+  if (kMode == kModeCsr) {
+    const int pos = block_excl_scan(cnt, warp_tot, &s_total);
+    int64_t o = row * args.stride + pos;
+    int sx = ix;
+    for (int cidx = cbeg; cidx < cend; cidx++) {
+      while (cidx >= slabs[sx].off + slabs[sx].wy * slabs[sx].wz) sx++;
+      const unsigned long long u = win[cidx];
+      if (u == 0ull) continue;
+      const Slab s = slabs[sx];
+      const int k = cidx - s.off;
+      const int iy = s.y0 + k / s.wz, iz = s.z0 + k % s.wz;
+      args.stage_col[o] = sx * G.nyz + iy * g.n[2] + iz;
+      args.stage_val[o] = fdiv(fmul(__ull2float_rn(u), G.fx_inv), invR);
+      o++;
+    }
+    if (threadIdx.x == 0) args.row_len[row] = s_total;
+  } else if (kMode == kModeForward) {
+    // deterministic block reduction in thread order
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    float v = fsum;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v = fadd(v, __shfl_down_sync(0xffffffffu, v, o));
+    if (lane == 0) red_f[w] = v;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      float t = 0.f;
+      for (int k = 0; k < kWalkThreads / 32; k++) t = fadd(t, red_f[k]);
+      args.y[row] = t;
+    }
+  }
+  (void)red_d;
+}
+
+// Gather staged rows into their final CSR positions (warp per row).
+__global__ void k_gather_rows(const int32_t* __restrict__ stage_col,
+                              const float* __restrict__ stage_val, int64_t stride,
+                              const int64_t* __restrict__ row_ptr, int64_t m,
+                              int32_t* __restrict__ col, float* __restrict__ val,
+                              int64_t cap) {
+  const int64_t row = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (row >= m) return;
+  const int64_t b = row_ptr[row], n = row_ptr[row + 1] - b;
+  if (b + n > cap) return;
+  const int32_t* sc = stage_col + row * stride;
+  const float* sv = stage_val + row * stride;
+  for (int64_t k = lane; k < n; k += 32) {
+    col[b + k] = sc[k];
+    val[b + k] = sv[k];
+  }
+}
+
+__global__ void k_len_to_i64(const int32_t* len, int64_t* out, int64_t m) {
+  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < m) out[i] = len[i] < 0 ? 0 : len[i];
+}
+
+__global__ void k_offset_rowptr(int64_t* rp, int64_t n, const int64_t* base) {
+  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) rp[i] += *base;
+}
+
+// ------------------------------------------------------------------ host
+
+static size_t walk_smem(const Geo& G, int cap_cells) {
+  return align256(sizeof(Slab) * G.p.grid.n[0]) + (size_t)cap_cells * 8;
+}
+
+static int g_max_smem = 0;
+static int max_dyn_smem() {
+  if (g_max_smem == 0) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&g_max_smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+    g_max_smem -= 4096;  // static shared memory of the kernel
+  }
+  return g_max_smem;
+}
+
+template <int kMode>
+static epet_status launch_walk(WalkArgs a, size_t smem, cudaStream_t st) {
+  if (a.m == 0) return EPET_OK;
+  EPET_CUDA(cudaFuncSetAttribute(k_walk<kMode>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)smem));
+  k_walk<kMode><<<(unsigned)a.m, kWalkThreads, smem, st>>>(a);
+  EPET_LAUNCHED();
+  return EPET_OK;
+}
+
+// Rows processed per chunk (rays and staging are chunk-sized).
+static int64_t chunk_rows(const Geo& G, int cap_cells) {
+  const int64_t per_row = (int64_t)G.p.nrays * 24 + (int64_t)cap_cells * 8 + 64;
+  int64_t c = ((int64_t)3 << 30) / per_row;  // ~3 GiB of chunk buffers
+  c = std::max<int64_t>(1024, std::min<int64_t>(c, 262144));
+  return c;
+}
+
+// Window capacity for a problem: the largest window over a sample of
+// channels spread over all angles, plus margin.  Rows whose window exceeds it
+// are reported and redone with their exact size.
+static epet_status sample_capacity(const Geo& G, cudaStream_t st, int* cap_out) {
+  const epet_setup& s = G.p.setup;
+  const int64_t nch = (int64_t)s.na * s.n0z * s.n0y * s.n1z * s.n1y;
+  const int64_t per_angle = nch / s.na;
+  std::vector<int32_t> sample;
+  const int pick = 64;
+  for (int a = 0; a < s.na; a++)
+    for (int k = 0; k < pick; k++) {
+      int64_t c = (int64_t)a * per_angle + (per_angle * k) / pick + (k * 7919) % std::max<int64_t>(1, per_angle / pick);
+      sample.push_back((int32_t)std::min<int64_t>(c, nch - 1));
+    }
+  // corner channels (largest obliquity)
+  for (int a = 0; a < s.na; a++) {
+    sample.push_back((int32_t)((int64_t)a * per_angle));
+    sample.push_back((int32_t)((int64_t)a * per_angle + per_angle - 1));
+  }
+  const int64_t n = (int64_t)sample.size();
+  int32_t *d_rows = nullptr, *d_cells = nullptr;
+  EPET_CUDA(cudaMallocAsync((void**)&d_rows, n * 4, st));
+  EPET_CUDA(cudaMallocAsync((void**)&d_cells, n * 4, st));
+  EPET_CUDA(cudaMemcpyAsync(d_rows, sample.data(), n * 4, cudaMemcpyHostToDevice, st));
+  WalkArgs a{};
+  a.G = G;
+  a.rows = d_rows;
+  a.m = n;
+  a.win_cells = d_cells;
+  epet_status rc = launch_walk<kModeWindow>(a, walk_smem(G, 0), st);
+  std::vector<int32_t> cells(n);
+  if (rc == EPET_OK) {
+    cudaError_t e = cudaMemcpyAsync(cells.data(), d_cells, n * 4, cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) rc = cuda_status(e, "window sample");
+  }
+  cudaFreeAsync(d_rows, st);
+  cudaFreeAsync(d_cells, st);
+  if (rc != EPET_OK) return rc;
+  int mx = 0;
+  for (int v : cells) mx = std::max(mx, v);
+  *cap_out = std::max(256, (int)(mx * 1.15) + 64);
+  return EPET_OK;
+}
+
+int auto_row_capacity(const epet_problem& p) {
+  (void)p;
+  return 0;
+}
+
+// Rows redone by the per-candidate path since load (statistics).
+static int64_t n_exact_rows_ = 0;
+int64_t exact_rows_total() { return n_exact_rows_; }
+
+// Generic driver: runs mode kMode over all rows in chunks.  For kModeCsr the
+// rows are staged and gathered into out (capacity cap).
+struct BuildOut {
+  epet_csr* csr = nullptr;
+  int64_t cap = 0;
+  // optional growth of csr->col/val: returns false on failure; must keep the
+  // first `keep` entries and update csr->col/val and cap
+  bool (*grow)(BuildOut* self, int64_t need, int64_t keep, int64_t rows_done,
+               int64_t rows_total) = nullptr;
+  int64_t nnz = 0;
+  const float* x = nullptr;
+  float* y = nullptr;
+  const float* e = nullptr;
+  float* c = nullptr;
+  double* s64 = nullptr;
+};
+
+size_t walk_workspace_size(const Geo& G, int64_t m, int cap_cells, bool csr) {
+  const int64_t ch = std::min<int64_t>(std::max<int64_t>(m, 1), chunk_rows(G, cap_cells));
+  size_t b = align256((size_t)ch * G.p.nrays * 24);         // rays
+  if (csr) {
+    b += 2 * align256((size_t)ch * cap_cells * 4);          // staging col/val
+    b += align256((size_t)ch * 4);                          // row_len
+    b += align256((size_t)(ch + 1) * 8) * 2;                // counts + rowptr chunk
+    b += align256(scan_tmp_elems(ch + 1) * 8);
+  }
+  b += 2 * align256((size_t)ch * 4) + 256;                  // overflow/exact rows + flags
+  return b;
+}
+
+template <int kMode>
+static epet_status run_walk(const Geo& G, const int32_t* rows, int64_t m,
+                            int cap_cells, BuildOut* out, void* ws, size_t ws_bytes,
+                            cudaStream_t st) {
+  const bool csr = kMode == kModeCsr;
+  const int64_t ch = std::min<int64_t>(std::max<int64_t>(m, 1), chunk_rows(G, cap_cells));
+  Scratch scr;
+  EPET_CHECK(scr.init(ws, ws_bytes, walk_workspace_size(G, m, cap_cells, csr), st));
+  float* rays = scr.take<float>((size_t)ch * G.p.nrays * 6);
+  int32_t *stage_col = nullptr, *row_len = nullptr;
+  float* stage_val = nullptr;
+  int64_t *cnt = nullptr, *rp_chunk = nullptr, *scan_tmp = nullptr;
+  if (csr) {
+    stage_col = scr.take<int32_t>((size_t)ch * cap_cells);
+    stage_val = scr.take<float>((size_t)ch * cap_cells);
+    row_len = scr.take<int32_t>(ch);
+    cnt = scr.take<int64_t>(ch + 1);
+    rp_chunk = scr.take<int64_t>(ch + 1);
+    scan_tmp = scr.take<int64_t>(scan_tmp_elems(ch + 1));
+  }
+  int32_t* ovf_rows = scr.take<int32_t>(ch);
+  int32_t* ex_rows = scr.take<int32_t>(ch);
+  int32_t* flags = scr.take<int32_t>(64);  // [0] overflow, [1] hits outside, [2] exact rows
+
+  EPET_CUDA(cudaMemsetAsync(flags, 0, 64 * 4, st));
+  if (csr) EPET_CUDA(cudaMemsetAsync(out->csr->row_ptr, 0, 8, st));
+  int64_t total_nnz = 0;
+  for (int64_t c0 = 0; c0 < m; c0 += ch) {
+    const int64_t mc = std::min(ch, m - c0);
+    EPET_CHECK(launch_rays(G, rows + c0, mc, rays, false, st));
+    WalkArgs a{};
+    a.G = G;
+    a.rows = rows + c0;
+    a.m = mc;
+    a.rays = rays;
+    a.cap_cells = cap_cells;
+    a.stride = cap_cells;
+    a.stage_col = stage_col;
+    a.stage_val = stage_val;
+    a.row_len = row_len;
+    a.x = out->x;
+    a.y = out->y ? out->y + c0 : nullptr;
+    a.e = out->e ? out->e + c0 : nullptr;
+    a.c = out->c;
+    a.s64 = out->s64;
+    a.overflow_rows = ovf_rows;
+    a.overflow_count = flags;
+    a.hit_outside = flags + 1;
+    a.exact_rows = ex_rows;
+    a.exact_count = flags + 2;
+    EPET_CUDA(cudaMemsetAsync(flags, 0, 4, st));
+    EPET_CUDA(cudaMemsetAsync(flags + 2, 0, 4, st));
+    EPET_CHECK(launch_walk<kMode>(a, walk_smem(G, cap_cells), st));
+    int32_t fl[3] = {0, 0, 0};
+    EPET_CUDA(cudaMemcpyAsync(fl, flags, 12, cudaMemcpyDeviceToHost, st));
+    EPET_CUDA(cudaStreamSynchronize(st));
+    if (fl[0] > 0)
+      return set_error(EPET_ERR_OVERFLOW,
+                       "%d rows exceed the per-row window of %d cells; pass a larger "
+                       "max_row_nnz", fl[0], cap_cells);
+    if (fl[2] > 0) {
+      // rows with an axis-parallel ray: per-candidate path
+      EPET_CHECK(exact_rows_apply(G, rows + c0, ex_rows, fl[2], kMode, cap_cells, stage_col,
+                                  stage_val, row_len, a.x, a.y, a.e, a.c, a.s64, st));
+      n_exact_rows_ += fl[2];
+    }
+    if (csr) {
+      const int T = 256;
+      k_len_to_i64<<<ceil_div(mc, T), T, 0, st>>>(row_len, cnt, mc);
+      EPET_LAUNCHED();
+      EPET_CHECK(exclusive_scan_i64(cnt, rp_chunk, mc, scan_tmp, st));
+      // global row pointers: chunk scan + running total
+      int64_t* rp = out->csr->row_ptr + c0;
+      EPET_CUDA(cudaMemcpyAsync(rp + 1, rp_chunk + 1, mc * 8, cudaMemcpyDeviceToDevice, st));
+      k_offset_rowptr<<<ceil_div(mc, T), T, 0, st>>>(rp + 1, mc, rp);
+      EPET_LAUNCHED();
+      int64_t chunk_total = 0;
+      EPET_CUDA(cudaMemcpyAsync(&chunk_total, rp_chunk + mc, 8, cudaMemcpyDeviceToHost, st));
+      EPET_CUDA(cudaStreamSynchronize(st));
+      if (total_nnz + chunk_total > out->cap && out->grow &&
+          !out->grow(out, total_nnz + chunk_total, total_nnz, c0 + mc, m))
+        return set_error(EPET_ERR_CUDA, "could not grow the system-matrix buffers");
+      k_gather_rows<<<ceil_div(mc * 32, T), T, 0, st>>>(stage_col, stage_val, cap_cells, rp, mc,
+                                                         out->csr->col, out->csr->val,
+                                                         out->cap);
+      EPET_LAUNCHED();
+      total_nnz += chunk_total;
+    }
+  }
+  int32_t outside = 0;
+  EPET_CUDA(cudaMemcpyAsync(&outside, flags + 1, 4, cudaMemcpyDeviceToHost, st));
+  EPET_CUDA(cudaStreamSynchronize(st));
+  if (outside)
+    return set_error(EPET_ERR_UNSUPPORTED,
+                     "%d ray-voxel hits fell outside the crystal-hull window (ray "
+                     "endpoints inside the grid are not supported)", outside);
+  out->nnz = total_nnz;
+  return EPET_OK;
+}
+
+static bool grow_device(BuildOut* self, int64_t need, int64_t keep, int64_t rows_done,
+                        int64_t rows_total) {
+  // extrapolate the final size from the rows done so far
+  double est = (double)need * (double)rows_total / (double)std::max<int64_t>(rows_done, 1);
+  int64_t ncap = std::max<int64_t>(need, (int64_t)(est * 1.03) + 1024);
+  int32_t* col = nullptr;
+  float* val = nullptr;
+  if (cudaMalloc((void**)&col, ncap * 4) != cudaSuccess) return false;
+  if (cudaMalloc((void**)&val, ncap * 4) != cudaSuccess) {
+    cudaFree(col);
+    return false;
+  }
+  if (keep > 0) {
+    cudaMemcpy(col, self->csr->col, keep * 4, cudaMemcpyDeviceToDevice);
+    cudaMemcpy(val, self->csr->val, keep * 4, cudaMemcpyDeviceToDevice);
+  }
+  if (self->csr->col) cudaFree(self->csr->col);
+  if (self->csr->val) cudaFree(self->csr->val);
+  self->csr->col = col;
+  self->csr->val = val;
+  self->cap = ncap;
+  return true;
+}
+
+static epet_status resolve_capacity(const Geo& G, int32_t max_row_nnz, cudaStream_t st,
+                                    int* cap) {
+  if (max_row_nnz > 0) {
+    *cap = max_row_nnz;
+  } else {
+    EPET_CHECK(sample_capacity(G, st, cap));
+  }
+  if (walk_smem(G, *cap) > (size_t)max_dyn_smem())
+    return set_error(EPET_ERR_UNSUPPORTED,
+                     "per-row window of %d cells exceeds shared memory", *cap);
+  if (G.p.grid.n[0] > kMaxSlabs)
+    return set_error(EPET_ERR_UNSUPPORTED, "grid nx > %d", kMaxSlabs);
+  return EPET_OK;
+}
+
+}  // namespace epet
+
+using namespace epet;
+
+static epet_status check_rows(const epet_problem* p, const int32_t* rows, int64_t m) {
+  EPET_CHECK(epet_problem_validate(p));
+  if (m < 0 || (m > 0 && !rows)) return set_error(EPET_ERR_INVALID, "bad rows");
+  return EPET_OK;
+}
+
+extern "C" {
+
+size_t epet_sm_build_workspace_size(const epet_problem* p, int64_t m,
+                                    int32_t max_row_nnz) {
+  if (epet_problem_validate(p) != EPET_OK || max_row_nnz <= 0) return 0;
+  return walk_workspace_size(make_geo(*p), m, max_row_nnz, true);
+}
+
+epet_status epet_sm_build(const epet_problem* p, const int32_t* rows_d,
+                          int64_t m, epet_csr* out, int64_t cap,
+                          int64_t* nnz_h, int32_t max_row_nnz, void* ws,
+                          size_t ws_bytes, epet_stream_t stream) {
+  EPET_CHECK(check_rows(p, rows_d, m));
+  if (!out || !out->row_ptr || (cap > 0 && (!out->col || !out->val)) || cap < 0)
+    return set_error(EPET_ERR_INVALID, "bad output CSR");
+  cudaStream_t st = (cudaStream_t)stream;
+  Geo G = make_geo(*p);
+  int capc = 0;
+  EPET_CHECK(resolve_capacity(G, max_row_nnz, st, &capc));
+  if (ws && max_row_nnz <= 0)
+    return set_error(EPET_ERR_INVALID, "a caller workspace needs an explicit max_row_nnz");
+  BuildOut bo;
+  bo.csr = out;
+  bo.cap = cap;
+  epet_status rc = run_walk<kModeCsr>(G, rows_d, m, capc, &bo, ws, ws_bytes, st);
+  if (rc != EPET_OK) return rc;
+  out->m = m;
+  out->n = G.V;
+  out->nnz = bo.nnz;
+  if (nnz_h) *nnz_h = bo.nnz;
+  if (bo.nnz > cap)
+    return set_error(EPET_ERR_CAPACITY, "nnz %lld exceeds capacity %lld",
+                     (long long)bo.nnz, (long long)cap);
+  return EPET_OK;
+}
+
+epet_status epet_project_forward(const epet_problem* p, const int32_t* rows_d,
+                                 int64_t m, const float* x_d, float* y_d,
+                                 int32_t max_row_nnz, void* ws,
+                                 size_t ws_bytes, epet_stream_t stream) {
+  EPET_CHECK(check_rows(p, rows_d, m));
+  if (!x_d || !y_d) return set_error(EPET_ERR_INVALID, "x/y NULL");
+  cudaStream_t st = (cudaStream_t)stream;
+  Geo G = make_geo(*p);
+  int capc = 0;
+  EPET_CHECK(resolve_capacity(G, max_row_nnz, st, &capc));
+  BuildOut bo;
+  bo.x = x_d;
+  bo.y = y_d;
+  return run_walk<kModeForward>(G, rows_d, m, capc, &bo, ws, ws_bytes, st);
+}
+
+epet_status epet_project_back(const epet_problem* p, const int32_t* rows_d,
+                              int64_t m, const float* e_d, float* c_d,
+                              int32_t max_row_nnz, void* ws, size_t ws_bytes,
+                              epet_stream_t stream) {
+  EPET_CHECK(check_rows(p, rows_d, m));
+  if (!e_d || !c_d) return set_error(EPET_ERR_INVALID, "e/c NULL");
+  cudaStream_t st = (cudaStream_t)stream;
+  Geo G = make_geo(*p);
+  int capc = 0;
+  EPET_CHECK(resolve_capacity(G, max_row_nnz, st, &capc));
+  BuildOut bo;
+  bo.e = e_d;
+  bo.c = c_d;
+  return run_walk<kModeBack>(G, rows_d, m, capc, &bo, ws, ws_bytes, st);
+}
+
+}  // extern "C"
+
+namespace epet {
+// CSR build into library-owned buffers (cudaMalloc'd, grown as needed).
+epet_status build_csr_growable(const epet_problem* p, const int32_t* rows, int64_t m,
+                               epet_csr* out, int64_t* cap, int32_t max_row_nnz,
+                               cudaStream_t st) {
+  Geo G = make_geo(*p);
+  int capc = 0;
+  EPET_CHECK(resolve_capacity(G, max_row_nnz, st, &capc));
+  if (!out->row_ptr) EPET_CUDA(cudaMalloc((void**)&out->row_ptr, (m + 1) * 8));
+  BuildOut bo;
+  bo.csr = out;
+  bo.cap = *cap;
+  bo.grow = grow_device;
+  epet_status rc = run_walk<kModeCsr>(G, rows, m, capc, &bo, nullptr, 0, st);
+  *cap = bo.cap;
+  if (rc != EPET_OK) return rc;
+  out->m = m;
+  out->n = G.V;
+  out->nnz = bo.nnz;
+  return EPET_OK;
+}
+
+epet_status column_sums(const epet_problem* p, const int32_t* rows_d, int64_t m,
+                        double* s64, int32_t max_row_nnz, void* ws, size_t ws_bytes,
+                        cudaStream_t st) {
+  Geo G = make_geo(*p);
+  int capc = 0;
+  EPET_CHECK(resolve_capacity(G, max_row_nnz, st, &capc));
+  BuildOut bo;
+  bo.s64 = s64;
+  return run_walk<kModeColSum>(G, rows_d, m, capc, &bo, ws, ws_bytes, st);
+}
+}  // namespace epet

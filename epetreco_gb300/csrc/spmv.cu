@@ -1,0 +1,295 @@
+// spmv.cu -- CSR/CSC matrix-vector products and the MLEM element-wise ops.
+//
+// Replaces cusparseScsrmv (csrmv.hpp:25-36; called at reco.cu:236-249 and
+// backprojection.cu:136-138) and the thrust transforms of mlemOperations.hpp.
+// The products are HBM-bound streams over (value, column) pairs: a group of
+// G lanes owns one row, each lane keeps four independent accumulators so
+// that eight loads per lane are in flight, and the matrix streams are read
+// with evict-first hints so the gathered vector stays cache-resident.  The
+// transpose reads the column-major copy (scatter-free, deterministic).
+// Epilogues fuse the MLEM steps: the forward product writes e = y / (A x)
+// and the Poisson log-likelihood terms; the transpose writes
+// x*c/s (s == 0 -> 1) and the image sum, both reduced in fp64 with a fixed
+// order (deterministic).
+#include <algorithm>
+
+#include "common.cuh"
+#include "internal.h"
+#include "spmv.cuh"
+
+namespace epet {
+
+// Matrix streams are read once per product: streaming (evict-first) loads.
+__device__ __forceinline__ float ld_stream(const float* p) { return __ldcs(p); }
+__device__ __forceinline__ int ld_stream(const int32_t* p) { return __ldcs(p); }
+
+// Dot product of row [beg, end) with x by a group of G lanes.
+template <int G>
+__device__ __forceinline__ float group_dot(const int32_t* __restrict__ idx,
+                                           const float* __restrict__ val,
+                                           const float* __restrict__ x, int64_t beg,
+                                           int64_t end, int lg) {
+  float a0 = 0.f, a1 = 0.f, a2 = 0.f, a3 = 0.f;
+  int64_t k = beg + lg;
+  for (; k + 3 * G < end; k += 4 * G) {
+    const float v0 = ld_stream(val + k), v1 = ld_stream(val + k + G);
+    const float v2 = ld_stream(val + k + 2 * G), v3 = ld_stream(val + k + 3 * G);
+    const int c0 = ld_stream(idx + k), c1 = ld_stream(idx + k + G);
+    const int c2 = ld_stream(idx + k + 2 * G), c3 = ld_stream(idx + k + 3 * G);
+    a0 = fmaf(v0, __ldg(x + c0), a0);
+    a1 = fmaf(v1, __ldg(x + c1), a1);
+    a2 = fmaf(v2, __ldg(x + c2), a2);
+    a3 = fmaf(v3, __ldg(x + c3), a3);
+  }
+  for (; k < end; k += G) a0 = fmaf(ld_stream(val + k), __ldg(x + ld_stream(idx + k)), a0);
+  float a = (a0 + a1) + (a2 + a3);
+#pragma unroll
+  for (int o = G / 2; o > 0; o >>= 1) a += __shfl_xor_sync(0xffffffffu, a, o, G);
+  return a;
+}
+
+// Generic row kernel: out = Epi(row, dot).  Block reduces Epi's fp64 partial
+// (when used) into partial[blockIdx.x].
+template <int G, class Epi>
+__global__ void __launch_bounds__(kSpmvThreads)
+k_rows(const int64_t* __restrict__ ptr, const int32_t* __restrict__ idx,
+       const float* __restrict__ val, const float* __restrict__ x, int64_t nrows, Epi epi,
+       double* __restrict__ partial) {
+  constexpr int RPB = kSpmvThreads / G;
+  __shared__ double red[kSpmvThreads / 32];
+  const int lg = threadIdx.x % G;
+  const int64_t row = (int64_t)blockIdx.x * RPB + threadIdx.x / G;
+  double part = 0.0;
+  if (row < nrows) {
+    const float d = group_dot<G>(idx, val, x, ptr[row], ptr[row + 1], lg);
+    if (lg == 0) part = epi(row, d);
+  }
+  if (partial) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) part += __shfl_xor_sync(0xffffffffu, part, o);
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = part;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      double t = 0.0;
+      for (int w = 0; w < kSpmvThreads / 32; w++) t += red[w];
+      partial[blockIdx.x] = t;
+    }
+  }
+}
+
+// Fixed-order sum of the block partials.
+__global__ void k_sum_partials(const double* __restrict__ p, int64_t n, double* out) {
+  __shared__ double red[32];
+  double s = 0.0;
+  for (int64_t i = threadIdx.x; i < n; i += blockDim.x) s += p[i];
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = s;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t = 0.0;
+    for (int w = 0; w < (int)(blockDim.x / 32); w++) t += red[w];
+    *out = t;
+  }
+}
+
+struct EpiAxpby {  // y = alpha*d + beta*y
+  float alpha, beta;
+  float* y;
+  __device__ double operator()(int64_t r, float d) const {
+    y[r] = beta == 0.f ? alpha * d : alpha * d + beta * y[r];
+    return 0.0;
+  }
+};
+
+int pick_group(double avg_len) {
+  if (avg_len >= 48) return 32;
+  if (avg_len >= 24) return 16;
+  if (avg_len >= 12) return 8;
+  return 4;
+}
+
+template <class Epi>
+epet_status launch_rows(int G, const int64_t* ptr, const int32_t* idx, const float* val,
+                        const float* x, int64_t nrows, Epi epi, double* partial,
+                        cudaStream_t st, int64_t* nblocks_out) {
+  if (nrows <= 0) {
+    if (nblocks_out) *nblocks_out = 0;
+    return EPET_OK;
+  }
+  const int rpb = kSpmvThreads / G;
+  const int64_t nb = (nrows + rpb - 1) / rpb;
+  if (nblocks_out) *nblocks_out = nb;
+  switch (G) {
+    case 32: k_rows<32, Epi><<<(unsigned)nb, kSpmvThreads, 0, st>>>(ptr, idx, val, x, nrows, epi, partial); break;
+    case 16: k_rows<16, Epi><<<(unsigned)nb, kSpmvThreads, 0, st>>>(ptr, idx, val, x, nrows, epi, partial); break;
+    case 8: k_rows<8, Epi><<<(unsigned)nb, kSpmvThreads, 0, st>>>(ptr, idx, val, x, nrows, epi, partial); break;
+    default: k_rows<4, Epi><<<(unsigned)nb, kSpmvThreads, 0, st>>>(ptr, idx, val, x, nrows, epi, partial); break;
+  }
+  EPET_LAUNCHED();
+  return EPET_OK;
+}
+
+template epet_status launch_rows<EpiMlemForward>(int, const int64_t*, const int32_t*,
+                                                 const float*, const float*, int64_t,
+                                                 EpiMlemForward, double*, cudaStream_t,
+                                                 int64_t*);
+template epet_status launch_rows<EpiMlemUpdate>(int, const int64_t*, const int32_t*,
+                                                const float*, const float*, int64_t,
+                                                EpiMlemUpdate, double*, cudaStream_t,
+                                                int64_t*);
+
+epet_status launch_sum_partials(const double* p, int64_t n, double* out, cudaStream_t st) {
+  k_sum_partials<<<1, 1024, 0, st>>>(p, n, out);
+  EPET_LAUNCHED();
+  return EPET_OK;
+}
+
+// Transpose by scatter (no CSC): y[col] += alpha * v * x[row].
+__global__ void k_csr_scatter_t(const int64_t* __restrict__ ptr, const int32_t* __restrict__ col,
+                                const float* __restrict__ val, const float* __restrict__ x,
+                                int64_t m, float alpha, float* __restrict__ y) {
+  const int64_t row = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (row >= m) return;
+  const float xr = alpha * x[row];
+  if (xr == 0.f) return;
+  for (int64_t k = ptr[row] + lane; k < ptr[row + 1]; k += 32)
+    atomicAdd(&y[col[k]], val[k] * xr);
+}
+
+__global__ void k_scale_vec(float* y, int64_t n, float beta) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) y[i] = beta == 0.f ? 0.f : beta * y[i];
+}
+
+// ------------------------------------------------------ element-wise ops
+__global__ void k_divides(float* r, const float* a, const float* b, int64_t n) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) r[i] = fdiv(a[i], b[i]);
+}
+__global__ void k_divides_multiplies(float* r, const float* a, const float* b, const float* c,
+                                     int64_t n) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) {
+    float dvs = c[i];
+    dvs = fadd(dvs, (float)(dvs == 0.f));
+    r[i] = fdiv(fmul(a[i], b[i]), dvs);
+  }
+}
+__global__ void k_scales(float* x, float alpha, int64_t n) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) x[i] = fmul(alpha, x[i]);
+}
+__global__ void k_sum_f64_part(const float* __restrict__ x, int64_t n,
+                               double* __restrict__ partial) {
+  __shared__ double red[8];
+  double s = 0.0;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x)
+    s += (double)x[i];
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = s;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t = 0.0;
+    for (int w = 0; w < (int)(blockDim.x / 32); w++) t += red[w];
+    partial[blockIdx.x] = t;
+  }
+}
+
+// x = xnew * float(1/sum)  (reco.cu:277-281: scales(x, val_t(1./norm)))
+__global__ void k_normalise(const float* __restrict__ xnew, const double* __restrict__ sum,
+                            int64_t n, float* __restrict__ x) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) x[i] = fmul((float)(1.0 / *sum), xnew[i]);
+}
+
+epet_status launch_normalise(const float* xnew, const double* sum, int64_t n, float* x,
+                             cudaStream_t st) {
+  k_normalise<<<ceil_div(n, 256), 256, 0, st>>>(xnew, sum, n, x);
+  EPET_LAUNCHED();
+  return EPET_OK;
+}
+
+epet_status sum_f64(const float* x, int64_t n, double* partial, int nblocks, double* out,
+                    cudaStream_t st) {
+  k_sum_f64_part<<<nblocks, 256, 0, st>>>(x, n, partial);
+  EPET_LAUNCHED();
+  return launch_sum_partials(partial, nblocks, out, st);
+}
+
+}  // namespace epet
+
+using namespace epet;
+
+extern "C" {
+
+epet_status epet_csrmv(int trans, const epet_csr* a, const epet_csc* csc, float alpha,
+                       const float* x_d, float beta, float* y_d, epet_stream_t stream) {
+  if (!a || !x_d || !y_d) return set_error(EPET_ERR_INVALID, "bad arguments");
+  cudaStream_t st = (cudaStream_t)stream;
+  if (!trans) {
+    const int G = pick_group(a->m ? (double)a->nnz / a->m : 0.0);
+    return launch_rows(G, a->row_ptr, a->col, a->val, x_d, a->m, EpiAxpby{alpha, beta, y_d},
+                       nullptr, st, nullptr);
+  }
+  if (csc) {
+    const int G = pick_group(csc->n ? (double)csc->nnz / csc->n : 0.0);
+    return launch_rows(G, csc->col_ptr, csc->row, csc->val, x_d, csc->n,
+                       EpiAxpby{alpha, beta, y_d}, nullptr, st, nullptr);
+  }
+  if (beta != 1.f) {
+    k_scale_vec<<<ceil_div(a->n, 256), 256, 0, st>>>(y_d, a->n, beta);
+    EPET_LAUNCHED();
+  }
+  if (a->m > 0) {
+    k_csr_scatter_t<<<ceil_div(a->m * 32, 256), 256, 0, st>>>(a->row_ptr, a->col, a->val, x_d,
+                                                               a->m, alpha, y_d);
+    EPET_LAUNCHED();
+  }
+  return EPET_OK;
+}
+
+epet_status epet_divides(float* r_d, const float* a_d, const float* b_d, int64_t n,
+                         epet_stream_t stream) {
+  if (n < 0 || (n > 0 && (!r_d || !a_d || !b_d)))
+    return set_error(EPET_ERR_INVALID, "bad arguments");
+  if (n == 0) return EPET_OK;
+  k_divides<<<ceil_div(n, 256), 256, 0, (cudaStream_t)stream>>>(r_d, a_d, b_d, n);
+  EPET_LAUNCHED();
+  return EPET_OK;
+}
+
+epet_status epet_divides_multiplies(float* r_d, const float* a_d, const float* b_d,
+                                    const float* c_d, int64_t n, epet_stream_t stream) {
+  if (n < 0 || (n > 0 && (!r_d || !a_d || !b_d || !c_d)))
+    return set_error(EPET_ERR_INVALID, "bad arguments");
+  if (n == 0) return EPET_OK;
+  k_divides_multiplies<<<ceil_div(n, 256), 256, 0, (cudaStream_t)stream>>>(r_d, a_d, b_d, c_d,
+                                                                            n);
+  EPET_LAUNCHED();
+  return EPET_OK;
+}
+
+epet_status epet_scales(float* x_d, float alpha, int64_t n, epet_stream_t stream) {
+  if (n < 0 || (n > 0 && !x_d)) return set_error(EPET_ERR_INVALID, "bad arguments");
+  if (n == 0) return EPET_OK;
+  k_scales<<<ceil_div(n, 256), 256, 0, (cudaStream_t)stream>>>(x_d, alpha, n);
+  EPET_LAUNCHED();
+  return EPET_OK;
+}
+
+epet_status epet_sum_f64(const float* x_d, int64_t n, double* out_d, epet_stream_t stream) {
+  if (n < 0 || !out_d || (n > 0 && !x_d)) return set_error(EPET_ERR_INVALID, "bad arguments");
+  cudaStream_t st = (cudaStream_t)stream;
+  const int nb = (int)std::max<int64_t>(1, std::min<int64_t>(ceil_div(n, 256), 1024));
+  double* part = nullptr;
+  EPET_CUDA(cudaMallocAsync((void**)&part, nb * 8, st));
+  epet_status rc = sum_f64(x_d, n, part, nb, out_d, st);
+  cudaFreeAsync(part, st);
+  return rc;
+}
+
+}  // extern "C"

@@ -1,0 +1,55 @@
+// spmv.cuh -- fused MLEM epilogues of the row kernels (spmv.cu).
+#pragma once
+#include "common.cuh"
+
+namespace epet {
+
+constexpr int kSpmvThreads = 256;
+
+// Forward projection epilogue: yb = A x (row r), e[r] = y[r] / yb with the
+// reference's divides (mlemOperations.hpp:22-32) but 0 where yb == 0 (the
+// reference would produce inf/NaN there); returns the Poisson log-likelihood
+// term y*log(yb) - yb in fp64.
+struct EpiMlemForward {
+  const float* y;
+  float* e;
+  float* ybar;  // optional
+  __device__ double operator()(int64_t r, float d) const {
+    if (ybar) ybar[r] = d;
+    const float yr = y[r];
+    e[r] = d > 0.f ? __fdiv_rn(yr, d) : 0.f;
+    return d > 0.f ? (double)yr * log((double)d) - (double)d : 0.0;
+  }
+};
+
+// Back-projection epilogue (column v, c = (A^T e)[v]): the reference's
+// dividesMultiplies (mlemOperations.hpp:38-79): xnew = x*c/s with s == 0 -> 1;
+// returns xnew for the image sum.
+struct EpiMlemUpdate {
+  const float* x;
+  const float* s;
+  float* xnew;
+  float* c_out;  // optional
+  __device__ double operator()(int64_t v, float c) const {
+    if (c_out) c_out[v] = c;
+    float dvs = s[v];
+    dvs = __fadd_rn(dvs, (float)(dvs == 0.f));
+    const float xn = __fdiv_rn(__fmul_rn(x[v], c), dvs);
+    xnew[v] = xn;
+    return (double)xn;
+  }
+};
+
+int pick_group(double avg_len);
+
+template <class Epi>
+epet_status launch_rows(int G, const int64_t* ptr, const int32_t* idx, const float* val,
+                        const float* x, int64_t nrows, Epi epi, double* partial,
+                        cudaStream_t st, int64_t* nblocks_out);
+epet_status launch_sum_partials(const double* p, int64_t n, double* out, cudaStream_t st);
+epet_status launch_normalise(const float* xnew, const double* sum, int64_t n, float* x,
+                             cudaStream_t st);
+epet_status sum_f64(const float* x, int64_t n, double* partial, int nblocks, double* out,
+                    cudaStream_t st);
+
+}  // namespace epet

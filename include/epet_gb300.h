@@ -1,0 +1,255 @@
+/* epet_gb300.h -- C ABI of the GB300 (sm_103a) implementation of epetreco's
+ * MLEM hot path.
+ *
+ * The reference has no plugin or FFI layer: its operator surface is a set of
+ * header templates called directly by its drivers (reco.cu, backprojection.cu,
+ * pureSMCalculation.cu) plus three __constant__ symbols.  Each entry point
+ * below names the reference interface it replaces (file:line, relative to
+ * the reference's src/ tree).  include/epet_gb300_shim.hpp re-exposes the
+ * reference's own C++ names on top of this ABI.
+ *
+ * Conventions
+ *  - Every function returns an epet_status and never throws or exits;
+ *    epet_last_error() gives a message for the calling thread.
+ *  - Pointers named *_d are device pointers; the caller owns every buffer.
+ *    Calls are stream-ordered on the given stream (0 = legacy default) and
+ *    do not synchronise unless documented ("synchronous").
+ *  - Functions taking (void* ws, size_t ws_bytes) need device scratch: pass
+ *    a caller buffer of at least the size reported by the matching
+ *    *_workspace_size(), or ws = NULL to let the library allocate it
+ *    stream-ordered (cudaMallocAsync) and free it before returning.
+ *  - Index types: channel and voxel ids int32, element counts and row
+ *    pointers int64 (the reference's int counts overflow at the full 52^3 x
+ *    5.1M-channel size). */
+#ifndef EPET_GB300_H
+#define EPET_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct CUstream_st* epet_stream_t; /* == cudaStream_t */
+
+typedef enum {
+  EPET_OK = 0,
+  EPET_ERR_INVALID = 1,     /* bad argument */
+  EPET_ERR_CAPACITY = 2,    /* output too small; required size reported */
+  EPET_ERR_CUDA = 3,        /* CUDA runtime error */
+  EPET_ERR_UNSUPPORTED = 4, /* geometry/format outside the supported range */
+  EPET_ERR_TIMEOUT = 5,     /* a bounded device wait gave up */
+  EPET_ERR_OVERFLOW = 6     /* a row exceeded the per-row accumulator */
+} epet_status;
+
+/* DefaultMeasurementSetup<float> (MeasurementSetup.hpp:124-164): two planar
+ * heads of n0z x n0y and n1z x n1y crystals of seg{x,y,z} metres, centres at
+ * x = pos0x / pos1x, rotated about y in na steps of da degrees. */
+typedef struct {
+  float pos0x, pos1x;
+  int32_t na, n0z, n0y, n1z, n1y;
+  float da, segx, segy, segz;
+} epet_setup;
+
+/* DefaultVoxelGrid<float> (VoxelGrid.hpp:88-200): origin o, pitch d, count n. */
+typedef struct {
+  float o[3];
+  float d[3];
+  int32_t n[3];
+} epet_grid;
+
+/* Replaces the process-global __constant__ grid_const / setup_const /
+ * nrays_const (device_constant_memory.hpp:14-26) with a value passed to each
+ * call; seed is RANDOM_SEED (1251 in getSystemMatrixFromWorkqueue.cu:22). */
+typedef struct {
+  epet_setup setup;
+  epet_grid grid;
+  int32_t nrays;
+  uint64_t seed;
+} epet_problem;
+
+/* CSR over a measurement list ("ECSR": row i is channel rows[i]).  col holds
+ * voxel ids ascending within each row. */
+typedef struct {
+  int64_t m;        /* rows */
+  int64_t n;        /* columns (voxels) */
+  int64_t nnz;
+  int64_t* row_ptr; /* m+1, device */
+  int32_t* col;     /* nnz, device */
+  float* val;       /* nnz, device */
+} epet_csr;
+
+/* Column-major copy of an epet_csr: col_ptr[n+1], row ids ascending within a
+ * column (used by the scatter-free back-projection). */
+typedef struct {
+  int64_t m, n, nnz;
+  int64_t* col_ptr;
+  int32_t* row;
+  float* val;
+} epet_csc;
+
+/* ------------------------------------------------------------- runtime */
+const char* epet_last_error(void);
+const char* epet_version(void);
+/* Number of kernels this library has launched in the process (CUDA-graph
+ * replays count the kernels they contain); for launch accounting. */
+long long epet_launch_count(void);
+/* Problem checks: index ranges fit int32, nrays >= 1, positive pitches. */
+epet_status epet_problem_validate(const epet_problem* p);
+
+/* ------------------------------------------------------------- geometry */
+/* sin/cos of each angle, interleaved [na][2], computed on the device as the
+ * reference's transform does (MeasurementSetupTrafo2CartCoord.hpp:67-68). */
+epet_status epet_trig_table(const epet_problem* p, float* sc_d,
+                            epet_stream_t stream);
+/* The cuRAND uniforms of each listed channel, out_d[m][nrays][6]
+ * (curand_init(seed, channel, 0) then 6 curand_uniform per ray, as in
+ * getSystemMatrixFromWorkqueue.cu:189-204). */
+epet_status epet_dump_uniforms(const epet_problem* p, const int32_t* rows_d,
+                               int64_t m, float* out_d, epet_stream_t stream);
+/* World-coordinate rays out_d[m][nrays][6] (RandRayGen, RayGenerators.hpp:
+ * 15-40 with the per-channel seeding of getSystemMatrixFromWorkqueue.cu). */
+epet_status epet_rays(const epet_problem* p, const int32_t* rows_d, int64_t m,
+                      float* out_d, epet_stream_t stream);
+
+/* ------------------------------------------------ candidate compaction */
+/* Replaces getWorkqueue (getWorkqueue.hpp:187-223) and the candidate test +
+ * compaction of getSystemMatrix (getSystemMatrixDeviceOnly.cu:25-77,
+ * :304-491): all (channel, voxel) pairs with dist(voxel centre, crystal-
+ * centre line) < sum of half diagonals, list-major and voxel-minor.
+ * row_count_d[m] receives per-row counts; *total_h the sum (synchronous). */
+epet_status epet_workqueue_count(const epet_problem* p, const int32_t* rows_d,
+                                 int64_t m, int64_t* row_count_d,
+                                 int64_t* total_h, epet_stream_t stream);
+/* Fills the pairs given row_off_d[m+1] (exclusive scan of the counts). */
+epet_status epet_workqueue_fill(const epet_problem* p, const int32_t* rows_d,
+                                int64_t m, const int64_t* row_off_d,
+                                int32_t* wq_cnl_d, int32_t* wq_vxl_d,
+                                epet_stream_t stream);
+/* Values for a row-grouped workqueue (CSR pattern over the list): each
+ * element is the mean over nrays of the slab chord length, summed in ray
+ * order in fp32 exactly as getSystemMatrixFromWorkqueue (:96-261), so it is
+ * bit-identical to the reference's per-channel-seeded values. */
+epet_status epet_sm_values(const epet_problem* p, const int32_t* rows_d,
+                           int64_t m, const int64_t* row_ptr_d,
+                           const int32_t* col_d, float* val_d, void* ws,
+                           size_t ws_bytes, epet_stream_t stream);
+size_t epet_sm_values_workspace_size(const epet_problem* p, int64_t m);
+
+/* ------------------------------------------------ system matrix (hot path) */
+/* Replaces systemMatrixCalculation (wrappers.hpp:166-247: getSystemMatrix +
+ * cooSort + coo2csr + csr2ecsr) with one fused build: per channel the rays
+ * are traced through the grid, chord lengths accumulate exactly per voxel,
+ * candidates with a non-zero value are emitted in voxel order straight into
+ * CSR (rows = rows_d, in order).  Stored zeros of the reference are dropped.
+ * out->row_ptr/col/val are caller buffers; cap = capacity of col/val.
+ * Synchronous.  On EPET_ERR_CAPACITY *nnz_h holds the required nnz and
+ * row_ptr is complete.  max_row_nnz: per-row accumulator capacity (0 = auto);
+ * EPET_ERR_OVERFLOW if a row exceeds it. */
+epet_status epet_sm_build(const epet_problem* p, const int32_t* rows_d,
+                          int64_t m, epet_csr* out, int64_t cap,
+                          int64_t* nnz_h, int32_t max_row_nnz, void* ws,
+                          size_t ws_bytes, epet_stream_t stream);
+size_t epet_sm_build_workspace_size(const epet_problem* p, int64_t m,
+                                    int32_t max_row_nnz);
+/* Matrix-free projections (no matrix stored): y_d[m] = A x_d (forward), or
+ * c_d[V] += A^T e_d (back-projection, fp32 atomics).  Same element values as
+ * epet_sm_build. */
+epet_status epet_project_forward(const epet_problem* p, const int32_t* rows_d,
+                                 int64_t m, const float* x_d, float* y_d,
+                                 int32_t max_row_nnz, void* ws,
+                                 size_t ws_bytes, epet_stream_t stream);
+epet_status epet_project_back(const epet_problem* p, const int32_t* rows_d,
+                              int64_t m, const float* e_d, float* c_d,
+                              int32_t max_row_nnz, void* ws, size_t ws_bytes,
+                              epet_stream_t stream);
+/* Sensitivity image (backprojection.cu:113-161 fed an all-ones measurement):
+ * s_d[V] = column sums of A over the listed channels, accumulated in fp64
+ * (s64_d, may be NULL) and normalised to sum 1 in s_d. */
+epet_status epet_sensitivity(const epet_problem* p, const int32_t* rows_d,
+                             int64_t m, float* s_d, double* s64_d,
+                             int32_t max_row_nnz, void* ws, size_t ws_bytes,
+                             epet_stream_t stream);
+
+/* ------------------------------------------------------ sparse formats */
+/* cooSort (cooSort.hpp:53-71): stable in-place sort of COO triples by
+ * (row, col), values follow. */
+epet_status epet_coo_sort(float* val_d, int32_t* row_d, int32_t* col_d,
+                          int64_t n, void* ws, size_t ws_bytes,
+                          epet_stream_t stream);
+size_t epet_coo_sort_workspace_size(int64_t n);
+/* convertCoo2Csr (cusparseWrapper.hpp:38-45): row pointer of row-sorted COO. */
+epet_status epet_coo2csr(const int32_t* row_d, int64_t nnz, int64_t m,
+                         int64_t* csr_d, epet_stream_t stream);
+/* convertCsr2Ecsr (convertCsr2Ecsr.hpp:34-47): ecsr[i] = csr[yRowId[i]],
+ * ecsr[nnzr] = csr[m]; one gather kernel instead of 3 copies per row. */
+epet_status epet_csr2ecsr(int64_t* ecsr_d, const int32_t* yrow_d, int64_t nnzr,
+                          const int64_t* csr_d, int64_t m,
+                          epet_stream_t stream);
+/* Column-major copy (stable: row ids ascending within each column). */
+epet_status epet_csr_to_csc(const epet_csr* a, epet_csc* out, void* ws,
+                            size_t ws_bytes, epet_stream_t stream);
+size_t epet_csr_to_csc_workspace_size(int64_t m, int64_t n, int64_t nnz);
+
+/* ---------------------------------------------------------------- SpMV */
+/* CSRmv<float>::operator() (csrmv.hpp:25-36): y = alpha*op(A)*x + beta*y,
+ * trans = 0 (NON_TRANSPOSE) or 1 (TRANSPOSE).  The transpose reads the CSC
+ * when csc != NULL (scatter-free, deterministic), else scatters with fp32
+ * atomics into y. */
+epet_status epet_csrmv(int trans, const epet_csr* a, const epet_csc* csc,
+                       float alpha, const float* x_d, float beta, float* y_d,
+                       epet_stream_t stream);
+
+/* -------------------------------------------------- MLEM element-wise ops */
+/* divides (mlemOperations.hpp:22-32): r = a / b, no guard (as reference). */
+epet_status epet_divides(float* r_d, const float* a_d, const float* b_d,
+                         int64_t n, epet_stream_t stream);
+/* dividesMultiplies (mlemOperations.hpp:38-79): r = a*b/c, c == 0 -> 1. */
+epet_status epet_divides_multiplies(float* r_d, const float* a_d,
+                                    const float* b_d, const float* c_d,
+                                    int64_t n, epet_stream_t stream);
+/* scales (mlemOperations.hpp:85-124): x *= alpha. */
+epet_status epet_scales(float* x_d, float alpha, int64_t n,
+                        epet_stream_t stream);
+/* sum (mlemOperations.hpp:133-139) in fp64 into a device scalar. */
+epet_status epet_sum_f64(const float* x_d, int64_t n, double* out_d,
+                         epet_stream_t stream);
+
+/* ---------------------------------------------------------- MLEM driver */
+/* One reconstruction (reco.cu:209-281) held on the device: measured rows,
+ * their counts, the system matrix (CSR + CSC), sensitivity and image. */
+typedef struct epet_mlem epet_mlem;
+
+typedef struct {
+  int32_t max_row_nnz; /* 0 = auto */
+  int32_t use_graph;   /* capture one iteration in a CUDA graph */
+  int32_t value_format; /* 0 = fp32 values; 1 = bf16 + row scale; 2 = fp16 + row scale */
+  int32_t reserved;
+} epet_mlem_options;
+
+/* Builds the system matrix for the measured rows (rows_d ascending channel
+ * ids with y_d > 0), keeps y, s (normalised here) and x = ones/V.
+ * Synchronous. */
+epet_status epet_mlem_create(const epet_problem* p, const int32_t* rows_d,
+                             const float* y_d, int64_t m, const float* s_d,
+                             const epet_mlem_options* opt, epet_mlem** out,
+                             epet_stream_t stream);
+epet_status epet_mlem_destroy(epet_mlem* h);
+/* Runs nit iterations: c = A^T (y / A x); x = x*c/s; x /= sum(x).  With
+ * loglik_h != NULL the fp64 Poisson log-likelihood of the last forward
+ * projection is returned (synchronous then). */
+epet_status epet_mlem_iterate(epet_mlem* h, int32_t nit, double* loglik_h,
+                              epet_stream_t stream);
+/* Image access (device pointer valid until destroy), copy-out, statistics. */
+float* epet_mlem_image(epet_mlem* h);
+epet_status epet_mlem_get_image(const epet_mlem* h, float* x_d, epet_stream_t stream);
+epet_status epet_mlem_set_image(epet_mlem* h, const float* x_d,
+                                epet_stream_t stream);
+epet_status epet_mlem_stats(const epet_mlem* h, int64_t* nnz_h,
+                            int64_t* bytes_per_iter_h);
+
+#ifdef __cplusplus
+}
+#endif
+#endif
