@@ -84,6 +84,13 @@ SIGNATURES = {
     "epet_divides_multiplies": [VP, VP, VP, VP, I64, VP],
     "epet_scales": [VP, F, I64, VP],
     "epet_sum_f64": [VP, I64, VP, VP],
+    "epet_coo2csr_i32": [VP, I64, I64, VP, VP],
+    "epet_csr2ecsr_i32": [VP, VP, I64, VP, I64, VP],
+    "epet_csrmv_i32": [C.c_int, I64, I64, I64, F, VP, VP, VP, VP, F, VP, VP],
+    "epet_index_i64_to_i32": [VP, I64, VP, VP],
+    "epet_csr_expand_rows": [VP, I64, VP, VP, VP],
+    "epet_set_constant_geometry": [C.POINTER(Setup), C.POINTER(Grid), I32],
+    "epet_get_constant_geometry": [P],
     "epet_mlem_create": [P, VP, VP, I64, VP, C.POINTER(MlemOptions), C.POINTER(VP), VP],
     "epet_mlem_destroy": [VP],
     "epet_mlem_iterate": [VP, I32, C.POINTER(C.c_double), VP],

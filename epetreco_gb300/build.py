@@ -17,8 +17,9 @@ ROOT = os.path.dirname(PKG)
 CSRC = os.path.join(PKG, "csrc")
 BUILD = os.path.join(PKG, "_build")
 LIB = os.path.join(PKG, "libepet_gb300.so")
+RECO = os.path.join(PKG, "epet_reco")  # C++ driver over the drop-in header
 SOURCES = ["runtime.cu", "geometry.cu", "workqueue.cu", "sm_build.cu", "sort.cu",
-           "spmv.cu", "mlem.cu"]
+           "spmv.cu", "mlem.cu", "compat.cu"]
 HEADERS = ["common.cuh", "internal.h", "spmv.cuh"]
 
 
@@ -27,6 +28,15 @@ def nvcc() -> str:
         if c and os.path.exists(c):
             return c
     raise RuntimeError("nvcc not found")
+
+
+def cuda_libdir() -> str:
+    base = os.path.dirname(os.path.dirname(os.path.realpath(nvcc())))
+    for d in ("lib64", "lib", os.path.join("targets", "sbsa-linux", "lib"),
+              os.path.join("targets", "x86_64-linux", "lib")):
+        if os.path.exists(os.path.join(base, d, "libcudart.so")):
+            return os.path.join(base, d)
+    return os.path.join(base, "lib64")
 
 
 FLAGS = ["-O3", "-std=c++17", "-gencode", "arch=compute_103a,code=sm_103a", "-lineinfo",
@@ -52,14 +62,32 @@ def build(verbose: bool = False) -> str:
     with cf.ThreadPoolExecutor(max_workers=min(8, os.cpu_count() or 4)) as ex:
         objs = list(ex.map(_compile, SOURCES))
     if not os.path.exists(LIB) or os.path.getmtime(LIB) < max(map(os.path.getmtime, objs)):
-        cmd = [nvcc(), "-shared", "-gencode", "arch=compute_103a,code=sm_103a", "-o", LIB] + \
-            objs + ["-lcudart"]
+        # shared CUDA runtime: in a process that already loaded one (torch),
+        # the loader reuses it, so there is a single runtime instance
+        cmd = [nvcc(), "-shared", "-cudart", "shared", "-gencode",
+               "arch=compute_103a,code=sm_103a", "-o", LIB] + objs + \
+            ["-Xlinker", "-rpath=" + cuda_libdir()]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError(f"link failed:\n{r.stderr}")
+    _build_driver()
     if verbose:
         print(LIB)
     return LIB
+
+
+def _build_driver() -> None:
+    src = os.path.join(CSRC, "reco_main.cpp")
+    deps = [src, LIB, os.path.join(ROOT, "include", "epet_gb300_shim.hpp")]
+    if os.path.exists(RECO) and os.path.getmtime(RECO) >= max(map(os.path.getmtime, deps)):
+        return
+    cmd = [nvcc(), "-O2", "-std=c++17", "-x", "cu", "-cudart", "shared", "-gencode",
+           "arch=compute_103a,code=sm_103a", "-I" + os.path.join(ROOT, "include"), src,
+           "-o", RECO, "-L" + PKG, "-lepet_gb300", "-Xlinker", "-rpath=$ORIGIN",
+           "-Xlinker", "-rpath=" + cuda_libdir()]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"driver build failed:\n{r.stderr}")
 
 
 if __name__ == "__main__":

@@ -42,13 +42,20 @@ struct Scratch {
   bool owned = false;
   cudaStream_t stream = 0;
   epet_status init(void* ws, size_t ws_bytes, size_t need, cudaStream_t s);
+  // Carves the next 256-byte-aligned piece; nullptr (and `overrun` set) if
+  // the workspace size computed for the call was too small.
   template <typename T>
   T* take(size_t count) {
     size_t bytes = (count * sizeof(T) + 255) & ~size_t(255);
+    if (used + bytes > size) {
+      overrun = true;
+      return nullptr;
+    }
     char* p = base + used;
     used += bytes;
     return reinterpret_cast<T*>(p);
   }
+  bool overrun = false;
   ~Scratch();
 };
 __host__ __device__ inline size_t align256(size_t b) { return (b + 255) & ~size_t(255); }

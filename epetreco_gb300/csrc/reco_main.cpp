@@ -1,0 +1,238 @@
+// reco_main.cpp -- the reference's MLEM driver flow (reco.cu:32-332) written
+// against the drop-in header include/epet_gb300_shim.hpp, single process,
+// no MPI, raw float32 files instead of HDF5.
+//
+//   epet_reco <measurement.f32> <out> <nrays> <sensitivity.f32> <nIt>
+//             <guess.f32|-> <geometry> [--matrix-once]
+//
+// measurement: dense float[NCHANNELS] (the reference's "messung" dataset);
+// sensitivity, guess, output: float[V] in voxel-id order.  <geometry> is 20
+// comma-separated numbers: pos0x,pos1x,na,n0z,n0y,n1z,n1y,da,segx,segy,segz,
+// ox,oy,oz,dx,dy,dz,nx,ny,nz.  Writes "<it>_<out>" after every iteration as
+// reco.cu does (reco.cu:284-291).
+//
+// Default: the reference's loop -- the system matrix of each row chunk is
+// rebuilt in every iteration (reco.cu:216-254).  --matrix-once: the library's
+// reconstruction object (matrix built once, iteration in a CUDA graph).
+#include <cstdio>
+#include <cstdlib>
+#include <sstream>
+#include <string>
+#include <vector>
+
+#include "../../include/epet_gb300_shim.hpp"
+
+namespace {
+
+// Minimal stand-ins of the reference's geometry value types (same accessors).
+struct Grid {
+  float o[3], d[3];
+  int n[3];
+  float gridox() const { return o[0]; }
+  float gridoy() const { return o[1]; }
+  float gridoz() const { return o[2]; }
+  float griddx() const { return d[0]; }
+  float griddy() const { return d[1]; }
+  float griddz() const { return d[2]; }
+  int gridnx() const { return n[0]; }
+  int gridny() const { return n[1]; }
+  int gridnz() const { return n[2]; }
+};
+struct Setup {
+  float p0, p1, a, sx, sy, sz;
+  int na_, n0z_, n0y_, n1z_, n1y_;
+  float pos0x() const { return p0; }
+  float pos1x() const { return p1; }
+  int na() const { return na_; }
+  float da() const { return a; }
+  int n0z() const { return n0z_; }
+  int n0y() const { return n0y_; }
+  int n1z() const { return n1z_; }
+  int n1y() const { return n1y_; }
+  float segx() const { return sx; }
+  float segy() const { return sy; }
+  float segz() const { return sz; }
+};
+struct RandRayGen {};  // the per-channel-seeded generator of the library
+
+std::vector<float> read_f32(const std::string& fn) {
+  std::vector<float> v;
+  FILE* f = fopen(fn.c_str(), "rb");
+  if (!f) return v;
+  fseek(f, 0, SEEK_END);
+  long n = ftell(f) / 4;
+  fseek(f, 0, SEEK_SET);
+  v.resize(n);
+  if (fread(v.data(), 4, n, f) != (size_t)n) v.clear();
+  fclose(f);
+  return v;
+}
+
+bool write_f32(const std::string& fn, const std::vector<float>& v) {
+  FILE* f = fopen(fn.c_str(), "wb");
+  if (!f) return false;
+  bool ok = fwrite(v.data(), 4, v.size(), f) == v.size();
+  fclose(f);
+  return ok;
+}
+
+#define CK(x) epet_shim::check_cuda((x), #x)
+
+}  // namespace
+
+int main(int argc, char** argv) {
+  if (argc < 8) {
+    fprintf(stderr,
+            "usage: %s measurement out nrays sensitivity nIt guess geometry [--matrix-once]\n",
+            argv[0]);
+    return EXIT_FAILURE;
+  }
+  const std::string fn(argv[1]), on(argv[2]), sfn(argv[4]), xfn(argv[6]);
+  const int nrays = atoi(argv[3]), nIt = atoi(argv[5]);
+  const bool once = argc > 8 && std::string(argv[8]) == "--matrix-once";
+  double g[20];
+  {
+    std::stringstream ss(argv[7]);
+    std::string tok;
+    for (int i = 0; i < 20; i++) {
+      if (!std::getline(ss, tok, ',')) {
+        fprintf(stderr, "geometry needs 20 numbers\n");
+        return EXIT_FAILURE;
+      }
+      g[i] = atof(tok.c_str());
+    }
+  }
+  Setup setup{(float)g[0], (float)g[1], (float)g[7], (float)g[8], (float)g[9], (float)g[10],
+              (int)g[2], (int)g[3], (int)g[4], (int)g[5], (int)g[6]};
+  Grid grid{{(float)g[11], (float)g[12], (float)g[13]},
+            {(float)g[14], (float)g[15], (float)g[16]},
+            {(int)g[17], (int)g[18], (int)g[19]}};
+  const int V = grid.n[0] * grid.n[1] * grid.n[2];
+  const long NCH = (long)setup.na_ * setup.n0z_ * setup.n0y_ * setup.n1z_ * setup.n1y_;
+  try {
+    epetSetConstantGeometry(grid, setup, nrays);
+
+    // measurement -> (row ids ascending, values), zero channels dropped
+    std::vector<float> meas = read_f32(fn);
+    if ((long)meas.size() != NCH) {
+      fprintf(stderr, "measurement must hold %ld floats\n", NCH);
+      return EXIT_FAILURE;
+    }
+    std::vector<int> yRowId;
+    std::vector<float> yVal;
+    for (long i = 0; i < NCH; i++)
+      if (meas[i] != 0.f) {
+        yRowId.push_back((int)i);
+        yVal.push_back(meas[i]);
+      }
+    const int effM = (int)yRowId.size();
+    int* yRowId_devi = nullptr;
+    float* yVal_devi = nullptr;
+    CK(cudaMalloc((void**)&yRowId_devi, sizeof(int) * std::max(effM, 1)));
+    CK(cudaMalloc((void**)&yVal_devi, sizeof(float) * std::max(effM, 1)));
+    CK(cudaMemcpy(yRowId_devi, yRowId.data(), sizeof(int) * effM, cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(yVal_devi, yVal.data(), sizeof(float) * effM, cudaMemcpyHostToDevice));
+
+    // density guess or homogeneous, normalised (reco.cu:113-137)
+    std::vector<float> x_host = read_f32(xfn);
+    const bool xgood = (int)x_host.size() == V;
+    if (!xgood) x_host.assign(V, 1.f);
+    float* x_devi = nullptr;
+    CK(cudaMalloc((void**)&x_devi, sizeof(float) * V));
+    CK(cudaMemcpy(x_devi, x_host.data(), sizeof(float) * V, cudaMemcpyHostToDevice));
+    if (!xgood) {
+      float norm = sum<float>(x_devi, V);
+      scales<float>(x_devi, (float)(1. / norm), V);
+    }
+    // sensitivity, normalised (reco.cu:150-183)
+    std::vector<float> s_host = read_f32(sfn);
+    if ((int)s_host.size() != V) {
+      fprintf(stderr, "sensitivity must hold %d floats\n", V);
+      return EXIT_FAILURE;
+    }
+    float* s_devi = nullptr;
+    CK(cudaMalloc((void**)&s_devi, sizeof(float) * V));
+    CK(cudaMemcpy(s_devi, s_host.data(), sizeof(float) * V, cudaMemcpyHostToDevice));
+    {
+      float norm = sum<float>(s_devi, V);
+      scales<float>(s_devi, (float)(1. / norm), V);
+    }
+
+    if (once) {
+      epet_problem p;
+      epet_shim::check(epet_get_constant_geometry(&p), "geometry");
+      epet_mlem_options o{0, 1, 0, 0};
+      epet_mlem* h = nullptr;
+      epet_shim::check(epet_mlem_create(&p, yRowId_devi, yVal_devi, effM, s_devi, &o, &h, 0),
+                       "epet_mlem_create");
+      if (xgood) epet_shim::check(epet_mlem_set_image(h, x_devi, 0), "set image");
+      for (int it = 0; it < nIt; it++) {
+        double ll = 0;
+        epet_shim::check(epet_mlem_iterate(h, 1, &ll, 0), "iterate");
+        epet_shim::check(epet_mlem_get_image(h, x_devi, 0), "image");
+        CK(cudaMemcpy(x_host.data(), x_devi, sizeof(float) * V, cudaMemcpyDeviceToHost));
+        std::stringstream ss;
+        ss << it;
+        write_f32(ss.str() + "_" + on, x_host);
+        printf("it %d loglik %.9g\n", it, ll);
+      }
+      epet_mlem_destroy(h);
+      return 0;
+    }
+
+    // the reference's loop: chunks of LIMM rows, matrix rebuilt per chunk and
+    // iteration (reco.cu:24-30, :209-254)
+    const unsigned long long LIMNNZ = (512ull * 1024 * 1024) / sizeof(float);
+    const int LIMM = (int)(LIMNNZ / V);
+    float *yt = nullptr, *e = nullptr, *c = nullptr, *xx = nullptr, *val = nullptr;
+    int *cnl = nullptr, *csr = nullptr, *ecsr = nullptr, *vxl = nullptr;
+    unsigned long long* nnz_devi = nullptr;
+    CK(cudaMalloc((void**)&yt, sizeof(float) * LIMM));
+    CK(cudaMalloc((void**)&e, sizeof(float) * LIMM));
+    CK(cudaMalloc((void**)&c, sizeof(float) * V));
+    CK(cudaMalloc((void**)&xx, sizeof(float) * V));
+    CK(cudaMalloc((void**)&cnl, sizeof(int) * (size_t)LIMM * V));
+    CK(cudaMalloc((void**)&csr, sizeof(int) * (NCH + 1)));
+    CK(cudaMalloc((void**)&ecsr, sizeof(int) * (LIMM + 1)));
+    CK(cudaMalloc((void**)&vxl, sizeof(int) * (size_t)LIMM * V));
+    CK(cudaMalloc((void**)&val, sizeof(float) * (size_t)LIMM * V));
+    CK(cudaMalloc((void**)&nnz_devi, sizeof(unsigned long long)));
+    cusparseHandle_t handle = nullptr;
+    cusparseMatDescr_t A = nullptr;
+    float zero = 0.f, one = 1.f;
+    const unsigned NChunks =
+        nChunks<unsigned, unsigned long long>((unsigned long long)effM * V,
+                                              (unsigned long long)LIMM * V);
+    for (int it = 0; it < nIt; it++) {
+      CK(cudaMemset(c, 0, sizeof(float) * V));
+      for (unsigned chunkId = 0; chunkId < NChunks; chunkId++) {
+        unsigned m = nInChunk<unsigned, unsigned>(chunkId, effM, LIMM);
+        unsigned ptr = chunkPtr<unsigned, unsigned>(chunkId, LIMM);
+        unsigned long long nnz_host = 0;
+        CK(cudaMemcpy(nnz_devi, &nnz_host, sizeof(nnz_host), cudaMemcpyHostToDevice));
+        const unsigned* mp = &m;
+        systemMatrixCalculation<float, unsigned, int, unsigned long long, RandRayGen>(
+            ecsr, vxl, val, nnz_devi, cnl, csr, &yRowId_devi[ptr], mp, handle);
+        CK(cudaMemcpy(&nnz_host, nnz_devi, sizeof(nnz_host), cudaMemcpyDeviceToHost));
+        CSRmv<float>()(handle, CUSPARSE_OPERATION_NON_TRANSPOSE, m, V, (int)nnz_host, &one, A,
+                       val, ecsr, vxl, x_devi, &zero, yt);
+        float* yv = &yVal_devi[ptr];
+        divides<float>(e, yv, yt, m);
+        CSRmv<float>()(handle, CUSPARSE_OPERATION_TRANSPOSE, m, V, (int)nnz_host, &one, A, val,
+                       ecsr, vxl, e, &one, c);
+      }
+      dividesMultiplies<float>(xx, x_devi, c, s_devi, V);
+      CK(cudaMemcpy(x_devi, xx, sizeof(float) * V, cudaMemcpyDeviceToDevice));
+      float norm = sum<float>(x_devi, V);
+      scales<float>(x_devi, (float)(1. / norm), V);
+      CK(cudaMemcpy(x_host.data(), x_devi, sizeof(float) * V, cudaMemcpyDeviceToHost));
+      std::stringstream ss;
+      ss << it;
+      write_f32(ss.str() + "_" + on, x_host);
+      printf("it %d norm %.9g\n", it, (double)sum<float>(x_devi, V));
+    }
+    return 0;
+  } catch (cudaException&) {
+    return EXIT_FAILURE;
+  }
+}

@@ -577,6 +577,7 @@ static epet_status run_walk(const Geo& G, const int32_t* rows, int64_t m,
   int32_t* ovf_rows = scr.take<int32_t>(ch);
   int32_t* ex_rows = scr.take<int32_t>(ch);
   int32_t* flags = scr.take<int32_t>(64);  // [0] overflow, [1] hits outside, [2] exact rows
+  if (scr.overrun) return set_error(EPET_ERR_INVALID, "internal: workspace size");
 
   EPET_CUDA(cudaMemsetAsync(flags, 0, 64 * 4, st));
   if (csr) EPET_CUDA(cudaMemsetAsync(out->csr->row_ptr, 0, 8, st));

@@ -342,8 +342,8 @@ extern "C" {
 
 size_t epet_coo_sort_workspace_size(int64_t n) {
   const size_t hist = radix_hist_elems(n);
-  return 2 * align256(n * 8) + 2 * align256(n * 4) + 2 * align256(hist * 8) +
-         align256(scan_tmp_elems(hist) * 8) + 256;
+  return 2 * align256(n * 8) + 2 * align256(n * 4) + align256(hist * 8) +
+         align256((hist + 1) * 8) + align256(scan_tmp_elems(hist) * 8) + 256;
 }
 
 epet_status epet_coo_sort(float* val_d, int32_t* row_d, int32_t* col_d, int64_t n,
@@ -363,6 +363,7 @@ epet_status epet_coo_sort(float* val_d, int32_t* row_d, int32_t* col_d, int64_t 
   int64_t* hist_scan = scr.take<int64_t>(hn + 1);
   int64_t* tmp = scr.take<int64_t>(scan_tmp_elems(hn));
   int* mx = scr.take<int>(4);
+  if (scr.overrun) return set_error(EPET_ERR_INVALID, "internal: workspace size");
   // index ranges (ids must be non-negative)
   int h_mx[2] = {0, 0}, h_mn[2] = {0, 0};
   EPET_CUDA(cudaMemsetAsync(mx, 0, 16, st));
@@ -410,8 +411,8 @@ size_t epet_csr_to_csc_workspace_size(int64_t m, int64_t n, int64_t nnz) {
   (void)m;
   (void)n;
   const size_t hist = radix_hist_elems(nnz);
-  return 2 * align256(nnz * 4) + 2 * align256(nnz * 8) + 2 * align256(hist * 8) +
-         align256(scan_tmp_elems(hist) * 8) + 256;
+  return 2 * align256(nnz * 4) + 2 * align256(nnz * 8) + align256(hist * 8) +
+         align256((hist + 1) * 8) + align256(scan_tmp_elems(hist) * 8) + 256;
 }
 
 epet_status epet_csr_to_csc(const epet_csr* a, epet_csc* out, void* ws, size_t ws_bytes,
@@ -437,6 +438,7 @@ epet_status epet_csr_to_csc(const epet_csr* a, epet_csc* out, void* ws, size_t w
   int64_t* hist = scr.take<int64_t>(hn);
   int64_t* hist_scan = scr.take<int64_t>(hn + 1);
   int64_t* tmp = scr.take<int64_t>(scan_tmp_elems(hn));
+  if (scr.overrun) return set_error(EPET_ERR_INVALID, "internal: workspace size");
   const int T = 256;
   k_csr_to_pairs<<<ceil_div(a->m * 32, T), T, 0, st>>>(a->row_ptr, a->m, a->col, a->val, key,
                                                         pv);

@@ -395,6 +395,7 @@ epet_status epet_sm_values(const epet_problem* p, const int32_t* rows_d,
   EPET_CHECK(scr.init(ws, ws_bytes, epet_sm_values_workspace_size(p, m), st));
   const int64_t ch = std::min<int64_t>(std::max<int64_t>(m, 1), 65536);
   float* rays = scr.take<float>((size_t)ch * p->nrays * 6);
+  if (scr.overrun) return set_error(EPET_ERR_INVALID, "internal: workspace size");
   for (int64_t c0 = 0; c0 < m; c0 += ch) {
     const int64_t mc = std::min(ch, m - c0);
     EPET_CHECK(launch_rays(G, rows_d + c0, mc, rays, false, st));

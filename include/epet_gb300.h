@@ -216,6 +216,35 @@ epet_status epet_scales(float* x_d, float alpha, int64_t n,
 epet_status epet_sum_f64(const float* x_d, int64_t n, double* out_d,
                          epet_stream_t stream);
 
+/* ------------------------------------------- int32-index compatibility */
+/* For callers holding the reference's int row pointers (mallocD_SystemMatrix,
+ * wrappers.hpp:64-74).  Same semantics as the int64 forms above. */
+epet_status epet_coo2csr_i32(const int32_t* row_d, int64_t nnz, int64_t m,
+                             int32_t* csr_d, epet_stream_t stream);
+epet_status epet_csr2ecsr_i32(int32_t* ecsr_d, const int32_t* yrow_d,
+                              int64_t nnzr, const int32_t* csr_d, int64_t m,
+                              epet_stream_t stream);
+/* CSRmv<float>::operator() with the reference's argument list (csrmv.hpp:
+ * 25-36): int32 row pointer; the transpose scatters with fp32 atomics. */
+epet_status epet_csrmv_i32(int trans, int64_t m, int64_t n, int64_t nnz,
+                           float alpha, const float* val_d,
+                           const int32_t* row_ptr_d, const int32_t* col_d,
+                           const float* x_d, float beta, float* y_d,
+                           epet_stream_t stream);
+epet_status epet_index_i64_to_i32(const int64_t* a_d, int64_t n, int32_t* b_d,
+                                  epet_stream_t stream);
+/* out_d[k] = rows_d[i] for every entry k of row i (the COO row ids that
+ * systemMatrixCalculation leaves in aCnlId_devi, wrappers.hpp:172-247). */
+epet_status epet_csr_expand_rows(const int64_t* row_ptr_d, int64_t m,
+                                 const int32_t* rows_d, int32_t* out_d,
+                                 epet_stream_t stream);
+/* Process-wide geometry for drivers written against the reference's
+ * __constant__ grid_const/setup_const/nrays_const (device_constant_memory.hpp:
+ * 14-26, set with cudaMemcpyToSymbol in reco.cu:64-72); seed 1251. */
+epet_status epet_set_constant_geometry(const epet_setup* setup,
+                                       const epet_grid* grid, int32_t nrays);
+epet_status epet_get_constant_geometry(epet_problem* out);
+
 /* ---------------------------------------------------------- MLEM driver */
 /* One reconstruction (reco.cu:209-281) held on the device: measured rows,
  * their counts, the system matrix (CSR + CSC), sensitivity and image. */
