@@ -66,6 +66,10 @@ struct WalkArgs {
   int32_t* hit_outside;    // count of hits outside the window (must stay 0)
   int32_t* exact_rows;     // rows left to the per-candidate path
   int32_t* exact_count;
+  // redo launch over rows whose window exceeded the first launch's capacity:
+  // block b handles chunk row sel[b] and stages at b*stride; ovf_idx[row] = b
+  const int32_t* sel;
+  int32_t* ovf_idx;
 };
 
 // Slab metadata in shared memory.
@@ -255,8 +259,9 @@ k_walk(WalkArgs args) {
   __shared__ double red_d[kWalkThreads / 32];
   __shared__ float red_f[kWalkThreads / 32];
 
-  const int64_t row = blockIdx.x;
-  if (row >= args.m) return;
+  if ((int64_t)blockIdx.x >= args.m) return;
+  const int64_t row = args.sel ? (int64_t)args.sel[blockIdx.x] : (int64_t)blockIdx.x;
+  const int64_t slot = blockIdx.x;  // staging slot
   const int cnl = args.rows[row];
 
   // ---- channel line, crystal corners
@@ -375,7 +380,7 @@ k_walk(WalkArgs args) {
   }
   if (kMode == kModeCsr) {
     const int pos = block_excl_scan(cnt, warp_tot, &s_total);
-    int64_t o = row * args.stride + pos;
+    int64_t o = slot * args.stride + pos;
     int sx = ix;
     for (int cidx = cbeg; cidx < cend; cidx++) {
       while (cidx >= slabs[sx].off + slabs[sx].wy * slabs[sx].wz) sx++;
@@ -388,7 +393,10 @@ k_walk(WalkArgs args) {
       args.stage_val[o] = fdiv(fmul(__ull2float_rn(u), G.fx_inv), invR);
       o++;
     }
-    if (threadIdx.x == 0) args.row_len[row] = s_total;
+    if (threadIdx.x == 0) {
+      args.row_len[row] = s_total;
+      if (args.sel) args.ovf_idx[row] = (int32_t)slot;
+    }
   } else if (kMode == kModeForward) {
     // deterministic block reduction in thread order
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
@@ -407,8 +415,13 @@ k_walk(WalkArgs args) {
 }
 
 // Gather staged rows into their final CSR positions (warp per row).
+// Rows redone with a larger window (ovf_idx[row] >= 0) come from the second
+// staging area.
 __global__ void k_gather_rows(const int32_t* __restrict__ stage_col,
                               const float* __restrict__ stage_val, int64_t stride,
+                              const int32_t* __restrict__ ovf_idx,
+                              const int32_t* __restrict__ stage2_col,
+                              const float* __restrict__ stage2_val, int64_t stride2,
                               const int64_t* __restrict__ row_ptr, int64_t m,
                               int32_t* __restrict__ col, float* __restrict__ val,
                               int64_t cap) {
@@ -417,13 +430,17 @@ __global__ void k_gather_rows(const int32_t* __restrict__ stage_col,
   if (row >= m) return;
   const int64_t b = row_ptr[row], n = row_ptr[row + 1] - b;
   if (b + n > cap) return;
-  const int32_t* sc = stage_col + row * stride;
-  const float* sv = stage_val + row * stride;
+  const int32_t oi = ovf_idx ? ovf_idx[row] : -1;
+  const int32_t* sc = oi >= 0 ? stage2_col + oi * stride2 : stage_col + row * stride;
+  const float* sv = oi >= 0 ? stage2_val + oi * stride2 : stage_val + row * stride;
   for (int64_t k = lane; k < n; k += 32) {
     col[b + k] = sc[k];
     val[b + k] = sv[k];
   }
 }
+
+__global__ void k_gather_i32(const int32_t* src, const int32_t* idx, int64_t n,
+                             int32_t* dst);
 
 __global__ void k_len_to_i64(const int32_t* len, int64_t* out, int64_t m) {
   int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -484,11 +501,14 @@ static epet_status sample_capacity(const Geo& G, cudaStream_t st, int* cap_out) 
       int64_t c = (int64_t)a * per_angle + (per_angle * k) / pick + (k * 7919) % std::max<int64_t>(1, per_angle / pick);
       sample.push_back((int32_t)std::min<int64_t>(c, nch - 1));
     }
-  // corner channels (largest obliquity)
-  for (int a = 0; a < s.na; a++) {
-    sample.push_back((int32_t)((int64_t)a * per_angle));
-    sample.push_back((int32_t)((int64_t)a * per_angle + per_angle - 1));
-  }
+  // the most oblique crystal pairs: every index at an end of its range
+  for (int a = 0; a < s.na; a++)
+    for (int k = 0; k < 16; k++) {
+      const int i0z = (k & 1) ? s.n0z - 1 : 0, i0y = (k & 2) ? s.n0y - 1 : 0;
+      const int i1z = (k & 4) ? s.n1z - 1 : 0, i1y = (k & 8) ? s.n1y - 1 : 0;
+      const int64_t c = (((((int64_t)a * s.n0z + i0z) * s.n0y + i0y) * s.n1z + i1z) * s.n1y) + i1y;
+      sample.push_back((int32_t)c);
+    }
   const int64_t n = (int64_t)sample.size();
   int32_t *d_rows = nullptr, *d_cells = nullptr;
   EPET_CUDA(cudaMallocAsync((void**)&d_rows, n * 4, st));
@@ -520,8 +540,9 @@ int auto_row_capacity(const epet_problem& p) {
   return 0;
 }
 
-// Rows redone by the per-candidate path since load (statistics).
+// Rows redone by the per-candidate path / with a larger window since load.
 static int64_t n_exact_rows_ = 0;
+static int64_t n_overflow_rows_ = 0;
 int64_t exact_rows_total() { return n_exact_rows_; }
 
 // Generic driver: runs mode kMode over all rows in chunks.  For kModeCsr the
@@ -550,8 +571,57 @@ size_t walk_workspace_size(const Geo& G, int64_t m, int cap_cells, bool csr) {
     b += align256((size_t)(ch + 1) * 8) * 2;                // counts + rowptr chunk
     b += align256(scan_tmp_elems(ch + 1) * 8);
   }
-  b += 2 * align256((size_t)ch * 4) + 256;                  // overflow/exact rows + flags
+  b += 3 * align256((size_t)ch * 4) + 256;                  // overflow/exact rows, ovf_idx, flags
   return b;
+}
+
+// Second launch over the rows listed in ovf_rows (chunk-local indices): their
+// window sizes are measured, the walk reruns with exactly that capacity; CSR
+// rows stage into a separate area (stride *cap2) indexed through ovf_idx.
+template <int kMode>
+static epet_status redo_overflow(WalkArgs a, const int32_t* ovf_rows, int n, int* cap2,
+                                 int32_t** s2c, float** s2v, int32_t* ovf_idx,
+                                 cudaStream_t st) {
+  int32_t *sel = nullptr, *cnl = nullptr, *cells = nullptr;
+  EPET_CUDA(cudaMallocAsync((void**)&sel, n * 4, st));
+  EPET_CUDA(cudaMallocAsync((void**)&cnl, n * 4, st));
+  EPET_CUDA(cudaMallocAsync((void**)&cells, n * 4, st));
+  EPET_CUDA(cudaMemcpyAsync(sel, ovf_rows, n * 4, cudaMemcpyDeviceToDevice, st));
+  k_gather_i32<<<ceil_div(n, 256), 256, 0, st>>>(a.rows, sel, n, cnl);
+  EPET_LAUNCHED();
+  WalkArgs w{};
+  w.G = a.G;
+  w.rows = cnl;
+  w.m = n;
+  w.win_cells = cells;
+  EPET_CHECK(launch_walk<kModeWindow>(w, walk_smem(a.G, 0), st));
+  std::vector<int32_t> h(n);
+  EPET_CUDA(cudaMemcpyAsync(h.data(), cells, n * 4, cudaMemcpyDeviceToHost, st));
+  EPET_CUDA(cudaStreamSynchronize(st));
+  int mx = 0;
+  for (int v : h) mx = std::max(mx, v);
+  *cap2 = std::max(mx, 1);
+  if (walk_smem(a.G, *cap2) > (size_t)max_dyn_smem())
+    return set_error(EPET_ERR_UNSUPPORTED, "per-row window of %d cells exceeds shared memory",
+                     *cap2);
+  WalkArgs b = a;
+  b.sel = sel;
+  b.m = n;
+  b.cap_cells = *cap2;
+  b.stride = *cap2;
+  b.ovf_idx = ovf_idx;
+  if (kMode == kModeCsr) {
+    EPET_CUDA(cudaMallocAsync((void**)s2c, (size_t)n * *cap2 * 4, st));
+    EPET_CUDA(cudaMallocAsync((void**)s2v, (size_t)n * *cap2 * 4, st));
+    b.stage_col = *s2c;
+    b.stage_val = *s2v;
+  }
+  EPET_CUDA(cudaMemsetAsync(a.overflow_count, 0, 4, st));
+  EPET_CHECK(launch_walk<kMode>(b, walk_smem(a.G, *cap2), st));
+  cudaFreeAsync(sel, st);
+  cudaFreeAsync(cnl, st);
+  cudaFreeAsync(cells, st);
+  return EPET_OK;
 }
 
 template <int kMode>
@@ -576,6 +646,7 @@ static epet_status run_walk(const Geo& G, const int32_t* rows, int64_t m,
   }
   int32_t* ovf_rows = scr.take<int32_t>(ch);
   int32_t* ex_rows = scr.take<int32_t>(ch);
+  int32_t* ovf_idx = scr.take<int32_t>(ch);
   int32_t* flags = scr.take<int32_t>(64);  // [0] overflow, [1] hits outside, [2] exact rows
   if (scr.overrun) return set_error(EPET_ERR_INVALID, "internal: workspace size");
 
@@ -611,10 +682,16 @@ static epet_status run_walk(const Geo& G, const int32_t* rows, int64_t m,
     int32_t fl[3] = {0, 0, 0};
     EPET_CUDA(cudaMemcpyAsync(fl, flags, 12, cudaMemcpyDeviceToHost, st));
     EPET_CUDA(cudaStreamSynchronize(st));
-    if (fl[0] > 0)
-      return set_error(EPET_ERR_OVERFLOW,
-                       "%d rows exceed the per-row window of %d cells; pass a larger "
-                       "max_row_nnz", fl[0], cap_cells);
+    // rows whose window exceeded the capacity: redo them with their exact size
+    int32_t* stage2_col = nullptr;
+    float* stage2_val = nullptr;
+    int cap2 = 0;
+    if (csr) EPET_CUDA(cudaMemsetAsync(ovf_idx, 0xff, mc * 4, st));
+    if (fl[0] > 0) {
+      EPET_CHECK(redo_overflow<kMode>(a, ovf_rows, fl[0], &cap2, &stage2_col, &stage2_val, ovf_idx,
+                                      st));
+      n_overflow_rows_ += fl[0];
+    }
     if (fl[2] > 0) {
       // rows with an axis-parallel ray: per-candidate path
       EPET_CHECK(exact_rows_apply(G, rows + c0, ex_rows, fl[2], kMode, cap_cells, stage_col,
@@ -637,11 +714,15 @@ static epet_status run_walk(const Geo& G, const int32_t* rows, int64_t m,
       if (total_nnz + chunk_total > out->cap && out->grow &&
           !out->grow(out, total_nnz + chunk_total, total_nnz, c0 + mc, m))
         return set_error(EPET_ERR_CUDA, "could not grow the system-matrix buffers");
-      k_gather_rows<<<ceil_div(mc * 32, T), T, 0, st>>>(stage_col, stage_val, cap_cells, rp, mc,
-                                                         out->csr->col, out->csr->val,
-                                                         out->cap);
+      k_gather_rows<<<ceil_div(mc * 32, T), T, 0, st>>>(
+          stage_col, stage_val, cap_cells, ovf_idx, stage2_col, stage2_val, cap2, rp, mc,
+          out->csr->col, out->csr->val, out->cap);
       EPET_LAUNCHED();
       total_nnz += chunk_total;
+    }
+    if (stage2_col) {
+      cudaFreeAsync(stage2_col, st);
+      cudaFreeAsync(stage2_val, st);
     }
   }
   int32_t outside = 0;

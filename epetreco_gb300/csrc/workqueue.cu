@@ -228,7 +228,7 @@ __global__ void k_apply_exact(int64_t n_ex, const int32_t* __restrict__ ex_rows,
 }
 
 __global__ void k_gather_i32(const int32_t* src, const int32_t* idx, int64_t n,
-                             int32_t* dst) {
+                             int32_t* dst) {  // dst[i] = src[idx[i]]
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i < n) dst[i] = src[idx[i]];
 }
