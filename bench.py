@@ -43,9 +43,11 @@ def parse():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--config", default="full", choices=["full", "small"])
-    ap.add_argument("--cpu-sample", type=int, default=48,
+    ap.add_argument("--cpu-sample", type=int, default=4096,
                     help="channels in the CPU-baseline sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--profile", action="store_true",
+                    help="one reconstruction with one iteration, nothing else (for ncu)")
     return ap.parse_args()
 
 
@@ -149,8 +151,8 @@ def reference_arm(args):
     if rank != 0:
         return
     per = []
-    for _ in range(args.warmup if args.warmup < 1 else 1):
-        cpu_baseline(args.config, max(4, args.cpu_sample // 4), seed=99)
+    if args.warmup > 0:
+        cpu_baseline(args.config, max(4, args.cpu_sample // 16), seed=99)
     info = None
     for k in range(args.steps):
         info = cpu_baseline(args.config, args.cpu_sample, seed=k)
@@ -211,6 +213,14 @@ def gb300_arm(args):
         if dist is not None:
             dist.barrier()
         torch.cuda.synchronize()
+
+    if args.profile:
+        R = api.Mlem(p, rows, y, s, use_graph=False)
+        R.iterate(1)
+        torch.cuda.synchronize()
+        print(json.dumps({"profile": True, "nnz": R.stats()["nnz"]}))
+        R.close()
+        return
 
     for _ in range(args.warmup):
         R = step(rows, y, s)

@@ -190,6 +190,35 @@ __device__ __forceinline__ float candidate_threshold(float nab, float sr) {
   return __uint_as_float(hi);  // first failing value
 }
 
+// The same threshold found by one warp: each round the 32 lanes test 32
+// points of [lo, hi] and keep the sub-interval where the outcome changes.
+// Must be called by all 32 lanes of a warp.
+__device__ __forceinline__ float candidate_threshold_warp(float nab, float sr) {
+  const int lane = threadIdx.x & 31;
+  auto pass = [&](uint32_t bits) {
+    return fdiv(fsqrt(__uint_as_float(bits)), nab) < sr;
+  };
+  if (!pass(0u)) return 0.0f;
+  uint32_t lo = 0u, hi = 0x7f800000u;  // pass(lo), !pass(hi)
+  while (hi - lo > 1u) {
+    const uint32_t span = hi - lo;
+    // lane l tests lo + ceil(span*(l+1)/33); strictly inside (lo, hi]
+    uint32_t pt = lo + (uint32_t)(((uint64_t)span * (uint32_t)(lane + 1) + 32u) / 33u);
+    if (pt <= lo) pt = lo + 1u;
+    if (pt > hi) pt = hi;
+    const unsigned okm = __ballot_sync(0xffffffffu, pt < hi && pass(pt));
+    // points are increasing in the lane index and pass() is monotone:
+    // the passing lanes form a prefix
+    const int npass = __popc(okm);
+    const uint32_t new_lo = npass ? __shfl_sync(0xffffffffu, pt, npass - 1) : lo;
+    uint32_t new_hi = npass < 32 ? __shfl_sync(0xffffffffu, pt, npass < 32 ? npass : 31) : hi;
+    if (new_hi > hi) new_hi = hi;
+    lo = new_lo;
+    hi = new_hi;
+  }
+  return __uint_as_float(hi);
+}
+
 __device__ __forceinline__ void channel_line(const Geo& G, int cnl,
                                              ChannelLine* L, int* ida_out,
                                              CrystalMat* m0, CrystalMat* m1) {

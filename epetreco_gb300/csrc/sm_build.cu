@@ -29,6 +29,7 @@
 #include <curand_kernel.h>
 
 #include <algorithm>
+#include <climits>
 #include <vector>
 
 #include "common.cuh"
@@ -101,64 +102,69 @@ __device__ __forceinline__ int block_excl_scan(int v, int* warp_tot, int* total)
   return r;
 }
 
-// Window of slab ix: y/z index range covered by the convex hull of the two
-// crystal boxes inside x in [X0, X1], padded by one index each side.
-__device__ void slab_window(const Geo& G, const float (*c0)[3],
-                            const float (*c1)[3], int ix, Slab* out) {
+// Order-preserving float <-> int keys for warp min/max reductions.
+__device__ __forceinline__ int fkey(float f) {
+  const int i = __float_as_int(f);
+  return i >= 0 ? i : i ^ 0x7fffffff;
+}
+__device__ __forceinline__ float fval(int k) {
+  return __int_as_float(k >= 0 ? k : k ^ 0x7fffffff);
+}
+
+// y/z index window of slab ix from the hull's cross-sections at its two
+// planes (pext[k] = {ymin, ymax, zmin, zmax} keys at plane k) and the hull
+// vertices (crystal corners) with x inside the slab; padded by one index.
+__device__ void slab_window(const Geo& G, const float (*c0)[3], const float (*c1)[3],
+                            const int4* pext, int ix, Slab* out) {
   const epet_grid& g = G.p.grid;
   const float X0 = voxel_plane(g, 0, ix), X1 = voxel_plane(g, 0, ix + 1);
-  float ymin = 3.4e38f, ymax = -3.4e38f, zmin = 3.4e38f, zmax = -3.4e38f;
-  bool any = false;
-  auto add = [&](float y, float z) {
-    ymin = fminf(ymin, y); ymax = fmaxf(ymax, y);
-    zmin = fminf(zmin, z); zmax = fmaxf(zmax, z);
-    any = true;
-  };
-  // hull vertices inside the slab
+  int ylo = min(pext[ix].x, pext[ix + 1].x), yhi = max(pext[ix].y, pext[ix + 1].y);
+  int zlo = min(pext[ix].z, pext[ix + 1].z), zhi = max(pext[ix].w, pext[ix + 1].w);
   for (int k = 0; k < 8; k++) {
-    if (c0[k][0] >= X0 && c0[k][0] <= X1) add(c0[k][1], c0[k][2]);
-    if (c1[k][0] >= X0 && c1[k][0] <= X1) add(c1[k][1], c1[k][2]);
-  }
-  // crossings of the corner-pair segments with the two slab planes
-  for (int a = 0; a < 8; a++) {
-    for (int b = 0; b < 8; b++) {
-      const float dx = c1[b][0] - c0[a][0];
-      if (dx == 0.f) continue;
-      const float dy = c1[b][1] - c0[a][1], dz = c1[b][2] - c0[a][2];
-      const float tA = (X0 - c0[a][0]) / dx, tB = (X1 - c0[a][0]) / dx;
-      if (tA >= 0.f && tA <= 1.f) add(c0[a][1] + tA * dy, c0[a][2] + tA * dz);
-      if (tB >= 0.f && tB <= 1.f) add(c0[a][1] + tB * dy, c0[a][2] + tB * dz);
+    if (c0[k][0] >= X0 && c0[k][0] <= X1) {
+      ylo = min(ylo, fkey(c0[k][1])); yhi = max(yhi, fkey(c0[k][1]));
+      zlo = min(zlo, fkey(c0[k][2])); zhi = max(zhi, fkey(c0[k][2]));
+    }
+    if (c1[k][0] >= X0 && c1[k][0] <= X1) {
+      ylo = min(ylo, fkey(c1[k][1])); yhi = max(yhi, fkey(c1[k][1]));
+      zlo = min(zlo, fkey(c1[k][2])); zhi = max(zhi, fkey(c1[k][2]));
     }
   }
-  if (!any) {
-    out->y0 = out->z0 = 0;
-    out->wy = out->wz = 0;
-    return;
-  }
+  out->y0 = out->z0 = 0;
+  out->wy = out->wz = 0;
+  if (ylo > yhi) return;  // the bundle does not reach this slab
+  const float ymin = fval(ylo), ymax = fval(yhi), zmin = fval(zlo), zmax = fval(zhi);
   const int ny = g.n[1], nz = g.n[2];
   int j0 = (int)floorf((ymin - g.o[1]) / g.d[1]) - 1;
   int j1 = (int)floorf((ymax - g.o[1]) / g.d[1]) + 1;
   int i0 = (int)floorf((zmin - g.o[2]) / g.d[2]) - 1;
   int i1 = (int)floorf((zmax - g.o[2]) / g.d[2]) + 1;
-  if (j1 < 0 || j0 > ny - 1 || i1 < 0 || i0 > nz - 1) {
-    out->y0 = out->z0 = 0;
-    out->wy = out->wz = 0;
-    return;
-  }
+  if (j1 < 0 || j0 > ny - 1 || i1 < 0 || i0 > nz - 1) return;
   j0 = clampi(j0, 0, ny - 1); j1 = clampi(j1, 0, ny - 1);
   i0 = clampi(i0, 0, nz - 1); i1 = clampi(i1, 0, nz - 1);
   out->y0 = j0; out->wy = j1 - j0 + 1;
   out->z0 = i0; out->wz = i1 - i0 + 1;
 }
 
-// Add `units` to voxel (ix,iy,iz) of the window; flags hits outside it.
-__device__ __forceinline__ void win_add(unsigned long long* win, const Slab* slabs,
-                                        int ix, int iy, int iz,
-                                        unsigned long long units, int* outside) {
+// The window holds each cell's exact 64-bit fixed-point sum as two 32-bit
+// words (native 32-bit shared atomics): the low word wraps, and the add whose
+// pre-value shows the wrap carries one into the high word.  The total is
+// independent of the order of the adds.
+struct Window {
+  uint32_t* lo;
+  uint32_t* hi;
+};
+
+__device__ __forceinline__ void win_add(const Window& w, const Slab* slabs, int ix, int iy,
+                                        int iz, unsigned long long units, int* outside) {
   const Slab s = slabs[ix];
   const unsigned jy = (unsigned)(iy - s.y0), jz = (unsigned)(iz - s.z0);
   if (jy < (unsigned)s.wy && jz < (unsigned)s.wz) {
-    atomicAdd(&win[s.off + (int)jy * s.wz + (int)jz], units);
+    const int c = s.off + (int)jy * s.wz + (int)jz;
+    const uint32_t l = (uint32_t)units, h = (uint32_t)(units >> 32);
+    const uint32_t old = atomicAdd(&w.lo[c], l);
+    const uint32_t carry = (old > 0xffffffffu - l) ? 1u : 0u;
+    if (h + carry) atomicAdd(&w.hi[c], h + carry);
   } else {
     atomicAdd(outside, 1);
   }
@@ -169,18 +175,84 @@ __device__ __forceinline__ unsigned long long to_units(float len, float scale) {
   return (u == 0ull && len > 0.f) ? 1ull : u;
 }
 
+// One axis of a ray walk: the ray's parameter at grid plane k is the
+// reference's quotient (plane_k - r0)/(r1 - r0), correctly rounded.
+struct WalkAxis {
+  float o, d, r0, dr;
+  int n, step, idx;
+  float lo, hi;  // parameter interval of the current cell along this axis
+  __device__ __forceinline__ float alpha(int k) const {
+    return fdiv(fsub(fadd(o, fmul((float)k, d)), r0), dr);
+  }
+  // cell with lo <= a < hi (a inside the axis' grid range)
+  __device__ __forceinline__ void enter(float a) {
+    int i = clampi((int)floorf((r0 + a * dr - o) / d), 0, n - 1);
+    if (step > 0) {  // interval of cell i: [alpha(i), alpha(i+1)]
+      while (i > 0 && alpha(i) > a) i--;
+      while (i < n - 1 && alpha(i + 1) <= a) i++;
+      lo = alpha(i);
+      hi = alpha(i + 1);
+    } else {         // interval of cell i: [alpha(i+1), alpha(i)]
+      while (i < n - 1 && alpha(i + 1) > a) i++;
+      while (i > 0 && alpha(i) <= a) i--;
+      lo = alpha(i + 1);
+      hi = alpha(i);
+    }
+    idx = i;
+  }
+  // across the exit plane; false when leaving the grid
+  __device__ __forceinline__ bool advance() {
+    const int ni = idx + step;
+    if (ni < 0 || ni >= n) return false;
+    idx = ni;
+    lo = hi;
+    hi = step > 0 ? alpha(ni + 1) : alpha(ni);
+    return true;
+  }
+};
+
+// Walks cells from the current state until leaving the grid or reaching the
+// cell (sx, sy, sz) (not processed); returns steps taken.
+__device__ __forceinline__ int walk_cells(WalkAxis& X, WalkAxis& Y, WalkAxis& Z, float L,
+                                          float scale, const Window& w, const Slab* slabs,
+                                          int* outside, int sx, int sy, int sz, int budget) {
+  int steps = 0;
+  for (; steps < budget; steps++) {
+    if (X.idx == sx && Y.idx == sy && Z.idx == sz) break;
+    const float amin = fmaxf(fmaxf(X.lo, Y.lo), Z.lo);
+    float amax;
+    int m;
+    if (X.hi <= Y.hi && X.hi <= Z.hi) {
+      amax = X.hi;
+      m = 0;
+    } else if (Y.hi <= Z.hi) {
+      amax = Y.hi;
+      m = 1;
+    } else {
+      amax = Z.hi;
+      m = 2;
+    }
+    if (amin < amax)
+      win_add(w, slabs, X.idx, Y.idx, Z.idx, to_units(fmul(fsub(amax, amin), L), scale),
+              outside);
+    const bool in = m == 0 ? X.advance() : (m == 1 ? Y.advance() : Z.advance());
+    if (!in) break;
+  }
+  return steps;
+}
+
 // Walk one ray through the grid and add its chord lengths to the window.
-// Parameters along the ray are the reference's quotients
-// (plane - r0)/(r1 - r0) per axis; voxel interval = [max lo, min hi];
-// length = (aMax - aMin)*|r1 - r0| (getSystemMatrixFromWorkqueue.cu:24-69).
-__device__ void walk_ray(const Geo& G, const float* ray, unsigned long long* win,
-                         const Slab* slabs, int* outside, int* needs_exact) {
+// Voxel interval = [max lo, min hi] over the axes; length = (aMax - aMin) *
+// |r1 - r0| (getSystemMatrixFromWorkqueue.cu:24-69).  The walk starts at the
+// parameter fraction `frac` of the ray's grid range, runs to the exit, then
+// covers the part from the entry up to the starting cell: rays of one channel
+// run in lock-step through the same voxels, and different starting points
+// keep the lanes of a warp on different cells.
+__device__ void walk_ray(const Geo& G, const float* ray, const Window& w, const Slab* slabs,
+                         int* outside, int* needs_exact, float frac) {
   const epet_grid& g = G.p.grid;
-  float r0[3] = {ray[0], ray[1], ray[2]};
-  float dr[3] = {fsub(ray[3], ray[0]), fsub(ray[4], ray[1]), fsub(ray[5], ray[2])};
-  const bool act[3] = {ray[0] != ray[3], ray[1] != ray[4], ray[2] != ray[5]};
-  if (!(act[0] || act[1] || act[2])) return;
-  if (!(act[0] && act[1] && act[2])) {
+  if (ray[0] == ray[3] && ray[1] == ray[4] && ray[2] == ray[5]) return;
+  if (ray[0] == ray[3] || ray[1] == ray[4] || ray[2] == ray[5]) {
     // A ray with equal coordinates on an axis: the reference leaves that
     // axis out of its slab test, so the chord reaches every candidate along
     // it, possibly beyond the bundle window.  Such (rare) rows are redone by
@@ -188,57 +260,39 @@ __device__ void walk_ray(const Geo& G, const float* ray, unsigned long long* win
     *needs_exact = 1;
     return;
   }
-  const float L = norm3(dr[0], dr[1], dr[2]);
-  auto A = [&](int d, int k) { return fdiv(fsub(voxel_plane(g, d, k), r0[d]), dr[d]); };
-
-  // Grid parameter range over the active axes.
-  float a_in = -3.4e38f, a_out = 3.4e38f;
-  for (int d = 0; d < 3; d++) {
-    if (!act[d]) continue;
-    float p0 = A(d, 0), p1 = A(d, g.n[d]);
-    a_in = fmaxf(a_in, fminf(p0, p1));
-    a_out = fminf(a_out, fmaxf(p0, p1));
+  WalkAxis X, Y, Z;
+  X.o = g.o[0]; X.d = g.d[0]; X.r0 = ray[0]; X.dr = fsub(ray[3], ray[0]); X.n = g.n[0];
+  Y.o = g.o[1]; Y.d = g.d[1]; Y.r0 = ray[1]; Y.dr = fsub(ray[4], ray[1]); Y.n = g.n[1];
+  Z.o = g.o[2]; Z.d = g.d[2]; Z.r0 = ray[2]; Z.dr = fsub(ray[5], ray[2]); Z.n = g.n[2];
+  X.step = X.dr > 0.f ? 1 : -1;
+  Y.step = Y.dr > 0.f ? 1 : -1;
+  Z.step = Z.dr > 0.f ? 1 : -1;
+  const float L = norm3(X.dr, Y.dr, Z.dr);
+  // grid parameter range
+  float a_in, a_out;
+  {
+    const float x0 = X.alpha(0), x1 = X.alpha(X.n);
+    const float y0 = Y.alpha(0), y1 = Y.alpha(Y.n);
+    const float z0 = Z.alpha(0), z1 = Z.alpha(Z.n);
+    a_in = fmaxf(fmaxf(fminf(x0, x1), fminf(y0, y1)), fminf(z0, z1));
+    a_out = fminf(fminf(fmaxf(x0, x1), fmaxf(y0, y1)), fmaxf(z0, z1));
   }
   if (!(a_in < a_out)) return;
-
-  // Entry cell per active axis: lo <= a_in < hi.
-  int idx[3] = {0, 0, 0}, step[3] = {1, 1, 1};
-  float lo[3] = {-3.4e38f, -3.4e38f, -3.4e38f}, hi[3] = {3.4e38f, 3.4e38f, 3.4e38f};
-  for (int d = 0; d < 3; d++) {
-    if (!act[d]) continue;
-    const int n = g.n[d];
-    step[d] = dr[d] > 0.f ? 1 : -1;
-    // estimate from the position at a_in, then correct with exact parameters
-    float pos = r0[d] + a_in * dr[d];
-    int i = clampi((int)floorf((pos - g.o[d]) / g.d[d]), 0, n - 1);
-    if (step[d] > 0) {  // interval of cell i: [A(i), A(i+1)]
-      while (i > 0 && A(d, i) > a_in) i--;
-      while (i < n - 1 && A(d, i + 1) <= a_in) i++;
-      lo[d] = A(d, i); hi[d] = A(d, i + 1);
-    } else {            // interval of cell i: [A(i+1), A(i)]
-      while (i < n - 1 && A(d, i + 1) > a_in) i++;
-      while (i > 0 && A(d, i) <= a_in) i--;
-      lo[d] = A(d, i + 1); hi[d] = A(d, i);
-    }
-    idx[d] = i;
-  }
-  for (int guard = 0; guard < g.n[0] + g.n[1] + g.n[2] + 3; guard++) {
-    const float amin = fmaxf(fmaxf(lo[0], lo[1]), lo[2]);
-    // exit axis: smallest hi (ties: lowest axis)
-    int mdim = 0;
-    float amax = hi[0];
-    if (hi[1] < amax) { amax = hi[1]; mdim = 1; }
-    if (hi[2] < amax) { amax = hi[2]; mdim = 2; }
-    if (amin < amax) {
-      const float len = fmul(fsub(amax, amin), L);
-      win_add(win, slabs, idx[0], idx[1], idx[2], to_units(len, G.fx_scale), outside);
-    }
-    // advance across the exit plane
-    const int ni = idx[mdim] + step[mdim];
-    if (ni < 0 || ni >= g.n[mdim]) break;
-    idx[mdim] = ni;
-    lo[mdim] = hi[mdim];
-    hi[mdim] = step[mdim] > 0 ? A(mdim, ni + 1) : A(mdim, ni);
+  float a_s = a_in + (a_out - a_in) * frac;
+  if (!(a_s >= a_in && a_s < a_out)) a_s = a_in;
+  const int budget = g.n[0] + g.n[1] + g.n[2] + 3;
+  // part 1: from the cell containing a_s to the exit
+  X.enter(a_s);
+  Y.enter(a_s);
+  Z.enter(a_s);
+  const int sx = X.idx, sy = Y.idx, sz = Z.idx;
+  int used = walk_cells(X, Y, Z, L, G.fx_scale, w, slabs, outside, -1, -1, -1, budget);
+  // part 2: from the entry up to (not including) the starting cell
+  if (a_s > a_in) {
+    X.enter(a_in);
+    Y.enter(a_in);
+    Z.enter(a_in);
+    walk_cells(X, Y, Z, L, G.fx_scale, w, slabs, outside, sx, sy, sz, budget - used);
   }
 }
 
@@ -250,8 +304,9 @@ k_walk(WalkArgs args) {
   const epet_grid& g = G.p.grid;
   const int nx = g.n[0];
   Slab* slabs = reinterpret_cast<Slab*>(smem);
-  unsigned long long* win =
-      reinterpret_cast<unsigned long long*>(smem + align256(sizeof(Slab) * nx));
+  Window win;
+  win.lo = reinterpret_cast<uint32_t*>(smem + align256(sizeof(Slab) * nx));
+  win.hi = win.lo + args.cap_cells;
   __shared__ float c0[8][3], c1[8][3];
   __shared__ ChannelLine line;
   __shared__ int warp_tot[kWalkThreads / 32];
@@ -264,18 +319,70 @@ k_walk(WalkArgs args) {
   const int64_t slot = blockIdx.x;  // staging slot
   const int cnl = args.rows[row];
 
-  // ---- channel line, crystal corners
+  // ---- channel geometry: crystal transforms (thread 0), corners (16
+  // threads), exact candidate threshold (warp 1, 32-way search)
+  __shared__ CrystalMat mats[2];
   if (threadIdx.x == 0) {
-    CrystalMat m0, m1;
-    ChannelLine L;
-    channel_line(G, cnl, &L, nullptr, &m0, &m1);
-    line = L;
-    for (int k = 0; k < 8; k++) {
-      crystal_apply(m0, (float)(k & 1), (float)((k >> 1) & 1), (float)(k >> 2), c0[k]);
-      crystal_apply(m1, (float)(k & 1), (float)((k >> 1) & 1), (float)(k >> 2), c1[k]);
-    }
+    int id[5];
+    channel_decode(G.p.setup, cnl, id);
+    float sn, cs;
+    angle_sincos(G.p.setup, id[0], &sn, &cs);
+    mats[0] = crystal_matrix(G.p.setup, sn, cs, 0, id[1], id[2]);
+    mats[1] = crystal_matrix(G.p.setup, sn, cs, 1, id[3], id[4]);
+    float b[3];
+    crystal_apply(mats[0], 0.5f, 0.5f, 0.5f, line.a);
+    crystal_apply(mats[1], 0.5f, 0.5f, 0.5f, b);
+    for (int d = 0; d < 3; d++) line.ab[d] = fsub(b[d], line.a[d]);
     s_outside = 0;
     s_exact = 0;
+  }
+  __syncthreads();
+  if (threadIdx.x < 16) {
+    const int k = threadIdx.x & 7;
+    float* dst = threadIdx.x < 8 ? c0[k] : c1[k];
+    crystal_apply(mats[threadIdx.x >> 3], (float)(k & 1), (float)((k >> 1) & 1),
+                  (float)(k >> 2), dst);
+  } else if ((threadIdx.x >> 5) == 1) {
+    const float nab = norm3(line.ab[0], line.ab[1], line.ab[2]);
+    const float thr = candidate_threshold_warp(nab, G.sum_radii);
+    if ((threadIdx.x & 31) == 0) line.s_max = thr;
+  }
+  __syncthreads();
+
+  // ---- hull cross-section at every x plane: warp per plane, lanes over
+  // the 64 crystal-corner pair lines
+  int4* pext = reinterpret_cast<int4*>(
+      smem + align256(sizeof(Slab) * nx) + (size_t)args.cap_cells * 8);
+  {
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    float ax[2], ay[2], az[2], inv[2], dy[2], dz[2];
+    bool ok[2];
+    for (int q = 0; q < 2; q++) {
+      const int pidx = lane + 32 * q, a = pidx >> 3, b = pidx & 7;
+      ax[q] = c0[a][0]; ay[q] = c0[a][1]; az[q] = c0[a][2];
+      const float dx = c1[b][0] - ax[q];
+      ok[q] = dx != 0.f;
+      inv[q] = ok[q] ? __frcp_rn(dx) : 0.f;
+      dy[q] = c1[b][1] - ay[q];
+      dz[q] = c1[b][2] - az[q];
+    }
+    for (int k = w; k <= nx; k += kWalkThreads / 32) {
+      const float X = voxel_plane(g, 0, k);
+      int ylo = INT_MAX, yhi = INT_MIN, zlo = INT_MAX, zhi = INT_MIN;
+      for (int q = 0; q < 2; q++) {
+        const float t = (X - ax[q]) * inv[q];
+        if (ok[q] && t >= 0.f && t <= 1.f) {
+          const int ky = fkey(ay[q] + t * dy[q]), kz = fkey(az[q] + t * dz[q]);
+          ylo = min(ylo, ky); yhi = max(yhi, ky);
+          zlo = min(zlo, kz); zhi = max(zhi, kz);
+        }
+      }
+      ylo = __reduce_min_sync(0xffffffffu, ylo);
+      yhi = __reduce_max_sync(0xffffffffu, yhi);
+      zlo = __reduce_min_sync(0xffffffffu, zlo);
+      zhi = __reduce_max_sync(0xffffffffu, zhi);
+      if (lane == 0) pext[k] = make_int4(ylo, yhi, zlo, zhi);
+    }
   }
   __syncthreads();
 
@@ -285,7 +392,7 @@ k_walk(WalkArgs args) {
   const int sbeg = threadIdx.x * per, send = min(nx, sbeg + per);
   for (int ix = sbeg; ix < send; ix++) {
     Slab s;
-    slab_window(G, c0, c1, ix, &s);
+    slab_window(G, c0, c1, pext, ix, &s);
     slabs[ix] = s;
     my_cells += s.wy * s.wz;
   }
@@ -313,7 +420,10 @@ k_walk(WalkArgs args) {
   }
 
   // ---- zero the window, walk the rays
-  for (int i = threadIdx.x; i < W; i += kWalkThreads) win[i] = 0ull;
+  for (int i = threadIdx.x; i < W; i += kWalkThreads) {
+    win.lo[i] = 0u;
+    win.hi[i] = 0u;
+  }
   __syncthreads();
   const int R = G.p.nrays;
   const float* rays = args.rays + row * (int64_t)R * 6;
@@ -322,7 +432,9 @@ k_walk(WalkArgs args) {
     const float2* rp = reinterpret_cast<const float2*>(rays + 6 * r);
     float2 a = rp[0], b = rp[1], c = rp[2];
     ray[0] = a.x; ray[1] = a.y; ray[2] = b.x; ray[3] = b.y; ray[4] = c.x; ray[5] = c.y;
-    walk_ray(G, ray, win, slabs, &s_outside, &s_exact);
+    // golden-ratio spread of the starting points over the rays
+    const float frac = (float)r * 0.6180339887f - floorf((float)r * 0.6180339887f);
+    walk_ray(G, ray, win, slabs, &s_outside, &s_exact, frac);
   }
   __syncthreads();
   if (threadIdx.x == 0 && s_outside) atomicAdd(args.hit_outside, s_outside);
@@ -358,13 +470,15 @@ k_walk(WalkArgs args) {
     int sx = ix;
     for (int cidx = cbeg; cidx < cend; cidx++) {
       while (cidx >= slabs[sx].off + slabs[sx].wy * slabs[sx].wz) sx++;
-      const unsigned long long u = win[cidx];
+      const unsigned long long u =
+          ((unsigned long long)win.hi[cidx] << 32) | (unsigned long long)win.lo[cidx];
       if (u == 0ull) continue;
       const Slab s = slabs[sx];
       const int k = cidx - s.off;
       const int iy = s.y0 + k / s.wz, iz = s.z0 + k % s.wz;
       if (!is_candidate(G, L, sx, iy, iz)) {
-        win[cidx] = 0ull;  // not a candidate of this channel: drop
+        win.lo[cidx] = 0u;  // not a candidate of this channel: drop
+        win.hi[cidx] = 0u;
         continue;
       }
       const float v = fdiv(fmul(__ull2float_rn(u), G.fx_inv), invR);
@@ -384,7 +498,8 @@ k_walk(WalkArgs args) {
     int sx = ix;
     for (int cidx = cbeg; cidx < cend; cidx++) {
       while (cidx >= slabs[sx].off + slabs[sx].wy * slabs[sx].wz) sx++;
-      const unsigned long long u = win[cidx];
+      const unsigned long long u =
+          ((unsigned long long)win.hi[cidx] << 32) | (unsigned long long)win.lo[cidx];
       if (u == 0ull) continue;
       const Slab s = slabs[sx];
       const int k = cidx - s.off;
@@ -455,7 +570,8 @@ __global__ void k_offset_rowptr(int64_t* rp, int64_t n, const int64_t* base) {
 // ------------------------------------------------------------------ host
 
 static size_t walk_smem(const Geo& G, int cap_cells) {
-  return align256(sizeof(Slab) * G.p.grid.n[0]) + (size_t)cap_cells * 8;
+  return align256(sizeof(Slab) * G.p.grid.n[0]) + (size_t)cap_cells * 8 +
+         (size_t)(G.p.grid.n[0] + 1) * sizeof(int4);
 }
 
 static int g_max_smem = 0;

@@ -228,7 +228,11 @@ extern "C" {
 
 epet_status epet_csrmv(int trans, const epet_csr* a, const epet_csc* csc, float alpha,
                        const float* x_d, float beta, float* y_d, epet_stream_t stream) {
-  if (!a || !x_d || !y_d) return set_error(EPET_ERR_INVALID, "bad arguments");
+  if (!a) return set_error(EPET_ERR_INVALID, "bad arguments");
+  const int64_t out_len = trans ? a->n : a->m, in_len = trans ? a->m : a->n;
+  if ((out_len > 0 && !y_d) || (in_len > 0 && !x_d))
+    return set_error(EPET_ERR_INVALID, "bad arguments");
+  if (out_len == 0) return EPET_OK;
   cudaStream_t st = (cudaStream_t)stream;
   if (!trans) {
     const int G = pick_group(a->m ? (double)a->nnz / a->m : 0.0);
