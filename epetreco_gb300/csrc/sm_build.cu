@@ -73,6 +73,20 @@ struct WalkArgs {
   int32_t* ovf_idx;
 };
 
+// Dynamic shared memory of the walk kernel; every section starts on a
+// 256-byte boundary (the plane extents are int4).
+struct WalkLayout {
+  size_t pext, lo, hi, total;
+};
+__host__ __device__ inline WalkLayout walk_layout(int nx, int cap_cells) {
+  WalkLayout L;
+  L.pext = align256((size_t)20 * nx);  // Slab[nx]
+  L.lo = L.pext + align256((size_t)(nx + 1) * 16);
+  L.hi = L.lo + align256((size_t)cap_cells * 4);
+  L.total = L.hi + align256((size_t)cap_cells * 4);
+  return L;
+}
+
 // Slab metadata in shared memory.
 struct Slab {
   int off;  // first cell
@@ -304,9 +318,10 @@ k_walk(WalkArgs args) {
   const epet_grid& g = G.p.grid;
   const int nx = g.n[0];
   Slab* slabs = reinterpret_cast<Slab*>(smem);
+  const WalkLayout lay = walk_layout(nx, args.cap_cells);
   Window win;
-  win.lo = reinterpret_cast<uint32_t*>(smem + align256(sizeof(Slab) * nx));
-  win.hi = win.lo + args.cap_cells;
+  win.lo = reinterpret_cast<uint32_t*>(smem + lay.lo);
+  win.hi = reinterpret_cast<uint32_t*>(smem + lay.hi);
   __shared__ float c0[8][3], c1[8][3];
   __shared__ ChannelLine line;
   __shared__ int warp_tot[kWalkThreads / 32];
@@ -351,8 +366,7 @@ k_walk(WalkArgs args) {
 
   // ---- hull cross-section at every x plane: warp per plane, lanes over
   // the 64 crystal-corner pair lines
-  int4* pext = reinterpret_cast<int4*>(
-      smem + align256(sizeof(Slab) * nx) + (size_t)args.cap_cells * 8);
+  int4* pext = reinterpret_cast<int4*>(smem + lay.pext);
   {
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     float ax[2], ay[2], az[2], inv[2], dy[2], dz[2];
@@ -570,8 +584,8 @@ __global__ void k_offset_rowptr(int64_t* rp, int64_t n, const int64_t* base) {
 // ------------------------------------------------------------------ host
 
 static size_t walk_smem(const Geo& G, int cap_cells) {
-  return align256(sizeof(Slab) * G.p.grid.n[0]) + (size_t)cap_cells * 8 +
-         (size_t)(G.p.grid.n[0] + 1) * sizeof(int4);
+  static_assert(sizeof(Slab) == 20, "walk_layout assumes 20-byte slabs");
+  return walk_layout(G.p.grid.n[0], cap_cells).total;
 }
 
 static int g_max_smem = 0;

@@ -109,50 +109,138 @@ epet_status exclusive_scan_i64(const int64_t* in, int64_t* out, int64_t n,
   return EPET_OK;
 }
 
+static int bits_for(int64_t maxval) {
+  int b = 0;
+  while (b < 63 && (int64_t(1) << b) <= maxval) b++;
+  return b;
+}
+
 // ------------------------------------------------------------ radix sort
+//
+// Stable LSD radix sort with BITS-bit digits.  Per pass: a histogram kernel
+// (tile x digit counts), an exclusive scan of the digit-major histogram, and
+// a scatter kernel.  The scatter ranks the tile's items stably -- warp w owns
+// items [w*512, (w+1)*512) and ranks them in 16 rounds of 32 consecutive
+// items with __match_any_sync -- then stages the tile in shared memory in
+// digit order, so the global writes of each digit are contiguous runs.
+// Input and output go through adapters, so the first pass can read a CSR
+// directly and the last pass can write the column-major arrays.
 constexpr int kRsThreads = 256, kRsItems = 16, kRsTile = kRsThreads * kRsItems;
 constexpr int kRsWarps = kRsThreads / 32;
 
-template <typename K>
+template <int BITS, typename K>
 __global__ void __launch_bounds__(kRsThreads)
 k_radix_hist(const K* __restrict__ keys, int64_t n, int shift, int64_t ntiles,
              int64_t* __restrict__ hist) {
-  __shared__ unsigned cnt[256];
-  cnt[threadIdx.x] = 0;
+  constexpr int BINS = 1 << BITS;
+  __shared__ unsigned cnt[BINS];
+  for (int d = threadIdx.x; d < BINS; d += kRsThreads) cnt[d] = 0;
   __syncthreads();
   const int64_t base = (int64_t)blockIdx.x * kRsTile;
 #pragma unroll 4
   for (int k = 0; k < kRsItems; k++) {
     const int64_t i = base + k * kRsThreads + threadIdx.x;
-    if (i < n) atomicAdd(&cnt[(unsigned)(keys[i] >> shift) & 255u], 1u);
+    if (i < n) atomicAdd(&cnt[(unsigned)(keys[i] >> shift) & (BINS - 1)], 1u);
   }
   __syncthreads();
-  hist[(int64_t)threadIdx.x * ntiles + blockIdx.x] = cnt[threadIdx.x];
+  for (int d = threadIdx.x; d < BINS; d += kRsThreads)
+    hist[(int64_t)d * ntiles + blockIdx.x] = cnt[d];
 }
 
-// Stable scatter: warp w ranks items [w*512, (w+1)*512) of the tile in 16
-// rounds of 32 consecutive items; ranks follow (warp, round, lane) order.
-template <typename K, typename Vt>
+// Plain arrays in / out.
+template <typename K, typename V>
+struct ArrIn {
+  const K* k;
+  const V* v;
+  __device__ void prepare(int64_t, int64_t) {}
+  __device__ K key(int64_t i) const { return k[i]; }
+  __device__ V val(int64_t i) const { return v[i]; }
+};
+template <typename K, typename V>
+struct ArrOut {
+  K* k;
+  V* v;
+  __device__ void put(int64_t pos, K key, V val) const {
+    k[pos] = key;
+    v[pos] = val;
+  }
+};
+
+// CSR in: key = column, value = (row << 32) | value bits.  The row of entry
+// i is found by binary search among the rows spanning the tile.
+struct CsrIn {
+  const int64_t* row_ptr;
+  int64_t m;
+  const int32_t* col;
+  const float* vals;
+  int64_t r_lo, r_hi;  // rows spanning the current tile
+  __device__ static int64_t row_of(const int64_t* rp, int64_t lo, int64_t hi, int64_t i) {
+    // last row r in [lo, hi] with rp[r] <= i
+    while (lo < hi) {
+      const int64_t mid = (lo + hi + 1) >> 1;
+      if (rp[mid] <= i) lo = mid;
+      else hi = mid - 1;
+    }
+    return lo;
+  }
+  __device__ void prepare(int64_t first, int64_t last) {
+    __shared__ int64_t rr[2];
+    if (threadIdx.x == 0) {
+      rr[0] = row_of(row_ptr, 0, m - 1, first);
+      rr[1] = row_of(row_ptr, 0, m - 1, last);
+    }
+    __syncthreads();
+    r_lo = rr[0];
+    r_hi = rr[1];
+  }
+  __device__ uint32_t key(int64_t i) const { return (uint32_t)col[i]; }
+  __device__ uint64_t val(int64_t i) const {
+    const int64_t r = row_of(row_ptr, r_lo, r_hi, i);
+    return ((uint64_t)(uint32_t)r << 32) | __float_as_uint(vals[i]);
+  }
+};
+
+// CSC out: row and value arrays, plus the sorted column ids.
+struct CscOut {
+  int32_t* row;
+  float* val;
+  uint32_t* key;
+  __device__ void put(int64_t pos, uint32_t k, uint64_t v) const {
+    row[pos] = (int32_t)(v >> 32);
+    val[pos] = __uint_as_float((uint32_t)v);
+    key[pos] = k;
+  }
+};
+
+template <int BITS, typename K, typename V, typename In, typename Out>
 __global__ void __launch_bounds__(kRsThreads)
-k_radix_scatter(const K* __restrict__ keys, const Vt* __restrict__ vals, int64_t n,
-                int shift, int64_t ntiles, const int64_t* __restrict__ offs,
-                K* __restrict__ okeys, Vt* __restrict__ ovals) {
-  __shared__ unsigned wcnt[kRsWarps][256];
-  __shared__ int64_t base_off[256];
+k_radix_scatter(In in, Out out, int64_t n, int shift, int64_t ntiles,
+                const int64_t* __restrict__ offs) {
+  constexpr int BINS = 1 << BITS;
+  __shared__ unsigned wcnt[kRsWarps][BINS];
+  __shared__ unsigned dstart[BINS + 1];
+  __shared__ unsigned warp_tot[kRsWarps];
+  extern __shared__ __align__(16) unsigned char rs_dyn[];  // staged tile
+  V* sv = reinterpret_cast<V*>(rs_dyn);
+  K* sk = reinterpret_cast<K*>(rs_dyn + sizeof(V) * kRsTile);
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-  for (int d = lane; d < 256; d += 32) wcnt[w][d] = 0;
-  base_off[threadIdx.x] = offs[(int64_t)threadIdx.x * ntiles + blockIdx.x];
+  const int64_t tile0 = (int64_t)blockIdx.x * kRsTile;
+  const int tile_n = (int)(n - tile0 < kRsTile ? n - tile0 : kRsTile);
+  in.prepare(tile0, tile0 + tile_n - 1);
+  for (int d = lane; d < BINS; d += 32) wcnt[w][d] = 0;
   __syncwarp();
-  const int64_t wbase = (int64_t)blockIdx.x * kRsTile + (int64_t)w * (kRsItems * 32);
+  const int64_t wbase = tile0 + (int64_t)w * (kRsItems * 32);
   K kk[kRsItems];
+  V vv[kRsItems];
   unsigned rank[kRsItems];
   const unsigned lt = (1u << lane) - 1u;
 #pragma unroll
   for (int r = 0; r < kRsItems; r++) {
     const int64_t i = wbase + r * 32 + lane;
     const bool ok = i < n;
-    kk[r] = ok ? keys[i] : K(0);
-    const unsigned dig = ok ? ((unsigned)(kk[r] >> shift) & 255u) : 256u + lane;
+    kk[r] = ok ? in.key(i) : K(0);
+    vv[r] = ok ? in.val(i) : V(0);
+    const unsigned dig = ok ? ((unsigned)(kk[r] >> shift) & (BINS - 1)) : BINS + lane;
     const unsigned peers = __match_any_sync(0xffffffffu, dig);
     unsigned before = 0;
     if (ok) before = wcnt[w][dig];
@@ -163,50 +251,111 @@ k_radix_scatter(const K* __restrict__ keys, const Vt* __restrict__ vals, int64_t
     __syncwarp();
   }
   __syncthreads();
-  // exclusive prefix over warps per digit
-  {
-    const int d = threadIdx.x;
+  // per digit: warp offsets (exclusive over warps) and the digit total
+  constexpr int DPT = (BINS + kRsThreads - 1) / kRsThreads;  // digits per thread
+  unsigned tot[DPT];
+  unsigned mysum = 0;
+#pragma unroll
+  for (int q = 0; q < DPT; q++) {
+    const int d = threadIdx.x * DPT + q;
     unsigned run = 0;
-    for (int ww = 0; ww < kRsWarps; ww++) {
-      unsigned c = wcnt[ww][d];
-      wcnt[ww][d] = run;
-      run += c;
+    if (d < BINS) {
+      for (int ww = 0; ww < kRsWarps; ww++) {
+        const unsigned c = wcnt[ww][d];
+        wcnt[ww][d] = run;
+        run += c;
+      }
+    }
+    tot[q] = run;
+    mysum += run;
+  }
+  // exclusive scan of the digit totals (block-wide, digits in thread order)
+  unsigned inc = mysum;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const unsigned t = __shfl_up_sync(0xffffffffu, inc, o);
+    if (lane >= o) inc += t;
+  }
+  if (lane == 31) warp_tot[w] = inc;
+  __syncthreads();
+  if (w == 0) {
+    const unsigned t = lane < kRsWarps ? warp_tot[lane] : 0u;
+    unsigned ti = t;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const unsigned u = __shfl_up_sync(0xffffffffu, ti, o);
+      if (lane >= o) ti += u;
+    }
+    if (lane < kRsWarps) warp_tot[lane] = ti - t;
+  }
+  __syncthreads();
+  {
+    unsigned run = warp_tot[w] + inc - mysum;
+#pragma unroll
+    for (int q = 0; q < DPT; q++) {
+      const int d = threadIdx.x * DPT + q;
+      if (d < BINS) dstart[d] = run;
+      run += tot[q];
     }
   }
   __syncthreads();
+  // stage in digit order
 #pragma unroll
   for (int r = 0; r < kRsItems; r++) {
     const int64_t i = wbase + r * 32 + lane;
     if (i < n) {
-      const unsigned dig = (unsigned)(kk[r] >> shift) & 255u;
-      const int64_t pos = base_off[dig] + wcnt[w][dig] + rank[r];
-      okeys[pos] = kk[r];
-      ovals[pos] = vals[i];
+      const unsigned dig = (unsigned)(kk[r] >> shift) & (BINS - 1);
+      const unsigned lp = dstart[dig] + wcnt[w][dig] + rank[r];
+      sk[lp] = kk[r];
+      sv[lp] = vv[r];
     }
+  }
+  __syncthreads();
+  // contiguous runs per digit
+  for (int j = threadIdx.x; j < tile_n; j += kRsThreads) {
+    const K key = sk[j];
+    const unsigned dig = (unsigned)(key >> shift) & (BINS - 1);
+    const int64_t pos = offs[(int64_t)dig * ntiles + blockIdx.x] + (j - (int)dstart[dig]);
+    out.put(pos, key, sv[j]);
   }
 }
 
 size_t radix_hist_elems(int64_t n) {
   const int64_t tiles = std::max<int64_t>(1, (n + kRsTile - 1) / kRsTile);
-  return (size_t)256 * tiles;
+  return (size_t)512 * tiles;
 }
 
+// One pass: histogram of the keys (any array holding this pass's keys), scan,
+// scatter from `in` to `out`.
+template <int BITS, typename K, typename V, typename In, typename Out>
+epet_status radix_pass(const K* hist_keys, In in, Out out, int64_t n, int shift, int64_t* hist,
+                       int64_t* hist_scan, int64_t* scan_tmp, cudaStream_t st) {
+  const int64_t ntiles = (n + kRsTile - 1) / kRsTile;
+  k_radix_hist<BITS, K><<<(unsigned)ntiles, kRsThreads, 0, st>>>(hist_keys, n, shift, ntiles,
+                                                                 hist);
+  EPET_LAUNCHED();
+  EPET_CHECK(exclusive_scan_i64(hist, hist_scan, (int64_t)(1 << BITS) * ntiles, scan_tmp, st));
+  const size_t dyn = (sizeof(K) + sizeof(V)) * (size_t)kRsTile;
+  EPET_CUDA(cudaFuncSetAttribute(k_radix_scatter<BITS, K, V, In, Out>,
+                                 cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn));
+  k_radix_scatter<BITS, K, V, In, Out><<<(unsigned)ntiles, kRsThreads, dyn, st>>>(
+      in, out, n, shift, ntiles, hist_scan);
+  EPET_LAUNCHED();
+  return EPET_OK;
+}
+
+// Sorts (keys, vals) in place on the low `bits` bits (8-bit digits).
 template <typename K, typename Vt>
 epet_status radix_sort(K* keys, Vt* vals, K* alt_keys, Vt* alt_vals, int64_t n, int bits,
                        int64_t* hist, int64_t* hist_scan, int64_t* scan_tmp,
                        cudaStream_t st) {
   if (n <= 1 || bits <= 0) return EPET_OK;
-  const int64_t ntiles = (n + kRsTile - 1) / kRsTile;
   K *src_k = keys, *dst_k = alt_keys;
   Vt *src_v = vals, *dst_v = alt_vals;
   int passes = 0;
   for (int shift = 0; shift < bits; shift += 8, passes++) {
-    k_radix_hist<K><<<(unsigned)ntiles, kRsThreads, 0, st>>>(src_k, n, shift, ntiles, hist);
-    EPET_LAUNCHED();
-    EPET_CHECK(exclusive_scan_i64(hist, hist_scan, 256 * ntiles, scan_tmp, st));
-    k_radix_scatter<K, Vt><<<(unsigned)ntiles, kRsThreads, 0, st>>>(
-        src_k, src_v, n, shift, ntiles, hist_scan, dst_k, dst_v);
-    EPET_LAUNCHED();
+    EPET_CHECK((radix_pass<8, K, Vt>(src_k, ArrIn<K, Vt>{src_k, src_v}, ArrOut<K, Vt>{dst_k, dst_v},
+                                      n, shift, hist, hist_scan, scan_tmp, st)));
     std::swap(src_k, dst_k);
     std::swap(src_v, dst_v);
   }
@@ -215,12 +364,6 @@ epet_status radix_sort(K* keys, Vt* vals, K* alt_keys, Vt* alt_vals, int64_t n, 
     EPET_CUDA(cudaMemcpyAsync(vals, src_v, n * sizeof(Vt), cudaMemcpyDeviceToDevice, st));
   }
   return EPET_OK;
-}
-
-static int bits_for(int64_t maxval) {
-  int b = 0;
-  while (b < 63 && (int64_t(1) << b) <= maxval) b++;
-  return b;
 }
 
 // ----------------------------------------------------------- COO helpers
@@ -297,28 +440,6 @@ __global__ void k_csr2ecsr(int64_t* ecsr, const int32_t* yrow, int64_t nnzr,
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i < nnzr) ecsr[i] = csr[yrow[i]];
   if (i == nnzr) ecsr[nnzr] = csr[m];
-}
-
-// CSR -> (key = column, value = row<<32 | value bits), rows ascending.
-__global__ void k_csr_to_pairs(const int64_t* __restrict__ row_ptr, int64_t m,
-                               const int32_t* __restrict__ col, const float* __restrict__ val,
-                               uint32_t* __restrict__ key, uint64_t* __restrict__ pv) {
-  const int64_t row = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  const int lane = threadIdx.x & 31;
-  if (row >= m) return;
-  for (int64_t k = row_ptr[row] + lane; k < row_ptr[row + 1]; k += 32) {
-    key[k] = (uint32_t)col[k];
-    pv[k] = ((uint64_t)(uint32_t)row << 32) | __float_as_uint(val[k]);
-  }
-}
-
-__global__ void k_pairs_to_csc(const uint64_t* __restrict__ pv, int64_t nnz,
-                               int32_t* __restrict__ row, float* __restrict__ val) {
-  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i < nnz) {
-    row[i] = (int32_t)(pv[i] >> 32);
-    val[i] = __uint_as_float((uint32_t)pv[i]);
-  }
 }
 
 __global__ void k_colptr_from_sorted(const uint32_t* __restrict__ key, int64_t nnz,
@@ -411,7 +532,7 @@ size_t epet_csr_to_csc_workspace_size(int64_t m, int64_t n, int64_t nnz) {
   (void)m;
   (void)n;
   const size_t hist = radix_hist_elems(nnz);
-  return 2 * align256(nnz * 4) + 2 * align256(nnz * 8) + align256(hist * 8) +
+  return 2 * align256(nnz * 4) + align256(nnz * 8) + align256(hist * 8) +
          align256((hist + 1) * 8) + align256(scan_tmp_elems(hist) * 8) + 256;
 }
 
@@ -433,21 +554,41 @@ epet_status epet_csr_to_csc(const epet_csr* a, epet_csc* out, void* ws, size_t w
   uint32_t* key = scr.take<uint32_t>(nnz);
   uint32_t* key2 = scr.take<uint32_t>(nnz);
   uint64_t* pv = scr.take<uint64_t>(nnz);
-  uint64_t* pv2 = scr.take<uint64_t>(nnz);
   const size_t hn = radix_hist_elems(nnz);
   int64_t* hist = scr.take<int64_t>(hn);
   int64_t* hist_scan = scr.take<int64_t>(hn + 1);
   int64_t* tmp = scr.take<int64_t>(scan_tmp_elems(hn));
   if (scr.overrun) return set_error(EPET_ERR_INVALID, "internal: workspace size");
   const int T = 256;
-  k_csr_to_pairs<<<ceil_div(a->m * 32, T), T, 0, st>>>(a->row_ptr, a->m, a->col, a->val, key,
-                                                        pv);
-  EPET_LAUNCHED();
-  EPET_CHECK((radix_sort<uint32_t, uint64_t>(key, pv, key2, pv2, nnz,
-                                             std::max(1, bits_for(a->n - 1)), hist, hist_scan,
-                                             tmp, st)));
-  k_pairs_to_csc<<<ceil_div(nnz, T), T, 0, st>>>(pv, nnz, out->row, out->val);
-  EPET_LAUNCHED();
+  const int bits = std::max(1, bits_for(a->n - 1));
+  CsrIn in{a->row_ptr, a->m, a->col, a->val, 0, 0};
+  if (bits <= 9) {
+    // one pass: CSR -> CSC
+    EPET_CHECK((radix_pass<9, uint32_t, uint64_t>(reinterpret_cast<const uint32_t*>(a->col), in,
+                                                  CscOut{out->row, out->val, key}, nnz, 0, hist,
+                                                  hist_scan, tmp, st)));
+  } else if (bits <= 18) {
+    const int b0 = (bits + 1) / 2;
+    // pass 1 (low digits): CSR -> (key, row|val)
+    if (b0 == 9) {
+      EPET_CHECK((radix_pass<9, uint32_t, uint64_t>(
+          reinterpret_cast<const uint32_t*>(a->col), in, ArrOut<uint32_t, uint64_t>{key, pv}, nnz,
+          0, hist, hist_scan, tmp, st)));
+      EPET_CHECK((radix_pass<9, uint32_t, uint64_t>(
+          key, ArrIn<uint32_t, uint64_t>{key, pv}, CscOut{out->row, out->val, key2}, nnz, 9, hist,
+          hist_scan, tmp, st)));
+    } else {
+      EPET_CHECK((radix_pass<8, uint32_t, uint64_t>(
+          reinterpret_cast<const uint32_t*>(a->col), in, ArrOut<uint32_t, uint64_t>{key, pv}, nnz,
+          0, hist, hist_scan, tmp, st)));
+      EPET_CHECK((radix_pass<9, uint32_t, uint64_t>(
+          key, ArrIn<uint32_t, uint64_t>{key, pv}, CscOut{out->row, out->val, key2}, nnz, 8, hist,
+          hist_scan, tmp, st)));
+    }
+    std::swap(key, key2);
+  } else {
+    return set_error(EPET_ERR_UNSUPPORTED, "more than 2^18 voxels in the column-major copy");
+  }
   k_colptr_from_sorted<<<ceil_div(a->n + 1, T), T, 0, st>>>(key, nnz, a->n, out->col_ptr);
   EPET_LAUNCHED();
   return EPET_OK;
