@@ -75,6 +75,7 @@ struct Geo {
   int32_t nyz;       // n[1]*n[2]
   float fx_scale;    // 2^s: chord length -> fixed point units
   float fx_inv;      // 2^-s
+  int fx_split;      // units = hi * 2^fx_split + lo, both parts summed in 32 bits
 };
 
 __device__ __forceinline__ float fmul(float a, float b) { return __fmul_rn(a, b); }

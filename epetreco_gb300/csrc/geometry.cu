@@ -70,13 +70,20 @@ Geo make_geo(const epet_problem& p) {
   G.sum_radii = 0.5f * sr;
   G.V = p.grid.n[0] * p.grid.n[1] * p.grid.n[2];
   G.nyz = p.grid.n[1] * p.grid.n[2];
-  // Fixed-point scale for exact chord sums: nrays chords of at most the
-  // voxel diagonal must stay below 2^62.
-  double maxsum = (double)p.nrays * (double)av * 1.01 + 1e-30;
-  int s = (int)floor(log2(4.611686018427388e18 / maxsum));
+  // Fixed-point chord sums: a cell gets at most nrays chords (one per ray),
+  // each split as hi * 2^b + lo with lo < 2^b; b and the scale 2^s are chosen
+  // so that nrays * 2^b <= 2^32 and nrays * max(hi) < 2^32, i.e. both halves
+  // sum in 32 bits without carries, exactly and in any order.  A chord is at
+  // most the voxel diagonal (av, +1% for rounding).
+  int lg = 0;
+  while ((1ll << lg) < (long long)p.nrays + 1) lg++;  // ceil(log2(nrays + 1))
+  const int b = 32 - lg;                               // lo bits
+  const int units_bits = 64 - 2 * lg;                  // chord units < 2^units_bits
+  int s = (int)floor(log2(ldexp(1.0, units_bits) / ((double)av * 1.01 + 1e-30)));
   if (s > 100) s = 100;
   G.fx_scale = ldexpf(1.0f, s);
   G.fx_inv = ldexpf(1.0f, -s);
+  G.fx_split = b;
   return G;
 }
 

@@ -4,10 +4,11 @@
 // their counts, the system matrix built once by the fused kernel (it is
 // deterministic, so the reference's rebuild in every iteration is not
 // needed), its column-major copy, the normalised sensitivity and the image.
-// An iteration is four kernels: forward product fused with e = y/(Ax) and
-// the log-likelihood terms; transpose product fused with x*c/s and the image
-// sum; the fixed-order sum; the normalisation.  With use_graph the four are
-// captured once in a CUDA graph and replayed.
+// An iteration is four kernels: forward product fused with e = y/(Ax);
+// transpose product fused with x*c/s and the image sum; the fixed-order sum;
+// the normalisation.  With use_graph the four are captured once in a CUDA
+// graph and replayed.  The Poisson log-likelihood of the last forward
+// projection is reduced in fp64 on request.
 #include <algorithm>
 #include <cmath>
 #include <cstring>
@@ -22,6 +23,7 @@ struct epet_mlem {
   int64_t m = 0, V = 0;
   int32_t* rows = nullptr;
   float *y = nullptr, *s = nullptr, *x = nullptr, *xnew = nullptr, *e = nullptr;
+  float* ybar = nullptr;  // last forward projection
   epet_csr A{};
   epet_csc At{};
   int64_t capA = 0;
@@ -44,7 +46,8 @@ static void mlem_free(epet_mlem* h) {
   if (!h) return;
   if (h->exec) cudaGraphExecDestroy(h->exec);
   if (h->graph) cudaGraphDestroy(h->graph);
-  void* bufs[] = {h->rows, h->y, h->s, h->x, h->xnew, h->e, h->A.row_ptr, h->A.col, h->A.val,
+  void* bufs[] = {h->rows, h->y, h->ybar, h->s, h->x, h->xnew, h->e, h->A.row_ptr, h->A.col,
+                  h->A.val,
                   h->At.col_ptr, h->At.row, h->At.val, h->part_ll, h->part_x, h->sums};
   for (void* b : bufs)
     if (b) cudaFree(b);
@@ -53,11 +56,10 @@ static void mlem_free(epet_mlem* h) {
 
 static epet_status mlem_iteration(epet_mlem* h, cudaStream_t st) {
   EPET_CHECK(launch_rows(h->g_fwd, h->A.row_ptr, h->A.col, h->A.val, h->x, h->m,
-                         EpiMlemForward{h->y, h->e, nullptr}, h->part_ll, st, nullptr));
+                         EpiMlemForward{h->y, h->e, h->ybar}, nullptr, st, nullptr));
   EPET_CHECK(launch_rows(h->g_bwd, h->At.col_ptr, h->At.row, h->At.val, h->e, h->V,
                          EpiMlemUpdate{h->x, h->s, h->xnew, nullptr}, h->part_x, st, nullptr));
   EPET_CHECK(launch_sum_partials(h->part_x, h->nb_bwd, h->sums + 1, st));
-  EPET_CHECK(launch_sum_partials(h->part_ll, h->nb_fwd, h->sums + 0, st));
   EPET_CHECK(launch_normalise(h->xnew, h->sums + 1, h->V, h->x, st));
   return EPET_OK;
 }
@@ -104,6 +106,7 @@ epet_status epet_mlem_create(const epet_problem* p, const int32_t* rows_d, const
   ALLOC(h->rows, m * 4);
   ALLOC(h->y, m * 4);
   ALLOC(h->e, m * 4);
+  ALLOC(h->ybar, m * 4);
   ALLOC(h->s, V * 4);
   ALLOC(h->x, V * 4);
   ALLOC(h->xnew, V * 4);
@@ -141,9 +144,8 @@ epet_status epet_mlem_create(const epet_problem* p, const int32_t* rows_d, const
   h->g_bwd = pick_group(V ? (double)nnz / V : 0.0);
   h->nb_fwd = (m + kSpmvThreads / h->g_fwd - 1) / (kSpmvThreads / h->g_fwd);
   h->nb_bwd = (V + kSpmvThreads / h->g_bwd - 1) / (kSpmvThreads / h->g_bwd);
-  ALLOC(h->part_ll, std::max<int64_t>(h->nb_fwd, 1) * 8);
+  ALLOC(h->part_ll, 1024 * 8);
   ALLOC(h->part_x, std::max<int64_t>(h->nb_bwd, 1) * 8);
-  cudaMemsetAsync(h->part_ll, 0, std::max<int64_t>(h->nb_fwd, 1) * 8, st);
 #undef ALLOC
   cudaError_t e = cudaStreamSynchronize(st);
   if (e != cudaSuccess) return fail(cuda_status(e, "mlem create"));
@@ -177,16 +179,22 @@ epet_status epet_mlem_iterate(epet_mlem* h, int32_t nit, double* loglik_h,
     }
     for (int it = 0; it < nit; it++) {
       EPET_CUDA(cudaGraphLaunch(h->exec, st));
-      note_launch(5);  // the captured iteration holds five kernels
+      note_launch(4);  // the captured iteration holds four kernels
     }
   } else {
     for (int it = 0; it < nit; it++) EPET_CHECK(mlem_iteration(h, st));
   }
   if (loglik_h) {
-    double s[2];
-    EPET_CUDA(cudaMemcpyAsync(s, h->sums, 16, cudaMemcpyDeviceToHost, st));
+    if (h->m > 0) {
+      const int nb = (int)std::max<int64_t>(1, std::min<int64_t>(ceil_div(h->m, 256), 1024));
+      EPET_CHECK(poisson_loglik(h->y, h->ybar, h->m, h->part_ll, nb, h->sums + 0, st));
+    } else {
+      EPET_CUDA(cudaMemsetAsync(h->sums, 0, 8, st));
+    }
+    double s0 = 0.0;
+    EPET_CUDA(cudaMemcpyAsync(&s0, h->sums, 8, cudaMemcpyDeviceToHost, st));
     EPET_CUDA(cudaStreamSynchronize(st));
-    *loglik_h = s[0];
+    *loglik_h = s0;
   }
   return EPET_OK;
 }

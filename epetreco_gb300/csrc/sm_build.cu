@@ -88,10 +88,14 @@ __host__ __device__ inline WalkLayout walk_layout(int nx, int cap_cells) {
 }
 
 // Slab metadata in shared memory.
+// The window is sliced along the slab axis sa (x or z, whichever the
+// channel's line follows more closely); within slab i the cells form the
+// rectangle [p0, p0+wp) x [q0, q0+wq) over the other two axes
+// (sa = 0: p = y, q = z; sa = 2: p = x, q = y).
 struct Slab {
   int off;  // first cell
-  int y0, wy;
-  int z0, wz;
+  int p0, wp;
+  int q0, wq;
 };
 
 __device__ __forceinline__ int clampi(int v, int lo, int hi) {
@@ -125,60 +129,66 @@ __device__ __forceinline__ float fval(int k) {
   return __int_as_float(k >= 0 ? k : k ^ 0x7fffffff);
 }
 
-// y/z index window of slab ix from the hull's cross-sections at its two
-// planes (pext[k] = {ymin, ymax, zmin, zmax} keys at plane k) and the hull
-// vertices (crystal corners) with x inside the slab; padded by one index.
+// Index window of slab i along axis sa from the hull's cross-sections at its
+// two planes (pext[k] = {pmin, pmax, qmin, qmax} keys at plane k) and the
+// hull vertices (crystal corners) inside the slab; padded by one index.
 __device__ void slab_window(const Geo& G, const float (*c0)[3], const float (*c1)[3],
-                            const int4* pext, int ix, Slab* out) {
+                            const int4* pext, int sa, int i, Slab* out) {
   const epet_grid& g = G.p.grid;
-  const float X0 = voxel_plane(g, 0, ix), X1 = voxel_plane(g, 0, ix + 1);
-  int ylo = min(pext[ix].x, pext[ix + 1].x), yhi = max(pext[ix].y, pext[ix + 1].y);
-  int zlo = min(pext[ix].z, pext[ix + 1].z), zhi = max(pext[ix].w, pext[ix + 1].w);
+  const int pa = sa == 0 ? 1 : 0, qa = sa == 0 ? 2 : 1;
+  const float P0 = voxel_plane(g, sa, i), P1 = voxel_plane(g, sa, i + 1);
+  int plo = min(pext[i].x, pext[i + 1].x), phi = max(pext[i].y, pext[i + 1].y);
+  int qlo = min(pext[i].z, pext[i + 1].z), qhi = max(pext[i].w, pext[i + 1].w);
   for (int k = 0; k < 8; k++) {
-    if (c0[k][0] >= X0 && c0[k][0] <= X1) {
-      ylo = min(ylo, fkey(c0[k][1])); yhi = max(yhi, fkey(c0[k][1]));
-      zlo = min(zlo, fkey(c0[k][2])); zhi = max(zhi, fkey(c0[k][2]));
+    if (c0[k][sa] >= P0 && c0[k][sa] <= P1) {
+      plo = min(plo, fkey(c0[k][pa])); phi = max(phi, fkey(c0[k][pa]));
+      qlo = min(qlo, fkey(c0[k][qa])); qhi = max(qhi, fkey(c0[k][qa]));
     }
-    if (c1[k][0] >= X0 && c1[k][0] <= X1) {
-      ylo = min(ylo, fkey(c1[k][1])); yhi = max(yhi, fkey(c1[k][1]));
-      zlo = min(zlo, fkey(c1[k][2])); zhi = max(zhi, fkey(c1[k][2]));
+    if (c1[k][sa] >= P0 && c1[k][sa] <= P1) {
+      plo = min(plo, fkey(c1[k][pa])); phi = max(phi, fkey(c1[k][pa]));
+      qlo = min(qlo, fkey(c1[k][qa])); qhi = max(qhi, fkey(c1[k][qa]));
     }
   }
-  out->y0 = out->z0 = 0;
-  out->wy = out->wz = 0;
-  if (ylo > yhi) return;  // the bundle does not reach this slab
-  const float ymin = fval(ylo), ymax = fval(yhi), zmin = fval(zlo), zmax = fval(zhi);
-  const int ny = g.n[1], nz = g.n[2];
-  int j0 = (int)floorf((ymin - g.o[1]) / g.d[1]) - 1;
-  int j1 = (int)floorf((ymax - g.o[1]) / g.d[1]) + 1;
-  int i0 = (int)floorf((zmin - g.o[2]) / g.d[2]) - 1;
-  int i1 = (int)floorf((zmax - g.o[2]) / g.d[2]) + 1;
-  if (j1 < 0 || j0 > ny - 1 || i1 < 0 || i0 > nz - 1) return;
-  j0 = clampi(j0, 0, ny - 1); j1 = clampi(j1, 0, ny - 1);
-  i0 = clampi(i0, 0, nz - 1); i1 = clampi(i1, 0, nz - 1);
-  out->y0 = j0; out->wy = j1 - j0 + 1;
-  out->z0 = i0; out->wz = i1 - i0 + 1;
+  out->p0 = out->q0 = 0;
+  out->wp = out->wq = 0;
+  if (plo > phi) return;  // the bundle does not reach this slab
+  const float pmin = fval(plo), pmax = fval(phi), qmin = fval(qlo), qmax = fval(qhi);
+  const int np = g.n[pa], nq = g.n[qa];
+  int a0 = (int)floorf((pmin - g.o[pa]) / g.d[pa]) - 1;
+  int a1 = (int)floorf((pmax - g.o[pa]) / g.d[pa]) + 1;
+  int b0 = (int)floorf((qmin - g.o[qa]) / g.d[qa]) - 1;
+  int b1 = (int)floorf((qmax - g.o[qa]) / g.d[qa]) + 1;
+  if (a1 < 0 || a0 > np - 1 || b1 < 0 || b0 > nq - 1) return;
+  a0 = clampi(a0, 0, np - 1); a1 = clampi(a1, 0, np - 1);
+  b0 = clampi(b0, 0, nq - 1); b1 = clampi(b1, 0, nq - 1);
+  out->p0 = a0; out->wp = a1 - a0 + 1;
+  out->q0 = b0; out->wq = b1 - b0 + 1;
 }
 
-// The window holds each cell's exact 64-bit fixed-point sum as two 32-bit
-// words (native 32-bit shared atomics): the low word wraps, and the add whose
-// pre-value shows the wrap carries one into the high word.  The total is
-// independent of the order of the adds.
+// The window holds each cell's exact fixed-point sum as two 32-bit words:
+// every chord's units are split as hi * 2^fx_split + lo and the halves are
+// summed separately with fire-and-forget 32-bit shared atomics; the split is
+// sized (make_geo) so neither half can overflow.  The total
+// (hi_sum << fx_split) + lo_sum is exact and independent of the order of the
+// adds.
 struct Window {
   uint32_t* lo;
   uint32_t* hi;
+  int split;
+  int sa;  // slab axis
 };
 
 __device__ __forceinline__ void win_add(const Window& w, const Slab* slabs, int ix, int iy,
                                         int iz, unsigned long long units, int* outside) {
-  const Slab s = slabs[ix];
-  const unsigned jy = (unsigned)(iy - s.y0), jz = (unsigned)(iz - s.z0);
-  if (jy < (unsigned)s.wy && jz < (unsigned)s.wz) {
-    const int c = s.off + (int)jy * s.wz + (int)jz;
-    const uint32_t l = (uint32_t)units, h = (uint32_t)(units >> 32);
-    const uint32_t old = atomicAdd(&w.lo[c], l);
-    const uint32_t carry = (old > 0xffffffffu - l) ? 1u : 0u;
-    if (h + carry) atomicAdd(&w.hi[c], h + carry);
+  const bool zs = w.sa == 2;
+  const Slab s = slabs[zs ? iz : ix];
+  const unsigned jp = (unsigned)((zs ? ix : iy) - s.p0), jq = (unsigned)((zs ? iy : iz) - s.q0);
+  if (jp < (unsigned)s.wp && jq < (unsigned)s.wq) {
+    const int c = s.off + (int)jp * s.wq + (int)jq;
+    const uint32_t l = (uint32_t)(units & ((1ull << w.split) - 1ull));
+    const uint32_t h = (uint32_t)(units >> w.split);
+    atomicAdd(&w.lo[c], l);
+    if (h) atomicAdd(&w.hi[c], h);
   } else {
     atomicAdd(outside, 1);
   }
@@ -318,14 +328,16 @@ k_walk(WalkArgs args) {
   const epet_grid& g = G.p.grid;
   const int nx = g.n[0];
   Slab* slabs = reinterpret_cast<Slab*>(smem);
-  const WalkLayout lay = walk_layout(nx, args.cap_cells);
+  const WalkLayout lay = walk_layout(max(g.n[0], g.n[2]), args.cap_cells);
   Window win;
   win.lo = reinterpret_cast<uint32_t*>(smem + lay.lo);
   win.hi = reinterpret_cast<uint32_t*>(smem + lay.hi);
+  win.split = G.fx_split;
+  win.sa = 0;  // set after the prologue
   __shared__ float c0[8][3], c1[8][3];
   __shared__ ChannelLine line;
   __shared__ int warp_tot[kWalkThreads / 32];
-  __shared__ int s_total, s_outside, s_exact;
+  __shared__ int s_total, s_outside, s_exact, s_sa;
   __shared__ double red_d[kWalkThreads / 32];
   __shared__ float red_f[kWalkThreads / 32];
 
@@ -350,8 +362,13 @@ k_walk(WalkArgs args) {
     for (int d = 0; d < 3; d++) line.ab[d] = fsub(b[d], line.a[d]);
     s_outside = 0;
     s_exact = 0;
+    // slab along the axis the line follows more closely (x or z)
+    s_sa = fabsf(line.ab[2]) > fabsf(line.ab[0]) ? 2 : 0;
   }
   __syncthreads();
+  const int sa = s_sa;
+  const int pa = sa == 0 ? 1 : 0, qa = sa == 0 ? 2 : 1;
+  const int ns = g.n[sa];  // slabs
   if (threadIdx.x < 16) {
     const int k = threadIdx.x & 7;
     float* dst = threadIdx.x < 8 ? c0[k] : c1[k];
@@ -371,17 +388,18 @@ k_walk(WalkArgs args) {
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     float ax[2], ay[2], az[2], inv[2], dy[2], dz[2];
     bool ok[2];
+    // per lane two pair lines, in (slab axis, p axis, q axis) coordinates
     for (int q = 0; q < 2; q++) {
       const int pidx = lane + 32 * q, a = pidx >> 3, b = pidx & 7;
-      ax[q] = c0[a][0]; ay[q] = c0[a][1]; az[q] = c0[a][2];
-      const float dx = c1[b][0] - ax[q];
+      ax[q] = c0[a][sa]; ay[q] = c0[a][pa]; az[q] = c0[a][qa];
+      const float dx = c1[b][sa] - ax[q];
       ok[q] = dx != 0.f;
       inv[q] = ok[q] ? __frcp_rn(dx) : 0.f;
-      dy[q] = c1[b][1] - ay[q];
-      dz[q] = c1[b][2] - az[q];
+      dy[q] = c1[b][pa] - ay[q];
+      dz[q] = c1[b][qa] - az[q];
     }
-    for (int k = w; k <= nx; k += kWalkThreads / 32) {
-      const float X = voxel_plane(g, 0, k);
+    for (int k = w; k <= ns; k += kWalkThreads / 32) {
+      const float X = voxel_plane(g, sa, k);
       int ylo = INT_MAX, yhi = INT_MIN, zlo = INT_MAX, zhi = INT_MIN;
       for (int q = 0; q < 2; q++) {
         const float t = (X - ax[q]) * inv[q];
@@ -402,20 +420,20 @@ k_walk(WalkArgs args) {
 
   // ---- per-slab windows and their offsets
   int my_cells = 0;
-  const int per = (nx + kWalkThreads - 1) / kWalkThreads;
-  const int sbeg = threadIdx.x * per, send = min(nx, sbeg + per);
+  const int per = (ns + kWalkThreads - 1) / kWalkThreads;
+  const int sbeg = threadIdx.x * per, send = min(ns, sbeg + per);
   for (int ix = sbeg; ix < send; ix++) {
     Slab s;
-    slab_window(G, c0, c1, pext, ix, &s);
+    slab_window(G, c0, c1, pext, sa, ix, &s);
     slabs[ix] = s;
-    my_cells += s.wy * s.wz;
+    my_cells += s.wp * s.wq;
   }
   const int excl = block_excl_scan(my_cells, warp_tot, &s_total);
   {
     int o = excl;
     for (int ix = sbeg; ix < send; ix++) {
       slabs[ix].off = o;
-      o += slabs[ix].wy * slabs[ix].wz;
+      o += slabs[ix].wp * slabs[ix].wq;
     }
   }
   __syncthreads();
@@ -433,6 +451,7 @@ k_walk(WalkArgs args) {
     return;
   }
 
+  win.sa = sa;
   // ---- zero the window, walk the rays
   for (int i = threadIdx.x; i < W; i += kWalkThreads) {
     win.lo[i] = 0u;
@@ -461,67 +480,102 @@ k_walk(WalkArgs args) {
     return;
   }
 
-  // ---- ordered extraction: thread t owns cells [t*cpt, (t+1)*cpt)
-  const int cpt = (W + kWalkThreads - 1) / kWalkThreads;
-  const int cbeg = min(W, (int)threadIdx.x * cpt), cend = min(W, cbeg + cpt);
-  // locate the slab of cbeg
-  int ix = 0;
-  {
-    int lo_s = 0, hi_s = nx - 1;
-    while (lo_s < hi_s) {  // last slab with off <= cbeg
-      int mid = (lo_s + hi_s + 1) >> 1;
-      if (slabs[mid].off <= cbeg) lo_s = mid;
-      else hi_s = mid - 1;
+  // ---- ordered extraction in voxel-id order.  Thread t owns a contiguous
+  // range of an id-ordered enumeration: the window cells themselves when
+  // slabs run along x (storage order is id order), else the bounding box
+  // [x range] x [y range] x [all z] of the z-slab window.
+  int bx0 = 0, bx1 = -1, by0 = 0, by1 = -1;  // box of a z-slab window
+  int E = W;                                 // enumeration length
+  if (sa == 2) {
+    __shared__ int bb[4];
+    if (threadIdx.x == 0) {
+      int a0 = INT_MAX, a1 = -1, b0 = INT_MAX, b1 = -1;
+      for (int k = 0; k < ns; k++) {
+        if (slabs[k].wp == 0 || slabs[k].wq == 0) continue;
+        a0 = min(a0, slabs[k].p0); a1 = max(a1, slabs[k].p0 + slabs[k].wp - 1);
+        b0 = min(b0, slabs[k].q0); b1 = max(b1, slabs[k].q0 + slabs[k].wq - 1);
+      }
+      bb[0] = a0; bb[1] = a1; bb[2] = b0; bb[3] = b1;
     }
-    ix = lo_s;
+    __syncthreads();
+    bx0 = bb[0]; bx1 = bb[1]; by0 = bb[2]; by1 = bb[3];
+    E = bx1 < bx0 ? 0 : (bx1 - bx0 + 1) * (by1 - by0 + 1) * g.n[2];
   }
+  const int cpt = (E + kWalkThreads - 1) / kWalkThreads;
+  const int cbeg = min(E, (int)threadIdx.x * cpt), cend = min(E, cbeg + cpt);
+  // Visits the thread's enumeration range in order; f(cell, ix, iy, iz)
+  // for every window cell met.
+  auto for_cells = [&](auto&& f) {
+    if (sa == 0) {
+      int lo_s = 0, hi_s = ns - 1;  // last slab with off <= cbeg
+      while (lo_s < hi_s) {
+        const int mid = (lo_s + hi_s + 1) >> 1;
+        if (slabs[mid].off <= cbeg) lo_s = mid;
+        else hi_s = mid - 1;
+      }
+      int sx = lo_s;
+      for (int cidx = cbeg; cidx < cend; cidx++) {
+        while (cidx >= slabs[sx].off + slabs[sx].wp * slabs[sx].wq) sx++;
+        const Slab sl = slabs[sx];
+        const int k = cidx - sl.off;
+        f(cidx, sx, sl.p0 + k / sl.wq, sl.q0 + k % sl.wq);
+      }
+    } else {
+      if (cbeg >= cend) return;
+      const int nz = g.n[2], wyb = by1 - by0 + 1;
+      int iz = cbeg % nz;
+      int t = cbeg / nz;
+      int iy = by0 + t % wyb, ix = bx0 + t / wyb;
+      for (int e = cbeg; e < cend; e++) {
+        const Slab sl = slabs[iz];
+        const unsigned jp = (unsigned)(ix - sl.p0), jq = (unsigned)(iy - sl.q0);
+        if (jp < (unsigned)sl.wp && jq < (unsigned)sl.wq)
+          f(sl.off + (int)jp * sl.wq + (int)jq, ix, iy, iz);
+        if (++iz == nz) {
+          iz = 0;
+          if (++iy > by1) {
+            iy = by0;
+            ++ix;
+          }
+        }
+      }
+    }
+  };
   const ChannelLine L = line;
-  const float invR = (float)R;
-  // pass 1: count passing non-zero cells
+  const float fR = (float)R;
+  // pass 1: candidate filter, count, projections
   int cnt = 0;
   float fsum = 0.f;
-  {
-    int sx = ix;
-    for (int cidx = cbeg; cidx < cend; cidx++) {
-      while (cidx >= slabs[sx].off + slabs[sx].wy * slabs[sx].wz) sx++;
-      const unsigned long long u =
-          ((unsigned long long)win.hi[cidx] << 32) | (unsigned long long)win.lo[cidx];
-      if (u == 0ull) continue;
-      const Slab s = slabs[sx];
-      const int k = cidx - s.off;
-      const int iy = s.y0 + k / s.wz, iz = s.z0 + k % s.wz;
-      if (!is_candidate(G, L, sx, iy, iz)) {
-        win.lo[cidx] = 0u;  // not a candidate of this channel: drop
-        win.hi[cidx] = 0u;
-        continue;
-      }
-      const float v = fdiv(fmul(__ull2float_rn(u), G.fx_inv), invR);
-      const int vox = sx * G.nyz + iy * g.n[2] + iz;
-      cnt++;
-      if (kMode == kModeForward) fsum = fadd(fsum, fmul(v, args.x[vox]));
-      if (kMode == kModeBack) {
-        const float ev = args.e[row];
-        if (ev != 0.f) atomicAdd(&args.c[vox], fmul(v, ev));
-      }
-      if (kMode == kModeColSum) atomicAdd(&args.s64[vox], (double)v);
+  for_cells([&](int cidx, int ix, int iy, int iz) {
+    const unsigned long long u =
+        ((unsigned long long)win.hi[cidx] << win.split) + (unsigned long long)win.lo[cidx];
+    if (u == 0ull) return;
+    if (!is_candidate(G, L, ix, iy, iz)) {
+      win.lo[cidx] = 0u;  // not a candidate of this channel: drop
+      win.hi[cidx] = 0u;
+      return;
     }
-  }
+    const float v = fdiv(fmul(__ull2float_rn(u), G.fx_inv), fR);
+    const int vox = ix * G.nyz + iy * g.n[2] + iz;
+    cnt++;
+    if (kMode == kModeForward) fsum = fadd(fsum, fmul(v, args.x[vox]));
+    if (kMode == kModeBack) {
+      const float ev = args.e[row];
+      if (ev != 0.f) atomicAdd(&args.c[vox], fmul(v, ev));
+    }
+    if (kMode == kModeColSum) atomicAdd(&args.s64[vox], (double)v);
+  });
   if (kMode == kModeCsr) {
     const int pos = block_excl_scan(cnt, warp_tot, &s_total);
     int64_t o = slot * args.stride + pos;
-    int sx = ix;
-    for (int cidx = cbeg; cidx < cend; cidx++) {
-      while (cidx >= slabs[sx].off + slabs[sx].wy * slabs[sx].wz) sx++;
+    for_cells([&](int cidx, int ix, int iy, int iz) {
       const unsigned long long u =
-          ((unsigned long long)win.hi[cidx] << 32) | (unsigned long long)win.lo[cidx];
-      if (u == 0ull) continue;
-      const Slab s = slabs[sx];
-      const int k = cidx - s.off;
-      const int iy = s.y0 + k / s.wz, iz = s.z0 + k % s.wz;
-      args.stage_col[o] = sx * G.nyz + iy * g.n[2] + iz;
-      args.stage_val[o] = fdiv(fmul(__ull2float_rn(u), G.fx_inv), invR);
+          ((unsigned long long)win.hi[cidx] << win.split) + (unsigned long long)win.lo[cidx];
+      if (u == 0ull) return;
+      args.stage_col[o] = ix * G.nyz + iy * g.n[2] + iz;
+      args.stage_val[o] = fdiv(fmul(__ull2float_rn(u), G.fx_inv), fR);
       o++;
-    }
+    });
     if (threadIdx.x == 0) {
       args.row_len[row] = s_total;
       if (args.sel) args.ovf_idx[row] = (int32_t)slot;
@@ -585,7 +639,7 @@ __global__ void k_offset_rowptr(int64_t* rp, int64_t n, const int64_t* base) {
 
 static size_t walk_smem(const Geo& G, int cap_cells) {
   static_assert(sizeof(Slab) == 20, "walk_layout assumes 20-byte slabs");
-  return walk_layout(G.p.grid.n[0], cap_cells).total;
+  return walk_layout(std::max(G.p.grid.n[0], G.p.grid.n[2]), cap_cells).total;
 }
 
 static int g_max_smem = 0;
@@ -900,8 +954,8 @@ static epet_status resolve_capacity(const Geo& G, int32_t max_row_nnz, cudaStrea
   if (walk_smem(G, *cap) > (size_t)max_dyn_smem())
     return set_error(EPET_ERR_UNSUPPORTED,
                      "per-row window of %d cells exceeds shared memory", *cap);
-  if (G.p.grid.n[0] > kMaxSlabs)
-    return set_error(EPET_ERR_UNSUPPORTED, "grid nx > %d", kMaxSlabs);
+  if (G.p.grid.n[0] > kMaxSlabs || G.p.grid.n[2] > kMaxSlabs)
+    return set_error(EPET_ERR_UNSUPPORTED, "grid nx or nz > %d", kMaxSlabs);
   return EPET_OK;
 }
 

@@ -213,6 +213,33 @@ epet_status launch_normalise(const float* xnew, const double* sum, int64_t n, fl
   return EPET_OK;
 }
 
+__global__ void k_loglik_part(const float* __restrict__ y, const float* __restrict__ yb,
+                              int64_t m, double* __restrict__ partial) {
+  __shared__ double red[8];
+  double s = 0.0;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < m;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const double d = (double)yb[i];
+    if (d > 0.0) s += (double)y[i] * log(d) - d;
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = s;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t = 0.0;
+    for (int w = 0; w < (int)(blockDim.x / 32); w++) t += red[w];
+    partial[blockIdx.x] = t;
+  }
+}
+
+epet_status poisson_loglik(const float* y, const float* ybar, int64_t m, double* partial,
+                           int nblocks, double* out, cudaStream_t st) {
+  k_loglik_part<<<nblocks, 256, 0, st>>>(y, ybar, m, partial);
+  EPET_LAUNCHED();
+  return launch_sum_partials(partial, nblocks, out, st);
+}
+
 epet_status sum_f64(const float* x, int64_t n, double* partial, int nblocks, double* out,
                     cudaStream_t st) {
   k_sum_f64_part<<<nblocks, 256, 0, st>>>(x, n, partial);

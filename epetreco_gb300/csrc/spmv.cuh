@@ -8,17 +8,16 @@ constexpr int kSpmvThreads = 256;
 
 // Forward projection epilogue: yb = A x (row r), e[r] = y[r] / yb with the
 // reference's divides (mlemOperations.hpp:22-32) but 0 where yb == 0 (the
-// reference would produce inf/NaN there); returns the Poisson log-likelihood
-// term y*log(yb) - yb in fp64.
+// reference would produce inf/NaN there); keeps yb for the log-likelihood,
+// which a separate kernel evaluates when asked for.
 struct EpiMlemForward {
   const float* y;
   float* e;
-  float* ybar;  // optional
+  float* ybar;
   __device__ double operator()(int64_t r, float d) const {
-    if (ybar) ybar[r] = d;
-    const float yr = y[r];
-    e[r] = d > 0.f ? __fdiv_rn(yr, d) : 0.f;
-    return d > 0.f ? (double)yr * log((double)d) - (double)d : 0.0;
+    ybar[r] = d;
+    e[r] = d > 0.f ? __fdiv_rn(y[r], d) : 0.f;
+    return 0.0;
   }
 };
 
@@ -51,5 +50,8 @@ epet_status launch_normalise(const float* xnew, const double* sum, int64_t n, fl
                              cudaStream_t st);
 epet_status sum_f64(const float* x, int64_t n, double* partial, int nblocks, double* out,
                     cudaStream_t st);
+// sum_i y_i log(ybar_i) - ybar_i over ybar_i > 0, fp64, fixed order.
+epet_status poisson_loglik(const float* y, const float* ybar, int64_t m, double* partial,
+                           int nblocks, double* out, cudaStream_t st);
 
 }  // namespace epet
