@@ -75,6 +75,7 @@ SIGNATURES = {
     "epet_sensitivity": [P, VP, I64, VP, VP, I32, VP, SZ, VP],
     "epet_coo_sort": [VP, VP, VP, I64, VP, SZ, VP],
     "epet_coo_sort_workspace_size": [I64],
+    "epet_coo_sort_noalloc": [VP, VP, VP, I64, VP],
     "epet_coo2csr": [VP, I64, I64, VP, VP],
     "epet_csr2ecsr": [VP, VP, I64, VP, I64, VP],
     "epet_csr_to_csc": [C.POINTER(CsrC), C.POINTER(CscC), VP, SZ, VP],

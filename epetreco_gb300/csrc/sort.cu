@@ -8,6 +8,7 @@
 // packed (row, col) key, stable within each tile by warp-ordered ranking
 // (__match_any_sync), a histogram+scan row pointer, and one gather kernel.
 #include <algorithm>
+#include <mutex>
 
 #include "common.cuh"
 #include "internal.h"
@@ -595,3 +596,58 @@ epet_status epet_csr_to_csc(const epet_csr* a, epet_csc* out, void* ws, size_t w
 }
 
 }  // extern "C"
+
+// ----------------------------------------------- allocation-free cooSort
+//
+// For callers that must not allocate device memory from inside the library
+// call: code running inside a captured stream region or a real-time loop
+// where cudaMalloc would synchronise the device or fail, a host process whose
+// allocator owns all device memory, or an integration whose memory budget is
+// fixed at start-up.  The sort's scratch lives in a file-scope device array
+// sized for kNoAllocCooSortMax entries (about 6.6 MB), which every GPU that
+// loads this library holds until the process exits.
+
+namespace epet {
+constexpr int64_t kNoAllocCooSortMax = int64_t(1) << 18;  // 262,144 triples
+constexpr size_t kNoAllocScratchBytes = size_t(7) << 20;  // 7 MiB
+static __device__ __align__(256) unsigned char g_coo_sort_scratch[kNoAllocScratchBytes];
+
+static std::mutex g_noalloc_mu;
+static void* g_noalloc_ptr[256];  // device address of the array, per device
+}  // namespace epet
+
+extern "C" epet_status epet_coo_sort_noalloc(float* val_d, int32_t* row_d, int32_t* col_d,
+                                             int64_t n, epet_stream_t stream) {
+  using namespace epet;
+  if (n < 0 || (n > 0 && (!val_d || !row_d || !col_d)))
+    return set_error(EPET_ERR_INVALID, "bad arguments");
+  if (n > kNoAllocCooSortMax)
+    return set_error(EPET_ERR_CAPACITY,
+                     "epet_coo_sort_noalloc sorts at most %lld triples (%lld given); use "
+                     "epet_coo_sort with a workspace for larger inputs",
+                     (long long)kNoAllocCooSortMax, (long long)n);
+  if (n <= 1) return EPET_OK;
+  const size_t need = epet_coo_sort_workspace_size(n);
+  if (need > kNoAllocScratchBytes)
+    return set_error(EPET_ERR_INVALID, "internal: static scratch too small (%zu > %zu)", need,
+                     kNoAllocScratchBytes);
+  // The array's host-side name is not a device address: resolve it once per
+  // device, with that device current.
+  int dev = 0;
+  EPET_CUDA(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= 256) return set_error(EPET_ERR_UNSUPPORTED, "device index %d", dev);
+  void* scratch = nullptr;
+  {
+    std::lock_guard<std::mutex> lk(g_noalloc_mu);
+    if (!g_noalloc_ptr[dev]) {
+      void* p = nullptr;
+      cudaError_t e = cudaGetSymbolAddress(&p, g_coo_sort_scratch);
+      if (e != cudaSuccess) return cuda_status(e, "cudaGetSymbolAddress(g_coo_sort_scratch)");
+      g_noalloc_ptr[dev] = p;
+    }
+    scratch = g_noalloc_ptr[dev];
+  }
+  // The caller-workspace path of epet_coo_sort allocates nothing; every
+  // scratch section it uses is written before it is read.
+  return epet_coo_sort(val_d, row_d, col_d, n, scratch, kNoAllocScratchBytes, stream);
+}

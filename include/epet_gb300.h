@@ -179,6 +179,18 @@ epet_status epet_coo_sort(float* val_d, int32_t* row_d, int32_t* col_d,
                           int64_t n, void* ws, size_t ws_bytes,
                           epet_stream_t stream);
 size_t epet_coo_sort_workspace_size(int64_t n);
+/* epet_coo_sort for callers that cannot allocate device memory during the
+ * call (inside a stream-capture region, a real-time loop, or an integration
+ * whose allocator owns the device memory).  No counterpart in the reference.
+ * Allocates nothing: its scratch is a file-scope device array of about 7 MB,
+ * held by every GPU that loads the library, so n is limited to 262,144
+ * triples (EPET_ERR_CAPACITY above that).  The first call on a device looks
+ * up the array's device address with that device current; make that first
+ * call before any stream capture.  All calls share the one array: calls that
+ * overlap on the GPU (different streams, or several host threads) race on it
+ * and must be serialised by the caller. */
+epet_status epet_coo_sort_noalloc(float* val_d, int32_t* row_d, int32_t* col_d,
+                                  int64_t n, epet_stream_t stream);
 /* convertCoo2Csr (cusparseWrapper.hpp:38-45): row pointer of row-sorted COO. */
 epet_status epet_coo2csr(const int32_t* row_d, int64_t nnz, int64_t m,
                          int64_t* csr_d, epet_stream_t stream);
