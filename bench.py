@@ -48,6 +48,10 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--profile", action="store_true",
                     help="one reconstruction with one iteration, nothing else (for ncu)")
+    ap.add_argument("--profile-kernels", type=int, default=0, metavar="ROWS",
+                    help="build the matrix of the first ROWS channels of the workload, its "
+                         "column-major copy, one forward and one transpose product (small "
+                         "case for full ncu captures)")
     return ap.parse_args()
 
 
@@ -192,6 +196,18 @@ def gb300_arm(args):
     cfg = config(args.config)
     p, nit, counts = cfg["problem"], cfg["iterations"], cfg["counts"]
     L = lib()
+
+    if args.profile_kernels:
+        rows = torch.arange(args.profile_kernels, dtype=torch.int32, device="cuda")
+        A = api.systemMatrixCalculation(p, rows)
+        At = api.csr_to_csc(A)
+        x = torch.full((p.nvoxels,), 1.0 / p.nvoxels, device="cuda")
+        e = torch.rand(rows.numel(), device="cuda")
+        api.CSRmv(0, A, x)
+        api.CSRmv(1, A, e, At=At)
+        torch.cuda.synchronize()
+        print(json.dumps({"profile_kernels": args.profile_kernels, "nnz": A.nnz}))
+        return
 
     # ---- inputs (not timed): measurement and sensitivity
     rows, y, _ = phantom.measurement(p, counts)

@@ -47,6 +47,12 @@ class CscC(C.Structure):
                 ("col_ptr", C.c_void_p), ("row", C.c_void_p), ("val", C.c_void_p)]
 
 
+class Csr16C(C.Structure):
+    _fields_ = [("m", C.c_int64), ("n", C.c_int64), ("nnz", C.c_int64),
+                ("row_ptr", C.c_void_p), ("base", C.c_void_p), ("scale", C.c_void_p),
+                ("delta", C.c_void_p), ("q", C.c_void_p), ("format", C.c_int32)]
+
+
 class MlemOptions(C.Structure):
     _fields_ = [("max_row_nnz", C.c_int32), ("use_graph", C.c_int32),
                 ("value_format", C.c_int32), ("reserved", C.c_int32)]
@@ -80,6 +86,9 @@ SIGNATURES = {
     "epet_csr2ecsr": [VP, VP, I64, VP, I64, VP],
     "epet_csr_to_csc": [C.POINTER(CsrC), C.POINTER(CscC), VP, SZ, VP],
     "epet_csr_to_csc_workspace_size": [I64, I64, I64],
+    "epet_csr16_count": [C.POINTER(CsrC), VP, C.POINTER(C.c_int64), VP],
+    "epet_csr_compress": [C.POINTER(CsrC), I32, C.POINTER(Csr16C), VP],
+    "epet_csr16_mv": [C.POINTER(Csr16C), F, VP, F, VP, VP],
     "epet_csrmv": [C.c_int, C.POINTER(CsrC), C.POINTER(CscC), F, VP, F, VP, VP],
     "epet_divides": [VP, VP, VP, I64, VP],
     "epet_divides_multiplies": [VP, VP, VP, VP, I64, VP],

@@ -26,6 +26,7 @@ struct epet_mlem {
   float* ybar = nullptr;  // last forward projection
   epet_csr A{};
   epet_csc At{};
+  epet_csr16 A16{}, At16{};  // 16-bit forms (value_format != FP32)
   int64_t capA = 0;
   double *part_ll = nullptr, *part_x = nullptr, *sums = nullptr;
   int64_t nb_fwd = 0, nb_bwd = 0;
@@ -46,7 +47,9 @@ static void mlem_free(epet_mlem* h) {
   if (!h) return;
   if (h->exec) cudaGraphExecDestroy(h->exec);
   if (h->graph) cudaGraphDestroy(h->graph);
-  void* bufs[] = {h->rows, h->y, h->ybar, h->s, h->x, h->xnew, h->e, h->A.row_ptr, h->A.col,
+  void* bufs[] = {h->A16.row_ptr, h->A16.base, h->A16.scale, h->A16.delta, h->A16.q,
+                  h->At16.row_ptr, h->At16.base, h->At16.scale, h->At16.delta, h->At16.q,
+                  h->rows, h->y, h->ybar, h->s, h->x, h->xnew, h->e, h->A.row_ptr, h->A.col,
                   h->A.val,
                   h->At.col_ptr, h->At.row, h->At.val, h->part_ll, h->part_x, h->sums};
   for (void* b : bufs)
@@ -55,6 +58,14 @@ static void mlem_free(epet_mlem* h) {
 }
 
 static epet_status mlem_iteration(epet_mlem* h, cudaStream_t st) {
+  if (h->opt.value_format != EPET_VALUES_FP32) {
+    EPET_CHECK(launch_rows16(&h->A16, h->x, EpiMlemForward{h->y, h->e, h->ybar}, nullptr, st));
+    EPET_CHECK(launch_rows16(&h->At16, h->e, EpiMlemUpdate{h->x, h->s, h->xnew, nullptr},
+                             h->part_x, st));
+    EPET_CHECK(launch_sum_partials(h->part_x, h->nb_bwd, h->sums + 1, st));
+    EPET_CHECK(launch_normalise(h->xnew, h->sums + 1, h->V, h->x, st));
+    return EPET_OK;
+  }
   EPET_CHECK(launch_rows(h->g_fwd, h->A.row_ptr, h->A.col, h->A.val, h->x, h->m,
                          EpiMlemForward{h->y, h->e, h->ybar}, nullptr, st, nullptr));
   EPET_CHECK(launch_rows(h->g_bwd, h->At.col_ptr, h->At.row, h->At.val, h->e, h->V,
@@ -84,9 +95,9 @@ epet_status epet_mlem_create(const epet_problem* p, const int32_t* rows_d, const
     return set_error(EPET_ERR_INVALID, "bad arguments");
   epet_mlem_options o{};
   if (opt) o = *opt;
-  if (o.value_format != 0)
-    return set_error(EPET_ERR_UNSUPPORTED, "value_format %d not supported by this driver",
-                     o.value_format);
+  if (o.value_format != EPET_VALUES_FP32 && o.value_format != EPET_VALUES_BF16 &&
+      o.value_format != EPET_VALUES_FP16)
+    return set_error(EPET_ERR_INVALID, "value_format %d", o.value_format);
   cudaStream_t st = (cudaStream_t)stream;
   epet_mlem* h = new epet_mlem();
   h->p = *p;
@@ -140,10 +151,42 @@ epet_status epet_mlem_create(const epet_problem* p, const int32_t* rows_d, const
   ALLOC(h->At.val, nnz * 4);
   rc = epet_csr_to_csc(&h->A, &h->At, nullptr, 0, stream);
   if (rc != EPET_OK) return fail(rc);
+  if (o.value_format != EPET_VALUES_FP32) {
+    // 16-bit forms of A and A^T (the column-major copy viewed as A^T's CSR);
+    // the 32-bit arrays are released afterwards
+    epet_csr At_as_csr{V, m, nnz, h->At.col_ptr, h->At.row, h->At.val};
+    struct {
+      const epet_csr* src;
+      epet_csr16* dst;
+      int64_t rows;
+    } jobs[2] = {{&h->A, &h->A16, m}, {&At_as_csr, &h->At16, V}};
+    for (auto& j : jobs) {
+      int64_t* cnt = nullptr;
+      ALLOC(cnt, (j.rows + 1) * 8);
+      int64_t n16 = 0;
+      rc = epet_csr16_count(j.src, cnt, &n16, stream);
+      cudaFree(cnt);
+      if (rc != EPET_OK) return fail(rc);
+      ALLOC(j.dst->row_ptr, (j.rows + 1) * 8);
+      ALLOC(j.dst->base, j.rows * 4);
+      ALLOC(j.dst->scale, j.rows * 4);
+      ALLOC(j.dst->delta, csr16_capacity(n16) * 2);
+      ALLOC(j.dst->q, csr16_capacity(n16) * 2);
+      j.dst->nnz = csr16_capacity(n16);
+      rc = epet_csr_compress(j.src, o.value_format, j.dst, stream);
+      if (rc != EPET_OK) return fail(rc);
+    }
+    EPET_CUDA(cudaStreamSynchronize(st));
+    cudaFree(h->A.col); h->A.col = nullptr;
+    cudaFree(h->A.val); h->A.val = nullptr;
+    cudaFree(h->At.row); h->At.row = nullptr;
+    cudaFree(h->At.val); h->At.val = nullptr;
+  }
   h->g_fwd = pick_group(m ? (double)nnz / m : 0.0);
   h->g_bwd = pick_group(V ? (double)nnz / V : 0.0);
   h->nb_fwd = (m + kSpmvThreads / h->g_fwd - 1) / (kSpmvThreads / h->g_fwd);
   h->nb_bwd = (V + kSpmvThreads / h->g_bwd - 1) / (kSpmvThreads / h->g_bwd);
+  if (o.value_format != EPET_VALUES_FP32) h->nb_bwd = rows16_blocks(&h->At16);
   ALLOC(h->part_ll, 1024 * 8);
   ALLOC(h->part_x, std::max<int64_t>(h->nb_bwd, 1) * 8);
 #undef ALLOC
@@ -218,7 +261,12 @@ epet_status epet_mlem_set_image(epet_mlem* h, const float* x_d, epet_stream_t st
 epet_status epet_mlem_stats(const epet_mlem* h, int64_t* nnz_h, int64_t* bytes_h) {
   if (!h) return set_error(EPET_ERR_INVALID, "bad arguments");
   if (nnz_h) *nnz_h = h->A.nnz;
-  if (bytes_h) {
+  if (bytes_h && h->opt.value_format != EPET_VALUES_FP32) {
+    // 4 bytes per stored entry; per row pointer + base + scale 16 bytes
+    const int64_t m = h->m, V = h->V;
+    *bytes_h = 4 * h->A16.nnz + 16 * m + 4 * V + 4 * m + 4 * m + 4 * h->At16.nnz + 16 * V +
+               4 * m + 4 * V + 4 * V + 4 * V + 4 * V + 4 * V;
+  } else if (bytes_h) {
     // forward: values+columns, row pointers, y, x (once), e written;
     // transpose: values+rows, column pointers, e (once), x, s, xnew written;
     // sum/normalise: xnew read, x written.

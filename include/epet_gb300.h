@@ -80,6 +80,26 @@ typedef struct {
   float* val;       /* nnz, device */
 } epet_csr;
 
+/* 16-bit storage of a CSR (value_format 1 = BF16, 2 = FP16): 4 bytes per
+ * entry.  Row r: col_k = base[r] + delta_0 + ... + delta_k (delta_0 = 0),
+ * value_k = scale[r] * q_k (scale = the row's largest value).  Steps wider
+ * than 65535 are split by zero-valued entries.  delta and q are read with
+ * 16-byte loads: 16-byte aligned, with room for nnz + 8 entries
+ * (epet_csr16_capacity). */
+#define EPET_VALUES_FP32 0
+#define EPET_VALUES_BF16 1
+#define EPET_VALUES_FP16 2
+typedef struct {
+  int64_t m, n;
+  int64_t nnz;       /* in: capacity of delta/q; out: stored entries */
+  int64_t* row_ptr;  /* m+1 */
+  int32_t* base;     /* m */
+  float* scale;      /* m */
+  uint16_t* delta;
+  uint16_t* q;
+  int32_t format;
+} epet_csr16;
+
 /* Column-major copy of an epet_csr: col_ptr[n+1], row ids ascending within a
  * column (used by the scatter-free back-projection). */
 typedef struct {
@@ -213,6 +233,18 @@ epet_status epet_csrmv(int trans, const epet_csr* a, const epet_csc* csc,
                        float alpha, const float* x_d, float beta, float* y_d,
                        epet_stream_t stream);
 
+/* 16-bit layout: per-row stored-entry counts (row_len16_d[m]) and their
+ * total; the CSR must have ascending columns within rows. */
+epet_status epet_csr16_count(const epet_csr* a, int64_t* row_len16_d,
+                             int64_t* nnz16_h, epet_stream_t stream);
+/* Converts a CSR (or, given a column-major copy viewed as the CSR of A^T,
+ * the transpose) into the 16-bit layout; out->nnz = capacity on input. */
+epet_status epet_csr_compress(const epet_csr* a, int32_t format, epet_csr16* out,
+                              epet_stream_t stream);
+/* y = alpha * A x + beta * y over the 16-bit layout (FP32 accumulation). */
+epet_status epet_csr16_mv(const epet_csr16* a, float alpha, const float* x_d,
+                          float beta, float* y_d, epet_stream_t stream);
+
 /* -------------------------------------------------- MLEM element-wise ops */
 /* divides (mlemOperations.hpp:22-32): r = a / b, no guard (as reference). */
 epet_status epet_divides(float* r_d, const float* a_d, const float* b_d,
@@ -265,7 +297,7 @@ typedef struct epet_mlem epet_mlem;
 typedef struct {
   int32_t max_row_nnz; /* 0 = auto */
   int32_t use_graph;   /* capture one iteration in a CUDA graph */
-  int32_t value_format; /* 0 = fp32 values; 1 = bf16 + row scale; 2 = fp16 + row scale */
+  int32_t value_format; /* EPET_VALUES_FP32 / _BF16 / _FP16 (16-bit values + row scale) */
   int32_t reserved;
 } epet_mlem_options;
 
