@@ -57,10 +57,62 @@ def _compile(src: str) -> str:
     return obj
 
 
+def _torch_flags():
+    import sysconfig
+
+    import torch
+    tdir = os.path.dirname(torch.__file__)
+    inc = [os.path.join(tdir, "include"), os.path.join(tdir, "include", "torch", "csrc", "api",
+                                                       "include"),
+           sysconfig.get_paths()["include"], os.path.join(ROOT, "include"),
+           os.path.join(os.path.dirname(cuda_libdir()), "include")]
+    abi = int(torch._C._GLIBCXX_USE_CXX11_ABI)
+    cflags = ["-O2", "-std=c++17", "-fPIC", f"-D_GLIBCXX_USE_CXX11_ABI={abi}",
+              "-DTORCH_EXTENSION_NAME=_autograd", "-DTORCH_API_INCLUDE_EXTENSION_H",
+              "-Wno-deprecated-declarations"] + ["-I" + d for d in inc]
+    libdir = os.path.join(tdir, "lib")
+    ldflags = ["-L" + libdir, "-lc10", "-lc10_cuda", "-ltorch", "-ltorch_cpu", "-ltorch_cuda",
+               "-ltorch_python", "-L" + PKG, "-lepet_gb300", "-L" + cuda_libdir(), "-lcudart",
+               "-Wl,-rpath," + libdir, "-Wl,-rpath,$ORIGIN", "-Wl,-rpath," + cuda_libdir()]
+    return cflags, ldflags
+
+
+def autograd_path() -> str:
+    import sysconfig
+    return os.path.join(PKG, "_autograd" + sysconfig.get_config_var("EXT_SUFFIX"))
+
+
+def _compile_autograd() -> str:
+    src = os.path.join(CSRC, "autograd.cpp")
+    obj = os.path.join(BUILD, "autograd.o")
+    deps = [src, os.path.join(ROOT, "include", "epet_gb300.h")]
+    if os.path.exists(obj) and os.path.getmtime(obj) >= max(map(os.path.getmtime, deps)):
+        return obj
+    cflags, _ = _torch_flags()
+    r = subprocess.run(["g++"] + cflags + ["-c", src, "-o", obj], capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"autograd extension compile failed:\n{r.stderr[-4000:]}")
+    return obj
+
+
+def _link_autograd(obj: str) -> None:
+    out = autograd_path()
+    if os.path.exists(out) and os.path.getmtime(out) >= max(os.path.getmtime(obj),
+                                                           os.path.getmtime(LIB)):
+        return
+    _, ldflags = _torch_flags()
+    r = subprocess.run(["g++", "-shared", obj, "-o", out] + ldflags, capture_output=True,
+                       text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"autograd extension link failed:\n{r.stderr[-4000:]}")
+
+
 def build(verbose: bool = False) -> str:
     os.makedirs(BUILD, exist_ok=True)
     with cf.ThreadPoolExecutor(max_workers=min(8, os.cpu_count() or 4)) as ex:
+        ag = ex.submit(_compile_autograd)
         objs = list(ex.map(_compile, SOURCES))
+        ag_obj = ag.result()
     if not os.path.exists(LIB) or os.path.getmtime(LIB) < max(map(os.path.getmtime, objs)):
         # shared CUDA runtime: in a process that already loaded one (torch),
         # the loader reuses it, so there is a single runtime instance
@@ -71,6 +123,7 @@ def build(verbose: bool = False) -> str:
         if r.returncode != 0:
             raise RuntimeError(f"link failed:\n{r.stderr}")
     _build_driver()
+    _link_autograd(ag_obj)
     if verbose:
         print(LIB)
     return LIB

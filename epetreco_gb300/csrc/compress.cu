@@ -209,6 +209,8 @@ template <class Epi>
 epet_status launch_rows16(const epet_csr16* a, const float* x, Epi epi, double* partial,
                           cudaStream_t st) {
   if (a->m <= 0) return EPET_OK;
+  if (((reinterpret_cast<uintptr_t>(a->delta) | reinterpret_cast<uintptr_t>(a->q)) & 15) != 0)
+    return set_error(EPET_ERR_INVALID, "16-bit matrix: delta and q must be 16-byte aligned");
   const int G = pick_group16(a->m ? (double)a->nnz / a->m : 0.0);
   if (a->format == EPET_VALUES_BF16) return launch16_fmt<1>(G, a, x, epi, partial, st);
   if (a->format == EPET_VALUES_FP16) return launch16_fmt<2>(G, a, x, epi, partial, st);

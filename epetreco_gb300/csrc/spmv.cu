@@ -23,12 +23,13 @@ namespace epet {
 __device__ __forceinline__ float ld_stream(const float* p) { return __ldcs(p); }
 __device__ __forceinline__ int ld_stream(const int32_t* p) { return __ldcs(p); }
 
-// Dot product of row [beg, end) with x by a group of G lanes.
+// Dot product of row [beg, end) with x by a group of G lanes, element-wise
+// loads (any alignment of idx / val).
 template <int G>
-__device__ __forceinline__ float group_dot(const int32_t* __restrict__ idx,
-                                           const float* __restrict__ val,
-                                           const float* __restrict__ x, int64_t beg,
-                                           int64_t end, int lg) {
+__device__ __forceinline__ float group_dot_scalar(const int32_t* __restrict__ idx,
+                                                  const float* __restrict__ val,
+                                                  const float* __restrict__ x, int64_t beg,
+                                                  int64_t end, int lg) {
   float a0 = 0.f, a1 = 0.f, a2 = 0.f, a3 = 0.f;
   int64_t k = beg + lg;
   for (; k + 3 * G < end; k += 4 * G) {
@@ -48,9 +49,53 @@ __device__ __forceinline__ float group_dot(const int32_t* __restrict__ idx,
   return a;
 }
 
+// The same with 16-byte loads; idx and val must be 16-byte aligned.  Lane l
+// reads 4-entry chunks at 16-byte boundaries (float4 / int4 loads), two
+// chunks per round so 64 bytes per lane are in flight; entries outside
+// [beg, end) are masked; the last partial chunk of a row is read
+// element-wise (the arrays may end there).
+template <int G>
+__device__ __forceinline__ float group_dot_vec(const int32_t* __restrict__ idx,
+                                           const float* __restrict__ val,
+                                           const float* __restrict__ x, int64_t beg,
+                                           int64_t end, int lg) {
+  float a0 = 0.f, a1 = 0.f;
+  const int64_t a_beg = beg & ~int64_t(3);
+  auto chunk = [&](int64_t k, float& acc) {
+    if (k + 3 < end) {
+      const float4 v = __ldcs(reinterpret_cast<const float4*>(val + k));
+      const int4 c = __ldcs(reinterpret_cast<const int4*>(idx + k));
+      if (k >= beg) {
+        acc = fmaf(v.x, __ldg(x + c.x), acc);
+        acc = fmaf(v.y, __ldg(x + c.y), acc);
+        acc = fmaf(v.z, __ldg(x + c.z), acc);
+        acc = fmaf(v.w, __ldg(x + c.w), acc);
+      } else {  // first chunk of the row starts before beg
+        if (k + 0 >= beg) acc = fmaf(v.x, __ldg(x + c.x), acc);
+        if (k + 1 >= beg) acc = fmaf(v.y, __ldg(x + c.y), acc);
+        if (k + 2 >= beg) acc = fmaf(v.z, __ldg(x + c.z), acc);
+        acc = fmaf(v.w, __ldg(x + c.w), acc);
+      }
+    } else {
+      for (int j = 0; j < 4; j++) {
+        const int64_t kj = k + j;
+        if (kj >= beg && kj < end) acc = fmaf(ld_stream(val + kj), __ldg(x + ld_stream(idx + kj)), acc);
+      }
+    }
+  };
+  for (int64_t k = a_beg + 4 * lg; k < end; k += 8 * G) {
+    chunk(k, a0);
+    if (k + 4 * G < end) chunk(k + 4 * G, a1);
+  }
+  float a = a0 + a1;
+#pragma unroll
+  for (int o = G / 2; o > 0; o >>= 1) a += __shfl_xor_sync(0xffffffffu, a, o, G);
+  return a;
+}
+
 // Generic row kernel: out = Epi(row, dot).  Block reduces Epi's fp64 partial
 // (when used) into partial[blockIdx.x].
-template <int G, class Epi>
+template <int G, bool VEC, class Epi>
 __global__ void __launch_bounds__(kSpmvThreads)
 k_rows(const int64_t* __restrict__ ptr, const int32_t* __restrict__ idx,
        const float* __restrict__ val, const float* __restrict__ x, int64_t nrows, Epi epi,
@@ -61,7 +106,8 @@ k_rows(const int64_t* __restrict__ ptr, const int32_t* __restrict__ idx,
   const int64_t row = (int64_t)blockIdx.x * RPB + threadIdx.x / G;
   double part = 0.0;
   if (row < nrows) {
-    const float d = group_dot<G>(idx, val, x, ptr[row], ptr[row + 1], lg);
+    const float d = VEC ? group_dot_vec<G>(idx, val, x, ptr[row], ptr[row + 1], lg)
+                        : group_dot_scalar<G>(idx, val, x, ptr[row], ptr[row + 1], lg);
     if (lg == 0) part = epi(row, d);
   }
   if (partial) {
@@ -120,12 +166,17 @@ epet_status launch_rows(int G, const int64_t* ptr, const int32_t* idx, const flo
   const int rpb = kSpmvThreads / G;
   const int64_t nb = (nrows + rpb - 1) / rpb;
   if (nblocks_out) *nblocks_out = nb;
+  // 16-byte loads only when both streams start on a 16-byte boundary
+  const bool vec = ((reinterpret_cast<uintptr_t>(idx) | reinterpret_cast<uintptr_t>(val)) & 15) == 0;
+#define EPET_ROWS(GG, V) \
+  k_rows<GG, V, Epi><<<(unsigned)nb, kSpmvThreads, 0, st>>>(ptr, idx, val, x, nrows, epi, partial)
   switch (G) {
-    case 32: k_rows<32, Epi><<<(unsigned)nb, kSpmvThreads, 0, st>>>(ptr, idx, val, x, nrows, epi, partial); break;
-    case 16: k_rows<16, Epi><<<(unsigned)nb, kSpmvThreads, 0, st>>>(ptr, idx, val, x, nrows, epi, partial); break;
-    case 8: k_rows<8, Epi><<<(unsigned)nb, kSpmvThreads, 0, st>>>(ptr, idx, val, x, nrows, epi, partial); break;
-    default: k_rows<4, Epi><<<(unsigned)nb, kSpmvThreads, 0, st>>>(ptr, idx, val, x, nrows, epi, partial); break;
+    case 32: if (vec) EPET_ROWS(32, true); else EPET_ROWS(32, false); break;
+    case 16: if (vec) EPET_ROWS(16, true); else EPET_ROWS(16, false); break;
+    case 8: if (vec) EPET_ROWS(8, true); else EPET_ROWS(8, false); break;
+    default: if (vec) EPET_ROWS(4, true); else EPET_ROWS(4, false); break;
   }
+#undef EPET_ROWS
   EPET_LAUNCHED();
   return EPET_OK;
 }

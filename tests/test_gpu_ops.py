@@ -224,3 +224,35 @@ def test_sensitivity_matches_oracle(small_recon, oracle):
     rp, col, val = (t.cpu().numpy() for t in (A.row_ptr, A.col, A.val))
     so = oracle.sensitivity(rp, col, val, p.nvoxels)
     assert np.allclose(s.cpu().numpy(), so, rtol=1e-5, atol=1e-12)
+
+
+@pytest.mark.parametrize("offset", [0, 1, 3])
+def test_csrmv_ragged_rows_any_alignment(gpu_lib, oracle, offset):
+    """Rows of every length from 0 up (starts at every residue mod 4), with the
+    value and column streams starting 0, 4 or 12 bytes past a 16-byte boundary
+    (the aligned form uses 16-byte loads, the others element loads)."""
+    import ctypes as C
+    from epetreco_gb300._lib import CscC, CsrC, check, lib
+    rng = np.random.default_rng(31 + offset)
+    n = 5000
+    lens = np.concatenate([np.arange(0, 70), rng.integers(0, 400, 900), [0, 1, 2, 3, 5000]])
+    rng.shuffle(lens)
+    rp = np.concatenate([[0], np.cumsum(lens)]).astype(np.int64)
+    nnz = int(rp[-1])
+    col = np.concatenate([np.sort(rng.choice(n, l, replace=False)) for l in lens]).astype(np.int32)
+    val = rng.random(nnz).astype(np.float32)
+    x = rng.random(n).astype(np.float32)
+    col_d = dev(np.concatenate([np.zeros(offset, np.int32), col]))
+    val_d = dev(np.concatenate([np.zeros(offset, np.float32), val]))
+    rp_d = dev(rp)
+    a = CsrC(len(lens), n, nnz, rp_d.data_ptr(), col_d.data_ptr() + 4 * offset,
+             val_d.data_ptr() + 4 * offset)
+    y = torch.zeros(len(lens), device="cuda")
+    st = C.c_void_p(torch.cuda.current_stream().cuda_stream)
+    check(lib().epet_csrmv(0, C.byref(a), None, 1.0, C.c_void_p(dev(x).data_ptr()), 0.0,
+                           C.c_void_p(y.data_ptr()), st))
+    yo = oracle.csrmv_f64(0, rp, col, val, x.astype(np.float64), n)
+    got = y.cpu().numpy()
+    assert (got[lens == 0] == 0).all()
+    nz = lens > 0
+    assert np.abs(got[nz] - yo[nz]).max() <= 1e-5 * np.abs(yo[nz]).max()

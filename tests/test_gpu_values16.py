@@ -142,3 +142,16 @@ def test_mlem_16bit_within_1e3_of_fp64(gpu_lib, oracle, fmt):
     assert err <= 1e-3, err
     st = R.stats()
     assert st["bytes_per_iteration"] < 0.6 * 16 * st["nnz"]
+
+
+def test_unaligned_16bit_streams_are_rejected(gpu_lib):
+    rp = np.array([0, 3], np.int64)
+    col = np.array([1, 2, 9], np.int32)
+    val = np.array([1.0, 2.0, 3.0], np.float32)
+    c16, out, _ = compress(rp, col, val, 10, 1)
+    c16.q = out["q"].data_ptr() + 2
+    y = torch.zeros(1, device="cuda")
+    x = torch.ones(10, device="cuda")
+    st = lib().epet_csr16_mv(C.byref(c16), 1.0, C.c_void_p(x.data_ptr()), 0.0,
+                             C.c_void_p(y.data_ptr()), stream())
+    assert st != 0 and b"aligned" in lib().epet_last_error()
