@@ -46,6 +46,14 @@ def parse():
     ap.add_argument("--cpu-sample", type=int, default=4096,
                     help="channels in the CPU-baseline sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--batch", type=int, default=64, metavar="N",
+                    help="problems of the batched-reconstruction measurement (0: skip)")
+    ap.add_argument("--batch-gb", type=float, default=160.0,
+                    help="device memory budget of the batched problems' matrices")
+    ap.add_argument("--batch-only", action="store_true",
+                    help="run only the batched-reconstruction measurement")
+    ap.add_argument("--no-forms", action="store_true",
+                    help="skip the 16-bit value forms")
     ap.add_argument("--profile", action="store_true",
                     help="one reconstruction with one iteration, nothing else (for ncu)")
     ap.add_argument("--profile-kernels", type=int, default=0, metavar="ROWS",
@@ -176,6 +184,94 @@ def reference_arm(args):
 
 # ------------------------------------------------------------------ GB300
 
+def batch_measure(args, api, torch, st, nit: int = 10):
+    """Batched form: args.batch seeded problems of uneven size (grids and
+    angle counts drawn from the batched workload's sets), each with its own
+    phantom and Poisson measurement.  Times nit iterations of all problems
+    through the batched launches (one CUDA graph per iteration) against the
+    same problems iterated one after another with the plain per-problem
+    driver (its own graph per problem), on the same device arrays."""
+    from epetreco_gb300.phantom import measurement, phantom_image
+    from epetreco_gb300.problem import batch_members
+    torch.cuda.empty_cache()
+    t0 = time.perf_counter()
+    members = batch_members(args.batch)
+    # The drawn problems' matrices together exceed the device memory (tens of
+    # GB each at 52^3-64^3 x 180 angles): problems are taken in draw order
+    # while the estimated CSR + CSC bytes (16 per non-zero; non-zeros per row
+    # from 512 sampled measured rows) fit the budget.
+    free, _ = torch.cuda.mem_get_info()
+    budget = min(args.batch_gb * 1e9, 0.6 * free)
+    probs, used, skipped = [], 0.0, 0
+    for b in members:
+        q = b.problem
+        rows, y, _ = measurement(q, b.counts, seed=b.poisson_seed,
+                                 x_true=phantom_image(q, b.phantom_seed, b.n_spheres))
+        m = rows.numel()
+        smp = rows[torch.linspace(0, max(m - 1, 0), min(m, 512), device=rows.device).long()]
+        est = 0.0
+        if m:
+            est = 16.0 * api.systemMatrixCalculation(q, smp).nnz / smp.numel() * m
+        if used + est > budget:
+            skipped += 1
+            continue
+        used += est
+        probs.append((q, rows, y, api.sensitivity(q)))
+    torch.cuda.synchronize()
+    t_data = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    B = api.MlemBatch(probs, use_graph=True, autotune=True)
+    torch.cuda.synchronize()
+    t_create = time.perf_counter() - t0
+    stats = B.stats()
+    views = [B.member(i) for i in range(len(probs))]
+    B.iterate(1)
+    for v in views:
+        v.iterate(1)
+    torch.cuda.synchronize()
+
+    def timed(fn, reps=3):
+        a = torch.cuda.Event(enable_timing=True)
+        b = torch.cuda.Event(enable_timing=True)
+        a.record(st)
+        for _ in range(reps):
+            fn()
+        b.record(st)
+        torch.cuda.synchronize()
+        return a.elapsed_time(b) / 1000.0 / reps
+
+    def seq():
+        for v in views:
+            v.iterate(nit)
+
+    t_batch = timed(lambda: B.iterate(nit))
+    t_seq = timed(seq)
+    peaks = {}
+    try:
+        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except Exception:
+        pass
+    peak = peaks.get("hbm_gbs", 6800.0)
+    gbs = stats["bytes_per_iteration"] * nit / t_batch / 1e9
+    out = {"problems": len(probs), "drawn": len(members), "skipped_for_memory": skipped,
+           "iterations": nit,
+           "workload": (f"{len(members)} seeded draws (grids {{24,32,40,52,64}}^3, angles "
+                        f"{{8,30,60,120,180}}, 20-100 rays, 1e5-1e8 counts, FP32 values); "
+                        f"the {len(probs)} whose matrices fit {budget / 1e9:.0f} GB, in draw "
+                        f"order"),
+           "grids": [q.grid.n[0] for q, *_ in probs], "angles": [q.setup.na for q, *_ in probs],
+           "measured_rows": int(sum(r.numel() for _, r, _, _ in probs)),
+           "nnz": stats["nnz"], "plan": stats["plan"],
+           "batched_ms": 1000 * t_batch, "sequential_plain_ms": 1000 * t_seq,
+           "speedup_vs_plain": t_seq / t_batch,
+           "problem_iterations_per_s": len(probs) * nit / t_batch,
+           "gbs": gbs, "frac_of_hbm_peak": gbs / peak,
+           "setup_s": {"data": t_data, "create": t_create}}
+    del views
+    B.close()
+    return out
+
+
 def gb300_arm(args):
     import numpy as np
     import torch
@@ -209,6 +305,11 @@ def gb300_arm(args):
         print(json.dumps({"profile_kernels": args.profile_kernels, "nnz": A.nnz}))
         return
 
+    if args.batch_only:
+        print(json.dumps({"batched": batch_measure(args, api, torch,
+                                                   torch.cuda.current_stream())}), flush=True)
+        return
+
     # ---- inputs (not timed): measurement and sensitivity
     rows, y, _ = phantom.measurement(p, counts)
     s = api.sensitivity(p)
@@ -220,9 +321,19 @@ def gb300_arm(args):
     x_h = torch.empty(p.nvoxels, dtype=torch.float32).pin_memory()
     st = torch.cuda.current_stream()
 
-    def step(r, yy, ss):
-        R = api.Mlem(p, r, yy, ss, use_graph=True)
-        R.iterate(nit)
+    it_events = []
+
+    def step(r, yy, ss, record=False):
+        R = api.Mlem(p, r, yy, ss, use_graph=True, autotune=True)
+        if record:
+            a = torch.cuda.Event(enable_timing=True)
+            b = torch.cuda.Event(enable_timing=True)
+            a.record(st)
+            R.iterate(nit)
+            b.record(st)
+            it_events.append((a, b))
+        else:
+            R.iterate(nit)
         return R
 
     def barrier():
@@ -252,13 +363,15 @@ def gb300_arm(args):
     barrier()
     ev0.record(st)
     for _ in range(args.steps):
-        R = step(rows, y, s)
+        R = step(rows, y, s, record=True)
         R.close()
     ev1.record(st)
     barrier()
     launches = (L.epet_launch_count() - n0) // args.steps
     t_step = ev0.elapsed_time(ev1) / 1000.0 / args.steps
     clocks = clk.stop()
+    # MLEM iterations inside the timed steps (CUDA events on the launch stream)
+    t_it_live = sum(a.elapsed_time(b) for a, b in it_events) / 1000.0 / (args.steps * nit)
 
     # ---- e2e: host buffers through the public API
     e0 = torch.cuda.Event(enable_timing=True)
@@ -276,10 +389,13 @@ def gb300_arm(args):
     barrier()
     t_e2e = e0.elapsed_time(e1) / 1000.0 / args.steps
 
-    # ---- breakdown and roofline of the dominant kernels (not timed above)
-    R = api.Mlem(p, rows, y, s, use_graph=False)
+    # ---- breakdown of the step's parts and the product kernels (after the
+    # timed region, same stream)
+    R = api.Mlem(p, rows, y, s, use_graph=True, autotune=True)
     stats = R.stats()
+    plan = R.plan()
     nnz = stats["nnz"]
+    bytes_it = stats["bytes_per_iteration"]
     A = api.systemMatrixCalculation(p, rows, cap=nnz)
     torch.cuda.synchronize()
 
@@ -303,7 +419,7 @@ def gb300_arm(args):
     t_fwd = timeit(lambda: api.CSRmv(0, A, x), reps=5)
     t_bwd = timeit(lambda: api.CSRmv(1, A, e, At=At), reps=5)
     t_iter = timeit(lambda: R.iterate(1), reps=5)
-    R.close()
+    del A, At
     peaks = {}
     try:
         peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
@@ -313,16 +429,41 @@ def gb300_arm(args):
     peak_src = "measured" if "hbm_gbs" in peaks else "fallback"
     fwd_bytes = 8 * nnz + 8 * (m + 1) + 4 * p.nvoxels + 4 * m
     bwd_bytes = 8 * nnz + 8 * (p.nvoxels + 1) + 4 * m + 4 * p.nvoxels
-    dominant = "spmv_transpose" if t_bwd >= t_fwd else "spmv_forward"
-    d_bytes, d_t = (bwd_bytes, t_bwd) if t_bwd >= t_fwd else (fwd_bytes, t_fwd)
-    achieved = d_bytes / d_t / 1e9
+    # roofline of the MLEM iteration (forward + transpose products with their
+    # fused epilogues, image sum, normalisation): algorithmic bytes per
+    # iteration over the iteration time measured inside the timed steps
+    achieved = bytes_it / t_it_live / 1e9
     traffic = None
     tp = os.path.join(ROOT, "profiles", "traffic_full.json")
     if os.path.exists(tp):
         try:
-            traffic = json.load(open(tp)).get(dominant)
+            traffic = json.load(open(tp)).get("mlem_iteration")
         except Exception:
             traffic = None
+
+    # ---- 16-bit value forms: iteration speed and image error vs FP32
+    forms = None
+    if not args.no_forms:
+        R.iterate(nit - 6)  # 1 + 5 iterations ran in timeit
+        x32 = R.image()
+        forms = {"fp32": {"iteration_ms": 1000 * t_iter, "it_per_s": 1.0 / t_iter},
+                 "iterations": nit}
+        for name, fmt in (("bf16", 1), ("fp16", 2)):
+            R16 = api.Mlem(p, rows, y, s, use_graph=True, value_format=fmt)
+            t16 = timeit(lambda: R16.iterate(1), reps=5)
+            R16.iterate(nit - 6)
+            x16 = R16.image()
+            err = float(((x16 - x32).double().norm() / x32.double().norm()).item())
+            st16 = R16.stats()
+            forms[name] = {"iteration_ms": 1000 * t16, "it_per_s": 1.0 / t16,
+                           "speedup_vs_fp32": t_iter / t16,
+                           "bytes_per_iteration": st16["bytes_per_iteration"],
+                           "image_rel_l2_vs_fp32": err}
+            R16.close()
+    R.close()
+    batched = None
+    if args.batch > 0 and world == 1:
+        batched = batch_measure(args, api, torch, st)
 
     # ---- aggregate over ranks
     vals = torch.tensor([t_step, t_e2e], device="cuda", dtype=torch.float64)
@@ -353,15 +494,22 @@ def gb300_arm(args):
                 "d2h_bytes_per_step": d2h},
         "gpu_launches": int(launches),
         "clocks": clocks,
-        "roofline": {"bound": "hbm", "kernel": dominant, "achieved": achieved, "peak": peak,
-                     "unit": "GB/s", "frac": achieved / peak, "traffic": traffic,
-                     "peak_source": peak_src, "algorithmic_bytes": d_bytes},
+        "roofline": {"bound": "hbm", "kernel": "mlem_iteration (spmv forward + transpose, "
+                                               "fused epilogues)",
+                     "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                     "traffic": traffic, "peak_source": peak_src,
+                     "algorithmic_bytes": bytes_it, "iteration_ms": 1000 * t_it_live},
         "breakdown_ms": {"sm_build": 1000 * t_build, "csc": 1000 * t_csc,
                          "spmv_forward": 1000 * t_fwd, "spmv_transpose": 1000 * t_bwd,
                          "iteration": 1000 * t_iter},
+        "plan": plan,
         "sm_build_nnz_per_s": nnz / t_build,
         "spmv_gbs": {"forward": fwd_bytes / t_fwd / 1e9, "transpose": bwd_bytes / t_bwd / 1e9},
     }
+    if forms is not None:
+        out["forms"] = forms
+    if batched is not None:
+        out["batched"] = batched
     if cpu is not None:
         out["cpu_baseline"] = cpu
     print(json.dumps(out), flush=True)

@@ -55,7 +55,7 @@ class Csr16C(C.Structure):
 
 class MlemOptions(C.Structure):
     _fields_ = [("max_row_nnz", C.c_int32), ("use_graph", C.c_int32),
-                ("value_format", C.c_int32), ("reserved", C.c_int32)]
+                ("value_format", C.c_int32), ("autotune", C.c_int32)]
 
 
 P, VP, I64, I32, F, D, SZ = (C.POINTER(ProblemC), C.c_void_p, C.c_int64, C.c_int32, C.c_float,
@@ -108,6 +108,14 @@ SIGNATURES = {
     "epet_mlem_get_image": [VP, VP, VP],
     "epet_mlem_set_image": [VP, VP, VP],
     "epet_mlem_stats": [VP, C.POINTER(C.c_int64), C.POINTER(C.c_int64)],
+    "epet_mlem_plan": [VP, C.POINTER(C.c_int32)],
+    "epet_mlem_batch_create": [I32, VP, VP, VP, VP, VP, C.POINTER(MlemOptions), C.POINTER(VP),
+                               VP],
+    "epet_mlem_batch_destroy": [VP],
+    "epet_mlem_batch_iterate": [VP, I32, VP, VP],
+    "epet_mlem_batch_get_image": [VP, I32, VP, VP],
+    "epet_mlem_batch_member": [VP, I32],
+    "epet_mlem_batch_stats": [VP, C.POINTER(C.c_int64), C.POINTER(C.c_int64), VP],
 }
 _RESTYPES = {
     "epet_last_error": C.c_char_p,
@@ -118,6 +126,7 @@ _RESTYPES = {
     "epet_coo_sort_workspace_size": SZ,
     "epet_csr_to_csc_workspace_size": SZ,
     "epet_mlem_image": VP,
+    "epet_mlem_batch_member": VP,
 }
 
 _LIB = None

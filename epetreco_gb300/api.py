@@ -26,7 +26,7 @@ from dataclasses import dataclass
 import torch
 
 from . import _lib
-from ._lib import CscC, CsrC, MlemOptions, check, lib, problem_struct
+from ._lib import CscC, CsrC, EpetError, MlemOptions, ProblemC, check, lib, problem_struct
 
 NON_TRANSPOSE = 0
 TRANSPOSE = 1
@@ -311,13 +311,14 @@ class Mlem:
     of the measured rows is built once at construction."""
 
     def __init__(self, p, rows, y, s, use_graph: bool = True, max_row_nnz: int = 0,
-                 value_format: int = 0):
+                 value_format: int = 0, autotune: bool = False):
         self.p = p
         rows = _i32(rows)
         y = y.to(torch.float32).contiguous()
         s = s.to(torch.float32).contiguous()
         self._h = C.c_void_p()
-        opt = MlemOptions(int(max_row_nnz), 1 if use_graph else 0, int(value_format), 0)
+        opt = MlemOptions(int(max_row_nnz), 1 if use_graph else 0, int(value_format),
+                          1 if autotune else 0)
         check(lib().epet_mlem_create(C.byref(problem_struct(p)), _ptr(rows), _ptr(y),
                                      rows.numel(), _ptr(s), C.byref(opt), C.byref(self._h),
                                      _stream()))
@@ -343,9 +344,79 @@ class Mlem:
         check(lib().epet_mlem_stats(self._h, C.byref(nnz), C.byref(b)))
         return {"nnz": nnz.value, "bytes_per_iteration": b.value}
 
+    def plan(self):
+        """Launch shapes of the products: {"forward": (G, U, grid), "transpose": ...}."""
+        pl = (C.c_int32 * 6)()
+        check(lib().epet_mlem_plan(self._h, pl))
+        return {"forward": tuple(pl[0:3]), "transpose": tuple(pl[3:6])}
+
+    def close(self):
+        if self._h and getattr(self, "_owner", None) is None:
+            lib().epet_mlem_destroy(self._h)
+        self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class MlemBatch:
+    """Many independent reconstructions iterated together: each step of an
+    iteration is one launch over all problems, the iteration one CUDA graph.
+    ``problems`` is a list of (Problem, rows, y, s) with device tensors."""
+
+    def __init__(self, problems, use_graph: bool = True, autotune: bool = True,
+                 max_row_nnz: int = 0):
+        n = len(problems)
+        self.ps = [q[0] for q in problems]
+        self._keep = []
+        structs = (ProblemC * n)(*[problem_struct(q[0]) for q in problems])
+        rows_p, m, y_p, s_p = (C.c_void_p * n)(), (C.c_int64 * n)(), (C.c_void_p * n)(), \
+            (C.c_void_p * n)()
+        for i, (p, rows, y, s) in enumerate(problems):
+            rows, y, s = _i32(rows), y.to(torch.float32).contiguous(), \
+                s.to(torch.float32).contiguous()
+            self._keep += [rows, y, s]
+            rows_p[i], y_p[i], s_p[i] = rows.data_ptr(), y.data_ptr(), s.data_ptr()
+            m[i] = rows.numel()
+        self._h = C.c_void_p()
+        opt = MlemOptions(int(max_row_nnz), 1 if use_graph else 0, 0, 1 if autotune else 0)
+        check(lib().epet_mlem_batch_create(n, C.byref(structs), rows_p, m, y_p, s_p,
+                                           C.byref(opt), C.byref(self._h), _stream()))
+        self._keep = []
+
+    def iterate(self, nit: int, loglik: bool = False):
+        ll = (C.c_double * len(self.ps))()
+        check(lib().epet_mlem_batch_iterate(self._h, int(nit), ll if loglik else None,
+                                            _stream()))
+        return list(ll) if loglik else None
+
+    def member(self, i: int) -> "Mlem":
+        """Problem i as a single reconstruction (a view owned by the batch)."""
+        h = lib().epet_mlem_batch_member(self._h, int(i))
+        if not h:
+            raise EpetError(lib().epet_last_error().decode())
+        v = Mlem.__new__(Mlem)
+        v.p, v._h, v._owner = self.ps[i], C.c_void_p(h), self
+        return v
+
+    def image(self, i: int) -> torch.Tensor:
+        out = torch.empty(self.ps[i].nvoxels, dtype=torch.float32, device="cuda")
+        check(lib().epet_mlem_batch_get_image(self._h, int(i), _ptr(out), _stream()))
+        return out
+
+    def stats(self):
+        nnz, b = C.c_int64(0), C.c_int64(0)
+        pl = (C.c_int32 * 6)()
+        check(lib().epet_mlem_batch_stats(self._h, C.byref(nnz), C.byref(b), pl))
+        return {"nnz": nnz.value, "bytes_per_iteration": b.value,
+                "plan": {"forward": tuple(pl[0:3]), "transpose": tuple(pl[3:6])}}
+
     def close(self):
         if self._h:
-            lib().epet_mlem_destroy(self._h)
+            lib().epet_mlem_batch_destroy(self._h)
             self._h = C.c_void_p()
 
     def __del__(self):

@@ -17,29 +17,7 @@
 #include "internal.h"
 #include "spmv.cuh"
 
-struct epet_mlem {
-  epet_problem p;
-  epet_mlem_options opt;
-  int64_t m = 0, V = 0;
-  int32_t* rows = nullptr;
-  float *y = nullptr, *s = nullptr, *x = nullptr, *xnew = nullptr, *e = nullptr;
-  float* ybar = nullptr;  // last forward projection
-  epet_csr A{};
-  epet_csc At{};
-  epet_csr16 A16{}, At16{};  // 16-bit forms (value_format != FP32)
-  int64_t capA = 0;
-  double *part_ll = nullptr, *part_x = nullptr, *sums = nullptr;
-  int64_t nb_fwd = 0, nb_bwd = 0;
-  int g_fwd = 32, g_bwd = 32;
-  cudaGraph_t graph = nullptr;
-  cudaGraphExec_t exec = nullptr;
-};
-
-namespace epet {
-epet_status build_csr_growable(const epet_problem* p, const int32_t* rows, int64_t m,
-                               epet_csr* out, int64_t* cap, int32_t max_row_nnz,
-                               cudaStream_t st);
-}
+#include "mlem_internal.h"
 
 using namespace epet;
 
@@ -66,10 +44,10 @@ static epet_status mlem_iteration(epet_mlem* h, cudaStream_t st) {
     EPET_CHECK(launch_normalise(h->xnew, h->sums + 1, h->V, h->x, st));
     return EPET_OK;
   }
-  EPET_CHECK(launch_rows(h->g_fwd, h->A.row_ptr, h->A.col, h->A.val, h->x, h->m,
-                         EpiMlemForward{h->y, h->e, h->ybar}, nullptr, st, nullptr));
-  EPET_CHECK(launch_rows(h->g_bwd, h->At.col_ptr, h->At.row, h->At.val, h->e, h->V,
-                         EpiMlemUpdate{h->x, h->s, h->xnew, nullptr}, h->part_x, st, nullptr));
+  EPET_CHECK(launch_rows(h->plan_fwd, h->A.row_ptr, h->A.col, h->A.val, h->x, h->m,
+                         EpiMlemForward{h->y, h->e, h->ybar}, nullptr, st));
+  EPET_CHECK(launch_rows(h->plan_bwd, h->At.col_ptr, h->At.row, h->At.val, h->e, h->V,
+                         EpiMlemUpdate{h->x, h->s, h->xnew, nullptr}, h->part_x, st));
   EPET_CHECK(launch_sum_partials(h->part_x, h->nb_bwd, h->sums + 1, st));
   EPET_CHECK(launch_normalise(h->xnew, h->sums + 1, h->V, h->x, st));
   return EPET_OK;
@@ -182,13 +160,33 @@ epet_status epet_mlem_create(const epet_problem* p, const int32_t* rows_d, const
     cudaFree(h->At.row); h->At.row = nullptr;
     cudaFree(h->At.val); h->At.val = nullptr;
   }
-  h->g_fwd = pick_group(m ? (double)nnz / m : 0.0);
-  h->g_bwd = pick_group(V ? (double)nnz / V : 0.0);
-  h->nb_fwd = (m + kSpmvThreads / h->g_fwd - 1) / (kSpmvThreads / h->g_fwd);
-  h->nb_bwd = (V + kSpmvThreads / h->g_bwd - 1) / (kSpmvThreads / h->g_bwd);
+  h->plan_fwd = default_plan(m ? (double)nnz / m : 0.0);
+  h->plan_bwd = default_plan(V ? (double)nnz / V : 0.0);
   if (o.value_format != EPET_VALUES_FP32) h->nb_bwd = rows16_blocks(&h->At16);
+  else h->nb_bwd = ceil_div(V, kSpmvThreads / 32);  // the most tiles of any plan
   ALLOC(h->part_ll, 1024 * 8);
   ALLOC(h->part_x, std::max<int64_t>(h->nb_bwd, 1) * 8);
+  if (o.autotune && o.value_format == EPET_VALUES_FP32) {
+    // both products are idempotent (they write e / ybar and xnew / partials
+    // from x, y, s): the candidates run the real epilogues
+    rc = tune_rows(
+        0, m, nnz, V, m ? (double)nnz / m : 0.0,
+        [&](const RowPlan& pl) {
+          return launch_rows(pl, h->A.row_ptr, h->A.col, h->A.val, h->x, h->m,
+                             EpiMlemForward{h->y, h->e, h->ybar}, nullptr, st);
+        },
+        st, &h->plan_fwd);
+    if (rc == EPET_OK)
+      rc = tune_rows(
+          1, V, nnz, m, V ? (double)nnz / V : 0.0,
+          [&](const RowPlan& pl) {
+            return launch_rows(pl, h->At.col_ptr, h->At.row, h->At.val, h->e, h->V,
+                               EpiMlemUpdate{h->x, h->s, h->xnew, nullptr}, h->part_x, st);
+          },
+          st, &h->plan_bwd);
+    if (rc != EPET_OK) return fail(rc);
+  }
+  if (o.value_format == EPET_VALUES_FP32) h->nb_bwd = plan_tiles(h->plan_bwd, V);
 #undef ALLOC
   cudaError_t e = cudaStreamSynchronize(st);
   if (e != cudaSuccess) return fail(cuda_status(e, "mlem create"));
@@ -274,6 +272,17 @@ epet_status epet_mlem_stats(const epet_mlem* h, int64_t* nnz_h, int64_t* bytes_h
     *bytes_h = 8 * nnz + 8 * (m + 1) + 4 * m + 4 * V + 4 * m +
                8 * nnz + 8 * (V + 1) + 4 * m + 4 * V + 4 * V + 4 * V +
                4 * V + 4 * V;
+  }
+  return EPET_OK;
+}
+
+epet_status epet_mlem_plan(const epet_mlem* h, int32_t plan_h[6]) {
+  if (!h || !plan_h) return set_error(EPET_ERR_INVALID, "bad arguments");
+  const RowPlan* ps[2] = {&h->plan_fwd, &h->plan_bwd};
+  for (int k = 0; k < 2; k++) {
+    plan_h[3 * k + 0] = ps[k]->G;
+    plan_h[3 * k + 1] = ps[k]->U;
+    plan_h[3 * k + 2] = ps[k]->grid;
   }
   return EPET_OK;
 }

@@ -1,0 +1,30 @@
+// mlem_internal.h -- the reconstruction object shared by mlem.cu (one
+// problem) and batch.cu (many problems iterated by batched launches).
+#pragma once
+#include "common.cuh"
+#include "spmv.cuh"
+
+struct epet_mlem {
+  epet_problem p;
+  epet_mlem_options opt;
+  int64_t m = 0, V = 0;
+  int32_t* rows = nullptr;
+  float *y = nullptr, *s = nullptr, *x = nullptr, *xnew = nullptr, *e = nullptr;
+  float* ybar = nullptr;  // last forward projection
+  epet_csr A{};
+  epet_csc At{};
+  epet_csr16 A16{}, At16{};  // 16-bit forms (value_format != FP32)
+  int64_t capA = 0;
+  double *part_ll = nullptr, *part_x = nullptr, *sums = nullptr;
+  int64_t nb_bwd = 0;  // tiles of the transpose launch (partial sums)
+  epet::RowPlan plan_fwd, plan_bwd;
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+};
+
+namespace epet {
+epet_status build_csr_growable(const epet_problem* p, const int32_t* rows, int64_t m,
+                               epet_csr* out, int64_t* cap, int32_t max_row_nnz,
+                               cudaStream_t st);
+}
+

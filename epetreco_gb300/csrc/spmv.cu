@@ -15,111 +15,31 @@
 
 #include "common.cuh"
 #include "internal.h"
+#include "rows.cuh"
 #include "spmv.cuh"
 
 namespace epet {
 
-// Matrix streams are read once per product: streaming (evict-first) loads.
-__device__ __forceinline__ float ld_stream(const float* p) { return __ldcs(p); }
-__device__ __forceinline__ int ld_stream(const int32_t* p) { return __ldcs(p); }
-
-// Dot product of row [beg, end) with x by a group of G lanes, element-wise
-// loads (any alignment of idx / val).
-template <int G>
-__device__ __forceinline__ float group_dot_scalar(const int32_t* __restrict__ idx,
-                                                  const float* __restrict__ val,
-                                                  const float* __restrict__ x, int64_t beg,
-                                                  int64_t end, int lg) {
-  float a0 = 0.f, a1 = 0.f, a2 = 0.f, a3 = 0.f;
-  int64_t k = beg + lg;
-  for (; k + 3 * G < end; k += 4 * G) {
-    const float v0 = ld_stream(val + k), v1 = ld_stream(val + k + G);
-    const float v2 = ld_stream(val + k + 2 * G), v3 = ld_stream(val + k + 3 * G);
-    const int c0 = ld_stream(idx + k), c1 = ld_stream(idx + k + G);
-    const int c2 = ld_stream(idx + k + 2 * G), c3 = ld_stream(idx + k + 3 * G);
-    a0 = fmaf(v0, __ldg(x + c0), a0);
-    a1 = fmaf(v1, __ldg(x + c1), a1);
-    a2 = fmaf(v2, __ldg(x + c2), a2);
-    a3 = fmaf(v3, __ldg(x + c3), a3);
-  }
-  for (; k < end; k += G) a0 = fmaf(ld_stream(val + k), __ldg(x + ld_stream(idx + k)), a0);
-  float a = (a0 + a1) + (a2 + a3);
-#pragma unroll
-  for (int o = G / 2; o > 0; o >>= 1) a += __shfl_xor_sync(0xffffffffu, a, o, G);
-  return a;
-}
-
-// The same with 16-byte loads; idx and val must be 16-byte aligned.  Lane l
-// reads 4-entry chunks at 16-byte boundaries (float4 / int4 loads), two
-// chunks per round so 64 bytes per lane are in flight; entries outside
-// [beg, end) are masked; the last partial chunk of a row is read
-// element-wise (the arrays may end there).
-template <int G>
-__device__ __forceinline__ float group_dot_vec(const int32_t* __restrict__ idx,
-                                           const float* __restrict__ val,
-                                           const float* __restrict__ x, int64_t beg,
-                                           int64_t end, int lg) {
-  float a0 = 0.f, a1 = 0.f;
-  const int64_t a_beg = beg & ~int64_t(3);
-  auto chunk = [&](int64_t k, float& acc) {
-    if (k + 3 < end) {
-      const float4 v = __ldcs(reinterpret_cast<const float4*>(val + k));
-      const int4 c = __ldcs(reinterpret_cast<const int4*>(idx + k));
-      if (k >= beg) {
-        acc = fmaf(v.x, __ldg(x + c.x), acc);
-        acc = fmaf(v.y, __ldg(x + c.y), acc);
-        acc = fmaf(v.z, __ldg(x + c.z), acc);
-        acc = fmaf(v.w, __ldg(x + c.w), acc);
-      } else {  // first chunk of the row starts before beg
-        if (k + 0 >= beg) acc = fmaf(v.x, __ldg(x + c.x), acc);
-        if (k + 1 >= beg) acc = fmaf(v.y, __ldg(x + c.y), acc);
-        if (k + 2 >= beg) acc = fmaf(v.z, __ldg(x + c.z), acc);
-        acc = fmaf(v.w, __ldg(x + c.w), acc);
-      }
-    } else {
-      for (int j = 0; j < 4; j++) {
-        const int64_t kj = k + j;
-        if (kj >= beg && kj < end) acc = fmaf(ld_stream(val + kj), __ldg(x + ld_stream(idx + kj)), acc);
-      }
-    }
-  };
-  for (int64_t k = a_beg + 4 * lg; k < end; k += 8 * G) {
-    chunk(k, a0);
-    if (k + 4 * G < end) chunk(k + 4 * G, a1);
-  }
-  float a = a0 + a1;
-#pragma unroll
-  for (int o = G / 2; o > 0; o >>= 1) a += __shfl_xor_sync(0xffffffffu, a, o, G);
-  return a;
-}
-
-// Generic row kernel: out = Epi(row, dot).  Block reduces Epi's fp64 partial
-// (when used) into partial[blockIdx.x].
-template <int G, bool VEC, class Epi>
+// Generic row kernel: out = Epi(row, dot) over tiles of kSpmvThreads / G
+// rows; a grid smaller than the tile count strides over the tiles.  With
+// partial, Epi's fp64 values are summed per tile into partial[tile].
+template <int G, int U, bool VEC, class Epi>
 __global__ void __launch_bounds__(kSpmvThreads)
 k_rows(const int64_t* __restrict__ ptr, const int32_t* __restrict__ idx,
        const float* __restrict__ val, const float* __restrict__ x, int64_t nrows, Epi epi,
        double* __restrict__ partial) {
-  constexpr int RPB = kSpmvThreads / G;
+  constexpr int RPT = kSpmvThreads / G;
   __shared__ double red[kSpmvThreads / 32];
   const int lg = threadIdx.x % G;
-  const int64_t row = (int64_t)blockIdx.x * RPB + threadIdx.x / G;
-  double part = 0.0;
-  if (row < nrows) {
-    const float d = VEC ? group_dot_vec<G>(idx, val, x, ptr[row], ptr[row + 1], lg)
-                        : group_dot_scalar<G>(idx, val, x, ptr[row], ptr[row + 1], lg);
-    if (lg == 0) part = epi(row, d);
-  }
-  if (partial) {
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) part += __shfl_xor_sync(0xffffffffu, part, o);
-    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = part;
-    __syncthreads();
-    if (threadIdx.x == 0) {
-      double t = 0.0;
-      for (int w = 0; w < kSpmvThreads / 32; w++) t += red[w];
-      partial[blockIdx.x] = t;
+  const int64_t ntiles = (nrows + RPT - 1) / RPT;
+  for (int64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+    const int64_t row = tile * RPT + threadIdx.x / G;
+    double part = 0.0;
+    if (row < nrows) {
+      const float d = row_dot<G, U, VEC>(idx, val, x, ptr[row], ptr[row + 1], lg);
+      if (lg == 0) part = epi(row, d);
     }
+    if (partial) block_sum_to(part, red, partial + tile);
   }
 }
 
@@ -155,40 +75,36 @@ int pick_group(double avg_len) {
   return 4;
 }
 
+RowPlan default_plan(double avg_len) {
+  RowPlan p;
+  p.G = pick_group(avg_len);
+  p.U = 2;
+  p.grid = 0;
+  return p;
+}
+
 template <class Epi>
-epet_status launch_rows(int G, const int64_t* ptr, const int32_t* idx, const float* val,
-                        const float* x, int64_t nrows, Epi epi, double* partial,
-                        cudaStream_t st, int64_t* nblocks_out) {
-  if (nrows <= 0) {
-    if (nblocks_out) *nblocks_out = 0;
-    return EPET_OK;
-  }
-  const int rpb = kSpmvThreads / G;
-  const int64_t nb = (nrows + rpb - 1) / rpb;
-  if (nblocks_out) *nblocks_out = nb;
+epet_status launch_rows(const RowPlan& plan, const int64_t* ptr, const int32_t* idx,
+                        const float* val, const float* x, int64_t nrows, Epi epi,
+                        double* partial, cudaStream_t st) {
+  if (nrows <= 0) return EPET_OK;
+  const int64_t nt = plan_tiles(plan, nrows);
+  const unsigned grid = (unsigned)(plan.grid > 0 ? std::min<int64_t>(nt, plan.grid) : nt);
   // 16-byte loads only when both streams start on a 16-byte boundary
-  const bool vec = ((reinterpret_cast<uintptr_t>(idx) | reinterpret_cast<uintptr_t>(val)) & 15) == 0;
-#define EPET_ROWS(GG, V) \
-  k_rows<GG, V, Epi><<<(unsigned)nb, kSpmvThreads, 0, st>>>(ptr, idx, val, x, nrows, epi, partial)
-  switch (G) {
-    case 32: if (vec) EPET_ROWS(32, true); else EPET_ROWS(32, false); break;
-    case 16: if (vec) EPET_ROWS(16, true); else EPET_ROWS(16, false); break;
-    case 8: if (vec) EPET_ROWS(8, true); else EPET_ROWS(8, false); break;
-    default: if (vec) EPET_ROWS(4, true); else EPET_ROWS(4, false); break;
-  }
-#undef EPET_ROWS
+  dispatch_plan(plan, aligned16(idx, val), [&](auto g, auto u, auto v) {
+    k_rows<decltype(g)::value, decltype(u)::value, decltype(v)::value, Epi>
+        <<<grid, kSpmvThreads, 0, st>>>(ptr, idx, val, x, nrows, epi, partial);
+  });
   EPET_LAUNCHED();
   return EPET_OK;
 }
 
-template epet_status launch_rows<EpiMlemForward>(int, const int64_t*, const int32_t*,
+template epet_status launch_rows<EpiMlemForward>(const RowPlan&, const int64_t*, const int32_t*,
                                                  const float*, const float*, int64_t,
-                                                 EpiMlemForward, double*, cudaStream_t,
-                                                 int64_t*);
-template epet_status launch_rows<EpiMlemUpdate>(int, const int64_t*, const int32_t*,
+                                                 EpiMlemForward, double*, cudaStream_t);
+template epet_status launch_rows<EpiMlemUpdate>(const RowPlan&, const int64_t*, const int32_t*,
                                                 const float*, const float*, int64_t,
-                                                EpiMlemUpdate, double*, cudaStream_t,
-                                                int64_t*);
+                                                EpiMlemUpdate, double*, cudaStream_t);
 
 epet_status launch_sum_partials(const double* p, int64_t n, double* out, cudaStream_t st) {
   k_sum_partials<<<1, 1024, 0, st>>>(p, n, out);
@@ -313,14 +229,13 @@ epet_status epet_csrmv(int trans, const epet_csr* a, const epet_csc* csc, float 
   if (out_len == 0) return EPET_OK;
   cudaStream_t st = (cudaStream_t)stream;
   if (!trans) {
-    const int G = pick_group(a->m ? (double)a->nnz / a->m : 0.0);
-    return launch_rows(G, a->row_ptr, a->col, a->val, x_d, a->m, EpiAxpby{alpha, beta, y_d},
-                       nullptr, st, nullptr);
+    return launch_rows(default_plan(a->m ? (double)a->nnz / a->m : 0.0), a->row_ptr, a->col,
+                       a->val, x_d, a->m, EpiAxpby{alpha, beta, y_d}, nullptr, st);
   }
   if (csc) {
-    const int G = pick_group(csc->n ? (double)csc->nnz / csc->n : 0.0);
-    return launch_rows(G, csc->col_ptr, csc->row, csc->val, x_d, csc->n,
-                       EpiAxpby{alpha, beta, y_d}, nullptr, st, nullptr);
+    return launch_rows(default_plan(csc->n ? (double)csc->nnz / csc->n : 0.0), csc->col_ptr,
+                       csc->row, csc->val, x_d, csc->n, EpiAxpby{alpha, beta, y_d}, nullptr,
+                       st);
   }
   if (beta != 1.f) {
     k_scale_vec<<<ceil_div(a->n, 256), 256, 0, st>>>(y_d, a->n, beta);

@@ -1,10 +1,11 @@
 // spmv.cuh -- fused MLEM epilogues of the row kernels (spmv.cu).
 #pragma once
+#include <functional>
+
 #include "common.cuh"
+#include "rows.cuh"
 
 namespace epet {
-
-constexpr int kSpmvThreads = 256;
 
 // Forward projection epilogue: yb = A x (row r), e[r] = y[r] / yb with the
 // reference's divides (mlemOperations.hpp:22-32) but 0 where yb == 0 (the
@@ -40,11 +41,21 @@ struct EpiMlemUpdate {
 };
 
 int pick_group(double avg_len);
+RowPlan default_plan(double avg_len);
 
 template <class Epi>
-epet_status launch_rows(int G, const int64_t* ptr, const int32_t* idx, const float* val,
-                        const float* x, int64_t nrows, Epi epi, double* partial,
-                        cudaStream_t st, int64_t* nblocks_out);
+epet_status launch_rows(const RowPlan& plan, const int64_t* ptr, const int32_t* idx,
+                        const float* val, const float* x, int64_t nrows, Epi epi,
+                        double* partial, cudaStream_t st);
+
+// Autotuner: times run(plan) over candidate plans around default_plan(avg)
+// (group sizes, unroll depths, persistent grids) and returns the fastest.
+// Results are cached per (device, kind, rows, nnz, cols) for the life of the
+// process (mutex-guarded).  run must be idempotent; the stream must not be
+// capturing.
+epet_status tune_rows(int kind, int64_t nrows, int64_t nnz, int64_t ncols, double avg,
+                      const std::function<epet_status(const RowPlan&)>& run, cudaStream_t st,
+                      RowPlan* out);
 template <class Epi>
 epet_status launch_rows16(const epet_csr16* a, const float* x, Epi epi, double* partial,
                           cudaStream_t st);

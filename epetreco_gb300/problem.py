@@ -130,3 +130,43 @@ CONFIGS = {
 
 def config(name: str) -> dict:
     return dict(CONFIGS[name])
+
+
+# Batched workload: independent reconstructions of uneven size.  Grids and
+# angle counts are drawn uniformly from these sets; 8 angles step 22.5 deg
+# (as the small workload), the others cover 360 deg (180 angles: 2 deg, as
+# the full workload).
+BATCH_GRIDS = (24, 32, 40, 52, 64)
+BATCH_ANGLES = (8, 30, 60, 120, 180)
+
+
+def batch_angle_step(na: int) -> float:
+    return 22.5 if na == 8 else 360.0 / na
+
+
+@dataclass(frozen=True)
+class BatchMember:
+    problem: Problem
+    counts: float       # total Poisson counts of the measurement
+    n_spheres: int      # hot spheres in the phantom
+    phantom_seed: int
+    poisson_seed: int
+
+
+def batch_members(n: int = 64, seed: int = 4242, grids=BATCH_GRIDS, angles=BATCH_ANGLES,
+                  rays=(20, 100), counts=(1e5, 1e8)) -> list[BatchMember]:
+    """n seeded draws: grid and angle count uniform from the sets, rays
+    uniform in [rays[0], rays[1]], counts log-uniform in [counts[0],
+    counts[1]], 1-4 hot spheres."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for i in range(n):
+        g = int(rng.choice(grids))
+        na = int(rng.choice(angles))
+        nr = int(rng.integers(rays[0], rays[1] + 1))
+        c = float(10 ** rng.uniform(np.log10(counts[0]), np.log10(counts[1])))
+        ns = int(rng.integers(1, 5))
+        out.append(BatchMember(Problem(two_head_setup(na, batch_angle_step(na)),
+                                       centred_grid(g), nr),
+                               c, ns, 100 + i, 200 + i))
+    return out

@@ -298,7 +298,10 @@ typedef struct {
   int32_t max_row_nnz; /* 0 = auto */
   int32_t use_graph;   /* capture one iteration in a CUDA graph */
   int32_t value_format; /* EPET_VALUES_FP32 / _BF16 / _FP16 (16-bit values + row scale) */
-  int32_t reserved;
+  int32_t autotune;    /* 1: time candidate launch shapes of the two products on this
+                          matrix at create (cached per matrix shape for the process);
+                          0: a fixed heuristic shape (results then depend only on the
+                          inputs, not on timings).  FP32 values only. */
 } epet_mlem_options;
 
 /* Builds the system matrix for the measured rows (rows_d ascending channel
@@ -321,6 +324,42 @@ epet_status epet_mlem_set_image(epet_mlem* h, const float* x_d,
                                 epet_stream_t stream);
 epet_status epet_mlem_stats(const epet_mlem* h, int64_t* nnz_h,
                             int64_t* bytes_per_iter_h);
+/* Launch shapes of the two products: plan_h[0..2] = forward lanes per row,
+ * 16-byte chunks in flight per lane, persistent grid (0 = one block per
+ * tile); plan_h[3..5] the same for the transpose. */
+epet_status epet_mlem_plan(const epet_mlem* h, int32_t plan_h[6]);
+
+/* ---------------------------------------------- batched reconstructions */
+/* Many independent reconstructions (each its own geometry, grid, rays,
+ * measured rows and sensitivity) iterated together: every step of an
+ * iteration is ONE kernel launch over all problems' rows or voxels, and the
+ * iteration (forward product + e = y/(Ax), transpose product + x*c/s,
+ * per-problem fp64 image sums, normalisation: four launches) is captured in
+ * one CUDA graph.  Launch shapes come from the autotuner unless
+ * opt->autotune == 0.  The reference runs one reconstruction per process
+ * (reco.cu:209-281); there is no batched counterpart.  FP32 values. */
+typedef struct epet_mlem_batch epet_mlem_batch;
+
+/* Arrays of nprob entries on the host; rows_d[i], y_d[i], s_d[i] are device
+ * pointers as for epet_mlem_create.  Synchronous. */
+epet_status epet_mlem_batch_create(int32_t nprob, const epet_problem* problems,
+                                   const int32_t* const* rows_d, const int64_t* m,
+                                   const float* const* y_d, const float* const* s_d,
+                                   const epet_mlem_options* opt, epet_mlem_batch** out,
+                                   epet_stream_t stream);
+epet_status epet_mlem_batch_destroy(epet_mlem_batch* h);
+/* nit iterations of every problem; loglik_h (nprob entries or NULL) as in
+ * epet_mlem_iterate. */
+epet_status epet_mlem_batch_iterate(epet_mlem_batch* h, int32_t nit, double* loglik_h,
+                                    epet_stream_t stream);
+epet_status epet_mlem_batch_get_image(const epet_mlem_batch* h, int32_t i, float* x_d,
+                                      epet_stream_t stream);
+/* Problem i as a single reconstruction (owned by the batch: do not destroy);
+ * iterating it alone runs the plain per-problem kernels on the same arrays. */
+epet_mlem* epet_mlem_batch_member(epet_mlem_batch* h, int32_t i);
+/* Totals over the problems; plan_h as epet_mlem_plan (may be NULL). */
+epet_status epet_mlem_batch_stats(const epet_mlem_batch* h, int64_t* nnz_h,
+                                  int64_t* bytes_per_iter_h, int32_t plan_h[6]);
 
 #ifdef __cplusplus
 }
