@@ -84,6 +84,19 @@ __device__ __forceinline__ float fsub(float a, float b) { return __fsub_rn(a, b)
 __device__ __forceinline__ float fdiv(float a, float b) { return __fdiv_rn(a, b); }
 __device__ __forceinline__ float fsqrt(float a) { return __fsqrt_rn(a); }
 
+// Correctly rounded quotient a / b from inv = RN(1/b), by Markstein's
+// theorem (P. Markstein, "Computation of elementary functions on the IBM
+// RISC System/6000 processor", IBM J. Res. Dev. 34(1), 1990): q0 = RN(a*inv)
+// lies within one ulp of a/b, the residual r = a - b*q0 is exact in one fma,
+// and RN(q0 + r*inv) = RN(a/b) for operands away from overflow and
+// underflow (the ray parameters here are of order 1).  One reciprocal per
+// ray and axis replaces a division per plane crossing.
+__device__ __forceinline__ float div_cr(float a, float b, float inv) {
+  const float q0 = __fmul_rn(a, inv);
+  const float r = __fmaf_rn(-q0, b, a);
+  return __fmaf_rn(r, inv, q0);
+}
+
 // sqrtf(a0*a0 + a1*a1 + a2*a2) (distancePointLine.h:19-24).
 __device__ __forceinline__ float norm3(float a0, float a1, float a2) {
   return fsqrt(fadd(fadd(fmul(a0, a0), fmul(a1, a1)), fmul(a2, a2)));

@@ -121,13 +121,24 @@ k_rows16(const int64_t* __restrict__ ptr, const int32_t* __restrict__ base,
   // round-aligned start (8-entry, 16-byte boundaries)
   const int64_t a0 = b & ~int64_t(7);
   const unsigned gmask = G == 32 ? 0xffffffffu : (((1u << G) - 1u) << (threadIdx.x & 31 & ~(G - 1)));
+  // software pipeline: the next round's loads are issued before this
+  // round's scan and gathers
+  uint4 dv = make_uint4(0, 0, 0, 0), qv = make_uint4(0, 0, 0, 0);
+  if (a0 + 8 * lg < e) {
+    dv = __ldcs(reinterpret_cast<const uint4*>(delta + a0 + 8 * lg));
+    qv = __ldcs(reinterpret_cast<const uint4*>(q + a0 + 8 * lg));
+  }
   for (int64_t c0 = a0; c0 < e; c0 += 8 * G) {
     const int64_t k = c0 + 8 * lg;  // this lane's first entry
-    uint4 dv = make_uint4(0, 0, 0, 0), qv = make_uint4(0, 0, 0, 0);
-    if (k < e) {
-      dv = __ldcs(reinterpret_cast<const uint4*>(delta + k));
-      qv = __ldcs(reinterpret_cast<const uint4*>(q + k));
+    uint4 dn = make_uint4(0, 0, 0, 0), qn = make_uint4(0, 0, 0, 0);
+    if (k + 8 * G < e) {
+      dn = __ldcs(reinterpret_cast<const uint4*>(delta + k + 8 * G));
+      qn = __ldcs(reinterpret_cast<const uint4*>(q + k + 8 * G));
     }
+    // entries j of this lane's chunk with lo <= j < hi lie in [b, e)
+    const int64_t dl = b - k, dh = e - k;
+    const int lo = dl > 0 ? (int)dl : 0;
+    const int hi = dh < 8 ? (dh > 0 ? (int)dh : 0) : 8;
     uint32_t dd[8], qq[8];
     dd[0] = dv.x & 0xffffu; dd[1] = dv.x >> 16; dd[2] = dv.y & 0xffffu; dd[3] = dv.y >> 16;
     dd[4] = dv.z & 0xffffu; dd[5] = dv.z >> 16; dd[6] = dv.w & 0xffffu; dd[7] = dv.w >> 16;
@@ -137,8 +148,7 @@ k_rows16(const int64_t* __restrict__ ptr, const int32_t* __restrict__ base,
     uint32_t lsum = 0;
 #pragma unroll
     for (int j = 0; j < 8; j++) {
-      const int64_t kj = k + j;
-      if (kj < b || kj >= e) dd[j] = 0;
+      if (j < lo || j >= hi) dd[j] = 0;
       lsum += dd[j];
     }
     // group exclusive scan of the lane sums
@@ -152,11 +162,12 @@ k_rows16(const int64_t* __restrict__ ptr, const int32_t* __restrict__ base,
     int32_t c = col + (int32_t)(inc - lsum);
 #pragma unroll
     for (int j = 0; j < 8; j++) {
-      const int64_t kj = k + j;
       c += (int32_t)dd[j];
-      if (kj >= b && kj < e) acc = fmaf(from_q<FMT>(qq[j]), __ldg(x + c), acc);
+      if (j >= lo && j < hi) acc = fmaf(from_q<FMT>(qq[j]), __ldg(x + c), acc);
     }
     col += (int32_t)total;
+    dv = dn;
+    qv = qn;
   }
 #pragma unroll
   for (int o = G / 2; o > 0; o >>= 1) acc += __shfl_xor_sync(gmask, acc, o, G);

@@ -98,11 +98,55 @@ epet_status launch_rays(const Geo& G, const int32_t* rows, int64_t m, float* out
   return EPET_OK;
 }
 
+// Self-test of div_cr against the correctly rounded division: n seeded
+// operand pairs, a with exponents in [2^-40, 2^5), b in [2^-20, 2^5), random
+// signs and mantissas; counts bitwise differences.
+__device__ __forceinline__ uint64_t splitmix64(uint64_t z) {
+  z += 0x9e3779b97f4a7c15ull;
+  z = (z ^ (z >> 30)) * 0xbf58476d1ce4e5b9ull;
+  z = (z ^ (z >> 27)) * 0x94d049bb133111ebull;
+  return z ^ (z >> 31);
+}
+
+__global__ void k_selftest_div(int64_t n, uint64_t seed, unsigned long long* bad) {
+  unsigned long long mine = 0;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const uint64_t r = splitmix64(seed ^ (uint64_t)i * 0x2545f4914f6cdd1dull);
+    const uint32_t ea = 127 - 40 + (uint32_t)((r >> 23) % 45u);
+    const uint32_t eb = 127 - 20 + (uint32_t)((r >> 46) % 25u);
+    const float a = (r & 0xfffff) == 0 ? 0.f
+                    : __uint_as_float(((uint32_t)(r >> 63) << 31) | (ea << 23) |
+                                      ((uint32_t)r & 0x7fffffu));
+    const float b = __uint_as_float(((uint32_t)(r >> 62 & 1u) << 31) | (eb << 23) |
+                                    ((uint32_t)(r >> 32) & 0x7fffffu));
+    if (__float_as_uint(div_cr(a, b, __frcp_rn(b))) != __float_as_uint(__fdiv_rn(a, b))) mine++;
+  }
+  if (mine) atomicAdd(bad, mine);
+}
+
 }  // namespace epet
 
 using namespace epet;
 
 extern "C" {
+
+epet_status epet_selftest_division(int64_t n, uint64_t seed, int64_t* mismatches_h,
+                                   epet_stream_t stream) {
+  if (n < 0 || !mismatches_h) return set_error(EPET_ERR_INVALID, "bad arguments");
+  cudaStream_t st = (cudaStream_t)stream;
+  unsigned long long* bad = nullptr;
+  EPET_CUDA(cudaMallocAsync((void**)&bad, 8, st));
+  EPET_CUDA(cudaMemsetAsync(bad, 0, 8, st));
+  k_selftest_div<<<1024, 256, 0, st>>>(n, seed, bad);
+  EPET_LAUNCHED();
+  unsigned long long h = 0;
+  EPET_CUDA(cudaMemcpyAsync(&h, bad, 8, cudaMemcpyDeviceToHost, st));
+  EPET_CUDA(cudaFreeAsync(bad, st));
+  EPET_CUDA(cudaStreamSynchronize(st));
+  *mismatches_h = (int64_t)h;
+  return EPET_OK;
+}
 
 epet_status epet_trig_table(const epet_problem* p, float* sc_d,
                             epet_stream_t stream) {

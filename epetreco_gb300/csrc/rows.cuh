@@ -54,9 +54,9 @@ __device__ __forceinline__ float group_dot_scalar(const int32_t* __restrict__ id
 // The same with 16-byte loads; idx and val must be 16-byte aligned.  The
 // row splits into a head (entries before the first 16-byte boundary, at most
 // 3), a body of 4-entry chunks (float4 / int4 loads) and a tail (at most 3
-// entries).  Lane l takes body chunks l, l + G, ...; each round issues the
-// loads of U chunks before any gather, so 32*U bytes per lane of the matrix
-// stream are in flight.
+// entries).  Lane l takes body chunks l, l + G, ...; a round covers U chunks
+// per lane and the next round's loads are issued before this round's
+// gathers, so up to 64*U bytes per lane of the matrix stream are in flight.
 template <int G, int U>
 __device__ __forceinline__ float group_dot_vec(const int32_t* __restrict__ idx,
                                                const float* __restrict__ val,
@@ -72,30 +72,41 @@ __device__ __forceinline__ float group_dot_vec(const int32_t* __restrict__ idx,
   const float4* __restrict__ v4 = reinterpret_cast<const float4*>(val + h);
   const int4* __restrict__ c4 = reinterpret_cast<const int4*>(idx + h);
   const int64_t nc = (t - h) >> 2;
-  int64_t j = lg;
-  for (; j + (U - 1) * G < nc; j += U * G) {
-    float4 v[U];
-    int4 c[U];
+  // software pipeline: the loads of round r + 1 are issued before the
+  // gathers of round r, so the matrix stream stays in flight while the
+  // gathers wait
+  float4 v[U];
+  int4 c[U];
 #pragma unroll
-    for (int u = 0; u < U; u++) {
-      v[u] = __ldcs(v4 + j + u * G);
-      c[u] = __ldcs(c4 + j + u * G);
-    }
-#pragma unroll
-    for (int u = 0; u < U; u++) {
-      acc[u] = fmaf(v[u].x, __ldg(x + c[u].x), acc[u]);
-      acc[u] = fmaf(v[u].y, __ldg(x + c[u].y), acc[u]);
-      acc[u] = fmaf(v[u].z, __ldg(x + c[u].z), acc[u]);
-      acc[u] = fmaf(v[u].w, __ldg(x + c[u].w), acc[u]);
+  for (int u = 0; u < U; u++) {
+    const int64_t jj = lg + u * G;
+    if (jj < nc) {
+      v[u] = __ldcs(v4 + jj);
+      c[u] = __ldcs(c4 + jj);
     }
   }
-  for (; j < nc; j += G) {
-    const float4 v = __ldcs(v4 + j);
-    const int4 c = __ldcs(c4 + j);
-    acc[0] = fmaf(v.x, __ldg(x + c.x), acc[0]);
-    acc[0] = fmaf(v.y, __ldg(x + c.y), acc[0]);
-    acc[0] = fmaf(v.z, __ldg(x + c.z), acc[0]);
-    acc[0] = fmaf(v.w, __ldg(x + c.w), acc[0]);
+  for (int64_t j = lg; j < nc; j += U * G) {
+    float4 vn[U];
+    int4 cn[U];
+#pragma unroll
+    for (int u = 0; u < U; u++) {
+      const int64_t jj = j + (U + u) * G;
+      if (jj < nc) {
+        vn[u] = __ldcs(v4 + jj);
+        cn[u] = __ldcs(c4 + jj);
+      }
+    }
+#pragma unroll
+    for (int u = 0; u < U; u++) {
+      if (j + u * G < nc) {
+        acc[u] = fmaf(v[u].x, __ldg(x + c[u].x), acc[u]);
+        acc[u] = fmaf(v[u].y, __ldg(x + c[u].y), acc[u]);
+        acc[u] = fmaf(v[u].z, __ldg(x + c[u].z), acc[u]);
+        acc[u] = fmaf(v[u].w, __ldg(x + c[u].w), acc[u]);
+      }
+      v[u] = vn[u];
+      c[u] = cn[u];
+    }
   }
   float a = acc[0];
 #pragma unroll

@@ -178,100 +178,46 @@ struct Window {
   int sa;  // slab axis
 };
 
-__device__ __forceinline__ void win_add(const Window& w, const Slab* slabs, int ix, int iy,
-                                        int iz, unsigned long long units, int* outside) {
-  const bool zs = w.sa == 2;
-  const Slab s = slabs[zs ? iz : ix];
-  const unsigned jp = (unsigned)((zs ? ix : iy) - s.p0), jq = (unsigned)((zs ? iy : iz) - s.q0);
-  if (jp < (unsigned)s.wp && jq < (unsigned)s.wq) {
-    const int c = s.off + (int)jp * s.wq + (int)jq;
-    const uint32_t l = (uint32_t)(units & ((1ull << w.split) - 1ull));
-    const uint32_t h = (uint32_t)(units >> w.split);
-    atomicAdd(&w.lo[c], l);
-    if (h) atomicAdd(&w.hi[c], h);
-  } else {
-    atomicAdd(outside, 1);
-  }
-}
-
-__device__ __forceinline__ unsigned long long to_units(float len, float scale) {
-  unsigned long long u = __float2ull_rn(fmul(len, scale));
-  return (u == 0ull && len > 0.f) ? 1ull : u;
-}
-
 // One axis of a ray walk: the ray's parameter at grid plane k is the
 // reference's quotient (plane_k - r0)/(r1 - r0), correctly rounded.
 struct WalkAxis {
-  float o, d, r0, dr;
+  float o, d, r0, dr, inv;  // plane k at o + k*d; ray at r0 + a*dr; inv = RN(1/dr)
   int n, step, idx;
   float lo, hi;  // parameter interval of the current cell along this axis
-  __device__ __forceinline__ float alpha(int k) const {
-    return fdiv(fsub(fadd(o, fmul((float)k, d)), r0), dr);
+  float kh;      // index (as a float) of the plane at hi
+  __device__ __forceinline__ float alpha(float k) const {
+    return div_cr(fsub(fadd(o, fmul(k, d)), r0), dr, inv);
   }
   // cell with lo <= a < hi (a inside the axis' grid range)
   __device__ __forceinline__ void enter(float a) {
     int i = clampi((int)floorf((r0 + a * dr - o) / d), 0, n - 1);
     if (step > 0) {  // interval of cell i: [alpha(i), alpha(i+1)]
-      while (i > 0 && alpha(i) > a) i--;
-      while (i < n - 1 && alpha(i + 1) <= a) i++;
-      lo = alpha(i);
-      hi = alpha(i + 1);
+      while (i > 0 && alpha((float)i) > a) i--;
+      while (i < n - 1 && alpha((float)(i + 1)) <= a) i++;
+      lo = alpha((float)i);
+      hi = alpha((float)(i + 1));
+      kh = (float)(i + 1);
     } else {         // interval of cell i: [alpha(i+1), alpha(i)]
-      while (i < n - 1 && alpha(i + 1) > a) i++;
-      while (i > 0 && alpha(i) <= a) i--;
-      lo = alpha(i + 1);
-      hi = alpha(i);
+      while (i < n - 1 && alpha((float)(i + 1)) > a) i++;
+      while (i > 0 && alpha((float)i) <= a) i--;
+      lo = alpha((float)(i + 1));
+      hi = alpha((float)i);
+      kh = (float)i;
     }
     idx = i;
   }
-  // across the exit plane; false when leaving the grid
-  __device__ __forceinline__ bool advance() {
-    const int ni = idx + step;
-    if (ni < 0 || ni >= n) return false;
-    idx = ni;
-    lo = hi;
-    hi = step > 0 ? alpha(ni + 1) : alpha(ni);
-    return true;
-  }
 };
-
-// Walks cells from the current state until leaving the grid or reaching the
-// cell (sx, sy, sz) (not processed); returns steps taken.
-__device__ __forceinline__ int walk_cells(WalkAxis& X, WalkAxis& Y, WalkAxis& Z, float L,
-                                          float scale, const Window& w, const Slab* slabs,
-                                          int* outside, int sx, int sy, int sz, int budget) {
-  int steps = 0;
-  for (; steps < budget; steps++) {
-    if (X.idx == sx && Y.idx == sy && Z.idx == sz) break;
-    const float amin = fmaxf(fmaxf(X.lo, Y.lo), Z.lo);
-    float amax;
-    int m;
-    if (X.hi <= Y.hi && X.hi <= Z.hi) {
-      amax = X.hi;
-      m = 0;
-    } else if (Y.hi <= Z.hi) {
-      amax = Y.hi;
-      m = 1;
-    } else {
-      amax = Z.hi;
-      m = 2;
-    }
-    if (amin < amax)
-      win_add(w, slabs, X.idx, Y.idx, Z.idx, to_units(fmul(fsub(amax, amin), L), scale),
-              outside);
-    const bool in = m == 0 ? X.advance() : (m == 1 ? Y.advance() : Z.advance());
-    if (!in) break;
-  }
-  return steps;
-}
 
 // Walk one ray through the grid and add its chord lengths to the window.
 // Voxel interval = [max lo, min hi] over the axes; length = (aMax - aMin) *
-// |r1 - r0| (getSystemMatrixFromWorkqueue.cu:24-69).  The walk starts at the
-// parameter fraction `frac` of the ray's grid range, runs to the exit, then
-// covers the part from the entry up to the starting cell: rays of one channel
-// run in lock-step through the same voxels, and different starting points
-// keep the lanes of a warp on different cells.
+// |r1 - r0| (getSystemMatrixFromWorkqueue.cu:24-69).  The walk starts in the
+// cell containing the parameter fraction `frac` of the ray's grid range,
+// runs to the exit, re-enters at the entry and stops at the starting cell
+// (the first cell entered at or after its entry parameter), all in one loop:
+// the lanes of a warp walk rays of one channel, each from a different
+// starting point (fewer atomic collisions), and stay converged.  Each step
+// is branch-free: the axis whose plane comes first is selected and advanced
+// with one division.
 __device__ void walk_ray(const Geo& G, const float* ray, const Window& w, const Slab* slabs,
                          int* outside, int* needs_exact, float frac) {
   const epet_grid& g = G.p.grid;
@@ -288,6 +234,9 @@ __device__ void walk_ray(const Geo& G, const float* ray, const Window& w, const 
   X.o = g.o[0]; X.d = g.d[0]; X.r0 = ray[0]; X.dr = fsub(ray[3], ray[0]); X.n = g.n[0];
   Y.o = g.o[1]; Y.d = g.d[1]; Y.r0 = ray[1]; Y.dr = fsub(ray[4], ray[1]); Y.n = g.n[1];
   Z.o = g.o[2]; Z.d = g.d[2]; Z.r0 = ray[2]; Z.dr = fsub(ray[5], ray[2]); Z.n = g.n[2];
+  X.inv = __frcp_rn(X.dr);
+  Y.inv = __frcp_rn(Y.dr);
+  Z.inv = __frcp_rn(Z.dr);
   X.step = X.dr > 0.f ? 1 : -1;
   Y.step = Y.dr > 0.f ? 1 : -1;
   Z.step = Z.dr > 0.f ? 1 : -1;
@@ -295,28 +244,75 @@ __device__ void walk_ray(const Geo& G, const float* ray, const Window& w, const 
   // grid parameter range
   float a_in, a_out;
   {
-    const float x0 = X.alpha(0), x1 = X.alpha(X.n);
-    const float y0 = Y.alpha(0), y1 = Y.alpha(Y.n);
-    const float z0 = Z.alpha(0), z1 = Z.alpha(Z.n);
+    const float x0 = X.alpha(0.f), x1 = X.alpha((float)X.n);
+    const float y0 = Y.alpha(0.f), y1 = Y.alpha((float)Y.n);
+    const float z0 = Z.alpha(0.f), z1 = Z.alpha((float)Z.n);
     a_in = fmaxf(fmaxf(fminf(x0, x1), fminf(y0, y1)), fminf(z0, z1));
     a_out = fminf(fminf(fmaxf(x0, x1), fmaxf(y0, y1)), fmaxf(z0, z1));
   }
   if (!(a_in < a_out)) return;
   float a_s = a_in + (a_out - a_in) * frac;
   if (!(a_s >= a_in && a_s < a_out)) a_s = a_in;
-  const int budget = g.n[0] + g.n[1] + g.n[2] + 3;
-  // part 1: from the cell containing a_s to the exit
   X.enter(a_s);
   Y.enter(a_s);
   Z.enter(a_s);
-  const int sx = X.idx, sy = Y.idx, sz = Z.idx;
-  int used = walk_cells(X, Y, Z, L, G.fx_scale, w, slabs, outside, -1, -1, -1, budget);
-  // part 2: from the entry up to (not including) the starting cell
-  if (a_s > a_in) {
-    X.enter(a_in);
-    Y.enter(a_in);
-    Z.enter(a_in);
-    walk_cells(X, Y, Z, L, G.fx_scale, w, slabs, outside, sx, sy, sz, budget - used);
+  const float a_start = fmaxf(fmaxf(X.lo, Y.lo), Z.lo);  // entry of the starting cell
+  bool second = !(a_s > a_in);  // nothing before the starting cell
+  float a_stop = INFINITY;
+  const bool zs = w.sa == 2;
+  Slab sl = slabs[zs ? Z.idx : X.idx];
+  const float scale = G.fx_scale;
+  const float two_s = __int_as_float((127 + w.split) << 23);   // 2^split
+  const float inv_two_s = __int_as_float((127 - w.split) << 23);
+  const int budget = g.n[0] + g.n[1] + g.n[2] + 4;
+  for (int steps = 0; steps < budget; steps++) {
+    const float amin = fmaxf(fmaxf(X.lo, Y.lo), Z.lo);
+    if (!(amin < a_stop)) break;
+    const bool mx = X.hi <= Y.hi && X.hi <= Z.hi;
+    const bool my = !mx && Y.hi <= Z.hi;
+    const bool mz = !mx && !my;
+    const float amax = mx ? X.hi : (my ? Y.hi : Z.hi);
+    if (amin < amax) {
+      const unsigned jp = (unsigned)((zs ? X.idx : Y.idx) - sl.p0);
+      const unsigned jq = (unsigned)((zs ? Y.idx : Z.idx) - sl.q0);
+      if (jp < (unsigned)sl.wp && jq < (unsigned)sl.wq) {
+        const int c = sl.off + (int)jp * sl.wq + (int)jq;
+        // units = RN(len * scale) split as hi * 2^split + lo; for a product
+        // >= 2^split the float is an integer and both parts are exact
+        const float v = fmul(fmul(fsub(amax, amin), L), scale);
+        const uint32_t h = __float2uint_rz(fmul(v, inv_two_s));
+        uint32_t l = __float2uint_rn(__fmaf_rn(-__uint2float_rn(h), two_s, v));
+        if ((h | l) == 0u) l = 1u;  // a positive chord counts at least one unit
+        atomicAdd(&w.lo[c], l);
+        if (h) atomicAdd(&w.hi[c], h);
+      } else {
+        atomicAdd(outside, 1);
+      }
+    }
+    // advance the axis whose plane comes first
+    const int st = mx ? X.step : (my ? Y.step : Z.step);
+    const int ni = (mx ? X.idx : (my ? Y.idx : Z.idx)) + st;
+    const int nn = mx ? X.n : (my ? Y.n : Z.n);
+    if (ni >= 0 && ni < nn) {
+      const float kh = (mx ? X.kh : (my ? Y.kh : Z.kh)) + (st > 0 ? 1.f : -1.f);
+      const float o = mx ? X.o : (my ? Y.o : Z.o), d = mx ? X.d : (my ? Y.d : Z.d);
+      const float r0 = mx ? X.r0 : (my ? Y.r0 : Z.r0), dr = mx ? X.dr : (my ? Y.dr : Z.dr);
+      const float inv = mx ? X.inv : (my ? Y.inv : Z.inv);
+      const float h = div_cr(fsub(fadd(o, fmul(kh, d)), r0), dr, inv);
+      X.lo = mx ? X.hi : X.lo; X.hi = mx ? h : X.hi; X.kh = mx ? kh : X.kh; X.idx = mx ? ni : X.idx;
+      Y.lo = my ? Y.hi : Y.lo; Y.hi = my ? h : Y.hi; Y.kh = my ? kh : Y.kh; Y.idx = my ? ni : Y.idx;
+      Z.lo = mz ? Z.hi : Z.lo; Z.hi = mz ? h : Z.hi; Z.kh = mz ? kh : Z.kh; Z.idx = mz ? ni : Z.idx;
+      if (zs ? mz : mx) sl = slabs[ni];
+    } else {
+      // left the grid: the part before the starting cell, if any
+      if (second) break;
+      second = true;
+      a_stop = a_start;
+      X.enter(a_in);
+      Y.enter(a_in);
+      Z.enter(a_in);
+      sl = slabs[zs ? Z.idx : X.idx];
+    }
   }
 }
 

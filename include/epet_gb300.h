@@ -128,6 +128,12 @@ epet_status epet_trig_table(const epet_problem* p, float* sc_d,
  * getSystemMatrixFromWorkqueue.cu:189-204). */
 epet_status epet_dump_uniforms(const epet_problem* p, const int32_t* rows_d,
                                int64_t m, float* out_d, epet_stream_t stream);
+/* Library self-test (no counterpart in the reference): compares the walk
+ * kernel's reciprocal-based correctly rounded division with the hardware's
+ * IEEE division on n seeded operand pairs; *mismatches_h counts differing
+ * results (0 expected).  Synchronous. */
+epet_status epet_selftest_division(int64_t n, uint64_t seed, int64_t* mismatches_h,
+                                   epet_stream_t stream);
 /* World-coordinate rays out_d[m][nrays][6] (RandRayGen, RayGenerators.hpp:
  * 15-40 with the per-channel seeding of getSystemMatrixFromWorkqueue.cu). */
 epet_status epet_rays(const epet_problem* p, const int32_t* rows_d, int64_t m,

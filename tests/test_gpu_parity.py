@@ -172,3 +172,14 @@ def test_csc_is_stable_transpose(case):
     assert (At.col_ptr.cpu().numpy() == np.cumsum(cp)).all()
     assert (At.row.cpu().numpy() == r[order]).all()
     assert (bits(At.val.cpu().numpy()) == bits(val[order])).all()
+
+
+def test_walk_division_is_correctly_rounded(gpu_lib):
+    """The walk divides by a per-ray reciprocal (Markstein's correction);
+    it must agree bit for bit with the IEEE division on the device."""
+    import ctypes as C
+    from epetreco_gb300._lib import check, lib
+    bad = C.c_int64(-1)
+    check(lib().epet_selftest_division(1 << 26, 20260512, C.byref(bad),
+                                       C.c_void_p(torch.cuda.current_stream().cuda_stream)))
+    assert bad.value == 0
