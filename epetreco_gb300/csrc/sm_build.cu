@@ -253,6 +253,15 @@ __device__ void walk_ray(const Geo& G, const float* ray, const Window& w, const 
   if (!(a_in < a_out)) return;
   float a_s = a_in + (a_out - a_in) * frac;
   if (!(a_s >= a_in && a_s < a_out)) a_s = a_in;
+  // entry state of the second part (the cells before the starting cell),
+  // computed up front by all lanes together: the switch in the loop is then
+  // a register copy, not a divergent search
+  X.enter(a_in);
+  Y.enter(a_in);
+  Z.enter(a_in);
+  const int ex = X.idx, ey = Y.idx, ez = Z.idx;
+  const float exl = X.lo, exh = X.hi, exk = X.kh, eyl = Y.lo, eyh = Y.hi, eyk = Y.kh;
+  const float ezl = Z.lo, ezh = Z.hi, ezk = Z.kh;
   X.enter(a_s);
   Y.enter(a_s);
   Z.enter(a_s);
@@ -308,10 +317,10 @@ __device__ void walk_ray(const Geo& G, const float* ray, const Window& w, const 
       if (second) break;
       second = true;
       a_stop = a_start;
-      X.enter(a_in);
-      Y.enter(a_in);
-      Z.enter(a_in);
-      sl = slabs[zs ? Z.idx : X.idx];
+      X.idx = ex; X.lo = exl; X.hi = exh; X.kh = exk;
+      Y.idx = ey; Y.lo = eyl; Y.hi = eyh; Y.kh = eyk;
+      Z.idx = ez; Z.lo = ezl; Z.hi = ezh; Z.kh = ezk;
+      sl = slabs[zs ? ez : ex];
     }
   }
 }
