@@ -18,26 +18,21 @@ __global__ void k_trig(epet_setup s, float* sc) {
 
 // One thread per channel: the cuRAND stream of a channel is sequential, so a
 // channel's 6*nrays draws stay on one thread; channels spread over threads.
-template <bool kUniformsOnly>
-__global__ void __launch_bounds__(128) k_rays(Geo G, const int32_t* __restrict__ rows,
-                                              int64_t m, float* __restrict__ out) {
-  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= m) return;
-  const int cnl = rows[i];
+// The uniforms-only form (a test and debugging interface) seeds every
+// channel with curand_init(seed, channel, 0) directly.
+__device__ __forceinline__ void emit_rays(const Geo& G, int cnl, curandState st, bool uniforms,
+                                          float2* o) {
   int id[5];
   channel_decode(G.p.setup, cnl, id);
   float sn, cs;
   angle_sincos(G.p.setup, id[0], &sn, &cs);
   const CrystalMat m0 = crystal_matrix(G.p.setup, sn, cs, 0, id[1], id[2]);
   const CrystalMat m1 = crystal_matrix(G.p.setup, sn, cs, 1, id[3], id[4]);
-  curandState st;
-  curand_init(G.p.seed, (unsigned long long)cnl, 0ull, &st);
-  float2* o = reinterpret_cast<float2*>(out + i * (int64_t)G.p.nrays * 6);
   for (int r = 0; r < G.p.nrays; r++) {
     float u[6];
 #pragma unroll
     for (int k = 0; k < 6; k++) u[k] = curand_uniform(&st);
-    if (kUniformsOnly) {
+    if (uniforms) {
       o[3 * r + 0] = make_float2(u[0], u[1]);
       o[3 * r + 1] = make_float2(u[2], u[3]);
       o[3 * r + 2] = make_float2(u[4], u[5]);
@@ -49,6 +44,44 @@ __global__ void __launch_bounds__(128) k_rays(Geo G, const int32_t* __restrict__
       o[3 * r + 1] = make_float2(p0[2], p1[0]);
       o[3 * r + 2] = make_float2(p1[1], p1[2]);
     }
+  }
+}
+
+__global__ void __launch_bounds__(128) k_uniforms(Geo G, const int32_t* __restrict__ rows,
+                                                  int64_t m, float* __restrict__ out) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= m) return;
+  curandState st;
+  curand_init(G.p.seed, (unsigned long long)rows[i], 0ull, &st);
+  emit_rays(G, rows[i], st, true,
+            reinterpret_cast<float2*>(out + i * (int64_t)G.p.nrays * 6));
+}
+
+// World rays.  Thread t handles rows t*K .. t*K+K-1: the first channel's
+// generator comes from curand_init, the next ones from the previous
+// channel's initial state advanced by the channel difference in
+// subsequences (skipahead_sequence): curand_init(seed, c, 0) is the seeded
+// state advanced c subsequences, so this yields the same states while a
+// typical step (consecutive channel ids) applies one jump matrix instead of
+// one per set bit of the channel id.
+constexpr int kRaysPerThread = 8;
+__global__ void __launch_bounds__(128) k_rays(Geo G, const int32_t* __restrict__ rows,
+                                              int64_t m, float* __restrict__ out) {
+  const int64_t i0 = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) * kRaysPerThread;
+  if (i0 >= m) return;
+  const int64_t i1 = i0 + kRaysPerThread < m ? i0 + kRaysPerThread : m;
+  curandState base;
+  int prev = rows[i0];
+  curand_init(G.p.seed, (unsigned long long)prev, 0ull, &base);
+  for (int64_t i = i0; i < i1; i++) {
+    const int cnl = rows[i];
+    if (i > i0) {
+      if (cnl > prev) skipahead_sequence((unsigned long long)(cnl - prev), &base);
+      else if (cnl != prev) curand_init(G.p.seed, (unsigned long long)cnl, 0ull, &base);
+      prev = cnl;
+    }
+    emit_rays(G, cnl, base, false,
+              reinterpret_cast<float2*>(out + i * (int64_t)G.p.nrays * 6));
   }
 }
 
@@ -91,9 +124,10 @@ epet_status launch_rays(const Geo& G, const int32_t* rows, int64_t m, float* out
                         bool uniforms_only, cudaStream_t st) {
   if (m == 0) return EPET_OK;
   const int T = 128;
-  const int nb = ceil_div(m, T);
-  if (uniforms_only) k_rays<true><<<nb, T, 0, st>>>(G, rows, m, out);
-  else k_rays<false><<<nb, T, 0, st>>>(G, rows, m, out);
+  if (uniforms_only)
+    k_uniforms<<<ceil_div(m, T), T, 0, st>>>(G, rows, m, out);
+  else
+    k_rays<<<ceil_div(ceil_div(m, kRaysPerThread), T), T, 0, st>>>(G, rows, m, out);
   EPET_LAUNCHED();
   return EPET_OK;
 }

@@ -506,7 +506,9 @@ k_walk(WalkArgs args) {
     bx0 = bb[0]; bx1 = bb[1]; by0 = bb[2]; by1 = bb[3];
     E = bx1 < bx0 ? 0 : (bx1 - bx0 + 1) * (by1 - by0 + 1) * g.n[2];
   }
-  const int cpt = (E + kWalkThreads - 1) / kWalkThreads;
+  // odd range length: the lanes' concurrent window reads fall in distinct
+  // shared-memory banks
+  const int cpt = ((E + kWalkThreads - 1) / kWalkThreads) | 1;
   const int cbeg = min(E, (int)threadIdx.x * cpt), cend = min(E, cbeg + cpt);
   // Visits the thread's enumeration range in order; f(cell, ix, iy, iz)
   // for every window cell met.
@@ -518,12 +520,21 @@ k_walk(WalkArgs args) {
         if (slabs[mid].off <= cbeg) lo_s = mid;
         else hi_s = mid - 1;
       }
+      if (cbeg >= cend) return;
       int sx = lo_s;
+      Slab sl = slabs[sx];  // holds cell cbeg (cbeg < W)
+      int jp = (cbeg - sl.off) / sl.wq, jq = cbeg - sl.off - jp * sl.wq;
       for (int cidx = cbeg; cidx < cend; cidx++) {
-        while (cidx >= slabs[sx].off + slabs[sx].wp * slabs[sx].wq) sx++;
-        const Slab sl = slabs[sx];
-        const int k = cidx - sl.off;
-        f(cidx, sx, sl.p0 + k / sl.wq, sl.q0 + k % sl.wq);
+        while (cidx >= sl.off + sl.wp * sl.wq) {  // next slab with cells
+          sl = slabs[++sx];
+          jp = 0;
+          jq = 0;
+        }
+        f(cidx, sx, sl.p0 + jp, sl.q0 + jq);
+        if (++jq == sl.wq) {
+          jq = 0;
+          ++jp;
+        }
       }
     } else {
       if (cbeg >= cend) return;
@@ -563,6 +574,7 @@ k_walk(WalkArgs args) {
     const float v = fdiv(fmul(__ull2float_rn(u), G.fx_inv), fR);
     const int vox = ix * G.nyz + iy * g.n[2] + iz;
     cnt++;
+    if (kMode == kModeCsr) win.lo[cidx] = __float_as_uint(v);  // > 0: read by pass 2
     if (kMode == kModeForward) fsum = fadd(fsum, fmul(v, args.x[vox]));
     if (kMode == kModeBack) {
       const float ev = args.e[row];
@@ -574,11 +586,10 @@ k_walk(WalkArgs args) {
     const int pos = block_excl_scan(cnt, warp_tot, &s_total);
     int64_t o = slot * args.stride + pos;
     for_cells([&](int cidx, int ix, int iy, int iz) {
-      const unsigned long long u =
-          ((unsigned long long)win.hi[cidx] << win.split) + (unsigned long long)win.lo[cidx];
-      if (u == 0ull) return;
+      const uint32_t vb = win.lo[cidx];  // the value's bits, 0 when dropped
+      if (vb == 0u) return;
       args.stage_col[o] = ix * G.nyz + iy * g.n[2] + iz;
-      args.stage_val[o] = fdiv(fmul(__ull2float_rn(u), G.fx_inv), fR);
+      args.stage_val[o] = __uint_as_float(vb);
       o++;
     });
     if (threadIdx.x == 0) {

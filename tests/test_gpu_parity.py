@@ -183,3 +183,19 @@ def test_walk_division_is_correctly_rounded(gpu_lib):
     check(lib().epet_selftest_division(1 << 26, 20260512, C.byref(bad),
                                        C.c_void_p(torch.cuda.current_stream().cuda_stream)))
     assert bad.value == 0
+
+
+def test_rays_every_row_any_order(gpu_lib, oracle):
+    """Rays of consecutive, gapped, repeated and descending channel lists:
+    the generator of each row must be curand_init(seed, channel, 0), however
+    the rays kernel reaches it."""
+    p = config("small")["problem"]
+    rng = np.random.default_rng(5)
+    rows = np.concatenate([np.arange(1000, 1300), np.sort(rng.choice(p.nchannels, 200, False)),
+                           [77, 77, 76, 3, 200000, 9]]).astype(np.int32)
+    trig = api.trig_table(p).cpu().numpy()
+    rnd = api.dump_uniforms(p, dev(rows)).cpu().numpy()
+    got = api.rays(p, dev(rows)).cpu().numpy()
+    for i in range(len(rows)):
+        want = oracle.rays(p, rows[i], rnd[i], trig=trig)
+        assert (bits(got[i]) == bits(want)).all(), i
