@@ -14,13 +14,8 @@ size_t scan_tmp_elems(int64_t n);
 epet_status exclusive_scan_i64(const int64_t* in, int64_t* out, int64_t n,
                                int64_t* tmp, cudaStream_t st);
 
-// Stable LSD radix sort of (uint64 key, uint64 value) pairs on the low `bits`
-// bits of the key.  keys/vals are sorted in place; alt_* are same-sized
-// buffers; hist holds radix_hist_elems(n) uint32.
+// Radix sort histogram size (int64 entries) for n items (sort.cu).
 size_t radix_hist_elems(int64_t n);
-epet_status radix_sort_pairs(uint64_t* keys, uint64_t* vals, uint64_t* alt_keys,
-                             uint64_t* alt_vals, int64_t n, int bits,
-                             uint32_t* hist, int64_t* scan_tmp, cudaStream_t st);
 
 // Row walk configuration chosen for a problem (per-row accumulator size).
 int auto_row_capacity(const epet_problem& p);

@@ -118,34 +118,52 @@ static int bits_for(int64_t maxval) {
 
 // ------------------------------------------------------------ radix sort
 //
-// Stable LSD radix sort with BITS-bit digits.  Per pass: a histogram kernel
-// (tile x digit counts), an exclusive scan of the digit-major histogram, and
-// a scatter kernel.  The scatter ranks the tile's items stably -- warp w owns
-// items [w*512, (w+1)*512) and ranks them in 16 rounds of 32 consecutive
-// items with __match_any_sync -- then stages the tile in shared memory in
-// digit order, so the global writes of each digit are contiguous runs.
-// Input and output go through adapters, so the first pass can read a CSR
-// directly and the last pass can write the column-major arrays.
+// Stable LSD radix sort with BITS-bit digits, reduce-then-scan over chunks:
+// the input is cut into nchunks equal runs of whole tiles (a few per SM);
+// the histogram kernel counts each chunk's digits (BINS x nchunks counts),
+// an exclusive scan of the digit-major counts gives every (digit, chunk) its
+// output start, and the scatter kernel walks its chunk's tiles in order,
+// keeping a running output offset per digit.  Within a tile, items are
+// ranked stably -- warp w owns items [w*512, (w+1)*512) and ranks them in 16
+// rounds of 32 consecutive items with __match_any_sync -- and staged in
+// shared memory in digit order, so each digit's global writes are
+// contiguous runs.  Input and output go through adapters, so the first pass
+// of the column-major copy reads a CSR directly and the last one writes the
+// CSC arrays and its column starts.
 constexpr int kRsThreads = 256, kRsItems = 16, kRsTile = kRsThreads * kRsItems;
 constexpr int kRsWarps = kRsThreads / 32;
+constexpr int kRsMaxChunks = 2048;
 
-template <int BITS, typename K>
+struct RsGrid {
+  int64_t tiles, tpc;  // tiles, tiles per chunk
+  int nchunks;
+};
+static RsGrid rs_grid(int64_t n) {
+  RsGrid g;
+  g.tiles = std::max<int64_t>(1, (n + kRsTile - 1) / kRsTile);
+  int dev = 0, sms = 148;
+  if (cudaGetDevice(&dev) == cudaSuccess)
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  const int64_t want = std::min<int64_t>(kRsMaxChunks, 3 * (int64_t)sms);
+  g.tpc = (g.tiles + want - 1) / want;
+  g.nchunks = (int)((g.tiles + g.tpc - 1) / g.tpc);
+  return g;
+}
+
+template <int BITS, typename In>
 __global__ void __launch_bounds__(kRsThreads)
-k_radix_hist(const K* __restrict__ keys, int64_t n, int shift, int64_t ntiles,
-             int64_t* __restrict__ hist) {
+k_radix_hist(In in, int64_t n, int shift, int64_t tpc, int nchunks, int64_t* __restrict__ hist) {
   constexpr int BINS = 1 << BITS;
   __shared__ unsigned cnt[BINS];
   for (int d = threadIdx.x; d < BINS; d += kRsThreads) cnt[d] = 0;
   __syncthreads();
-  const int64_t base = (int64_t)blockIdx.x * kRsTile;
-#pragma unroll 4
-  for (int k = 0; k < kRsItems; k++) {
-    const int64_t i = base + k * kRsThreads + threadIdx.x;
-    if (i < n) atomicAdd(&cnt[(unsigned)(keys[i] >> shift) & (BINS - 1)], 1u);
-  }
+  const int64_t beg = (int64_t)blockIdx.x * tpc * kRsTile;
+  const int64_t end = min(n, beg + tpc * kRsTile);
+  for (int64_t i = beg + threadIdx.x; i < end; i += kRsThreads)
+    atomicAdd(&cnt[(unsigned)(in.key(i) >> shift) & (BINS - 1)], 1u);
   __syncthreads();
   for (int d = threadIdx.x; d < BINS; d += kRsThreads)
-    hist[(int64_t)d * ntiles + blockIdx.x] = cnt[d];
+    hist[(int64_t)d * nchunks + blockIdx.x] = cnt[d];
 }
 
 // Plain arrays in / out.
@@ -153,194 +171,198 @@ template <typename K, typename V>
 struct ArrIn {
   const K* k;
   const V* v;
-  __device__ void prepare(int64_t, int64_t) {}
+  __device__ void begin(int64_t) {}
   __device__ K key(int64_t i) const { return k[i]; }
-  __device__ V val(int64_t i) const { return v[i]; }
+  __device__ V val(int64_t i) { return v[i]; }
 };
 template <typename K, typename V>
 struct ArrOut {
   K* k;
   V* v;
-  __device__ void put(int64_t pos, K key, V val) const {
+  __device__ void put(int64_t pos, K key, V val, bool) const {
     k[pos] = key;
     v[pos] = val;
   }
 };
 
-// CSR in: key = column, value = (row << 32) | value bits.  The row of entry
-// i is found by binary search among the rows spanning the tile.
+// CSR in: key = column, value = (row << 32) | value bits.  Each lane tracks
+// the row of the entries it reads: a warp-uniform binary search for the
+// first entry of the warp's range, then forward steps (a lane's entries
+// increase).
 struct CsrIn {
   const int64_t* row_ptr;
   int64_t m;
   const int32_t* col;
   const float* vals;
-  int64_t r_lo, r_hi;  // rows spanning the current tile
-  __device__ static int64_t row_of(const int64_t* rp, int64_t lo, int64_t hi, int64_t i) {
-    // last row r in [lo, hi] with rp[r] <= i
+  int64_t cur;  // this lane's current row
+  __device__ void begin(int64_t first) {
+    int64_t lo = 0, hi = m - 1;  // last row r with row_ptr[r] <= first
     while (lo < hi) {
       const int64_t mid = (lo + hi + 1) >> 1;
-      if (rp[mid] <= i) lo = mid;
+      if (row_ptr[mid] <= first) lo = mid;
       else hi = mid - 1;
     }
-    return lo;
-  }
-  __device__ void prepare(int64_t first, int64_t last) {
-    __shared__ int64_t rr[2];
-    if (threadIdx.x == 0) {
-      rr[0] = row_of(row_ptr, 0, m - 1, first);
-      rr[1] = row_of(row_ptr, 0, m - 1, last);
-    }
-    __syncthreads();
-    r_lo = rr[0];
-    r_hi = rr[1];
+    cur = lo;
   }
   __device__ uint32_t key(int64_t i) const { return (uint32_t)col[i]; }
-  __device__ uint64_t val(int64_t i) const {
-    const int64_t r = row_of(row_ptr, r_lo, r_hi, i);
-    return ((uint64_t)(uint32_t)r << 32) | __float_as_uint(vals[i]);
+  __device__ uint64_t val(int64_t i) {
+    while (cur + 1 < m && row_ptr[cur + 1] <= i) cur++;
+    return ((uint64_t)(uint32_t)cur << 32) | __float_as_uint(vals[i]);
   }
 };
 
-// CSC out: row and value arrays, plus the sorted column ids.
+// CSC out: row and value arrays; the first position of every column goes to
+// col_first (atomicMin, initialised to nnz; empty columns are filled in
+// afterwards by a suffix minimum).  Only the last pass writes this form, so
+// a staged run of one digit is sorted by the full key.
 struct CscOut {
   int32_t* row;
   float* val;
-  uint32_t* key;
-  __device__ void put(int64_t pos, uint32_t k, uint64_t v) const {
+  int64_t* col_first;
+  __device__ void put(int64_t pos, uint32_t k, uint64_t v, bool first) const {
     row[pos] = (int32_t)(v >> 32);
     val[pos] = __uint_as_float((uint32_t)v);
-    key[pos] = k;
+    if (first) atomicMin(reinterpret_cast<unsigned long long*>(col_first + k),
+                         (unsigned long long)pos);
   }
 };
 
 template <int BITS, typename K, typename V, typename In, typename Out>
 __global__ void __launch_bounds__(kRsThreads)
-k_radix_scatter(In in, Out out, int64_t n, int shift, int64_t ntiles,
+k_radix_scatter(In in, Out out, int64_t n, int shift, int64_t tpc, int nchunks,
                 const int64_t* __restrict__ offs) {
   constexpr int BINS = 1 << BITS;
   __shared__ unsigned wcnt[kRsWarps][BINS];
   __shared__ unsigned dstart[BINS + 1];
   __shared__ unsigned warp_tot[kRsWarps];
+  __shared__ int64_t run[BINS];  // output position of the chunk's next item of each digit
   extern __shared__ __align__(16) unsigned char rs_dyn[];  // staged tile
   V* sv = reinterpret_cast<V*>(rs_dyn);
   K* sk = reinterpret_cast<K*>(rs_dyn + sizeof(V) * kRsTile);
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-  const int64_t tile0 = (int64_t)blockIdx.x * kRsTile;
-  const int tile_n = (int)(n - tile0 < kRsTile ? n - tile0 : kRsTile);
-  in.prepare(tile0, tile0 + tile_n - 1);
-  for (int d = lane; d < BINS; d += 32) wcnt[w][d] = 0;
-  __syncwarp();
-  const int64_t wbase = tile0 + (int64_t)w * (kRsItems * 32);
-  K kk[kRsItems];
-  V vv[kRsItems];
-  unsigned rank[kRsItems];
-  const unsigned lt = (1u << lane) - 1u;
-#pragma unroll
-  for (int r = 0; r < kRsItems; r++) {
-    const int64_t i = wbase + r * 32 + lane;
-    const bool ok = i < n;
-    kk[r] = ok ? in.key(i) : K(0);
-    vv[r] = ok ? in.val(i) : V(0);
-    const unsigned dig = ok ? ((unsigned)(kk[r] >> shift) & (BINS - 1)) : BINS + lane;
-    const unsigned peers = __match_any_sync(0xffffffffu, dig);
-    unsigned before = 0;
-    if (ok) before = wcnt[w][dig];
-    rank[r] = before + __popc(peers & lt);
-    __syncwarp();
-    const int leader = 31 - __clz(peers);
-    if (ok && lane == leader) wcnt[w][dig] = before + __popc(peers);
-    __syncwarp();
-  }
-  __syncthreads();
-  // per digit: warp offsets (exclusive over warps) and the digit total
+  for (int d = threadIdx.x; d < BINS; d += kRsThreads) run[d] = offs[(int64_t)d * nchunks + blockIdx.x];
   constexpr int DPT = (BINS + kRsThreads - 1) / kRsThreads;  // digits per thread
-  unsigned tot[DPT];
-  unsigned mysum = 0;
+  const unsigned lt = (1u << lane) - 1u;
+  for (int64_t t = 0; t < tpc; t++) {
+    const int64_t tile0 = ((int64_t)blockIdx.x * tpc + t) * kRsTile;
+    if (tile0 >= n) break;
+    const int tile_n = (int)(n - tile0 < kRsTile ? n - tile0 : kRsTile);
+    for (int d = lane; d < BINS; d += 32) wcnt[w][d] = 0;
+    __syncwarp();
+    const int64_t wbase = tile0 + (int64_t)w * (kRsItems * 32);
+    if (wbase < n) in.begin(wbase);  // uniform across the warp
+    K kk[kRsItems];
+    V vv[kRsItems];
+    unsigned rank[kRsItems];
 #pragma unroll
-  for (int q = 0; q < DPT; q++) {
-    const int d = threadIdx.x * DPT + q;
-    unsigned run = 0;
-    if (d < BINS) {
-      for (int ww = 0; ww < kRsWarps; ww++) {
-        const unsigned c = wcnt[ww][d];
-        wcnt[ww][d] = run;
-        run += c;
-      }
+    for (int r = 0; r < kRsItems; r++) {
+      const int64_t i = wbase + r * 32 + lane;
+      const bool ok = i < n;
+      kk[r] = ok ? in.key(i) : K(0);
+      vv[r] = ok ? in.val(i) : V(0);
+      const unsigned dig = ok ? ((unsigned)(kk[r] >> shift) & (BINS - 1)) : BINS + lane;
+      const unsigned peers = __match_any_sync(0xffffffffu, dig);
+      unsigned before = 0;
+      if (ok) before = wcnt[w][dig];
+      rank[r] = before + __popc(peers & lt);
+      __syncwarp();
+      const int leader = 31 - __clz(peers);
+      if (ok && lane == leader) wcnt[w][dig] = before + __popc(peers);
+      __syncwarp();
     }
-    tot[q] = run;
-    mysum += run;
-  }
-  // exclusive scan of the digit totals (block-wide, digits in thread order)
-  unsigned inc = mysum;
-#pragma unroll
-  for (int o = 1; o < 32; o <<= 1) {
-    const unsigned t = __shfl_up_sync(0xffffffffu, inc, o);
-    if (lane >= o) inc += t;
-  }
-  if (lane == 31) warp_tot[w] = inc;
-  __syncthreads();
-  if (w == 0) {
-    const unsigned t = lane < kRsWarps ? warp_tot[lane] : 0u;
-    unsigned ti = t;
-#pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-      const unsigned u = __shfl_up_sync(0xffffffffu, ti, o);
-      if (lane >= o) ti += u;
-    }
-    if (lane < kRsWarps) warp_tot[lane] = ti - t;
-  }
-  __syncthreads();
-  {
-    unsigned run = warp_tot[w] + inc - mysum;
+    __syncthreads();
+    // per digit: warp offsets (exclusive over warps) and the digit total
+    unsigned tot[DPT];
+    unsigned mysum = 0;
 #pragma unroll
     for (int q = 0; q < DPT; q++) {
       const int d = threadIdx.x * DPT + q;
-      if (d < BINS) dstart[d] = run;
-      run += tot[q];
+      unsigned acc = 0;
+      if (d < BINS) {
+        for (int ww = 0; ww < kRsWarps; ww++) {
+          const unsigned c = wcnt[ww][d];
+          wcnt[ww][d] = acc;
+          acc += c;
+        }
+      }
+      tot[q] = acc;
+      mysum += acc;
     }
-  }
-  __syncthreads();
-  // stage in digit order
+    // exclusive scan of the digit totals (block-wide, digits in thread order)
+    unsigned inc = mysum;
 #pragma unroll
-  for (int r = 0; r < kRsItems; r++) {
-    const int64_t i = wbase + r * 32 + lane;
-    if (i < n) {
-      const unsigned dig = (unsigned)(kk[r] >> shift) & (BINS - 1);
-      const unsigned lp = dstart[dig] + wcnt[w][dig] + rank[r];
-      sk[lp] = kk[r];
-      sv[lp] = vv[r];
+    for (int o = 1; o < 32; o <<= 1) {
+      const unsigned u = __shfl_up_sync(0xffffffffu, inc, o);
+      if (lane >= o) inc += u;
     }
-  }
-  __syncthreads();
-  // contiguous runs per digit
-  for (int j = threadIdx.x; j < tile_n; j += kRsThreads) {
-    const K key = sk[j];
-    const unsigned dig = (unsigned)(key >> shift) & (BINS - 1);
-    const int64_t pos = offs[(int64_t)dig * ntiles + blockIdx.x] + (j - (int)dstart[dig]);
-    out.put(pos, key, sv[j]);
+    if (lane == 31) warp_tot[w] = inc;
+    __syncthreads();
+    if (w == 0) {
+      const unsigned u = lane < kRsWarps ? warp_tot[lane] : 0u;
+      unsigned ti = u;
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const unsigned x = __shfl_up_sync(0xffffffffu, ti, o);
+        if (lane >= o) ti += x;
+      }
+      if (lane < kRsWarps) warp_tot[lane] = ti - u;
+    }
+    __syncthreads();
+    {
+      unsigned acc = warp_tot[w] + inc - mysum;
+#pragma unroll
+      for (int q = 0; q < DPT; q++) {
+        const int d = threadIdx.x * DPT + q;
+        if (d < BINS) dstart[d] = acc;
+        acc += tot[q];
+      }
+      if (threadIdx.x == kRsThreads - 1) dstart[BINS] = acc;
+    }
+    __syncthreads();
+    // stage in digit order
+#pragma unroll
+    for (int r = 0; r < kRsItems; r++) {
+      const int64_t i = wbase + r * 32 + lane;
+      if (i < n) {
+        const unsigned dig = (unsigned)(kk[r] >> shift) & (BINS - 1);
+        const unsigned lp = dstart[dig] + wcnt[w][dig] + rank[r];
+        sk[lp] = kk[r];
+        sv[lp] = vv[r];
+      }
+    }
+    __syncthreads();
+    // contiguous runs per digit
+    for (int j = threadIdx.x; j < tile_n; j += kRsThreads) {
+      const K key = sk[j];
+      const unsigned dig = (unsigned)(key >> shift) & (BINS - 1);
+      const bool first = (unsigned)j == dstart[dig] || sk[j - 1] != key;
+      out.put(run[dig] + (j - (int)dstart[dig]), key, sv[j], first);
+    }
+    __syncthreads();
+    for (int d = threadIdx.x; d < BINS; d += kRsThreads) run[d] += dstart[d + 1] - dstart[d];
+    __syncthreads();
   }
 }
 
 size_t radix_hist_elems(int64_t n) {
   const int64_t tiles = std::max<int64_t>(1, (n + kRsTile - 1) / kRsTile);
-  return (size_t)512 * tiles;
+  return (size_t)512 * (size_t)std::min<int64_t>(tiles, kRsMaxChunks);
 }
 
-// One pass: histogram of the keys (any array holding this pass's keys), scan,
-// scatter from `in` to `out`.
+// One pass: histogram of `in`'s keys, scan, scatter from `in` to `out`.
 template <int BITS, typename K, typename V, typename In, typename Out>
-epet_status radix_pass(const K* hist_keys, In in, Out out, int64_t n, int shift, int64_t* hist,
-                       int64_t* hist_scan, int64_t* scan_tmp, cudaStream_t st) {
-  const int64_t ntiles = (n + kRsTile - 1) / kRsTile;
-  k_radix_hist<BITS, K><<<(unsigned)ntiles, kRsThreads, 0, st>>>(hist_keys, n, shift, ntiles,
-                                                                 hist);
+epet_status radix_pass(In in, Out out, int64_t n, int shift, int64_t* hist, int64_t* hist_scan,
+                       int64_t* scan_tmp, cudaStream_t st) {
+  const RsGrid g = rs_grid(n);
+  k_radix_hist<BITS, In><<<(unsigned)g.nchunks, kRsThreads, 0, st>>>(in, n, shift, g.tpc,
+                                                                     g.nchunks, hist);
   EPET_LAUNCHED();
-  EPET_CHECK(exclusive_scan_i64(hist, hist_scan, (int64_t)(1 << BITS) * ntiles, scan_tmp, st));
+  EPET_CHECK(exclusive_scan_i64(hist, hist_scan, (int64_t)(1 << BITS) * g.nchunks, scan_tmp, st));
   const size_t dyn = (sizeof(K) + sizeof(V)) * (size_t)kRsTile;
   EPET_CUDA(cudaFuncSetAttribute(k_radix_scatter<BITS, K, V, In, Out>,
                                  cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn));
-  k_radix_scatter<BITS, K, V, In, Out><<<(unsigned)ntiles, kRsThreads, dyn, st>>>(
-      in, out, n, shift, ntiles, hist_scan);
+  k_radix_scatter<BITS, K, V, In, Out><<<(unsigned)g.nchunks, kRsThreads, dyn, st>>>(
+      in, out, n, shift, g.tpc, g.nchunks, hist_scan);
   EPET_LAUNCHED();
   return EPET_OK;
 }
@@ -355,7 +377,7 @@ epet_status radix_sort(K* keys, Vt* vals, K* alt_keys, Vt* alt_vals, int64_t n, 
   Vt *src_v = vals, *dst_v = alt_vals;
   int passes = 0;
   for (int shift = 0; shift < bits; shift += 8, passes++) {
-    EPET_CHECK((radix_pass<8, K, Vt>(src_k, ArrIn<K, Vt>{src_k, src_v}, ArrOut<K, Vt>{dst_k, dst_v},
+    EPET_CHECK((radix_pass<8, K, Vt>(ArrIn<K, Vt>{src_k, src_v}, ArrOut<K, Vt>{dst_k, dst_v},
                                       n, shift, hist, hist_scan, scan_tmp, st)));
     std::swap(src_k, dst_k);
     std::swap(src_v, dst_v);
@@ -443,17 +465,33 @@ __global__ void k_csr2ecsr(int64_t* ecsr, const int32_t* yrow, int64_t nnzr,
   if (i == nnzr) ecsr[nnzr] = csr[m];
 }
 
-__global__ void k_colptr_from_sorted(const uint32_t* __restrict__ key, int64_t nnz,
-                                     int64_t n, int64_t* __restrict__ col_ptr) {
-  const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (c > n) return;
-  int64_t lo = 0, hi = nnz;
-  while (lo < hi) {
-    const int64_t mid = (lo + hi) >> 1;
-    if ((int64_t)key[mid] < c) lo = mid + 1;
-    else hi = mid;
+__global__ void k_fill_i64(int64_t* p, int64_t n, int64_t v) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) p[i] = v;
+}
+
+// p[i] = min(p[i..n-1]) by one block: per-thread chunk minima, a block-wide
+// suffix scan of them, then the chunks.
+__global__ void __launch_bounds__(1024) k_suffix_min_i64(int64_t* p, int64_t n) {
+  __shared__ int64_t cm[1024];
+  const int t = threadIdx.x;
+  const int64_t per = (n + 1023) / 1024;
+  const int64_t b = min(n, t * per), e = min(n, b + per);
+  int64_t m = INT64_MAX;
+  for (int64_t i = e - 1; i >= b; i--) m = min(m, p[i]);
+  cm[t] = m;
+  __syncthreads();
+  for (int o = 1; o < 1024; o <<= 1) {
+    const int64_t v = t + o < 1024 ? cm[t + o] : INT64_MAX;
+    __syncthreads();
+    cm[t] = min(cm[t], v);
+    __syncthreads();
   }
-  col_ptr[c] = lo;
+  int64_t run = t + 1 < 1024 ? cm[t + 1] : INT64_MAX;
+  for (int64_t i = e - 1; i >= b; i--) {
+    run = min(run, p[i]);
+    p[i] = run;
+  }
 }
 
 }  // namespace epet
@@ -533,7 +571,7 @@ size_t epet_csr_to_csc_workspace_size(int64_t m, int64_t n, int64_t nnz) {
   (void)m;
   (void)n;
   const size_t hist = radix_hist_elems(nnz);
-  return 2 * align256(nnz * 4) + align256(nnz * 8) + align256(hist * 8) +
+  return align256(nnz * 4) + align256(nnz * 8) + align256(hist * 8) +
          align256((hist + 1) * 8) + align256(scan_tmp_elems(hist) * 8) + 256;
 }
 
@@ -553,44 +591,34 @@ epet_status epet_csr_to_csc(const epet_csr* a, epet_csc* out, void* ws, size_t w
   Scratch scr;
   EPET_CHECK(scr.init(ws, ws_bytes, epet_csr_to_csc_workspace_size(a->m, a->n, nnz), st));
   uint32_t* key = scr.take<uint32_t>(nnz);
-  uint32_t* key2 = scr.take<uint32_t>(nnz);
   uint64_t* pv = scr.take<uint64_t>(nnz);
   const size_t hn = radix_hist_elems(nnz);
   int64_t* hist = scr.take<int64_t>(hn);
   int64_t* hist_scan = scr.take<int64_t>(hn + 1);
   int64_t* tmp = scr.take<int64_t>(scan_tmp_elems(hn));
   if (scr.overrun) return set_error(EPET_ERR_INVALID, "internal: workspace size");
-  const int T = 256;
   const int bits = std::max(1, bits_for(a->n - 1));
-  CsrIn in{a->row_ptr, a->m, a->col, a->val, 0, 0};
+  if (bits > 18)
+    return set_error(EPET_ERR_UNSUPPORTED, "more than 2^18 voxels in the column-major copy");
+  CsrIn in{a->row_ptr, a->m, a->col, a->val, 0};
+  CscOut co{out->row, out->val, out->col_ptr};
+  k_fill_i64<<<ceil_div(a->n + 1, 256), 256, 0, st>>>(out->col_ptr, a->n + 1, nnz);
+  EPET_LAUNCHED();
   if (bits <= 9) {
     // one pass: CSR -> CSC
-    EPET_CHECK((radix_pass<9, uint32_t, uint64_t>(reinterpret_cast<const uint32_t*>(a->col), in,
-                                                  CscOut{out->row, out->val, key}, nnz, 0, hist,
-                                                  hist_scan, tmp, st)));
-  } else if (bits <= 18) {
-    const int b0 = (bits + 1) / 2;
-    // pass 1 (low digits): CSR -> (key, row|val)
-    if (b0 == 9) {
-      EPET_CHECK((radix_pass<9, uint32_t, uint64_t>(
-          reinterpret_cast<const uint32_t*>(a->col), in, ArrOut<uint32_t, uint64_t>{key, pv}, nnz,
-          0, hist, hist_scan, tmp, st)));
-      EPET_CHECK((radix_pass<9, uint32_t, uint64_t>(
-          key, ArrIn<uint32_t, uint64_t>{key, pv}, CscOut{out->row, out->val, key2}, nnz, 9, hist,
-          hist_scan, tmp, st)));
-    } else {
-      EPET_CHECK((radix_pass<8, uint32_t, uint64_t>(
-          reinterpret_cast<const uint32_t*>(a->col), in, ArrOut<uint32_t, uint64_t>{key, pv}, nnz,
-          0, hist, hist_scan, tmp, st)));
-      EPET_CHECK((radix_pass<9, uint32_t, uint64_t>(
-          key, ArrIn<uint32_t, uint64_t>{key, pv}, CscOut{out->row, out->val, key2}, nnz, 8, hist,
-          hist_scan, tmp, st)));
-    }
-    std::swap(key, key2);
+    EPET_CHECK((radix_pass<9, uint32_t, uint64_t>(in, co, nnz, 0, hist, hist_scan, tmp, st)));
   } else {
-    return set_error(EPET_ERR_UNSUPPORTED, "more than 2^18 voxels in the column-major copy");
+    // low digits: CSR -> (key, row|val); high digits -> CSC
+    const int b0 = bits - 9;
+    ArrOut<uint32_t, uint64_t> mid{key, pv};
+    ArrIn<uint32_t, uint64_t> mid_in{key, pv};
+    if (b0 <= 8) EPET_CHECK((radix_pass<8, uint32_t, uint64_t>(in, mid, nnz, 0, hist, hist_scan, tmp, st)));
+    else EPET_CHECK((radix_pass<9, uint32_t, uint64_t>(in, mid, nnz, 0, hist, hist_scan, tmp, st)));
+    EPET_CHECK((radix_pass<9, uint32_t, uint64_t>(mid_in, co, nnz, b0 <= 8 ? 8 : 9, hist,
+                                                  hist_scan, tmp, st)));
   }
-  k_colptr_from_sorted<<<ceil_div(a->n + 1, T), T, 0, st>>>(key, nnz, a->n, out->col_ptr);
+  // empty columns start where the next non-empty one does
+  k_suffix_min_i64<<<1, 1024, 0, st>>>(out->col_ptr, a->n + 1);
   EPET_LAUNCHED();
   return EPET_OK;
 }
