@@ -171,9 +171,8 @@ template <typename K, typename V>
 struct ArrIn {
   const K* k;
   const V* v;
-  __device__ void begin(int64_t) {}
   __device__ K key(int64_t i) const { return k[i]; }
-  __device__ V val(int64_t i) { return v[i]; }
+  __device__ V val(int64_t i) const { return v[i]; }
 };
 template <typename K, typename V>
 struct ArrOut {
@@ -185,31 +184,26 @@ struct ArrOut {
   }
 };
 
-// CSR in: key = column, value = (row << 32) | value bits.  Each lane tracks
-// the row of the entries it reads: a warp-uniform binary search for the
-// first entry of the warp's range, then forward steps (a lane's entries
-// increase).
+// CSR in, with the row of every entry precomputed (k_row_ids): key =
+// column, value = (row << 32) | value bits.
 struct CsrIn {
-  const int64_t* row_ptr;
-  int64_t m;
   const int32_t* col;
+  const int32_t* row;
   const float* vals;
-  int64_t cur;  // this lane's current row
-  __device__ void begin(int64_t first) {
-    int64_t lo = 0, hi = m - 1;  // last row r with row_ptr[r] <= first
-    while (lo < hi) {
-      const int64_t mid = (lo + hi + 1) >> 1;
-      if (row_ptr[mid] <= first) lo = mid;
-      else hi = mid - 1;
-    }
-    cur = lo;
-  }
   __device__ uint32_t key(int64_t i) const { return (uint32_t)col[i]; }
-  __device__ uint64_t val(int64_t i) {
-    while (cur + 1 < m && row_ptr[cur + 1] <= i) cur++;
-    return ((uint64_t)(uint32_t)cur << 32) | __float_as_uint(vals[i]);
+  __device__ uint64_t val(int64_t i) const {
+    return ((uint64_t)(uint32_t)row[i] << 32) | __float_as_uint(vals[i]);
   }
 };
+
+// Row id of every CSR entry (a warp per row).
+__global__ void k_row_ids(const int64_t* __restrict__ row_ptr, int64_t m,
+                          int32_t* __restrict__ row) {
+  const int64_t r = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  if (r >= m) return;
+  for (int64_t k = row_ptr[r] + (threadIdx.x & 31); k < row_ptr[r + 1]; k += 32)
+    row[k] = (int32_t)r;
+}
 
 // CSC out: row and value arrays; the first position of every column goes to
 // col_first (atomicMin, initialised to nnz; empty columns are filled in
@@ -228,7 +222,7 @@ struct CscOut {
 };
 
 template <int BITS, typename K, typename V, typename In, typename Out>
-__global__ void __launch_bounds__(kRsThreads)
+__global__ void __launch_bounds__(kRsThreads, 3)
 k_radix_scatter(In in, Out out, int64_t n, int shift, int64_t tpc, int nchunks,
                 const int64_t* __restrict__ offs) {
   constexpr int BINS = 1 << BITS;
@@ -250,16 +244,18 @@ k_radix_scatter(In in, Out out, int64_t n, int shift, int64_t tpc, int nchunks,
     for (int d = lane; d < BINS; d += 32) wcnt[w][d] = 0;
     __syncwarp();
     const int64_t wbase = tile0 + (int64_t)w * (kRsItems * 32);
-    if (wbase < n) in.begin(wbase);  // uniform across the warp
+    // keys only in registers (ranking); values are read once, when staged
     K kk[kRsItems];
-    V vv[kRsItems];
     unsigned rank[kRsItems];
 #pragma unroll
     for (int r = 0; r < kRsItems; r++) {
       const int64_t i = wbase + r * 32 + lane;
+      kk[r] = i < n ? in.key(i) : K(0);
+    }
+#pragma unroll
+    for (int r = 0; r < kRsItems; r++) {
+      const int64_t i = wbase + r * 32 + lane;
       const bool ok = i < n;
-      kk[r] = ok ? in.key(i) : K(0);
-      vv[r] = ok ? in.val(i) : V(0);
       const unsigned dig = ok ? ((unsigned)(kk[r] >> shift) & (BINS - 1)) : BINS + lane;
       const unsigned peers = __match_any_sync(0xffffffffu, dig);
       unsigned before = 0;
@@ -327,7 +323,7 @@ k_radix_scatter(In in, Out out, int64_t n, int shift, int64_t tpc, int nchunks,
         const unsigned dig = (unsigned)(kk[r] >> shift) & (BINS - 1);
         const unsigned lp = dstart[dig] + wcnt[w][dig] + rank[r];
         sk[lp] = kk[r];
-        sv[lp] = vv[r];
+        sv[lp] = in.val(i);
       }
     }
     __syncthreads();
@@ -571,7 +567,7 @@ size_t epet_csr_to_csc_workspace_size(int64_t m, int64_t n, int64_t nnz) {
   (void)m;
   (void)n;
   const size_t hist = radix_hist_elems(nnz);
-  return align256(nnz * 4) + align256(nnz * 8) + align256(hist * 8) +
+  return 2 * align256(nnz * 4) + align256(nnz * 8) + align256(hist * 8) +
          align256((hist + 1) * 8) + align256(scan_tmp_elems(hist) * 8) + 256;
 }
 
@@ -600,7 +596,11 @@ epet_status epet_csr_to_csc(const epet_csr* a, epet_csc* out, void* ws, size_t w
   const int bits = std::max(1, bits_for(a->n - 1));
   if (bits > 18)
     return set_error(EPET_ERR_UNSUPPORTED, "more than 2^18 voxels in the column-major copy");
-  CsrIn in{a->row_ptr, a->m, a->col, a->val, 0};
+  int32_t* rid = scr.take<int32_t>(nnz);
+  if (scr.overrun) return set_error(EPET_ERR_INVALID, "internal: workspace size");
+  k_row_ids<<<ceil_div(a->m * 32, 256), 256, 0, st>>>(a->row_ptr, a->m, rid);
+  EPET_LAUNCHED();
+  CsrIn in{a->col, rid, a->val};
   CscOut co{out->row, out->val, out->col_ptr};
   k_fill_i64<<<ceil_div(a->n + 1, 256), 256, 0, st>>>(out->col_ptr, a->n + 1, nnz);
   EPET_LAUNCHED();

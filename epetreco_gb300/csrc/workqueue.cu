@@ -153,7 +153,9 @@ __device__ __forceinline__ float isect_len(const epet_grid& g, int ix, int iy,
 
 constexpr int kValThreads = 128;
 
-// CTA per row: the row's rays in shared memory, threads over its elements.
+// CTA (row, slice): the row's rays in shared memory, the slice's threads
+// over every gridDim.y-th group of kValThreads elements (few rows get many
+// slices, so a short list of long rows still fills the device).
 __global__ void __launch_bounds__(kValThreads)
 k_values(Geo G, const float* __restrict__ rays, int64_t m,
          const int64_t* __restrict__ row_ptr, const int32_t* __restrict__ col,
@@ -161,13 +163,15 @@ k_values(Geo G, const float* __restrict__ rays, int64_t m,
   extern __shared__ float sray[];
   const int64_t row = blockIdx.x;
   if (row >= m) return;
+  const int64_t b = row_ptr[row], e = row_ptr[row + 1];
+  const int64_t first = b + (int64_t)blockIdx.y * kValThreads;
+  if (first >= e) return;  // uniform across the block
   const int R = G.p.nrays;
   const float* src = rays + row * (int64_t)R * 6;
   for (int i = threadIdx.x; i < R * 6; i += kValThreads) sray[i] = src[i];
   __syncthreads();
   const epet_grid& g = G.p.grid;
-  const int64_t b = row_ptr[row], e = row_ptr[row + 1];
-  for (int64_t k = b + threadIdx.x; k < e; k += kValThreads) {
+  for (int64_t k = first + threadIdx.x; k < e; k += (int64_t)gridDim.y * kValThreads) {
     const int v = col[k];
     const int ix = v / G.nyz, rem = v - ix * G.nyz;
     const int iy = rem / g.n[2], iz = rem - iy * g.n[2];
@@ -269,7 +273,8 @@ epet_status launch_values(const Geo& G, const float* rays, int64_t m,
     return set_error(EPET_ERR_UNSUPPORTED, "nrays too large for the values kernel");
   EPET_CUDA(cudaFuncSetAttribute(k_values, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  (int)smem));
-  k_values<<<(unsigned)m, kValThreads, smem, st>>>(G, rays, m, row_ptr, col, val);
+  const unsigned slices = (unsigned)std::min<int64_t>(64, std::max<int64_t>(1, 4096 / m));
+  k_values<<<dim3((unsigned)m, slices), kValThreads, smem, st>>>(G, rays, m, row_ptr, col, val);
   EPET_LAUNCHED();
   return EPET_OK;
 }
