@@ -194,6 +194,7 @@ def batch_measure(args, api, torch, st, nit: int = 10):
     from epetreco_gb300.phantom import measurement, phantom_image
     from epetreco_gb300.problem import batch_members
     torch.cuda.empty_cache()
+    api.trim_memory()
     t0 = time.perf_counter()
     members = batch_members(args.batch)
     # The drawn problems' matrices together exceed the device memory (tens of

@@ -306,6 +306,11 @@ def nChunks(maxNnz: int, maxNChunk: int) -> int:
 
 # --------------------------------------------------------------- MLEM driver
 
+def trim_memory(keep_bytes: int = 0) -> None:
+    """Returns the library's reserved device memory above keep_bytes."""
+    check(lib().epet_trim_memory(int(keep_bytes)))
+
+
 class Mlem:
     """One reconstruction on the device (reco.cu's loop): the system matrix
     of the measured rows is built once at construction."""

@@ -135,11 +135,12 @@ namespace {
 
 void batch_free(epet_mlem_batch* h) {
   if (!h) return;
+  cudaDeviceSynchronize();
   if (h->exec) cudaGraphExecDestroy(h->exec);
   if (h->graph) cudaGraphDestroy(h->graph);
   for (epet_mlem* p : h->probs) epet_mlem_destroy(p);
   for (void* b : {(void*)h->desc, (void*)h->tiles, (void*)h->partial, (void*)h->sums})
-    if (b) cudaFree(b);
+    if (b) dev_free(b, 0);
   delete h;
 }
 
@@ -232,8 +233,8 @@ epet_status epet_mlem_batch_create(int32_t nprob, const epet_problem* problems,
   }
 #define ALLOC(ptr, bytes)                                                    \
   do {                                                                       \
-    cudaError_t e_ = cudaMalloc((void**)&(ptr), std::max<size_t>(bytes, 8)); \
-    if (e_ != cudaSuccess) return fail(cuda_status(e_, "cudaMalloc " #ptr)); \
+    cudaError_t e_ = dev_alloc((void**)&(ptr), std::max<size_t>(bytes, 8), st); \
+    if (e_ != cudaSuccess) return fail(cuda_status(e_, "allocation " #ptr)); \
   } while (0)
   ALLOC(h->desc, np * sizeof(BatchDesc));
   ALLOC(h->tiles, h->tiles_h.size() * 8);

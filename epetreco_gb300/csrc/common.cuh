@@ -62,6 +62,10 @@ __host__ __device__ inline size_t align256(size_t b) { return (b + 255) & ~size_
 
 inline int ceil_div(int64_t a, int64_t b) { return (int)((a + b - 1) / b); }
 int num_sms();
+// Library device memory (a stream-ordered pool per device, see runtime.cu).
+cudaError_t dev_alloc(void** p, size_t bytes, cudaStream_t st);
+cudaError_t dev_free(void* p, cudaStream_t st);
+epet_status trim_memory(size_t keep_bytes);
 // Counts the library's kernel launches (graph replays count their kernels).
 void note_launch(int n = 1);
 

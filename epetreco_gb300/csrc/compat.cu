@@ -104,12 +104,12 @@ epet_status epet_csrmv_i32(int trans, int64_t m, int64_t n, int64_t nnz, float a
     return set_error(EPET_ERR_INVALID, "bad arguments");
   cudaStream_t st = (cudaStream_t)stream;
   int64_t* rp = nullptr;
-  EPET_CUDA(cudaMallocAsync((void**)&rp, (m + 1) * 8, st));
+  EPET_CUDA(dev_alloc((void**)&rp, (m + 1) * 8, st));
   k_ptr_i32_to_i64<<<ceil_div(m + 1, 256), 256, 0, st>>>(row_ptr_d, m + 1, rp);
   note_launch();
   epet_csr a{m, n, nnz, rp, const_cast<int32_t*>(col_d), const_cast<float*>(val_d)};
   epet_status rc = epet_csrmv(trans, &a, nullptr, alpha, x_d, beta, y_d, stream);
-  cudaFreeAsync(rp, st);
+  dev_free(rp, st);
   return rc;
 }
 

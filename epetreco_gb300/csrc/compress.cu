@@ -255,16 +255,16 @@ epet_status epet_csr16_count(const epet_csr* a, int64_t* row_len16_d, int64_t* n
   EPET_LAUNCHED();
   int64_t* tmp = nullptr;
   int64_t* off = nullptr;
-  EPET_CUDA(cudaMallocAsync((void**)&tmp, scan_tmp_elems(a->m + 1) * 8, st));
-  EPET_CUDA(cudaMallocAsync((void**)&off, (a->m + 1) * 8, st));
+  EPET_CUDA(dev_alloc((void**)&tmp, scan_tmp_elems(a->m + 1) * 8, st));
+  EPET_CUDA(dev_alloc((void**)&off, (a->m + 1) * 8, st));
   epet_status rc = exclusive_scan_i64(row_len16_d, off, a->m, tmp, st);
   if (rc == EPET_OK) {
     cudaError_t e = cudaMemcpyAsync(nnz16_h, off + a->m, 8, cudaMemcpyDeviceToHost, st);
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);
     if (e != cudaSuccess) rc = cuda_status(e, "csr16 count");
   }
-  cudaFreeAsync(tmp, st);
-  cudaFreeAsync(off, st);
+  dev_free(tmp, st);
+  dev_free(off, st);
   return rc;
 }
 
@@ -284,7 +284,7 @@ epet_status epet_csr_compress(const epet_csr* a, int32_t format, epet_csr16* out
     return EPET_OK;
   }
   int64_t* cnt = nullptr;
-  EPET_CUDA(cudaMallocAsync((void**)&cnt, (a->m + 1) * 8, st));
+  EPET_CUDA(dev_alloc((void**)&cnt, (a->m + 1) * 8, st));
   int64_t nnz16 = 0;
   epet_status rc = epet_csr16_count(a, cnt, &nnz16, stream);
   if (rc == EPET_OK && nnz16 > out->nnz && out->nnz >= 0 && (out->delta || out->q)) {
@@ -295,9 +295,9 @@ epet_status epet_csr_compress(const epet_csr* a, int32_t format, epet_csr16* out
     rc = set_error(EPET_ERR_INVALID, "delta/q buffers missing");
   if (rc == EPET_OK) {
     int64_t* tmp = nullptr;
-    cudaMallocAsync((void**)&tmp, scan_tmp_elems(a->m + 1) * 8, st);
+    dev_alloc((void**)&tmp, scan_tmp_elems(a->m + 1) * 8, st);
     rc = exclusive_scan_i64(cnt, out->row_ptr, a->m, tmp, st);
-    cudaFreeAsync(tmp, st);
+    dev_free(tmp, st);
   }
   if (rc == EPET_OK) {
     const unsigned nb = (unsigned)ceil_div(a->m * 32, 256);
@@ -312,7 +312,7 @@ epet_status epet_csr_compress(const epet_csr* a, int32_t format, epet_csr16* out
     if (e != cudaSuccess) rc = cuda_status(e, "k_c16_fill");
     out->nnz = nnz16;
   }
-  cudaFreeAsync(cnt, st);
+  dev_free(cnt, st);
   return rc;
 }
 

@@ -170,13 +170,13 @@ epet_status epet_selftest_division(int64_t n, uint64_t seed, int64_t* mismatches
   if (n < 0 || !mismatches_h) return set_error(EPET_ERR_INVALID, "bad arguments");
   cudaStream_t st = (cudaStream_t)stream;
   unsigned long long* bad = nullptr;
-  EPET_CUDA(cudaMallocAsync((void**)&bad, 8, st));
+  EPET_CUDA(dev_alloc((void**)&bad, 8, st));
   EPET_CUDA(cudaMemsetAsync(bad, 0, 8, st));
   k_selftest_div<<<1024, 256, 0, st>>>(n, seed, bad);
   EPET_LAUNCHED();
   unsigned long long h = 0;
   EPET_CUDA(cudaMemcpyAsync(&h, bad, 8, cudaMemcpyDeviceToHost, st));
-  EPET_CUDA(cudaFreeAsync(bad, st));
+  EPET_CUDA(dev_free(bad, st));
   EPET_CUDA(cudaStreamSynchronize(st));
   *mismatches_h = (int64_t)h;
   return EPET_OK;

@@ -23,6 +23,7 @@ using namespace epet;
 
 static void mlem_free(epet_mlem* h) {
   if (!h) return;
+  cudaDeviceSynchronize();  // nothing in flight uses the arrays
   if (h->exec) cudaGraphExecDestroy(h->exec);
   if (h->graph) cudaGraphDestroy(h->graph);
   void* bufs[] = {h->A16.row_ptr, h->A16.base, h->A16.scale, h->A16.delta, h->A16.q,
@@ -31,7 +32,7 @@ static void mlem_free(epet_mlem* h) {
                   h->A.val,
                   h->At.col_ptr, h->At.row, h->At.val, h->part_ll, h->part_x, h->sums};
   for (void* b : bufs)
-    if (b) cudaFree(b);
+    if (b) dev_free(b, 0);
   delete h;
 }
 
@@ -89,8 +90,8 @@ epet_status epet_mlem_create(const epet_problem* p, const int32_t* rows_d, const
   };
 #define ALLOC(ptr, bytes)                                                    \
   do {                                                                       \
-    cudaError_t e_ = cudaMalloc((void**)&(ptr), std::max<size_t>(bytes, 8)); \
-    if (e_ != cudaSuccess) return fail(cuda_status(e_, "cudaMalloc " #ptr)); \
+    cudaError_t e_ = dev_alloc((void**)&(ptr), std::max<size_t>(bytes, 8), st); \
+    if (e_ != cudaSuccess) return fail(cuda_status(e_, "allocation " #ptr)); \
   } while (0)
   ALLOC(h->rows, m * 4);
   ALLOC(h->y, m * 4);
@@ -112,7 +113,7 @@ epet_status epet_mlem_create(const epet_problem* p, const int32_t* rows_d, const
     ALLOC(part, nb * 8);
     epet_status rc = sum_f64(h->s, V, part, nb, h->sums + 2, st);
     if (rc == EPET_OK) rc = launch_normalise(h->s, h->sums + 2, V, h->s, st);
-    cudaFree(part);
+    dev_free(part, st);
     if (rc != EPET_OK) return fail(rc);
   }
   // x = ones / sum(ones) (reco.cu:126-136)
@@ -143,7 +144,7 @@ epet_status epet_mlem_create(const epet_problem* p, const int32_t* rows_d, const
       ALLOC(cnt, (j.rows + 1) * 8);
       int64_t n16 = 0;
       rc = epet_csr16_count(j.src, cnt, &n16, stream);
-      cudaFree(cnt);
+      dev_free(cnt, st);
       if (rc != EPET_OK) return fail(rc);
       ALLOC(j.dst->row_ptr, (j.rows + 1) * 8);
       ALLOC(j.dst->base, j.rows * 4);
@@ -155,10 +156,10 @@ epet_status epet_mlem_create(const epet_problem* p, const int32_t* rows_d, const
       if (rc != EPET_OK) return fail(rc);
     }
     EPET_CUDA(cudaStreamSynchronize(st));
-    cudaFree(h->A.col); h->A.col = nullptr;
-    cudaFree(h->A.val); h->A.val = nullptr;
-    cudaFree(h->At.row); h->At.row = nullptr;
-    cudaFree(h->At.val); h->At.val = nullptr;
+    dev_free(h->A.col, st); h->A.col = nullptr;
+    dev_free(h->A.val, st); h->A.val = nullptr;
+    dev_free(h->At.row, st); h->At.row = nullptr;
+    dev_free(h->At.val, st); h->At.val = nullptr;
   }
   h->plan_fwd = default_plan(m ? (double)nnz / m : 0.0);
   h->plan_bwd = default_plan(V ? (double)nnz / V : 0.0);
@@ -287,6 +288,8 @@ epet_status epet_mlem_plan(const epet_mlem* h, int32_t plan_h[6]) {
   return EPET_OK;
 }
 
+epet_status epet_trim_memory(size_t keep_bytes) { return trim_memory(keep_bytes); }
+
 epet_status epet_sensitivity(const epet_problem* p, const int32_t* rows_d, int64_t m,
                              float* s_d, double* s64_d, int32_t max_row_nnz, void* ws,
                              size_t ws_bytes, epet_stream_t stream) {
@@ -295,7 +298,7 @@ epet_status epet_sensitivity(const epet_problem* p, const int32_t* rows_d, int64
   cudaStream_t st = (cudaStream_t)stream;
   const int64_t V = (int64_t)p->grid.n[0] * p->grid.n[1] * p->grid.n[2];
   double* s64 = s64_d;
-  if (!s64) EPET_CUDA(cudaMallocAsync((void**)&s64, V * 8, st));
+  if (!s64) EPET_CUDA(dev_alloc((void**)&s64, V * 8, st));
   EPET_CUDA(cudaMemsetAsync(s64, 0, V * 8, st));
   epet_status rc = column_sums(p, rows_d, m, s64, max_row_nnz, ws, ws_bytes, st);
   if (rc == EPET_OK) {
@@ -304,12 +307,12 @@ epet_status epet_sensitivity(const epet_problem* p, const int32_t* rows_d, int64
     // normalised to sum 1 as backprojection.cu:157-161
     const int nb = (int)std::max<int64_t>(1, std::min<int64_t>(ceil_div(V, 256), 1024));
     double* part = nullptr;
-    cudaMallocAsync((void**)&part, (nb + 1) * 8, st);
+    dev_alloc((void**)&part, (nb + 1) * 8, st);
     rc = sum_f64(s_d, V, part, nb, part + nb, st);
     if (rc == EPET_OK) rc = launch_normalise(s_d, part + nb, V, s_d, st);
-    cudaFreeAsync(part, st);
+    dev_free(part, st);
   }
-  if (!s64_d) cudaFreeAsync(s64, st);
+  if (!s64_d) dev_free(s64, st);
   return rc;
 }
 

@@ -4,10 +4,64 @@
 #include <cstdio>
 #include <cstring>
 #include <atomic>
+#include <cstdint>
+#include <mutex>
 
 #include "common.cuh"
 
 namespace epet {
+
+// Device memory of the library comes from one stream-ordered pool per
+// device that keeps freed memory reserved (release threshold: unlimited), so
+// a reconstruction set up again with the same sizes maps no new memory;
+// epet_trim_memory hands the reserve back.
+static std::mutex g_pool_mu;
+static cudaMemPool_t g_pool[64] = {};
+
+static cudaMemPool_t lib_pool(cudaError_t* err) {
+  int dev = 0;
+  *err = cudaGetDevice(&dev);
+  if (*err != cudaSuccess || dev < 0 || dev >= 64) return nullptr;
+  std::lock_guard<std::mutex> lock(g_pool_mu);
+  if (!g_pool[dev]) {
+    cudaMemPoolProps props = {};
+    props.allocType = cudaMemAllocationTypePinned;
+    props.location.type = cudaMemLocationTypeDevice;
+    props.location.id = dev;
+    *err = cudaMemPoolCreate(&g_pool[dev], &props);
+    if (*err != cudaSuccess) {
+      g_pool[dev] = nullptr;
+      return nullptr;
+    }
+    uint64_t keep = UINT64_MAX;
+    cudaMemPoolSetAttribute(g_pool[dev], cudaMemPoolAttrReleaseThreshold, &keep);
+  }
+  return g_pool[dev];
+}
+
+cudaError_t dev_alloc(void** p, size_t bytes, cudaStream_t st) {
+  cudaError_t e = cudaSuccess;
+  cudaMemPool_t pool = lib_pool(&e);
+  if (!pool) return e != cudaSuccess ? e : cudaErrorInvalidDevice;
+  return cudaMallocFromPoolAsync(p, bytes, pool, st);
+}
+
+cudaError_t dev_free(void* p, cudaStream_t st) { return cudaFreeAsync(p, st); }
+
+epet_status trim_memory(size_t keep_bytes) {
+  std::lock_guard<std::mutex> lock(g_pool_mu);
+  for (int d = 0; d < 64; d++) {
+    if (!g_pool[d]) continue;
+    int cur = 0;
+    cudaGetDevice(&cur);
+    cudaSetDevice(d);
+    cudaDeviceSynchronize();
+    cudaError_t e = cudaMemPoolTrimTo(g_pool[d], keep_bytes);
+    cudaSetDevice(cur);
+    if (e != cudaSuccess) return cuda_status(e, "cudaMemPoolTrimTo");
+  }
+  return EPET_OK;
+}
 
 static thread_local char g_err[512] = "";
 
@@ -40,17 +94,17 @@ epet_status Scratch::init(void* ws, size_t ws_bytes, size_t need,
     owned = false;
     return EPET_OK;
   }
-  cudaError_t e = cudaMallocAsync(reinterpret_cast<void**>(&base), need, s);
+  cudaError_t e = dev_alloc(reinterpret_cast<void**>(&base), need, s);
   if (e != cudaSuccess) {
     base = nullptr;
-    return cuda_status(e, "cudaMallocAsync(workspace)");
+    return cuda_status(e, "workspace allocation");
   }
   owned = true;
   return EPET_OK;
 }
 
 Scratch::~Scratch() {
-  if (owned && base) cudaFreeAsync(base, stream);
+  if (owned && base) dev_free(base, stream);
 }
 
 static std::atomic<long long> g_launches{0};

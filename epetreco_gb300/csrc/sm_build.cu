@@ -711,8 +711,8 @@ static epet_status sample_capacity(const Geo& G, cudaStream_t st, int* cap_out) 
     }
   const int64_t n = (int64_t)sample.size();
   int32_t *d_rows = nullptr, *d_cells = nullptr;
-  EPET_CUDA(cudaMallocAsync((void**)&d_rows, n * 4, st));
-  EPET_CUDA(cudaMallocAsync((void**)&d_cells, n * 4, st));
+  EPET_CUDA(dev_alloc((void**)&d_rows, n * 4, st));
+  EPET_CUDA(dev_alloc((void**)&d_cells, n * 4, st));
   EPET_CUDA(cudaMemcpyAsync(d_rows, sample.data(), n * 4, cudaMemcpyHostToDevice, st));
   WalkArgs a{};
   a.G = G;
@@ -726,8 +726,8 @@ static epet_status sample_capacity(const Geo& G, cudaStream_t st, int* cap_out) 
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);
     if (e != cudaSuccess) rc = cuda_status(e, "window sample");
   }
-  cudaFreeAsync(d_rows, st);
-  cudaFreeAsync(d_cells, st);
+  dev_free(d_rows, st);
+  dev_free(d_cells, st);
   if (rc != EPET_OK) return rc;
   int mx = 0;
   for (int v : cells) mx = std::max(mx, v);
@@ -750,6 +750,7 @@ int64_t exact_rows_total() { return n_exact_rows_; }
 struct BuildOut {
   epet_csr* csr = nullptr;
   int64_t cap = 0;
+  cudaStream_t stream = nullptr;  // stream of the build (growth is ordered on it)
   // optional growth of csr->col/val: returns false on failure; must keep the
   // first `keep` entries and update csr->col/val and cap
   bool (*grow)(BuildOut* self, int64_t need, int64_t keep, int64_t rows_done,
@@ -783,9 +784,9 @@ static epet_status redo_overflow(WalkArgs a, const int32_t* ovf_rows, int n, int
                                  int32_t** s2c, float** s2v, int32_t* ovf_idx,
                                  cudaStream_t st) {
   int32_t *sel = nullptr, *cnl = nullptr, *cells = nullptr;
-  EPET_CUDA(cudaMallocAsync((void**)&sel, n * 4, st));
-  EPET_CUDA(cudaMallocAsync((void**)&cnl, n * 4, st));
-  EPET_CUDA(cudaMallocAsync((void**)&cells, n * 4, st));
+  EPET_CUDA(dev_alloc((void**)&sel, n * 4, st));
+  EPET_CUDA(dev_alloc((void**)&cnl, n * 4, st));
+  EPET_CUDA(dev_alloc((void**)&cells, n * 4, st));
   EPET_CUDA(cudaMemcpyAsync(sel, ovf_rows, n * 4, cudaMemcpyDeviceToDevice, st));
   k_gather_i32<<<ceil_div(n, 256), 256, 0, st>>>(a.rows, sel, n, cnl);
   EPET_LAUNCHED();
@@ -811,16 +812,16 @@ static epet_status redo_overflow(WalkArgs a, const int32_t* ovf_rows, int n, int
   b.stride = *cap2;
   b.ovf_idx = ovf_idx;
   if (kMode == kModeCsr) {
-    EPET_CUDA(cudaMallocAsync((void**)s2c, (size_t)n * *cap2 * 4, st));
-    EPET_CUDA(cudaMallocAsync((void**)s2v, (size_t)n * *cap2 * 4, st));
+    EPET_CUDA(dev_alloc((void**)s2c, (size_t)n * *cap2 * 4, st));
+    EPET_CUDA(dev_alloc((void**)s2v, (size_t)n * *cap2 * 4, st));
     b.stage_col = *s2c;
     b.stage_val = *s2v;
   }
   EPET_CUDA(cudaMemsetAsync(a.overflow_count, 0, 4, st));
   EPET_CHECK(launch_walk<kMode>(b, walk_smem(a.G, *cap2), st));
-  cudaFreeAsync(sel, st);
-  cudaFreeAsync(cnl, st);
-  cudaFreeAsync(cells, st);
+  dev_free(sel, st);
+  dev_free(cnl, st);
+  dev_free(cells, st);
   return EPET_OK;
 }
 
@@ -921,8 +922,8 @@ static epet_status run_walk(const Geo& G, const int32_t* rows, int64_t m,
       total_nnz += chunk_total;
     }
     if (stage2_col) {
-      cudaFreeAsync(stage2_col, st);
-      cudaFreeAsync(stage2_val, st);
+      dev_free(stage2_col, st);
+      dev_free(stage2_val, st);
     }
   }
   int32_t outside = 0;
@@ -943,17 +944,18 @@ static bool grow_device(BuildOut* self, int64_t need, int64_t keep, int64_t rows
   int64_t ncap = std::max<int64_t>(need, (int64_t)(est * 1.03) + 1024);
   int32_t* col = nullptr;
   float* val = nullptr;
-  if (cudaMalloc((void**)&col, ncap * 4) != cudaSuccess) return false;
-  if (cudaMalloc((void**)&val, ncap * 4) != cudaSuccess) {
-    cudaFree(col);
+  const cudaStream_t st = self->stream;
+  if (dev_alloc((void**)&col, ncap * 4, st) != cudaSuccess) return false;
+  if (dev_alloc((void**)&val, ncap * 4, st) != cudaSuccess) {
+    dev_free(col, st);
     return false;
   }
   if (keep > 0) {
-    cudaMemcpy(col, self->csr->col, keep * 4, cudaMemcpyDeviceToDevice);
-    cudaMemcpy(val, self->csr->val, keep * 4, cudaMemcpyDeviceToDevice);
+    cudaMemcpyAsync(col, self->csr->col, keep * 4, cudaMemcpyDeviceToDevice, st);
+    cudaMemcpyAsync(val, self->csr->val, keep * 4, cudaMemcpyDeviceToDevice, st);
   }
-  if (self->csr->col) cudaFree(self->csr->col);
-  if (self->csr->val) cudaFree(self->csr->val);
+  if (self->csr->col) dev_free(self->csr->col, st);
+  if (self->csr->val) dev_free(self->csr->val, st);
   self->csr->col = col;
   self->csr->val = val;
   self->cap = ncap;
@@ -1056,16 +1058,18 @@ epet_status epet_project_back(const epet_problem* p, const int32_t* rows_d,
 }  // extern "C"
 
 namespace epet {
-// CSR build into library-owned buffers (cudaMalloc'd, grown as needed).
+// CSR build into library-owned buffers (from the library pool, grown as
+// needed).
 epet_status build_csr_growable(const epet_problem* p, const int32_t* rows, int64_t m,
                                epet_csr* out, int64_t* cap, int32_t max_row_nnz,
                                cudaStream_t st) {
   Geo G = make_geo(*p);
   int capc = 0;
   EPET_CHECK(resolve_capacity(G, max_row_nnz, st, &capc));
-  if (!out->row_ptr) EPET_CUDA(cudaMalloc((void**)&out->row_ptr, (m + 1) * 8));
+  if (!out->row_ptr) EPET_CUDA(dev_alloc((void**)&out->row_ptr, (m + 1) * 8, st));
   BuildOut bo;
   bo.csr = out;
+  bo.stream = st;
   bo.cap = *cap;
   bo.grow = grow_device;
   epet_status rc = run_walk<kModeCsr>(G, rows, m, capc, &bo, nullptr, 0, st);

@@ -283,9 +283,9 @@ epet_status epet_sum_f64(const float* x_d, int64_t n, double* out_d, epet_stream
   cudaStream_t st = (cudaStream_t)stream;
   const int nb = (int)std::max<int64_t>(1, std::min<int64_t>(ceil_div(n, 256), 1024));
   double* part = nullptr;
-  EPET_CUDA(cudaMallocAsync((void**)&part, nb * 8, st));
+  EPET_CUDA(dev_alloc((void**)&part, nb * 8, st));
   epet_status rc = sum_f64(x_d, n, part, nb, out_d, st);
-  cudaFreeAsync(part, st);
+  dev_free(part, st);
   return rc;
 }
 

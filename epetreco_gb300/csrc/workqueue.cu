@@ -288,11 +288,11 @@ epet_status exact_rows_apply(const Geo& G, const int32_t* rows, const int32_t* e
   int32_t* cnl = nullptr;
   int64_t *cnt = nullptr, *off = nullptr, *tmp = nullptr;
   int32_t* flag = nullptr;
-  EPET_CUDA(cudaMallocAsync((void**)&cnl, n_ex * 4, st));
-  EPET_CUDA(cudaMallocAsync((void**)&cnt, (n_ex + 1) * 8, st));
-  EPET_CUDA(cudaMallocAsync((void**)&off, (n_ex + 1) * 8, st));
-  EPET_CUDA(cudaMallocAsync((void**)&tmp, scan_tmp_elems(n_ex + 1) * 8, st));
-  EPET_CUDA(cudaMallocAsync((void**)&flag, 4, st));
+  EPET_CUDA(dev_alloc((void**)&cnl, n_ex * 4, st));
+  EPET_CUDA(dev_alloc((void**)&cnt, (n_ex + 1) * 8, st));
+  EPET_CUDA(dev_alloc((void**)&off, (n_ex + 1) * 8, st));
+  EPET_CUDA(dev_alloc((void**)&tmp, scan_tmp_elems(n_ex + 1) * 8, st));
+  EPET_CUDA(dev_alloc((void**)&flag, 4, st));
   EPET_CUDA(cudaMemsetAsync(flag, 0, 4, st));
   k_gather_i32<<<ceil_div(n_ex, 256), 256, 0, st>>>(rows, ex_rows, n_ex, cnl);
   EPET_LAUNCHED();
@@ -304,10 +304,10 @@ epet_status exact_rows_apply(const Geo& G, const int32_t* rows, const int32_t* e
   int32_t *wc = nullptr, *wv = nullptr;
   float *wval = nullptr, *rays = nullptr;
   const int64_t tt = std::max<int64_t>(total, 1);
-  EPET_CUDA(cudaMallocAsync((void**)&wc, tt * 4, st));
-  EPET_CUDA(cudaMallocAsync((void**)&wv, tt * 4, st));
-  EPET_CUDA(cudaMallocAsync((void**)&wval, tt * 4, st));
-  EPET_CUDA(cudaMallocAsync((void**)&rays, n_ex * (int64_t)G.p.nrays * 24, st));
+  EPET_CUDA(dev_alloc((void**)&wc, tt * 4, st));
+  EPET_CUDA(dev_alloc((void**)&wv, tt * 4, st));
+  EPET_CUDA(dev_alloc((void**)&wval, tt * 4, st));
+  EPET_CUDA(dev_alloc((void**)&rays, n_ex * (int64_t)G.p.nrays * 24, st));
   EPET_CHECK(launch_workqueue_fill(G, cnl, n_ex, off, wc, wv, st));
   EPET_CHECK(launch_rays(G, cnl, n_ex, rays, false, st));
   EPET_CHECK(launch_values(G, rays, n_ex, off, wv, wval, st));
@@ -327,9 +327,9 @@ epet_status exact_rows_apply(const Geo& G, const int32_t* rows, const int32_t* e
   int32_t too_long = 0;
   EPET_CUDA(cudaMemcpyAsync(&too_long, flag, 4, cudaMemcpyDeviceToHost, st));
   EPET_CUDA(cudaStreamSynchronize(st));
-  cudaFreeAsync(cnl, st); cudaFreeAsync(cnt, st); cudaFreeAsync(off, st);
-  cudaFreeAsync(tmp, st); cudaFreeAsync(flag, st); cudaFreeAsync(wc, st);
-  cudaFreeAsync(wv, st); cudaFreeAsync(wval, st); cudaFreeAsync(rays, st);
+  dev_free(cnl, st); dev_free(cnt, st); dev_free(off, st);
+  dev_free(tmp, st); dev_free(flag, st); dev_free(wc, st);
+  dev_free(wv, st); dev_free(wval, st); dev_free(rays, st);
   if (too_long)
     return set_error(EPET_ERR_OVERFLOW, "%d exact-path rows exceed the row capacity %lld",
                      too_long, (long long)stride);
@@ -355,14 +355,14 @@ epet_status epet_workqueue_count(const epet_problem* p, const int32_t* rows_d,
     *total_h = 0;
     if (m > 0) {
       int64_t *off = nullptr, *tmp = nullptr;
-      EPET_CUDA(cudaMallocAsync((void**)&off, (m + 1) * 8, st));
-      EPET_CUDA(cudaMallocAsync((void**)&tmp, scan_tmp_elems(m + 1) * 8, st));
+      EPET_CUDA(dev_alloc((void**)&off, (m + 1) * 8, st));
+      EPET_CUDA(dev_alloc((void**)&tmp, scan_tmp_elems(m + 1) * 8, st));
       epet_status rc = exclusive_scan_i64(row_count_d, off, m, tmp, st);
       if (rc == EPET_OK) {
         EPET_CUDA(cudaMemcpyAsync(total_h, off + m, 8, cudaMemcpyDeviceToHost, st));
       }
-      cudaFreeAsync(off, st);
-      cudaFreeAsync(tmp, st);
+      dev_free(off, st);
+      dev_free(tmp, st);
       EPET_CUDA(cudaStreamSynchronize(st));
       if (rc != EPET_OK) return rc;
     }

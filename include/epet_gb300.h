@@ -295,6 +295,16 @@ epet_status epet_set_constant_geometry(const epet_setup* setup,
                                        const epet_grid* grid, int32_t nrays);
 epet_status epet_get_constant_geometry(epet_problem* out);
 
+/* ------------------------------------------------------------- memory */
+/* Device memory the library allocates itself (reconstruction objects,
+ * workspaces not passed by the caller) comes from a stream-ordered pool per
+ * device that keeps freed memory reserved, so setting up a reconstruction of
+ * the same size again maps no new memory.  This call returns the reserve
+ * above keep_bytes to the device (synchronises every device the library
+ * used).  No counterpart in the reference (it allocates with cudaMalloc and
+ * frees nothing between iterations). */
+epet_status epet_trim_memory(size_t keep_bytes);
+
 /* ---------------------------------------------------------- MLEM driver */
 /* One reconstruction (reco.cu:209-281) held on the device: measured rows,
  * their counts, the system matrix (CSR + CSC), sensitivity and image. */
