@@ -218,8 +218,13 @@ struct WalkAxis {
 // starting point (fewer atomic collisions), and stay converged.  Each step
 // is branch-free: the axis whose plane comes first is selected and advanced
 // with one division.
+//
+// With npieces > 1 the lane walks only piece `piece` of the ray: the cells
+// entered in [a_lo, a_hi), the piece's share of the grid range (no wrap).
+// The pieces of a ray compute their common bounds with the same expression,
+// so every cell belongs to exactly one piece.
 __device__ void walk_ray(const Geo& G, const float* ray, const Window& w, const Slab* slabs,
-                         int* outside, int* needs_exact, float frac) {
+                         int* outside, int* needs_exact, float frac, int piece, int npieces) {
   const epet_grid& g = G.p.grid;
   if (ray[0] == ray[3] && ray[1] == ray[4] && ray[2] == ray[5]) return;
   if (ray[0] == ray[3] || ray[1] == ray[4] || ray[2] == ray[5]) {
@@ -251,23 +256,36 @@ __device__ void walk_ray(const Geo& G, const float* ray, const Window& w, const 
     a_out = fminf(fminf(fmaxf(x0, x1), fmaxf(y0, y1)), fmaxf(z0, z1));
   }
   if (!(a_in < a_out)) return;
-  float a_s = a_in + (a_out - a_in) * frac;
-  if (!(a_s >= a_in && a_s < a_out)) a_s = a_in;
-  // entry state of the second part (the cells before the starting cell),
-  // computed up front by all lanes together: the switch in the loop is then
-  // a register copy, not a divergent search
-  X.enter(a_in);
-  Y.enter(a_in);
-  Z.enter(a_in);
-  const int ex = X.idx, ey = Y.idx, ez = Z.idx;
-  const float exl = X.lo, exh = X.hi, exk = X.kh, eyl = Y.lo, eyh = Y.hi, eyk = Y.kh;
-  const float ezl = Z.lo, ezh = Z.hi, ezk = Z.kh;
+  const float span = fsub(a_out, a_in);
+  float a_s, a_lo = -INFINITY, a_stop = INFINITY;
+  int ex = 0, ey = 0, ez = 0;
+  float exl = 0.f, exh = 0.f, exk = 0.f, eyl = 0.f, eyh = 0.f, eyk = 0.f;
+  float ezl = 0.f, ezh = 0.f, ezk = 0.f;
+  bool second;
+  if (npieces > 1) {
+    if (piece > 0) a_lo = fadd(a_in, fmul(span, (float)piece / (float)npieces));
+    if (piece + 1 < npieces) a_stop = fadd(a_in, fmul(span, (float)(piece + 1) / (float)npieces));
+    a_s = piece > 0 ? a_lo : a_in;
+    if (!(a_s < a_out)) return;
+    second = true;  // no wrap
+  } else {
+    a_s = a_in + span * frac;
+    if (!(a_s >= a_in && a_s < a_out)) a_s = a_in;
+    // entry state of the second part (the cells before the starting cell),
+    // computed up front by all lanes together: the switch in the loop is
+    // then a register copy, not a divergent search
+    X.enter(a_in);
+    Y.enter(a_in);
+    Z.enter(a_in);
+    ex = X.idx; ey = Y.idx; ez = Z.idx;
+    exl = X.lo; exh = X.hi; exk = X.kh; eyl = Y.lo; eyh = Y.hi; eyk = Y.kh;
+    ezl = Z.lo; ezh = Z.hi; ezk = Z.kh;
+    second = !(a_s > a_in);  // nothing before the starting cell
+  }
   X.enter(a_s);
   Y.enter(a_s);
   Z.enter(a_s);
   const float a_start = fmaxf(fmaxf(X.lo, Y.lo), Z.lo);  // entry of the starting cell
-  bool second = !(a_s > a_in);  // nothing before the starting cell
-  float a_stop = INFINITY;
   const bool zs = w.sa == 2;
   Slab sl = slabs[zs ? Z.idx : X.idx];
   const float scale = G.fx_scale;
@@ -281,7 +299,7 @@ __device__ void walk_ray(const Geo& G, const float* ray, const Window& w, const 
     const bool my = !mx && Y.hi <= Z.hi;
     const bool mz = !mx && !my;
     const float amax = mx ? X.hi : (my ? Y.hi : Z.hi);
-    if (amin < amax) {
+    if (amin < amax && amin >= a_lo) {  // cells entered before a_lo: previous piece
       const unsigned jp = (unsigned)((zs ? X.idx : Y.idx) - sl.p0);
       const unsigned jq = (unsigned)((zs ? Y.idx : Z.idx) - sl.q0);
       if (jp < (unsigned)sl.wp && jq < (unsigned)sl.wq) {
@@ -465,14 +483,32 @@ k_walk(WalkArgs args) {
   __syncthreads();
   const int R = G.p.nrays;
   const float* rays = args.rays + row * (int64_t)R * 6;
-  for (int r = threadIdx.x; r < R; r += kWalkThreads) {
-    float ray[6];
-    const float2* rp = reinterpret_cast<const float2*>(rays + 6 * r);
-    float2 a = rp[0], b = rp[1], c = rp[2];
-    ray[0] = a.x; ray[1] = a.y; ray[2] = b.x; ray[3] = b.y; ray[4] = c.x; ray[5] = c.y;
-    // golden-ratio spread of the starting points over the rays
-    const float frac = (float)r * 0.6180339887f - floorf((float)r * 0.6180339887f);
-    walk_ray(G, ray, win, slabs, &s_outside, &s_exact, frac);
+  // Rays to lanes: whole rays, one per lane, in rounds of kWalkThreads;
+  // in the last round, whole warps take one ray per lane and the remaining
+  // rays are cut into equal pieces over the remaining lanes (100 rays: 3
+  // warps of whole rays, 4 rays in 8 pieces each on the fourth warp).
+  {
+    auto walk = [&](int r, int piece, int np) {
+      float ray[6];
+      const float2* rp = reinterpret_cast<const float2*>(rays + 6 * r);
+      const float2 a = rp[0], b = rp[1], c = rp[2];
+      ray[0] = a.x; ray[1] = a.y; ray[2] = b.x; ray[3] = b.y; ray[4] = c.x; ray[5] = c.y;
+      // golden-ratio spread of the starting points of whole rays
+      const float frac = (float)r * 0.6180339887f - floorf((float)r * 0.6180339887f);
+      walk_ray(G, ray, win, slabs, &s_outside, &s_exact, frac, piece, np);
+    };
+    const int t = threadIdx.x;
+    const int rounds = R / kWalkThreads;
+    for (int k = 0; k < rounds; k++) walk(k * kWalkThreads + t, 0, 1);
+    const int rr = R - rounds * kWalkThreads, r0 = rounds * kWalkThreads;
+    const int fw = rr / 32;  // warps of whole rays
+    if (t < fw * 32) {
+      walk(r0 + t, 0, 1);
+    } else if (rr > fw * 32) {
+      const int rem = rr - fw * 32, lanes = kWalkThreads - fw * 32;
+      const int np = lanes / rem, l = t - fw * 32;
+      if (l < rem * np) walk(r0 + fw * 32 + l / np, l % np, np);
+    }
   }
   __syncthreads();
   if (threadIdx.x == 0 && s_outside) atomicAdd(args.hit_outside, s_outside);
