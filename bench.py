@@ -60,6 +60,8 @@ def parse():
                     help="build the matrix of the first ROWS channels of the workload, its "
                          "column-major copy, one forward and one transpose product (small "
                          "case for full ncu captures)")
+    ap.add_argument("--profile-16bit", action="store_true",
+                    help="with --profile-kernels: also the BF16 forms of both products")
     return ap.parse_args()
 
 
@@ -302,6 +304,11 @@ def gb300_arm(args):
         e = torch.rand(rows.numel(), device="cuda")
         api.CSRmv(0, A, x)
         api.CSRmv(1, A, e, At=At)
+        if args.profile_16bit:
+            A16 = api.compress(A, api.BF16)
+            At16 = api.compress(api.csc_as_csr(At), api.BF16)
+            api.csr16_mv(A16, x)
+            api.csr16_mv(At16, e)
         torch.cuda.synchronize()
         print(json.dumps({"profile_kernels": args.profile_kernels, "nnz": A.nnz}))
         return

@@ -26,7 +26,8 @@ from dataclasses import dataclass
 import torch
 
 from . import _lib
-from ._lib import CscC, CsrC, EpetError, MlemOptions, ProblemC, check, lib, problem_struct
+from ._lib import (Csr16C, CscC, CsrC, EpetError, MlemOptions, ProblemC, check, lib,
+                   problem_struct)
 
 NON_TRANSPOSE = 0
 TRANSPOSE = 1
@@ -258,6 +259,68 @@ def CSRmv(transA: int, A: Csr, x: torch.Tensor, alpha: float = 1.0, beta: float 
     check(lib().epet_csrmv(int(transA), C.byref(ca), C.byref(cc) if cc else None, float(alpha),
                            _ptr(x.contiguous()), float(beta), _ptr(y), _stream()))
     return y
+
+
+# ------------------------------------------------------ 16-bit value storage
+
+BF16, FP16 = 1, 2
+
+
+@dataclass
+class Csr16:
+    """16-bit storage of a CSR: per-row base column and FP32 scale, 16-bit
+    column steps and BF16/FP16 values (4 bytes per stored entry)."""
+    row_ptr: torch.Tensor  # int64 [m+1]
+    base: torch.Tensor     # int32 [m]
+    scale: torch.Tensor    # float32 [m]
+    delta: torch.Tensor    # int16 [capacity]
+    q: torch.Tensor        # int16 [capacity]
+    n: int
+    fmt: int
+    stored: int            # entries written (escape entries included)
+
+    @property
+    def m(self) -> int:
+        return self.row_ptr.numel() - 1
+
+    def cstruct(self) -> Csr16C:
+        return Csr16C(self.m, self.n, self.delta.numel(), self.row_ptr.data_ptr(),
+                      self.base.data_ptr(), self.scale.data_ptr(), self.delta.data_ptr(),
+                      self.q.data_ptr(), self.fmt)
+
+
+def compress(A: Csr, fmt: int = BF16) -> Csr16:
+    """The 16-bit form of A (epet_csr16_count + epet_csr_compress)."""
+    m = A.m
+    ca = A.cstruct()
+    cnt = torch.empty(m + 1, dtype=torch.int64, device="cuda")
+    n16 = C.c_int64(0)
+    check(lib().epet_csr16_count(C.byref(ca), _ptr(cnt), C.byref(n16), _stream()))
+    cap = n16.value + 8
+    out = Csr16(torch.empty(m + 1, dtype=torch.int64, device="cuda"),
+                torch.empty(max(m, 1), dtype=torch.int32, device="cuda"),
+                torch.empty(max(m, 1), dtype=torch.float32, device="cuda"),
+                torch.zeros(cap, dtype=torch.int16, device="cuda"),
+                torch.zeros(cap, dtype=torch.int16, device="cuda"), A.n, int(fmt), n16.value)
+    c16 = out.cstruct()
+    check(lib().epet_csr_compress(C.byref(ca), int(fmt), C.byref(c16), _stream()))
+    return out
+
+
+def csr16_mv(A: Csr16, x: torch.Tensor, alpha: float = 1.0, beta: float = 0.0,
+             y: torch.Tensor | None = None) -> torch.Tensor:
+    """y = alpha * A x + beta * y over the 16-bit form (FP32 accumulation)."""
+    if y is None:
+        y = torch.zeros(A.m, dtype=torch.float32, device="cuda")
+    c16 = A.cstruct()
+    check(lib().epet_csr16_mv(C.byref(c16), float(alpha), _ptr(x.contiguous()), float(beta),
+                              _ptr(y), _stream()))
+    return y
+
+
+def csc_as_csr(At: Csc) -> Csr:
+    """The column-major copy viewed as the CSR of the transpose."""
+    return Csr(At.col_ptr, At.row, At.val, At.m)
 
 
 # ---------------------------------------------------------- MLEM operations
