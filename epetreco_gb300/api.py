@@ -268,10 +268,11 @@ BF16, FP16 = 1, 2
 
 @dataclass
 class Csr16:
-    """16-bit storage of a CSR: per-row base column and FP32 scale, 16-bit
-    column steps and BF16/FP16 values (4 bytes per stored entry)."""
-    row_ptr: torch.Tensor  # int64 [m+1]
-    base: torch.Tensor     # int32 [m]
+    """16-bit storage of a CSR: rows in chunks of 8 entries with a 32-bit
+    column base per chunk, 16-bit column offsets, BF16/FP16 values and an FP32
+    scale per row (about 4.5 bytes per stored entry)."""
+    row_ptr: torch.Tensor  # int64 [m+1], stored entries (multiples of 8)
+    base: torch.Tensor     # int32 [capacity / 8]
     scale: torch.Tensor    # float32 [m]
     delta: torch.Tensor    # int16 [capacity]
     q: torch.Tensor        # int16 [capacity]
@@ -296,9 +297,9 @@ def compress(A: Csr, fmt: int = BF16) -> Csr16:
     cnt = torch.empty(m + 1, dtype=torch.int64, device="cuda")
     n16 = C.c_int64(0)
     check(lib().epet_csr16_count(C.byref(ca), _ptr(cnt), C.byref(n16), _stream()))
-    cap = n16.value + 8
+    cap = max(n16.value, 8)
     out = Csr16(torch.empty(m + 1, dtype=torch.int64, device="cuda"),
-                torch.empty(max(m, 1), dtype=torch.int32, device="cuda"),
+                torch.empty(cap // 8, dtype=torch.int32, device="cuda"),
                 torch.empty(max(m, 1), dtype=torch.float32, device="cuda"),
                 torch.zeros(cap, dtype=torch.int16, device="cuda"),
                 torch.zeros(cap, dtype=torch.int16, device="cuda"), A.n, int(fmt), n16.value)

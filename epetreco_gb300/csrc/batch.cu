@@ -58,7 +58,7 @@ __device__ __forceinline__ int find_problem(const int64_t* __restrict__ tiles, i
 }
 
 // Forward (FWD) or transpose product of every problem, MLEM epilogues fused.
-template <int G, int U, bool FWD>
+template <int G, int U, bool VEC, bool FWD>
 __global__ void __launch_bounds__(kSpmvThreads)
 k_batch_rows(const BatchDesc* __restrict__ desc, const int64_t* __restrict__ tiles, int np,
              double* __restrict__ partial) {
@@ -73,12 +73,12 @@ k_batch_rows(const BatchDesc* __restrict__ desc, const int64_t* __restrict__ til
     double part = 0.0;
     if constexpr (FWD) {
       if (r < d.m) {
-        const float v = row_dot<G, U, true>(d.col, d.val, d.x, d.row_ptr[r], d.row_ptr[r + 1], lg);
+        const float v = row_dot<G, U, VEC>(d.col, d.val, d.x, d.row_ptr[r], d.row_ptr[r + 1], lg);
         if (lg == 0) EpiMlemForward{d.y, d.e, d.ybar}(r, v);
       }
     } else {
       if (r < d.V) {
-        const float c = row_dot<G, U, true>(d.row, d.cval, d.e, d.col_ptr[r], d.col_ptr[r + 1], lg);
+        const float c = row_dot<G, U, VEC>(d.row, d.cval, d.e, d.col_ptr[r], d.col_ptr[r + 1], lg);
         if (lg == 0) part = EpiMlemUpdate{d.x, d.s, d.xnew, nullptr}(r, c);
       }
       block_sum_to(part, red, partial + tile);
@@ -151,12 +151,12 @@ epet_status launch_batch_rows(const epet_mlem_batch* h, const RowPlan& plan, boo
   if (nt <= 0) return EPET_OK;
   const unsigned grid = (unsigned)(plan.grid > 0 ? std::min<int64_t>(nt, plan.grid) : nt);
   const int64_t* tiles = fwd ? h->fwd_tiles(G) : h->bwd_tiles(G);
-  dispatch_plan(plan, true, [&](auto g, auto u, auto) {
+  dispatch_plan(plan, true, [&](auto g, auto u, auto v) {
     if (fwd)
-      k_batch_rows<decltype(g)::value, decltype(u)::value, true>
+      k_batch_rows<decltype(g)::value, decltype(u)::value, decltype(v)::value, true>
           <<<grid, kSpmvThreads, 0, st>>>(h->desc, tiles, h->np(), nullptr);
     else
-      k_batch_rows<decltype(g)::value, decltype(u)::value, false>
+      k_batch_rows<decltype(g)::value, decltype(u)::value, decltype(v)::value, false>
           <<<grid, kSpmvThreads, 0, st>>>(h->desc, tiles, h->np(), h->partial);
   });
   EPET_LAUNCHED();
@@ -343,7 +343,7 @@ epet_status epet_mlem_batch_stats(const epet_mlem_batch* h, int64_t* nnz_h,
     const RowPlan* ps[2] = {&h->plan_fwd, &h->plan_bwd};
     for (int k = 0; k < 2; k++) {
       plan_h[3 * k + 0] = ps[k]->G;
-      plan_h[3 * k + 1] = ps[k]->U;
+      plan_h[3 * k + 1] = ps[k]->vec ? ps[k]->U : 0;
       plan_h[3 * k + 2] = ps[k]->grid;
     }
   }

@@ -1,14 +1,18 @@
 // compress.cu -- 16-bit system-matrix storage: BF16/FP16 values with a per-row
-// FP32 scale and 16-bit column steps (4 bytes per entry instead of 8), and
-// the products over it.
+// FP32 scale and 16-bit column offsets (4.5 bytes per entry instead of 8),
+// and the products over it.
 //
-// Row r holds entries k = 0..len-1: col_k = base[r] + sum_{j<=k} delta_j
-// (delta_0 = 0) and value_k = scale[r] * q_k, q_k the 16-bit float of
-// value_k / scale[r], scale[r] = max value of the row.  A step wider than
-// 65535 is split by zero-valued entries of step 65535, so every matrix is
-// representable; at 52^3 voxels no step in a row exceeds ny*nz = 2704.
-// The same layout over the column-major copy stores A^T, so one kernel serves
-// both products.  The products accumulate in FP32.
+// A row is stored as chunks of 8 entries: chunk c has a 32-bit column base
+// cbase[c] (the column of its first entry), 16-bit offsets
+// (col = cbase[c] + offset) and 16-bit values (value = scale[r] * q, q the
+// 16-bit float of value / scale[r], scale[r] = the row's largest value).
+// Rows are padded to whole chunks with zero-valued entries of offset 0, so a
+// chunk never mixes rows and a lane decodes its chunk alone: no scan over
+// steps, no masks.  A chunk ends early (and is padded) before an entry
+// 65536 or more columns past its first, so every matrix is representable;
+// at 52^3 voxels 8 consecutive entries of a row span far less.  The same
+// layout over the column-major copy stores A^T, so one kernel serves both
+// products.  The products accumulate in FP32.
 #include <cuda_bf16.h>
 #include <cuda_fp16.h>
 
@@ -20,22 +24,41 @@
 
 namespace epet {
 
-constexpr uint32_t kMaxStep = 65535u;
+constexpr int kChunk = 8;
+constexpr int32_t kMaxSpan = 65535;
 
-// Entries a row needs (escapes included).
+// True (warp-uniform) when the fixed chunks [b + 8c, b + 8c + 8) of row
+// [b, e) all span at most kMaxSpan columns.
+__device__ __forceinline__ bool fixed_chunks(const int32_t* __restrict__ idx, int64_t b,
+                                             int64_t e, int lane) {
+  bool ok = true;
+  for (int64_t k = b + (int64_t)kChunk * lane; k < e; k += 32 * kChunk) {
+    const int64_t last = k + kChunk - 1 < e ? k + kChunk - 1 : e - 1;
+    if (idx[last] - idx[k] > kMaxSpan) ok = false;
+  }
+  return __all_sync(0xffffffffu, ok);
+}
+
+// Greedy chunks of row [b, e) (one thread): a chunk takes up to 8 entries
+// within kMaxSpan columns of its first.  Returns the number of chunks; with
+// out pointers given, writes them.
+template <int FMT>
+__device__ int64_t greedy_chunks(const int32_t* __restrict__ idx, const float* __restrict__ val,
+                                 int64_t b, int64_t e, float sc, int64_t out,
+                                 int32_t* cbase, uint16_t* off, uint16_t* q);
+
+// Stored entries of every row (multiples of 8).
 __global__ void k_c16_count(const int64_t* __restrict__ ptr, const int32_t* __restrict__ idx,
                             int64_t m, int64_t* __restrict__ cnt) {
   const int64_t r = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int lane = threadIdx.x & 31;
   if (r >= m) return;
   const int64_t b = ptr[r], e = ptr[r + 1];
-  int64_t extra = 0;
-  for (int64_t k = b + 1 + lane; k < e; k += 32) {
-    const uint32_t d = (uint32_t)(idx[k] - idx[k - 1]);
-    extra += (d - 1u) / kMaxStep;
+  if (fixed_chunks(idx, b, e, lane)) {
+    if (lane == 0) cnt[r] = (e - b + kChunk - 1) / kChunk * kChunk;
+  } else if (lane == 0) {
+    cnt[r] = greedy_chunks<1>(idx, nullptr, b, e, 1.f, -1, nullptr, nullptr, nullptr) * kChunk;
   }
-  for (int o = 16; o > 0; o >>= 1) extra += __shfl_xor_sync(0xffffffffu, extra, o);
-  if (lane == 0) cnt[r] = (e - b) + extra;
 }
 
 template <int FMT>
@@ -50,139 +73,133 @@ __device__ __forceinline__ float from_q(uint32_t q) {
   return __half2float(__ushort_as_half((unsigned short)q));
 }
 
-// Fill: warp per row; chunks of 32 entries, escapes placed by a warp scan.
+template <int FMT>
+__device__ int64_t greedy_chunks(const int32_t* __restrict__ idx, const float* __restrict__ val,
+                                 int64_t b, int64_t e, float sc, int64_t out, int32_t* cbase,
+                                 uint16_t* off, uint16_t* q) {
+  int64_t n = 0;
+  int64_t k = b;
+  while (k < e) {
+    const int32_t c0 = idx[k];
+    int j = 0;
+    for (; j < kChunk && k + j < e && idx[k + j] - c0 <= kMaxSpan; j++) {
+      if (out >= 0) {
+        off[out + n * kChunk + j] = (uint16_t)(idx[k + j] - c0);
+        q[out + n * kChunk + j] = to_q<FMT>(__fdiv_rn(val[k + j], sc));
+      }
+    }
+    if (out >= 0) {
+      cbase[(out >> 3) + n] = c0;
+      for (int p = j; p < kChunk; p++) {
+        off[out + n * kChunk + p] = 0;
+        q[out + n * kChunk + p] = 0;
+      }
+    }
+    k += j;
+    n++;
+  }
+  return n;
+}
+
+// Fill: warp per row; fixed chunks lane-parallel, otherwise lane 0 greedy.
 template <int FMT>
 __global__ void k_c16_fill(const int64_t* __restrict__ ptr, const int32_t* __restrict__ idx,
                            const float* __restrict__ val, int64_t m,
-                           const int64_t* __restrict__ ptr16, int32_t* __restrict__ base,
-                           float* __restrict__ scale, uint16_t* __restrict__ delta,
+                           const int64_t* __restrict__ ptr16, int32_t* __restrict__ cbase,
+                           float* __restrict__ scale, uint16_t* __restrict__ off,
                            uint16_t* __restrict__ q) {
   const int64_t r = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int lane = threadIdx.x & 31;
   if (r >= m) return;
   const int64_t b = ptr[r], e = ptr[r + 1];
-  // row scale: max value
+  // row scale: largest value
   float mx = 0.f;
   for (int64_t k = b + lane; k < e; k += 32) mx = fmaxf(mx, fabsf(val[k]));
   for (int o = 16; o > 0; o >>= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
   const float sc = mx > 0.f ? mx : 1.f;
-  if (lane == 0) {
-    scale[r] = sc;
-    base[r] = e > b ? idx[b] : 0;
-  }
-  int64_t out = ptr16[r];
-  for (int64_t k0 = b; k0 < e; k0 += 32) {
-    const int64_t k = k0 + lane;
-    uint32_t d = 0, ex = 0;
-    if (k < e && k > b) {
-      d = (uint32_t)(idx[k] - idx[k - 1]);
-      ex = (d - 1u) / kMaxStep;
-    }
-    uint32_t inc = ex;
-    for (int o = 1; o < 32; o <<= 1) {
-      const uint32_t t = __shfl_up_sync(0xffffffffu, inc, o);
-      if (lane >= o) inc += t;
-    }
-    const uint32_t tot = __shfl_sync(0xffffffffu, inc, 31);
-    if (k < e) {
-      int64_t o = out + (k - k0) + (inc - ex);
-      for (uint32_t j = 0; j < ex; j++) {  // escape entries
-        delta[o] = (uint16_t)kMaxStep;
-        q[o] = 0;
-        o++;
+  if (lane == 0) scale[r] = sc;
+  const int64_t out = ptr16[r];
+  if (fixed_chunks(idx, b, e, lane)) {
+    const int64_t len = e - b, padded = (len + kChunk - 1) / kChunk * kChunk;
+    for (int64_t p0 = 0; p0 < padded; p0 += 32) {
+      const int64_t p = p0 + lane;
+      const bool real = p < len;
+      const int32_t col = real ? idx[b + p] : 0;
+      // column of the chunk's first entry (lane & ~7 holds it)
+      const int32_t base = __shfl_sync(0xffffffffu, col, lane & ~(kChunk - 1));
+      if (p < padded) {
+        off[out + p] = real ? (uint16_t)(col - base) : (uint16_t)0;
+        q[out + p] = real ? to_q<FMT>(__fdiv_rn(val[b + p], sc)) : (uint16_t)0;
+        if ((p & (kChunk - 1)) == 0) cbase[(out + p) >> 3] = base;
       }
-      delta[o] = (uint16_t)(d - ex * kMaxStep);
-      q[o] = to_q<FMT>(__fdiv_rn(val[k], sc));
     }
-    const int64_t nthis = e - k0 < 32 ? e - k0 : 32;
-    out += nthis + tot;
+  } else if (lane == 0) {
+    greedy_chunks<FMT>(idx, val, b, e, sc, out, cbase, off, q);
   }
 }
 
-// Product over the 16-bit layout: a group of G lanes per row, each lane
-// reading 8 consecutive entries (16-byte loads of steps and values) per
-// round; columns come from the group-wide prefix sum of the steps.
+// Product over the 16-bit layout: a group of G lanes per row; lane l takes
+// the entry pairs l, l + G, ... of the row (32-bit loads of offsets and
+// values), so the lanes of a warp gather x at consecutive entries of the row
+// (neighbouring columns share cache sectors); four pairs per round, and the
+// next round's loads are issued before this round's gathers.
 template <int G, int FMT, class Epi>
 __global__ void __launch_bounds__(kSpmvThreads)
-k_rows16(const int64_t* __restrict__ ptr, const int32_t* __restrict__ base,
-         const float* __restrict__ scale, const uint16_t* __restrict__ delta,
+k_rows16(const int64_t* __restrict__ ptr, const int32_t* __restrict__ cbase,
+         const float* __restrict__ scale, const uint16_t* __restrict__ off,
          const uint16_t* __restrict__ q, const float* __restrict__ x, int64_t nrows, Epi epi,
          double* __restrict__ partial) {
-  constexpr int RPB = kSpmvThreads / G;
+  constexpr int RPT = kSpmvThreads / G, P = 4;
   __shared__ double red[kSpmvThreads / 32];
   const int lg = threadIdx.x % G;
-  const int64_t row = (int64_t)blockIdx.x * RPB + threadIdx.x / G;
-  double part = 0.0;
-  // all lanes of a group take part in the group shuffles
-  const bool live = row < nrows;
-  const int64_t b = live ? ptr[row] : 0, e = live ? ptr[row + 1] : 0;
-  int32_t col = live ? base[row] : 0;  // column of the entry before the chunk
-  float acc = 0.f;
-  // round-aligned start (8-entry, 16-byte boundaries)
-  const int64_t a0 = b & ~int64_t(7);
+  const int64_t row = (int64_t)blockIdx.x * RPT + threadIdx.x / G;
   const unsigned gmask = G == 32 ? 0xffffffffu : (((1u << G) - 1u) << (threadIdx.x & 31 & ~(G - 1)));
-  // software pipeline: the next round's loads are issued before this
-  // round's scan and gathers
-  uint4 dv = make_uint4(0, 0, 0, 0), qv = make_uint4(0, 0, 0, 0);
-  if (a0 + 8 * lg < e) {
-    dv = __ldcs(reinterpret_cast<const uint4*>(delta + a0 + 8 * lg));
-    qv = __ldcs(reinterpret_cast<const uint4*>(q + a0 + 8 * lg));
-  }
-  for (int64_t c0 = a0; c0 < e; c0 += 8 * G) {
-    const int64_t k = c0 + 8 * lg;  // this lane's first entry
-    uint4 dn = make_uint4(0, 0, 0, 0), qn = make_uint4(0, 0, 0, 0);
-    if (k + 8 * G < e) {
-      dn = __ldcs(reinterpret_cast<const uint4*>(delta + k + 8 * G));
-      qn = __ldcs(reinterpret_cast<const uint4*>(q + k + 8 * G));
-    }
-    // entries j of this lane's chunk with lo <= j < hi lie in [b, e)
-    const int64_t dl = b - k, dh = e - k;
-    const int lo = dl > 0 ? (int)dl : 0;
-    const int hi = dh < 8 ? (dh > 0 ? (int)dh : 0) : 8;
-    uint32_t dd[8], qq[8];
-    dd[0] = dv.x & 0xffffu; dd[1] = dv.x >> 16; dd[2] = dv.y & 0xffffu; dd[3] = dv.y >> 16;
-    dd[4] = dv.z & 0xffffu; dd[5] = dv.z >> 16; dd[6] = dv.w & 0xffffu; dd[7] = dv.w >> 16;
-    qq[0] = qv.x & 0xffffu; qq[1] = qv.x >> 16; qq[2] = qv.y & 0xffffu; qq[3] = qv.y >> 16;
-    qq[4] = qv.z & 0xffffu; qq[5] = qv.z >> 16; qq[6] = qv.w & 0xffffu; qq[7] = qv.w >> 16;
-    // entries outside [b, e) do not step
-    uint32_t lsum = 0;
+  double part = 0.0;
+  const bool live = row < nrows;
+  const int64_t p0 = live ? ptr[row] >> 1 : 0, p1 = live ? ptr[row + 1] >> 1 : 0;  // pairs
+  const uint32_t* __restrict__ o2 = reinterpret_cast<const uint32_t*>(off);
+  const uint32_t* __restrict__ q2 = reinterpret_cast<const uint32_t*>(q);
+  float acc[P];
+  uint32_t oc[P], vc[P];
+  int32_t bc[P];
 #pragma unroll
-    for (int j = 0; j < 8; j++) {
-      if (j < lo || j >= hi) dd[j] = 0;
-      lsum += dd[j];
-    }
-    // group exclusive scan of the lane sums
-    uint32_t inc = lsum;
-#pragma unroll
-    for (int o = 1; o < G; o <<= 1) {
-      const uint32_t t = __shfl_up_sync(gmask, inc, o, G);
-      if (lg >= o) inc += t;
-    }
-    const uint32_t total = __shfl_sync(gmask, inc, G - 1, G);
-    int32_t c = col + (int32_t)(inc - lsum);
-#pragma unroll
-    for (int j = 0; j < 8; j++) {
-      c += (int32_t)dd[j];
-      if (j >= lo && j < hi) acc = fmaf(from_q<FMT>(qq[j]), __ldg(x + c), acc);
-    }
-    col += (int32_t)total;
-    dv = dn;
-    qv = qn;
-  }
-#pragma unroll
-  for (int o = G / 2; o > 0; o >>= 1) acc += __shfl_xor_sync(gmask, acc, o, G);
-  if (live && lg == 0) part = epi(row, acc * scale[row]);
-  if (partial) {
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) part += __shfl_xor_sync(0xffffffffu, part, o);
-    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = part;
-    __syncthreads();
-    if (threadIdx.x == 0) {
-      double t = 0.0;
-      for (int w = 0; w < kSpmvThreads / 32; w++) t += red[w];
-      partial[blockIdx.x] = t;
+  for (int u = 0; u < P; u++) {
+    acc[u] = 0.f;
+    const int64_t pp = p0 + lg + u * G;
+    oc[u] = 0u; vc[u] = 0u; bc[u] = 0;
+    if (pp < p1) {
+      oc[u] = __ldcs(o2 + pp);
+      vc[u] = __ldcs(q2 + pp);
+      bc[u] = __ldg(cbase + (pp >> 2));
     }
   }
+  for (int64_t pb = p0 + lg; pb < p1; pb += P * G) {
+    uint32_t on[P], vn[P];
+    int32_t bn[P];
+#pragma unroll
+    for (int u = 0; u < P; u++) {
+      const int64_t pp = pb + (P + u) * G;
+      on[u] = 0u; vn[u] = 0u; bn[u] = 0;
+      if (pp < p1) {
+        on[u] = __ldcs(o2 + pp);
+        vn[u] = __ldcs(q2 + pp);
+        bn[u] = __ldg(cbase + (pp >> 2));
+      }
+    }
+#pragma unroll
+    for (int u = 0; u < P; u++) {
+      if (pb + u * G < p1) {
+        acc[u] = fmaf(from_q<FMT>(vc[u] & 0xffffu), __ldg(x + bc[u] + (int32_t)(oc[u] & 0xffffu)), acc[u]);
+        acc[u] = fmaf(from_q<FMT>(vc[u] >> 16), __ldg(x + bc[u] + (int32_t)(oc[u] >> 16)), acc[u]);
+      }
+      oc[u] = on[u]; vc[u] = vn[u]; bc[u] = bn[u];
+    }
+  }
+  float a = (acc[0] + acc[1]) + (acc[2] + acc[3]);
+#pragma unroll
+  for (int o = G / 2; o > 0; o >>= 1) a += __shfl_xor_sync(gmask, a, o, G);
+  if (live && lg == 0) part = epi(row, a * scale[row]);
+  if (partial) block_sum_to(part, red, partial + blockIdx.x);
 }
 
 struct EpiStore {  // y = alpha*d + beta*y
@@ -209,10 +226,12 @@ static epet_status launch16_fmt(int G, const epet_csr16* a, const float* x, Epi 
   return EPET_OK;
 }
 
+// Lanes per row from the mean stored entries per row (a lane takes two
+// entries per step, four steps per round).
 int pick_group16(double avg_len) {
   if (avg_len >= 256) return 32;
   if (avg_len >= 96) return 16;
-  if (avg_len >= 40) return 8;
+  if (avg_len >= 32) return 8;
   return 4;
 }
 
@@ -222,6 +241,8 @@ epet_status launch_rows16(const epet_csr16* a, const float* x, Epi epi, double* 
   if (a->m <= 0) return EPET_OK;
   if (((reinterpret_cast<uintptr_t>(a->delta) | reinterpret_cast<uintptr_t>(a->q)) & 15) != 0)
     return set_error(EPET_ERR_INVALID, "16-bit matrix: delta and q must be 16-byte aligned");
+  if (!a->base || !a->scale || !a->row_ptr)
+    return set_error(EPET_ERR_INVALID, "16-bit matrix: missing arrays");
   const int G = pick_group16(a->m ? (double)a->nnz / a->m : 0.0);
   if (a->format == EPET_VALUES_BF16) return launch16_fmt<1>(G, a, x, epi, partial, st);
   if (a->format == EPET_VALUES_FP16) return launch16_fmt<2>(G, a, x, epi, partial, st);

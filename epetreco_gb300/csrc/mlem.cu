@@ -147,7 +147,7 @@ epet_status epet_mlem_create(const epet_problem* p, const int32_t* rows_d, const
       dev_free(cnt, st);
       if (rc != EPET_OK) return fail(rc);
       ALLOC(j.dst->row_ptr, (j.rows + 1) * 8);
-      ALLOC(j.dst->base, j.rows * 4);
+      ALLOC(j.dst->base, csr16_capacity(n16) / 8 * 4);  // one base per 8-entry chunk
       ALLOC(j.dst->scale, j.rows * 4);
       ALLOC(j.dst->delta, csr16_capacity(n16) * 2);
       ALLOC(j.dst->q, csr16_capacity(n16) * 2);
@@ -261,10 +261,12 @@ epet_status epet_mlem_stats(const epet_mlem* h, int64_t* nnz_h, int64_t* bytes_h
   if (!h) return set_error(EPET_ERR_INVALID, "bad arguments");
   if (nnz_h) *nnz_h = h->A.nnz;
   if (bytes_h && h->opt.value_format != EPET_VALUES_FP32) {
-    // 4 bytes per stored entry; per row pointer + base + scale 16 bytes
+    // per stored entry 4 bytes (offset + value) and a 4-byte base per 8;
+    // per row a pointer and a scale (12 bytes); vectors as in FP32
     const int64_t m = h->m, V = h->V;
-    *bytes_h = 4 * h->A16.nnz + 16 * m + 4 * V + 4 * m + 4 * m + 4 * h->At16.nnz + 16 * V +
-               4 * m + 4 * V + 4 * V + 4 * V + 4 * V + 4 * V;
+    *bytes_h = 4 * h->A16.nnz + h->A16.nnz / 2 + 12 * m + 4 * m + 4 * V + 4 * m +
+               4 * h->At16.nnz + h->At16.nnz / 2 + 12 * V + 4 * m + 4 * V + 4 * V + 4 * V +
+               4 * V + 4 * V;
   } else if (bytes_h) {
     // forward: values+columns, row pointers, y, x (once), e written;
     // transpose: values+rows, column pointers, e (once), x, s, xnew written;
@@ -282,7 +284,7 @@ epet_status epet_mlem_plan(const epet_mlem* h, int32_t plan_h[6]) {
   const RowPlan* ps[2] = {&h->plan_fwd, &h->plan_bwd};
   for (int k = 0; k < 2; k++) {
     plan_h[3 * k + 0] = ps[k]->G;
-    plan_h[3 * k + 1] = ps[k]->U;
+    plan_h[3 * k + 1] = ps[k]->vec ? ps[k]->U : 0;
     plan_h[3 * k + 2] = ps[k]->grid;
   }
   return EPET_OK;

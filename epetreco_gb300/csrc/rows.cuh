@@ -9,11 +9,14 @@ namespace epet {
 
 constexpr int kSpmvThreads = 256;
 
-// Launch plan of a row kernel: G lanes per row, U 16-byte chunks in flight
-// per lane, grid = 0 for one block per tile of kSpmvThreads / G rows, else a
-// persistent grid of that many blocks striding over the tiles.
+// Launch plan of a row kernel: G lanes per row; vec: each lane reads 16-byte
+// chunks of 4 consecutive entries, U chunks per round (else the lanes
+// interleave single entries, which keeps a warp's gathers of x on
+// neighbouring columns); grid = 0 for one block per tile of kSpmvThreads / G
+// rows, else a persistent grid of that many blocks striding over the tiles.
 struct RowPlan {
   int G = 32, U = 2, grid = 0;
+  bool vec = true;  // 16-byte chunks per lane (else lanes interleave entries)
 };
 inline int plan_rows_per_tile(const RowPlan& p) { return kSpmvThreads / p.G; }
 inline int64_t plan_tiles(const RowPlan& p, int64_t nrows) {
@@ -143,10 +146,12 @@ __device__ __forceinline__ void block_sum_to(double part, double* red, double* o
 }
 
 // Calls f(integral_constant<G>, integral_constant<U>, bool_constant<VEC>)
-// for the plan's values (the scalar form has one unroll).
+// for the plan's values (the interleaved form has one unroll; it is also the
+// form for streams not on 16-byte boundaries).
 template <class F>
-void dispatch_plan(const RowPlan& p, bool vec, F&& f) {
+void dispatch_plan(const RowPlan& p, bool aligned, F&& f) {
   using std::integral_constant;
+  const bool vec = aligned && p.vec;
   auto with_u = [&](auto g) {
     if (!vec) return f(g, integral_constant<int, 1>{}, std::false_type{});
     switch (p.U) {

@@ -60,7 +60,7 @@ template <class Epi>
 epet_status launch_rows16(const epet_csr16* a, const float* x, Epi epi, double* partial,
                           cudaStream_t st);
 int64_t rows16_blocks(const epet_csr16* a);
-inline int64_t csr16_capacity(int64_t nnz16) { return nnz16 + 8; }
+inline int64_t csr16_capacity(int64_t nnz16) { return nnz16; }
 epet_status launch_sum_partials(const double* p, int64_t n, double* out, cudaStream_t st);
 epet_status launch_normalise(const float* xnew, const double* sum, int64_t n, float* x,
                              cudaStream_t st);

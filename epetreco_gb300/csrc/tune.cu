@@ -6,8 +6,9 @@
 // can beat one block per tile when tiles are short.  tune_rows times the
 // candidates on the caller's own matrix and remembers the winner for the
 // process.  Candidates: G in {g/2, g, 2g} (g = the heuristic group size for
-// the mean row length), U in {1, 2, 4}; then, for the fastest (G, U), a
-// persistent grid of 4 and 8 blocks per SM.  Each candidate runs once to
+// the mean row length) with 16-byte chunks per lane (U in {1, 2, 4}) or
+// interleaved entries; then, for the fastest, a persistent grid of 4 and 8
+// blocks per SM.  Each candidate runs once to
 // warm up and is then timed over three runs with CUDA events.
 #include <algorithm>
 #include <map>
@@ -65,7 +66,8 @@ epet_status tune_rows(int kind, int64_t nrows, int64_t nnz, int64_t ncols, doubl
   std::vector<RowPlan> cands;
   for (int g : {base.G / 2, base.G, base.G * 2}) {
     if (g < 4 || g > 32) continue;
-    for (int u : {1, 2, 4}) cands.push_back(RowPlan{g, u, 0});
+    for (int u : {1, 2, 4}) cands.push_back(RowPlan{g, u, 0, true});
+    cands.push_back(RowPlan{g, 1, 0, false});
   }
   cudaEvent_t e0 = nullptr, e1 = nullptr;
   EPET_CUDA(cudaEventCreate(&e0));

@@ -80,20 +80,23 @@ typedef struct {
   float* val;       /* nnz, device */
 } epet_csr;
 
-/* 16-bit storage of a CSR (value_format 1 = BF16, 2 = FP16): 4 bytes per
- * entry.  Row r: col_k = base[r] + delta_0 + ... + delta_k (delta_0 = 0),
- * value_k = scale[r] * q_k (scale = the row's largest value).  Steps wider
- * than 65535 are split by zero-valued entries.  delta and q are read with
- * 16-byte loads: 16-byte aligned, with room for nnz + 8 entries
- * (epet_csr16_capacity). */
+/* 16-bit storage of a CSR (value_format 1 = BF16, 2 = FP16): about 4.5 bytes
+ * per entry.  A row is stored as chunks of 8 entries (rows padded with
+ * zero-valued entries of offset 0): chunk c has a column base base[c], the
+ * entries' 16-bit offsets delta (col = base[c] + delta_k) and 16-bit values
+ * q (value = scale[r] * q_k, scale = the row's largest value).  A chunk ends
+ * early before an entry 65536 or more columns past its first.  row_ptr
+ * counts stored entries (multiples of 8).  delta and q are read with 16-byte
+ * loads: 16-byte aligned; nnz = their capacity in entries, base holds nnz/8
+ * chunks, scale m rows. */
 #define EPET_VALUES_FP32 0
 #define EPET_VALUES_BF16 1
 #define EPET_VALUES_FP16 2
 typedef struct {
   int64_t m, n;
-  int64_t nnz;       /* in: capacity of delta/q; out: stored entries */
+  int64_t nnz;       /* in: capacity of delta/q (entries); out: stored entries */
   int64_t* row_ptr;  /* m+1 */
-  int32_t* base;     /* m */
+  int32_t* base;     /* nnz / 8 (one per chunk) */
   float* scale;      /* m */
   uint16_t* delta;
   uint16_t* q;
@@ -341,8 +344,9 @@ epet_status epet_mlem_set_image(epet_mlem* h, const float* x_d,
 epet_status epet_mlem_stats(const epet_mlem* h, int64_t* nnz_h,
                             int64_t* bytes_per_iter_h);
 /* Launch shapes of the two products: plan_h[0..2] = forward lanes per row,
- * 16-byte chunks in flight per lane, persistent grid (0 = one block per
- * tile); plan_h[3..5] the same for the transpose. */
+ * 16-byte chunks per lane and round (0 = lanes interleave single entries),
+ * persistent grid (0 = one block per tile); plan_h[3..5] the same for the
+ * transpose. */
 epet_status epet_mlem_plan(const epet_mlem* h, int32_t plan_h[6]);
 
 /* ---------------------------------------------- batched reconstructions */
