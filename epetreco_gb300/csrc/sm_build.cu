@@ -74,16 +74,18 @@ struct WalkArgs {
 };
 
 // Dynamic shared memory of the walk kernel; every section starts on a
-// 256-byte boundary (the plane extents are int4).
+// 256-byte boundary (the plane extents are int4).  The pool holds, per
+// channel, the window's column table (8 bytes per column) followed by the
+// two 32-bit sum words of every window cell (8 bytes per cell): a channel
+// needs columns + cells <= cap_cells.
 struct WalkLayout {
-  size_t pext, lo, hi, total;
+  size_t pext, pool, total;
 };
-__host__ __device__ inline WalkLayout walk_layout(int nx, int cap_cells) {
+__host__ __device__ inline WalkLayout walk_layout(int nslab, int cap_cells) {
   WalkLayout L;
-  L.pext = align256((size_t)20 * nx);  // Slab[nx]
-  L.lo = L.pext + align256((size_t)(nx + 1) * 16);
-  L.hi = L.lo + align256((size_t)cap_cells * 4);
-  L.total = L.hi + align256((size_t)cap_cells * 4);
+  L.pext = align256((size_t)20 * nslab);  // Slab[nslab]
+  L.pool = L.pext + align256((size_t)(nslab + 1) * 16);
+  L.total = L.pool + align256((size_t)cap_cells * 8);
   return L;
 }
 
@@ -165,18 +167,38 @@ __device__ void slab_window(const Geo& G, const float (*c0)[3], const float (*c1
   out->q0 = b0; out->wq = b1 - b0 + 1;
 }
 
-// The window holds each cell's exact fixed-point sum as two 32-bit words:
-// every chord's units are split as hi * 2^fx_split + lo and the halves are
-// summed separately with fire-and-forget 32-bit shared atomics; the split is
-// sized (make_geo) so neither half can overflow.  The total
-// (hi_sum << fx_split) + lo_sum is exact and independent of the order of the
-// adds.
+// The window: the cells of a channel's hull, as a table over the columns
+// (ix, iy) of its (x, y) bounding box, each column a run of consecutive z
+// cells [zlo, zhi]; cells are stored column after column (x major, then y,
+// then z), which is voxel-id order.  Each cell holds its exact fixed-point
+// sum as two 32-bit words: every chord's units are split as
+// hi * 2^fx_split + lo and the halves are summed separately with
+// fire-and-forget 32-bit shared atomics; the split is sized (make_geo) so
+// neither half can overflow.  The total (hi_sum << fx_split) + lo_sum is
+// exact and independent of the order of the adds.
 struct Window {
   uint32_t* lo;
   uint32_t* hi;
+  const int2* cols;  // per column: {first cell, zlo | zhi << 16}; empty: zlo 1, zhi 0
+  int bx0, by0, wbx, wby;
   int split;
-  int sa;  // slab axis
 };
+
+// A lane's cached column: first cell, first z, number of z cells.
+struct Col {
+  int off, zlo, zn;
+};
+__device__ __forceinline__ Col load_col(const Window& w, int ix, int iy) {
+  Col c{0, 0, 0};
+  const unsigned cx = (unsigned)(ix - w.bx0), cy = (unsigned)(iy - w.by0);
+  if (cx < (unsigned)w.wbx && cy < (unsigned)w.wby) {
+    const int2 e = w.cols[cx * w.wby + cy];
+    c.off = e.x;
+    c.zlo = e.y & 0xffff;
+    c.zn = (e.y >> 16) - c.zlo + 1;
+  }
+  return c;
+}
 
 // One axis of a ray walk: the ray's parameter at grid plane k is the
 // reference's quotient (plane_k - r0)/(r1 - r0), correctly rounded.
@@ -223,8 +245,8 @@ struct WalkAxis {
 // entered in [a_lo, a_hi), the piece's share of the grid range (no wrap).
 // The pieces of a ray compute their common bounds with the same expression,
 // so every cell belongs to exactly one piece.
-__device__ void walk_ray(const Geo& G, const float* ray, const Window& w, const Slab* slabs,
-                         int* outside, int* needs_exact, float frac, int piece, int npieces) {
+__device__ void walk_ray(const Geo& G, const float* ray, const Window& w, int* outside,
+                         int* needs_exact, float frac, int piece, int npieces) {
   const epet_grid& g = G.p.grid;
   if (ray[0] == ray[3] && ray[1] == ray[4] && ray[2] == ray[5]) return;
   if (ray[0] == ray[3] || ray[1] == ray[4] || ray[2] == ray[5]) {
@@ -286,8 +308,7 @@ __device__ void walk_ray(const Geo& G, const float* ray, const Window& w, const 
   Y.enter(a_s);
   Z.enter(a_s);
   const float a_start = fmaxf(fmaxf(X.lo, Y.lo), Z.lo);  // entry of the starting cell
-  const bool zs = w.sa == 2;
-  Slab sl = slabs[zs ? Z.idx : X.idx];
+  Col col = load_col(w, X.idx, Y.idx);
   const float scale = G.fx_scale;
   const float two_s = __int_as_float((127 + w.split) << 23);   // 2^split
   const float inv_two_s = __int_as_float((127 - w.split) << 23);
@@ -300,10 +321,9 @@ __device__ void walk_ray(const Geo& G, const float* ray, const Window& w, const 
     const bool mz = !mx && !my;
     const float amax = mx ? X.hi : (my ? Y.hi : Z.hi);
     if (amin < amax && amin >= a_lo) {  // cells entered before a_lo: previous piece
-      const unsigned jp = (unsigned)((zs ? X.idx : Y.idx) - sl.p0);
-      const unsigned jq = (unsigned)((zs ? Y.idx : Z.idx) - sl.q0);
-      if (jp < (unsigned)sl.wp && jq < (unsigned)sl.wq) {
-        const int c = sl.off + (int)jp * sl.wq + (int)jq;
+      const unsigned dz = (unsigned)(Z.idx - col.zlo);
+      if (dz < (unsigned)col.zn) {
+        const int c = col.off + (int)dz;
         // units = RN(len * scale) split as hi * 2^split + lo; for a product
         // >= 2^split the float is an integer and both parts are exact
         const float v = fmul(fmul(fsub(amax, amin), L), scale);
@@ -329,7 +349,7 @@ __device__ void walk_ray(const Geo& G, const float* ray, const Window& w, const 
       X.lo = mx ? X.hi : X.lo; X.hi = mx ? h : X.hi; X.kh = mx ? kh : X.kh; X.idx = mx ? ni : X.idx;
       Y.lo = my ? Y.hi : Y.lo; Y.hi = my ? h : Y.hi; Y.kh = my ? kh : Y.kh; Y.idx = my ? ni : Y.idx;
       Z.lo = mz ? Z.hi : Z.lo; Z.hi = mz ? h : Z.hi; Z.kh = mz ? kh : Z.kh; Z.idx = mz ? ni : Z.idx;
-      if (zs ? mz : mx) sl = slabs[ni];
+      if (!mz) col = load_col(w, X.idx, Y.idx);  // x or y moved: another column
     } else {
       // left the grid: the part before the starting cell, if any
       if (second) break;
@@ -338,7 +358,7 @@ __device__ void walk_ray(const Geo& G, const float* ray, const Window& w, const 
       X.idx = ex; X.lo = exl; X.hi = exh; X.kh = exk;
       Y.idx = ey; Y.lo = eyl; Y.hi = eyh; Y.kh = eyk;
       Z.idx = ez; Z.lo = ezl; Z.hi = ezh; Z.kh = ezk;
-      sl = slabs[zs ? ez : ex];
+      col = load_col(w, ex, ey);
     }
   }
 }
@@ -353,14 +373,11 @@ k_walk(WalkArgs args) {
   Slab* slabs = reinterpret_cast<Slab*>(smem);
   const WalkLayout lay = walk_layout(max(g.n[0], g.n[2]), args.cap_cells);
   Window win;
-  win.lo = reinterpret_cast<uint32_t*>(smem + lay.lo);
-  win.hi = reinterpret_cast<uint32_t*>(smem + lay.hi);
   win.split = G.fx_split;
-  win.sa = 0;  // set after the prologue
   __shared__ float c0[8][3], c1[8][3];
   __shared__ ChannelLine line;
   __shared__ int warp_tot[kWalkThreads / 32];
-  __shared__ int s_total, s_outside, s_exact, s_sa;
+  __shared__ int s_total, s_outside, s_exact, s_sa, s_box[4];
   __shared__ double red_d[kWalkThreads / 32];
   __shared__ float red_f[kWalkThreads / 32];
 
@@ -385,6 +402,7 @@ k_walk(WalkArgs args) {
     for (int d = 0; d < 3; d++) line.ab[d] = fsub(b[d], line.a[d]);
     s_outside = 0;
     s_exact = 0;
+    s_box[0] = INT_MAX; s_box[1] = INT_MIN; s_box[2] = INT_MAX; s_box[3] = INT_MIN;
     // slab along the axis the line follows more closely (x or z)
     s_sa = fabsf(line.ab[2]) > fabsf(line.ab[0]) ? 2 : 0;
   }
@@ -441,31 +459,141 @@ k_walk(WalkArgs args) {
   }
   __syncthreads();
 
-  // ---- per-slab windows and their offsets
+  // ---- per-slab windows (rectangles over the other two axes), their
+  // flattened offsets, and the (x, y) bounding box of all of them
   int my_cells = 0;
   const int per = (ns + kWalkThreads - 1) / kWalkThreads;
   const int sbeg = threadIdx.x * per, send = min(ns, sbeg + per);
-  for (int ix = sbeg; ix < send; ix++) {
-    Slab s;
-    slab_window(G, c0, c1, pext, sa, ix, &s);
-    slabs[ix] = s;
-    my_cells += s.wp * s.wq;
+  {
+    int xlo = INT_MAX, xhi = INT_MIN, ylo = INT_MAX, yhi = INT_MIN;
+    for (int i = sbeg; i < send; i++) {
+      Slab sl;
+      slab_window(G, c0, c1, pext, sa, i, &sl);
+      slabs[i] = sl;
+      my_cells += sl.wp * sl.wq;
+      if (sl.wp > 0 && sl.wq > 0) {
+        if (sa == 0) {  // slab = x, rectangle over (y, z)
+          xlo = min(xlo, i); xhi = max(xhi, i);
+          ylo = min(ylo, sl.p0); yhi = max(yhi, sl.p0 + sl.wp - 1);
+        } else {        // slab = z, rectangle over (x, y)
+          xlo = min(xlo, sl.p0); xhi = max(xhi, sl.p0 + sl.wp - 1);
+          ylo = min(ylo, sl.q0); yhi = max(yhi, sl.q0 + sl.wq - 1);
+        }
+      }
+    }
+    if (xlo <= xhi) {
+      atomicMin(&s_box[0], xlo); atomicMax(&s_box[1], xhi);
+      atomicMin(&s_box[2], ylo); atomicMax(&s_box[3], yhi);
+    }
   }
   const int excl = block_excl_scan(my_cells, warp_tot, &s_total);
   {
     int o = excl;
-    for (int ix = sbeg; ix < send; ix++) {
-      slabs[ix].off = o;
-      o += slabs[ix].wp * slabs[ix].wq;
+    for (int i = sbeg; i < send; i++) {
+      slabs[i].off = o;
+      o += slabs[i].wp * slabs[i].wq;
     }
   }
   __syncthreads();
-  const int W = s_total;
+  const int n_rect = s_total;  // cells of all slab rectangles
+  win.bx0 = s_box[0];
+  win.by0 = s_box[2];
+  win.wbx = s_box[1] >= s_box[0] ? s_box[1] - s_box[0] + 1 : 0;
+  win.wby = s_box[3] >= s_box[2] ? s_box[3] - s_box[2] + 1 : 0;
+  const int A = win.wbx * win.wby;  // columns of the table
+  // z range of column k = (ix, iy): for x slabs the range of slab ix's
+  // rectangle at iy; for z slabs the first and last slab whose rectangle
+  // holds (ix, iy)
+  auto col_range_scan = [&](int k, int* zlo, int* zhi) {  // z slabs, no storage
+    const int ix = win.bx0 + k / win.wby, iy = win.by0 + k % win.wby;
+    int lo = INT_MAX, hi = INT_MIN;
+    for (int iz = 0; iz < ns; iz++) {
+      const Slab sl = slabs[iz];
+      if ((unsigned)(ix - sl.p0) < (unsigned)sl.wp && (unsigned)(iy - sl.q0) < (unsigned)sl.wq) {
+        lo = min(lo, iz);
+        hi = iz;
+      }
+    }
+    *zlo = lo;
+    *zhi = hi;
+  };
+  auto col_range_x = [&](int k, int* zlo, int* zhi) {  // x slabs
+    const int ix = win.bx0 + k / win.wby, iy = win.by0 + k % win.wby;
+    const Slab sl = slabs[ix];
+    if ((unsigned)(iy - sl.p0) < (unsigned)sl.wp) {
+      *zlo = sl.q0;
+      *zhi = sl.q0 + sl.wq - 1;
+    } else {
+      *zlo = INT_MAX;
+      *zhi = INT_MIN;
+    }
+  };
+  const int kper = (A + kWalkThreads - 1) / kWalkThreads;
+  const int kbeg = min(A, (int)threadIdx.x * kper), kend = min(A, kbeg + kper);
   if (kMode == kModeWindow) {
-    if (threadIdx.x == 0) args.win_cells[row] = W;
+    // columns + cells, computed without the table
+    int n = 0;
+    for (int k = kbeg; k < kend; k++) {
+      int zlo, zhi;
+      if (sa == 0) col_range_x(k, &zlo, &zhi);
+      else col_range_scan(k, &zlo, &zhi);
+      if (zhi >= zlo) n += zhi - zlo + 1;
+    }
+    block_excl_scan(n, warp_tot, &s_total);
+    if (threadIdx.x == 0) args.win_cells[row] = A + s_total;
     return;
   }
-  if (W > args.cap_cells) {
+  int2* cols = reinterpret_cast<int2*>(smem + lay.pool);
+  const bool table_fits = A <= args.cap_cells;
+  if (table_fits) {
+    if (sa == 0) {
+      for (int k = kbeg; k < kend; k++) {
+        int zlo, zhi;
+        col_range_x(k, &zlo, &zhi);
+        cols[k] = make_int2(zlo, zhi);
+      }
+    } else {
+      for (int k = threadIdx.x; k < A; k += kWalkThreads) cols[k] = make_int2(INT_MAX, INT_MIN);
+      __syncthreads();
+      // every rectangle cell widens its column's range (shared atomics)
+      const int rpt = (n_rect + kWalkThreads - 1) / kWalkThreads;
+      const int rbeg = min(n_rect, (int)threadIdx.x * rpt), rend = min(n_rect, rbeg + rpt);
+      if (rbeg < rend) {
+        int lo_s = 0, hi_s = ns - 1;  // last slab with off <= rbeg
+        while (lo_s < hi_s) {
+          const int mid = (lo_s + hi_s + 1) >> 1;
+          if (slabs[mid].off <= rbeg) lo_s = mid;
+          else hi_s = mid - 1;
+        }
+        int iz = lo_s;
+        Slab sl = slabs[iz];
+        int jp = (rbeg - sl.off) / max(sl.wq, 1), jq = rbeg - sl.off - jp * sl.wq;
+        for (int r = rbeg; r < rend; r++) {
+          while (r >= sl.off + sl.wp * sl.wq) {
+            sl = slabs[++iz];
+            jp = 0;
+            jq = 0;
+          }
+          const int k = (sl.p0 + jp - win.bx0) * win.wby + (sl.q0 + jq - win.by0);
+          atomicMin(&cols[k].x, iz);
+          atomicMax(&cols[k].y, iz);
+          if (++jq == sl.wq) {
+            jq = 0;
+            ++jp;
+          }
+        }
+      }
+    }
+  }
+  __syncthreads();
+  // column lengths -> first cells (exclusive scan), packed ranges
+  int n_mine = 0;
+  if (table_fits)
+    for (int k = kbeg; k < kend; k++)
+      if (cols[k].y >= cols[k].x) n_mine += cols[k].y - cols[k].x + 1;
+  const int cexcl = block_excl_scan(n_mine, warp_tot, &s_total);
+  const int W = s_total;  // window cells
+  if (!table_fits || A + W > args.cap_cells) {
     if (threadIdx.x == 0) {
       int k = atomicAdd(args.overflow_count, 1);
       args.overflow_rows[k] = (int32_t)row;
@@ -473,8 +601,21 @@ k_walk(WalkArgs args) {
     }
     return;
   }
-
-  win.sa = sa;
+  {
+    int o = cexcl;
+    for (int k = kbeg; k < kend; k++) {
+      const int2 r = cols[k];
+      if (r.y >= r.x) {
+        cols[k] = make_int2(o, r.x | (r.y << 16));
+        o += r.y - r.x + 1;
+      } else {
+        cols[k] = make_int2(o, 1);  // empty: zlo 1, zhi 0
+      }
+    }
+  }
+  win.cols = cols;
+  win.lo = reinterpret_cast<uint32_t*>(smem + lay.pool + (size_t)A * 8);  // 8A + 8W <= pool
+  win.hi = win.lo + W;
   // ---- zero the window, walk the rays
   for (int i = threadIdx.x; i < W; i += kWalkThreads) {
     win.lo[i] = 0u;
@@ -495,7 +636,7 @@ k_walk(WalkArgs args) {
       ray[0] = a.x; ray[1] = a.y; ray[2] = b.x; ray[3] = b.y; ray[4] = c.x; ray[5] = c.y;
       // golden-ratio spread of the starting points of whole rays
       const float frac = (float)r * 0.6180339887f - floorf((float)r * 0.6180339887f);
-      walk_ray(G, ray, win, slabs, &s_outside, &s_exact, frac, piece, np);
+      walk_ray(G, ray, win, &s_outside, &s_exact, frac, piece, np);
     };
     const int t = threadIdx.x;
     const int rounds = R / kWalkThreads;
@@ -521,76 +662,38 @@ k_walk(WalkArgs args) {
     return;
   }
 
-  // ---- ordered extraction in voxel-id order.  Thread t owns a contiguous
-  // range of an id-ordered enumeration: the window cells themselves when
-  // slabs run along x (storage order is id order), else the bounding box
-  // [x range] x [y range] x [all z] of the z-slab window.
-  int bx0 = 0, bx1 = -1, by0 = 0, by1 = -1;  // box of a z-slab window
-  int E = W;                                 // enumeration length
-  if (sa == 2) {
-    __shared__ int bb[4];
-    if (threadIdx.x == 0) {
-      int a0 = INT_MAX, a1 = -1, b0 = INT_MAX, b1 = -1;
-      for (int k = 0; k < ns; k++) {
-        if (slabs[k].wp == 0 || slabs[k].wq == 0) continue;
-        a0 = min(a0, slabs[k].p0); a1 = max(a1, slabs[k].p0 + slabs[k].wp - 1);
-        b0 = min(b0, slabs[k].q0); b1 = max(b1, slabs[k].q0 + slabs[k].wq - 1);
-      }
-      bb[0] = a0; bb[1] = a1; bb[2] = b0; bb[3] = b1;
-    }
-    __syncthreads();
-    bx0 = bb[0]; bx1 = bb[1]; by0 = bb[2]; by1 = bb[3];
-    E = bx1 < bx0 ? 0 : (bx1 - bx0 + 1) * (by1 - by0 + 1) * g.n[2];
-  }
-  // odd range length: the lanes' concurrent window reads fall in distinct
-  // shared-memory banks
-  const int cpt = ((E + kWalkThreads - 1) / kWalkThreads) | 1;
-  const int cbeg = min(E, (int)threadIdx.x * cpt), cend = min(E, cbeg + cpt);
-  // Visits the thread's enumeration range in order; f(cell, ix, iy, iz)
-  // for every window cell met.
+  // ---- ordered extraction: the cells are stored in voxel-id order, thread
+  // t takes a contiguous range of them (odd length: the lanes' concurrent
+  // reads fall in distinct shared-memory banks)
+  const int cpt = ((W + kWalkThreads - 1) / kWalkThreads) | 1;
+  const int cbeg = min(W, (int)threadIdx.x * cpt), cend = min(W, cbeg + cpt);
+  // Visits the thread's range in order; f(cell, ix, iy, iz).
   auto for_cells = [&](auto&& f) {
-    if (sa == 0) {
-      int lo_s = 0, hi_s = ns - 1;  // last slab with off <= cbeg
-      while (lo_s < hi_s) {
-        const int mid = (lo_s + hi_s + 1) >> 1;
-        if (slabs[mid].off <= cbeg) lo_s = mid;
-        else hi_s = mid - 1;
-      }
-      if (cbeg >= cend) return;
-      int sx = lo_s;
-      Slab sl = slabs[sx];  // holds cell cbeg (cbeg < W)
-      int jp = (cbeg - sl.off) / sl.wq, jq = cbeg - sl.off - jp * sl.wq;
-      for (int cidx = cbeg; cidx < cend; cidx++) {
-        while (cidx >= sl.off + sl.wp * sl.wq) {  // next slab with cells
-          sl = slabs[++sx];
-          jp = 0;
-          jq = 0;
+    if (cbeg >= cend) return;
+    int lo_k = 0, hi_k = A - 1;  // last column with first cell <= cbeg
+    while (lo_k < hi_k) {
+      const int mid = (lo_k + hi_k + 1) >> 1;
+      if (cols[mid].x <= cbeg) lo_k = mid;
+      else hi_k = mid - 1;
+    }
+    int k = lo_k;
+    int2 e = cols[k];
+    int zhi = e.y >> 16;
+    int cx = k / win.wby, cy = k - cx * win.wby;
+    int iz = (e.y & 0xffff) + (cbeg - e.x);
+    for (int cidx = cbeg; cidx < cend; cidx++) {
+      while (iz > zhi) {  // next non-empty column
+        ++k;
+        if (++cy == win.wby) {
+          cy = 0;
+          ++cx;
         }
-        f(cidx, sx, sl.p0 + jp, sl.q0 + jq);
-        if (++jq == sl.wq) {
-          jq = 0;
-          ++jp;
-        }
+        e = cols[k];
+        iz = e.y & 0xffff;
+        zhi = e.y >> 16;
       }
-    } else {
-      if (cbeg >= cend) return;
-      const int nz = g.n[2], wyb = by1 - by0 + 1;
-      int iz = cbeg % nz;
-      int t = cbeg / nz;
-      int iy = by0 + t % wyb, ix = bx0 + t / wyb;
-      for (int e = cbeg; e < cend; e++) {
-        const Slab sl = slabs[iz];
-        const unsigned jp = (unsigned)(ix - sl.p0), jq = (unsigned)(iy - sl.q0);
-        if (jp < (unsigned)sl.wp && jq < (unsigned)sl.wq)
-          f(sl.off + (int)jp * sl.wq + (int)jq, ix, iy, iz);
-        if (++iz == nz) {
-          iz = 0;
-          if (++iy > by1) {
-            iy = by0;
-            ++ix;
-          }
-        }
-      }
+      f(cidx, win.bx0 + cx, win.by0 + cy, iz);
+      ++iz;
     }
   };
   const ChannelLine L = line;
