@@ -826,9 +826,9 @@ static int64_t chunk_rows(const Geo& G, int cap_cells) {
   return c;
 }
 
-// Window capacity for a problem: the largest window over a sample of
-// channels spread over all angles, plus margin.  Rows whose window exceeds it
-// are reported and redone with their exact size.
+// Window capacity for a problem from a sample of channels spread over all
+// angles.  Rows whose window exceeds it are reported and redone with their
+// exact size.
 static epet_status sample_capacity(const Geo& G, cudaStream_t st, int* cap_out) {
   const epet_setup& s = G.p.setup;
   const int64_t nch = (int64_t)s.na * s.n0z * s.n0y * s.n1z * s.n1y;
@@ -868,9 +868,13 @@ static epet_status sample_capacity(const Geo& G, cudaStream_t st, int* cap_out) 
   dev_free(d_rows, st);
   dev_free(d_cells, st);
   if (rc != EPET_OK) return rc;
-  int mx = 0;
-  for (int v : cells) mx = std::max(mx, v);
-  *cap_out = std::max(256, (int)(mx * 1.15) + 64);
+  // Sized for the 90th percentile of the sample, not its maximum: every CTA
+  // reserves the capacity in shared memory, so a smaller one keeps more
+  // channels resident per SM; the few larger windows are redone with their
+  // exact size (redo_overflow).
+  std::sort(cells.begin(), cells.end());
+  const int p90 = cells.empty() ? 0 : cells[(cells.size() * 9) / 10];
+  *cap_out = std::max(256, (int)(p90 * 1.10) + 64);
   return EPET_OK;
 }
 
