@@ -188,10 +188,10 @@ struct Window {
 struct Col {
   int off, zlo, zn;
 };
-__device__ __forceinline__ Col load_col(const Window& w, int ix, int iy) {
+// Column (cx, cy) relative to the box corner; outside the box: no cells.
+__device__ __forceinline__ Col load_col(const Window& w, int cx, int cy) {
   Col c{0, 0, 0};
-  const unsigned cx = (unsigned)(ix - w.bx0), cy = (unsigned)(iy - w.by0);
-  if (cx < (unsigned)w.wbx && cy < (unsigned)w.wby) {
+  if ((unsigned)cx < (unsigned)w.wbx && (unsigned)cy < (unsigned)w.wby) {
     const int2 e = w.cols[cx * w.wby + cy];
     c.off = e.x;
     c.zlo = e.y & 0xffff;
@@ -308,13 +308,17 @@ __device__ void walk_ray(const Geo& G, const float* ray, const Window& w, int* o
   Y.enter(a_s);
   Z.enter(a_s);
   const float a_start = fmaxf(fmaxf(X.lo, Y.lo), Z.lo);  // entry of the starting cell
-  Col col = load_col(w, X.idx, Y.idx);
+  // The entry parameter of the current cell is always the latest crossing
+  // (the largest of the axes' lo), so it is carried as one value; the cell
+  // whose exit parameter reaches a_out is the last before the grid's exit.
+  float amin = a_start;
+  int cx = X.idx - w.bx0, cy = Y.idx - w.by0;  // column relative to the box
+  Col col = load_col(w, cx, cy);
   const float scale = G.fx_scale;
   const float two_s = __int_as_float((127 + w.split) << 23);   // 2^split
   const float inv_two_s = __int_as_float((127 - w.split) << 23);
   const int budget = g.n[0] + g.n[1] + g.n[2] + 4;
   for (int steps = 0; steps < budget; steps++) {
-    const float amin = fmaxf(fmaxf(X.lo, Y.lo), Z.lo);
     if (!(amin < a_stop)) break;
     const bool mx = X.hi <= Y.hi && X.hi <= Z.hi;
     const bool my = !mx && Y.hi <= Z.hi;
@@ -336,29 +340,35 @@ __device__ void walk_ray(const Geo& G, const float* ray, const Window& w, int* o
         atomicAdd(outside, 1);
       }
     }
-    // advance the axis whose plane comes first
-    const int st = mx ? X.step : (my ? Y.step : Z.step);
-    const int ni = (mx ? X.idx : (my ? Y.idx : Z.idx)) + st;
-    const int nn = mx ? X.n : (my ? Y.n : Z.n);
-    if (ni >= 0 && ni < nn) {
-      const float kh = (mx ? X.kh : (my ? Y.kh : Z.kh)) + (st > 0 ? 1.f : -1.f);
-      const float o = mx ? X.o : (my ? Y.o : Z.o), d = mx ? X.d : (my ? Y.d : Z.d);
-      const float r0 = mx ? X.r0 : (my ? Y.r0 : Z.r0), dr = mx ? X.dr : (my ? Y.dr : Z.dr);
-      const float inv = mx ? X.inv : (my ? Y.inv : Z.inv);
-      const float h = div_cr(fsub(fadd(o, fmul(kh, d)), r0), dr, inv);
-      X.lo = mx ? X.hi : X.lo; X.hi = mx ? h : X.hi; X.kh = mx ? kh : X.kh; X.idx = mx ? ni : X.idx;
-      Y.lo = my ? Y.hi : Y.lo; Y.hi = my ? h : Y.hi; Y.kh = my ? kh : Y.kh; Y.idx = my ? ni : Y.idx;
-      Z.lo = mz ? Z.hi : Z.lo; Z.hi = mz ? h : Z.hi; Z.kh = mz ? kh : Z.kh; Z.idx = mz ? ni : Z.idx;
-      if (!mz) col = load_col(w, X.idx, Y.idx);  // x or y moved: another column
-    } else {
-      // left the grid: the part before the starting cell, if any
+    if (amax >= a_out) {
+      // last cell: the part before the starting cell, if any
       if (second) break;
       second = true;
       a_stop = a_start;
-      X.idx = ex; X.lo = exl; X.hi = exh; X.kh = exk;
-      Y.idx = ey; Y.lo = eyl; Y.hi = eyh; Y.kh = eyk;
-      Z.idx = ez; Z.lo = ezl; Z.hi = ezh; Z.kh = ezk;
-      col = load_col(w, ex, ey);
+      X.idx = ex; X.hi = exh; X.kh = exk;
+      Y.idx = ey; Y.hi = eyh; Y.kh = eyk;
+      Z.idx = ez; Z.hi = ezh; Z.kh = ezk;
+      amin = fmaxf(fmaxf(exl, eyl), ezl);
+      cx = ex - w.bx0;
+      cy = ey - w.by0;
+      col = load_col(w, cx, cy);
+      continue;
+    }
+    // advance the axis whose plane comes first
+    const int st = mx ? X.step : (my ? Y.step : Z.step);
+    const float kh = (mx ? X.kh : (my ? Y.kh : Z.kh)) + (st > 0 ? 1.f : -1.f);
+    const float o = mx ? X.o : (my ? Y.o : Z.o), d = mx ? X.d : (my ? Y.d : Z.d);
+    const float r0 = mx ? X.r0 : (my ? Y.r0 : Z.r0), dr = mx ? X.dr : (my ? Y.dr : Z.dr);
+    const float inv = mx ? X.inv : (my ? Y.inv : Z.inv);
+    const float h = div_cr(fsub(fadd(o, fmul(kh, d)), r0), dr, inv);
+    X.hi = mx ? h : X.hi; X.kh = mx ? kh : X.kh; X.idx += mx ? st : 0;
+    Y.hi = my ? h : Y.hi; Y.kh = my ? kh : Y.kh; Y.idx += my ? st : 0;
+    Z.hi = mz ? h : Z.hi; Z.kh = mz ? kh : Z.kh; Z.idx += mz ? st : 0;
+    amin = amax;
+    if (!mz) {  // x or y moved: another column
+      cx += mx ? st : 0;
+      cy += my ? st : 0;
+      col = load_col(w, cx, cy);
     }
   }
 }
