@@ -38,6 +38,7 @@
 namespace epet {
 
 constexpr int kWalkThreads = 128;
+constexpr int kGeomFloats = 56;  // per-channel geometry record (k_channel_geom)
 constexpr int kMaxSlabs = 1024;  // nx limit of the walk kernel
 
 enum WalkMode { kModeCsr = 0, kModeForward = 1, kModeBack = 2, kModeColSum = 3,
@@ -48,6 +49,7 @@ struct WalkArgs {
   const int32_t* rows;  // this launch's rows
   int64_t m;
   const float* rays;    // [m][nrays][6]
+  const float* geom;    // [m][kGeomFloats] channel geometry (k_channel_geom)
   int cap_cells;        // window capacity (cells) of this launch
   // CSR staging (row i writes stage_col/val[i*stride ...], row_len[i])
   int64_t stride;
@@ -373,6 +375,45 @@ __device__ void walk_ray(const Geo& G, const float* ray, const Window& w, int* o
   }
 }
 
+// Per-channel geometry for the walk, one thread per channel: the 16 crystal
+// corners (8 per crystal), the crystal-centre line a, ab, and the exact
+// candidate threshold on |ab x ap|^2.  Laid out as kGeomFloats floats per row
+// (corners of crystal 0, of crystal 1, a, ab, threshold, padding).
+__global__ void k_channel_geom(Geo G, const int32_t* __restrict__ rows, int64_t m,
+                               float* __restrict__ geom) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= m) return;
+  int id[5];
+  channel_decode(G.p.setup, rows[i], id);
+  float sn, cs;
+  angle_sincos(G.p.setup, id[0], &sn, &cs);
+  const CrystalMat m0 = crystal_matrix(G.p.setup, sn, cs, 0, id[1], id[2]);
+  const CrystalMat m1 = crystal_matrix(G.p.setup, sn, cs, 1, id[3], id[4]);
+  float g[kGeomFloats];
+  for (int k = 0; k < 8; k++) {
+    crystal_apply(m0, (float)(k & 1), (float)((k >> 1) & 1), (float)(k >> 2), &g[3 * k]);
+    crystal_apply(m1, (float)(k & 1), (float)((k >> 1) & 1), (float)(k >> 2), &g[24 + 3 * k]);
+  }
+  float b[3];
+  crystal_apply(m0, 0.5f, 0.5f, 0.5f, &g[48]);
+  crystal_apply(m1, 0.5f, 0.5f, 0.5f, b);
+  for (int d = 0; d < 3; d++) g[51 + d] = fsub(b[d], g[48 + d]);
+  g[54] = candidate_threshold(norm3(g[51], g[52], g[53]), G.sum_radii);
+  g[55] = 0.f;
+  float4* o = reinterpret_cast<float4*>(geom + i * kGeomFloats);
+#pragma unroll
+  for (int q = 0; q < kGeomFloats / 4; q++)
+    o[q] = make_float4(g[4 * q], g[4 * q + 1], g[4 * q + 2], g[4 * q + 3]);
+}
+
+static epet_status launch_channel_geom(const Geo& G, const int32_t* rows, int64_t m, float* geom,
+                                       cudaStream_t st) {
+  if (m == 0) return EPET_OK;
+  k_channel_geom<<<ceil_div(m, 128), 128, 0, st>>>(G, rows, m, geom);
+  EPET_LAUNCHED();
+  return EPET_OK;
+}
+
 template <int kMode>
 __global__ void __launch_bounds__(kWalkThreads)
 k_walk(WalkArgs args) {
@@ -384,53 +425,33 @@ k_walk(WalkArgs args) {
   const WalkLayout lay = walk_layout(max(g.n[0], g.n[2]), args.cap_cells);
   Window win;
   win.split = G.fx_split;
-  __shared__ float c0[8][3], c1[8][3];
-  __shared__ ChannelLine line;
+  __shared__ __align__(16) float s_geom[kGeomFloats];
+  const float(*c0)[3] = reinterpret_cast<const float(*)[3]>(s_geom);
+  const float(*c1)[3] = reinterpret_cast<const float(*)[3]>(s_geom + 24);
+  const ChannelLine& line = *reinterpret_cast<const ChannelLine*>(s_geom + 48);
   __shared__ int warp_tot[kWalkThreads / 32];
-  __shared__ int s_total, s_outside, s_exact, s_sa, s_box[4];
+  __shared__ int s_total, s_outside, s_exact, s_box[4];
   __shared__ double red_d[kWalkThreads / 32];
   __shared__ float red_f[kWalkThreads / 32];
 
   if ((int64_t)blockIdx.x >= args.m) return;
   const int64_t row = args.sel ? (int64_t)args.sel[blockIdx.x] : (int64_t)blockIdx.x;
   const int64_t slot = blockIdx.x;  // staging slot
-  const int cnl = args.rows[row];
 
-  // ---- channel geometry: crystal transforms (thread 0), corners (16
-  // threads), exact candidate threshold (warp 1, 32-way search)
-  __shared__ CrystalMat mats[2];
+  // ---- channel geometry (k_channel_geom): corners, line, threshold
+  if (threadIdx.x < kGeomFloats / 4)
+    reinterpret_cast<float4*>(s_geom)[threadIdx.x] =
+        reinterpret_cast<const float4*>(args.geom + row * kGeomFloats)[threadIdx.x];
   if (threadIdx.x == 0) {
-    int id[5];
-    channel_decode(G.p.setup, cnl, id);
-    float sn, cs;
-    angle_sincos(G.p.setup, id[0], &sn, &cs);
-    mats[0] = crystal_matrix(G.p.setup, sn, cs, 0, id[1], id[2]);
-    mats[1] = crystal_matrix(G.p.setup, sn, cs, 1, id[3], id[4]);
-    float b[3];
-    crystal_apply(mats[0], 0.5f, 0.5f, 0.5f, line.a);
-    crystal_apply(mats[1], 0.5f, 0.5f, 0.5f, b);
-    for (int d = 0; d < 3; d++) line.ab[d] = fsub(b[d], line.a[d]);
     s_outside = 0;
     s_exact = 0;
     s_box[0] = INT_MAX; s_box[1] = INT_MIN; s_box[2] = INT_MAX; s_box[3] = INT_MIN;
-    // slab along the axis the line follows more closely (x or z)
-    s_sa = fabsf(line.ab[2]) > fabsf(line.ab[0]) ? 2 : 0;
   }
   __syncthreads();
-  const int sa = s_sa;
+  // slabs along the axis the line follows more closely (x or z)
+  const int sa = fabsf(line.ab[2]) > fabsf(line.ab[0]) ? 2 : 0;
   const int pa = sa == 0 ? 1 : 0, qa = sa == 0 ? 2 : 1;
   const int ns = g.n[sa];  // slabs
-  if (threadIdx.x < 16) {
-    const int k = threadIdx.x & 7;
-    float* dst = threadIdx.x < 8 ? c0[k] : c1[k];
-    crystal_apply(mats[threadIdx.x >> 3], (float)(k & 1), (float)((k >> 1) & 1),
-                  (float)(k >> 2), dst);
-  } else if ((threadIdx.x >> 5) == 1) {
-    const float nab = norm3(line.ab[0], line.ab[1], line.ab[2]);
-    const float thr = candidate_threshold_warp(nab, G.sum_radii);
-    if ((threadIdx.x & 31) == 0) line.s_max = thr;
-  }
-  __syncthreads();
 
   // ---- hull cross-section at every x plane: warp per plane, lanes over
   // the 64 crystal-corner pair lines
@@ -860,15 +881,19 @@ static epet_status sample_capacity(const Geo& G, cudaStream_t st, int* cap_out) 
     }
   const int64_t n = (int64_t)sample.size();
   int32_t *d_rows = nullptr, *d_cells = nullptr;
+  float* d_geom = nullptr;
   EPET_CUDA(dev_alloc((void**)&d_rows, n * 4, st));
   EPET_CUDA(dev_alloc((void**)&d_cells, n * 4, st));
+  EPET_CUDA(dev_alloc((void**)&d_geom, n * kGeomFloats * 4, st));
   EPET_CUDA(cudaMemcpyAsync(d_rows, sample.data(), n * 4, cudaMemcpyHostToDevice, st));
   WalkArgs a{};
   a.G = G;
   a.rows = d_rows;
   a.m = n;
   a.win_cells = d_cells;
-  epet_status rc = launch_walk<kModeWindow>(a, walk_smem(G, 0), st);
+  a.geom = d_geom;
+  epet_status rc = launch_channel_geom(G, d_rows, n, d_geom, st);
+  if (rc == EPET_OK) rc = launch_walk<kModeWindow>(a, walk_smem(G, 0), st);
   std::vector<int32_t> cells(n);
   if (rc == EPET_OK) {
     cudaError_t e = cudaMemcpyAsync(cells.data(), d_cells, n * 4, cudaMemcpyDeviceToHost, st);
@@ -877,6 +902,7 @@ static epet_status sample_capacity(const Geo& G, cudaStream_t st, int* cap_out) 
   }
   dev_free(d_rows, st);
   dev_free(d_cells, st);
+  dev_free(d_geom, st);
   if (rc != EPET_OK) return rc;
   // Sized for the 90th percentile of the sample, not its maximum: every CTA
   // reserves the capacity in shared memory, so a smaller one keeps more
@@ -919,6 +945,7 @@ struct BuildOut {
 size_t walk_workspace_size(const Geo& G, int64_t m, int cap_cells, bool csr) {
   const int64_t ch = std::min<int64_t>(std::max<int64_t>(m, 1), chunk_rows(G, cap_cells));
   size_t b = align256((size_t)ch * G.p.nrays * 24);         // rays
+  b += align256((size_t)ch * kGeomFloats * 4);              // channel geometry
   if (csr) {
     b += 2 * align256((size_t)ch * cap_cells * 4);          // staging col/val
     b += align256((size_t)ch * 4);                          // row_len
@@ -943,11 +970,15 @@ static epet_status redo_overflow(WalkArgs a, const int32_t* ovf_rows, int n, int
   EPET_CUDA(cudaMemcpyAsync(sel, ovf_rows, n * 4, cudaMemcpyDeviceToDevice, st));
   k_gather_i32<<<ceil_div(n, 256), 256, 0, st>>>(a.rows, sel, n, cnl);
   EPET_LAUNCHED();
+  float* geom = nullptr;
+  EPET_CUDA(dev_alloc((void**)&geom, (size_t)n * kGeomFloats * 4, st));
+  EPET_CHECK(launch_channel_geom(a.G, cnl, n, geom, st));
   WalkArgs w{};
   w.G = a.G;
   w.rows = cnl;
   w.m = n;
   w.win_cells = cells;
+  w.geom = geom;
   EPET_CHECK(launch_walk<kModeWindow>(w, walk_smem(a.G, 0), st));
   std::vector<int32_t> h(n);
   EPET_CUDA(cudaMemcpyAsync(h.data(), cells, n * 4, cudaMemcpyDeviceToHost, st));
@@ -975,6 +1006,7 @@ static epet_status redo_overflow(WalkArgs a, const int32_t* ovf_rows, int n, int
   dev_free(sel, st);
   dev_free(cnl, st);
   dev_free(cells, st);
+  dev_free(geom, st);
   return EPET_OK;
 }
 
@@ -987,6 +1019,7 @@ static epet_status run_walk(const Geo& G, const int32_t* rows, int64_t m,
   Scratch scr;
   EPET_CHECK(scr.init(ws, ws_bytes, walk_workspace_size(G, m, cap_cells, csr), st));
   float* rays = scr.take<float>((size_t)ch * G.p.nrays * 6);
+  float* geom = scr.take<float>((size_t)ch * kGeomFloats);
   int32_t *stage_col = nullptr, *row_len = nullptr;
   float* stage_val = nullptr;
   int64_t *cnt = nullptr, *rp_chunk = nullptr, *scan_tmp = nullptr;
@@ -1010,11 +1043,13 @@ static epet_status run_walk(const Geo& G, const int32_t* rows, int64_t m,
   for (int64_t c0 = 0; c0 < m; c0 += ch) {
     const int64_t mc = std::min(ch, m - c0);
     EPET_CHECK(launch_rays(G, rows + c0, mc, rays, false, st));
+    EPET_CHECK(launch_channel_geom(G, rows + c0, mc, geom, st));
     WalkArgs a{};
     a.G = G;
     a.rows = rows + c0;
     a.m = mc;
     a.rays = rays;
+    a.geom = geom;
     a.cap_cells = cap_cells;
     a.stride = cap_cells;
     a.stage_col = stage_col;
