@@ -186,7 +186,7 @@ def reference_arm(args):
 
 # ------------------------------------------------------------------ GB300
 
-def batch_measure(args, api, torch, st, nit: int = 10):
+def batch_measure(args, api, torch, st, nit: int = 10, grids=None, angles=None):
     """Batched form: args.batch seeded problems of uneven size (grids and
     angle counts drawn from the batched workload's sets), each with its own
     phantom and Poisson measurement.  Times nit iterations of all problems
@@ -198,7 +198,10 @@ def batch_measure(args, api, torch, st, nit: int = 10):
     torch.cuda.empty_cache()
     api.trim_memory()
     t0 = time.perf_counter()
-    members = batch_members(args.batch)
+    from epetreco_gb300.problem import BATCH_ANGLES, BATCH_GRIDS
+    grids = grids or BATCH_GRIDS
+    angles = angles or BATCH_ANGLES
+    members = batch_members(args.batch, grids=grids, angles=angles)
     # The drawn problems' matrices together exceed the device memory (tens of
     # GB each at 52^3-64^3 x 180 angles): problems are taken in draw order
     # while the estimated CSR + CSC bytes (16 per non-zero; non-zeros per row
@@ -258,8 +261,8 @@ def batch_measure(args, api, torch, st, nit: int = 10):
     gbs = stats["bytes_per_iteration"] * nit / t_batch / 1e9
     out = {"problems": len(probs), "drawn": len(members), "skipped_for_memory": skipped,
            "iterations": nit,
-           "workload": (f"{len(members)} seeded draws (grids {{24,32,40,52,64}}^3, angles "
-                        f"{{8,30,60,120,180}}, 20-100 rays, 1e5-1e8 counts, FP32 values); "
+           "workload": (f"{len(members)} seeded draws (grids {set(grids)}^3, angles "
+                        f"{set(angles)}, 20-100 rays, 1e5-1e8 counts, FP32 values); "
                         f"the {len(probs)} whose matrices fit {budget / 1e9:.0f} GB, in draw "
                         f"order"),
            "grids": [q.grid.n[0] for q, *_ in probs], "angles": [q.setup.na for q, *_ in probs],
@@ -314,8 +317,10 @@ def gb300_arm(args):
         return
 
     if args.batch_only:
-        print(json.dumps({"batched": batch_measure(args, api, torch,
-                                                   torch.cuda.current_stream())}), flush=True)
+        cs = torch.cuda.current_stream()
+        print(json.dumps({"batched": batch_measure(args, api, torch, cs),
+                          "batched_small": batch_measure(args, api, torch, cs, grids=(24, 32),
+                                                         angles=(8,))}), flush=True)
         return
 
     # ---- inputs (not timed): measurement and sensitivity
@@ -469,9 +474,12 @@ def gb300_arm(args):
                            "image_rel_l2_vs_fp32": err}
             R16.close()
     R.close()
-    batched = None
+    batched = batched_small = None
     if args.batch > 0 and world == 1:
         batched = batch_measure(args, api, torch, st)
+        # the same form on small problems, where one launch per problem
+        # leaves the GPU mostly idle
+        batched_small = batch_measure(args, api, torch, st, grids=(24, 32), angles=(8,))
 
     # ---- aggregate over ranks
     vals = torch.tensor([t_step, t_e2e], device="cuda", dtype=torch.float64)
@@ -518,6 +526,8 @@ def gb300_arm(args):
         out["forms"] = forms
     if batched is not None:
         out["batched"] = batched
+    if batched_small is not None:
+        out["batched_small"] = batched_small
     if cpu is not None:
         out["cpu_baseline"] = cpu
     print(json.dumps(out), flush=True)

@@ -517,8 +517,9 @@ k_walk(WalkArgs args) {
       atomicMin(&s_box[2], ylo); atomicMax(&s_box[3], yhi);
     }
   }
-  const int excl = block_excl_scan(my_cells, warp_tot, &s_total);
-  {
+  int n_rect = 0;  // cells of all slab rectangles (z slabs only: offsets for the table)
+  if (sa == 2) {   // uniform across the block
+    const int excl = block_excl_scan(my_cells, warp_tot, &s_total);
     int o = excl;
     for (int i = sbeg; i < send; i++) {
       slabs[i].off = o;
@@ -526,7 +527,7 @@ k_walk(WalkArgs args) {
     }
   }
   __syncthreads();
-  const int n_rect = s_total;  // cells of all slab rectangles
+  if (sa == 2) n_rect = s_total;
   win.bx0 = s_box[0];
   win.by0 = s_box[2];
   win.wbx = s_box[1] >= s_box[0] ? s_box[1] - s_box[0] + 1 : 0;
