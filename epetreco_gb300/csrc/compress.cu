@@ -138,16 +138,25 @@ __global__ void k_c16_fill(const int64_t* __restrict__ ptr, const int32_t* __res
   }
 }
 
+// The gathered vector: FP32, or BF16 bits (the MLEM ratio e of the 16-bit
+// forms: half the gather traffic of the transpose product).
+__device__ __forceinline__ float ld_x(const float* __restrict__ x, int32_t i) {
+  return __ldg(x + i);
+}
+__device__ __forceinline__ float ld_x(const uint16_t* __restrict__ x, int32_t i) {
+  return __uint_as_float((uint32_t)__ldg(reinterpret_cast<const unsigned short*>(x) + i) << 16);
+}
+
 // Product over the 16-bit layout: a group of G lanes per row; lane l takes
 // the entry pairs l, l + G, ... of the row (32-bit loads of offsets and
 // values), so the lanes of a warp gather x at consecutive entries of the row
 // (neighbouring columns share cache sectors); four pairs per round, and the
 // next round's loads are issued before this round's gathers.
-template <int G, int FMT, class Epi>
+template <int G, int FMT, class Epi, class XT>
 __global__ void __launch_bounds__(kSpmvThreads)
 k_rows16(const int64_t* __restrict__ ptr, const int32_t* __restrict__ cbase,
          const float* __restrict__ scale, const uint16_t* __restrict__ off,
-         const uint16_t* __restrict__ q, const float* __restrict__ x, int64_t nrows, Epi epi,
+         const uint16_t* __restrict__ q, const XT* __restrict__ x, int64_t nrows, Epi epi,
          double* __restrict__ partial) {
   constexpr int RPT = kSpmvThreads / G, P = 4;
   __shared__ double red[kSpmvThreads / 32];
@@ -189,8 +198,8 @@ k_rows16(const int64_t* __restrict__ ptr, const int32_t* __restrict__ cbase,
 #pragma unroll
     for (int u = 0; u < P; u++) {
       if (pb + u * G < p1) {
-        acc[u] = fmaf(from_q<FMT>(vc[u] & 0xffffu), __ldg(x + bc[u] + (int32_t)(oc[u] & 0xffffu)), acc[u]);
-        acc[u] = fmaf(from_q<FMT>(vc[u] >> 16), __ldg(x + bc[u] + (int32_t)(oc[u] >> 16)), acc[u]);
+        acc[u] = fmaf(from_q<FMT>(vc[u] & 0xffffu), ld_x(x, bc[u] + (int32_t)(oc[u] & 0xffffu)), acc[u]);
+        acc[u] = fmaf(from_q<FMT>(vc[u] >> 16), ld_x(x, bc[u] + (int32_t)(oc[u] >> 16)), acc[u]);
       }
       oc[u] = on[u]; vc[u] = vn[u]; bc[u] = bn[u];
     }
@@ -211,16 +220,16 @@ struct EpiStore {  // y = alpha*d + beta*y
   }
 };
 
-template <int FMT, class Epi>
-static epet_status launch16_fmt(int G, const epet_csr16* a, const float* x, Epi epi,
+template <int FMT, class Epi, class XT>
+static epet_status launch16_fmt(int G, const epet_csr16* a, const XT* x, Epi epi,
                                 double* partial, cudaStream_t st) {
   const int rpb = kSpmvThreads / G;
   const unsigned nb = (unsigned)((a->m + rpb - 1) / rpb);
   switch (G) {
-    case 32: k_rows16<32, FMT, Epi><<<nb, kSpmvThreads, 0, st>>>(a->row_ptr, a->base, a->scale, a->delta, a->q, x, a->m, epi, partial); break;
-    case 16: k_rows16<16, FMT, Epi><<<nb, kSpmvThreads, 0, st>>>(a->row_ptr, a->base, a->scale, a->delta, a->q, x, a->m, epi, partial); break;
-    case 8: k_rows16<8, FMT, Epi><<<nb, kSpmvThreads, 0, st>>>(a->row_ptr, a->base, a->scale, a->delta, a->q, x, a->m, epi, partial); break;
-    default: k_rows16<4, FMT, Epi><<<nb, kSpmvThreads, 0, st>>>(a->row_ptr, a->base, a->scale, a->delta, a->q, x, a->m, epi, partial); break;
+    case 32: k_rows16<32, FMT, Epi, XT><<<nb, kSpmvThreads, 0, st>>>(a->row_ptr, a->base, a->scale, a->delta, a->q, x, a->m, epi, partial); break;
+    case 16: k_rows16<16, FMT, Epi, XT><<<nb, kSpmvThreads, 0, st>>>(a->row_ptr, a->base, a->scale, a->delta, a->q, x, a->m, epi, partial); break;
+    case 8: k_rows16<8, FMT, Epi, XT><<<nb, kSpmvThreads, 0, st>>>(a->row_ptr, a->base, a->scale, a->delta, a->q, x, a->m, epi, partial); break;
+    default: k_rows16<4, FMT, Epi, XT><<<nb, kSpmvThreads, 0, st>>>(a->row_ptr, a->base, a->scale, a->delta, a->q, x, a->m, epi, partial); break;
   }
   EPET_LAUNCHED();
   return EPET_OK;
@@ -235,8 +244,8 @@ int pick_group16(double avg_len) {
   return 4;
 }
 
-template <class Epi>
-epet_status launch_rows16(const epet_csr16* a, const float* x, Epi epi, double* partial,
+template <class Epi, class XT>
+epet_status launch_rows16(const epet_csr16* a, const XT* x, Epi epi, double* partial,
                           cudaStream_t st) {
   if (a->m <= 0) return EPET_OK;
   if (((reinterpret_cast<uintptr_t>(a->delta) | reinterpret_cast<uintptr_t>(a->q)) & 15) != 0)
@@ -249,10 +258,11 @@ epet_status launch_rows16(const epet_csr16* a, const float* x, Epi epi, double* 
   return set_error(EPET_ERR_INVALID, "unknown value format %d", a->format);
 }
 
-template epet_status launch_rows16<EpiMlemForward>(const epet_csr16*, const float*,
-                                                   EpiMlemForward, double*, cudaStream_t);
-template epet_status launch_rows16<EpiMlemUpdate>(const epet_csr16*, const float*,
-                                                  EpiMlemUpdate, double*, cudaStream_t);
+template epet_status launch_rows16<EpiMlemForward16, float>(const epet_csr16*, const float*,
+                                                            EpiMlemForward16, double*,
+                                                            cudaStream_t);
+template epet_status launch_rows16<EpiMlemUpdate, uint16_t>(const epet_csr16*, const uint16_t*,
+                                                            EpiMlemUpdate, double*, cudaStream_t);
 
 int64_t rows16_blocks(const epet_csr16* a) {
   const int G = pick_group16(a->m ? (double)a->nnz / a->m : 0.0);
@@ -341,7 +351,8 @@ epet_status epet_csr16_mv(const epet_csr16* a, float alpha, const float* x_d, fl
                           float* y_d, epet_stream_t stream) {
   if (!a || (a->m > 0 && !y_d) || (a->n > 0 && !x_d))
     return set_error(EPET_ERR_INVALID, "bad arguments");
-  return launch_rows16(a, x_d, EpiStore{alpha, beta, y_d}, nullptr, (cudaStream_t)stream);
+  return launch_rows16<EpiStore, float>(a, x_d, EpiStore{alpha, beta, y_d}, nullptr,
+                                       (cudaStream_t)stream);
 }
 
 }  // extern "C"

@@ -28,7 +28,7 @@ static void mlem_free(epet_mlem* h) {
   if (h->graph) cudaGraphDestroy(h->graph);
   void* bufs[] = {h->A16.row_ptr, h->A16.base, h->A16.scale, h->A16.delta, h->A16.q,
                   h->At16.row_ptr, h->At16.base, h->At16.scale, h->At16.delta, h->At16.q,
-                  h->rows, h->y, h->ybar, h->s, h->x, h->xnew, h->e, h->A.row_ptr, h->A.col,
+                  h->rows, h->y, h->ybar, h->e16, h->s, h->x, h->xnew, h->e, h->A.row_ptr, h->A.col,
                   h->A.val,
                   h->At.col_ptr, h->At.row, h->At.val, h->part_ll, h->part_x, h->sums};
   for (void* b : bufs)
@@ -38,9 +38,10 @@ static void mlem_free(epet_mlem* h) {
 
 static epet_status mlem_iteration(epet_mlem* h, cudaStream_t st) {
   if (h->opt.value_format != EPET_VALUES_FP32) {
-    EPET_CHECK(launch_rows16(&h->A16, h->x, EpiMlemForward{h->y, h->e, h->ybar}, nullptr, st));
-    EPET_CHECK(launch_rows16(&h->At16, h->e, EpiMlemUpdate{h->x, h->s, h->xnew, nullptr},
-                             h->part_x, st));
+    EPET_CHECK((launch_rows16<EpiMlemForward16, float>(
+        &h->A16, h->x, EpiMlemForward16{h->y, h->e16, h->ybar}, nullptr, st)));
+    EPET_CHECK((launch_rows16<EpiMlemUpdate, uint16_t>(
+        &h->At16, h->e16, EpiMlemUpdate{h->x, h->s, h->xnew, nullptr}, h->part_x, st)));
     EPET_CHECK(launch_sum_partials(h->part_x, h->nb_bwd, h->sums + 1, st));
     EPET_CHECK(launch_normalise(h->xnew, h->sums + 1, h->V, h->x, st));
     return EPET_OK;
@@ -97,6 +98,7 @@ epet_status epet_mlem_create(const epet_problem* p, const int32_t* rows_d, const
   ALLOC(h->y, m * 4);
   ALLOC(h->e, m * 4);
   ALLOC(h->ybar, m * 4);
+  if (o.value_format != EPET_VALUES_FP32) ALLOC(h->e16, m * 2);
   ALLOC(h->s, V * 4);
   ALLOC(h->x, V * 4);
   ALLOC(h->xnew, V * 4);
@@ -264,8 +266,9 @@ epet_status epet_mlem_stats(const epet_mlem* h, int64_t* nnz_h, int64_t* bytes_h
     // per stored entry 4 bytes (offset + value) and a 4-byte base per 8;
     // per row a pointer and a scale (12 bytes); vectors as in FP32
     const int64_t m = h->m, V = h->V;
-    *bytes_h = 4 * h->A16.nnz + h->A16.nnz / 2 + 12 * m + 4 * m + 4 * V + 4 * m +
-               4 * h->At16.nnz + h->At16.nnz / 2 + 12 * V + 4 * m + 4 * V + 4 * V + 4 * V +
+    // (e written and gathered as 2-byte BF16)
+    *bytes_h = 4 * h->A16.nnz + h->A16.nnz / 2 + 12 * m + 4 * m + 4 * V + 2 * m + 4 * m +
+               4 * h->At16.nnz + h->At16.nnz / 2 + 12 * V + 2 * m + 4 * V + 4 * V + 4 * V +
                4 * V + 4 * V;
   } else if (bytes_h) {
     // forward: values+columns, row pointers, y, x (once), e written;

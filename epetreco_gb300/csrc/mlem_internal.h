@@ -11,6 +11,7 @@ struct epet_mlem {
   int32_t* rows = nullptr;
   float *y = nullptr, *s = nullptr, *x = nullptr, *xnew = nullptr, *e = nullptr;
   float* ybar = nullptr;  // last forward projection
+  uint16_t* e16 = nullptr;  // ratio e as BF16 bits (16-bit forms)
   epet_csr A{};
   epet_csc At{};
   epet_csr16 A16{}, At16{};  // 16-bit forms (value_format != FP32)

@@ -22,6 +22,22 @@ struct EpiMlemForward {
   }
 };
 
+// The same for the 16-bit forms: e is kept as BF16 bits (relative error
+// <= 2^-9), which halves the bytes of the transpose product's gathers.
+struct EpiMlemForward16 {
+  const float* y;
+  uint16_t* e16;
+  float* ybar;
+  __device__ double operator()(int64_t r, float d) const {
+    ybar[r] = d;
+    const float ev = d > 0.f ? __fdiv_rn(y[r], d) : 0.f;
+    // round to nearest even on the upper 16 bits (e is finite and >= 0)
+    const uint32_t b = __float_as_uint(ev);
+    e16[r] = (uint16_t)((b + 0x7fffu + ((b >> 16) & 1u)) >> 16);
+    return 0.0;
+  }
+};
+
 // Back-projection epilogue (column v, c = (A^T e)[v]): the reference's
 // dividesMultiplies (mlemOperations.hpp:38-79): xnew = x*c/s with s == 0 -> 1;
 // returns xnew for the image sum.
@@ -56,8 +72,8 @@ epet_status launch_rows(const RowPlan& plan, const int64_t* ptr, const int32_t* 
 epet_status tune_rows(int kind, int64_t nrows, int64_t nnz, int64_t ncols, double avg,
                       const std::function<epet_status(const RowPlan&)>& run, cudaStream_t st,
                       RowPlan* out);
-template <class Epi>
-epet_status launch_rows16(const epet_csr16* a, const float* x, Epi epi, double* partial,
+template <class Epi, class XT>
+epet_status launch_rows16(const epet_csr16* a, const XT* x, Epi epi, double* partial,
                           cudaStream_t st);
 int64_t rows16_blocks(const epet_csr16* a);
 inline int64_t csr16_capacity(int64_t nnz16) { return nnz16; }
