@@ -184,6 +184,7 @@ struct Window {
   const int2* cols;  // per column: {first cell, zlo | zhi << 16}; empty: zlo 1, zhi 0
   int bx0, by0, wbx, wby;
   int split;
+  int trash;  // cell W past the window: absorbs the (zero) adds of steps with nothing to add
 };
 
 // A lane's cached column: first cell, first z, number of z cells.
@@ -191,14 +192,14 @@ struct Col {
   int off, zlo, zn;
 };
 // Column (cx, cy) relative to the box corner; outside the box: no cells.
+// Branch-free: an index outside the box reads entry 0 and gets zn = 0.
 __device__ __forceinline__ Col load_col(const Window& w, int cx, int cy) {
-  Col c{0, 0, 0};
-  if ((unsigned)cx < (unsigned)w.wbx && (unsigned)cy < (unsigned)w.wby) {
-    const int2 e = w.cols[cx * w.wby + cy];
-    c.off = e.x;
-    c.zlo = e.y & 0xffff;
-    c.zn = (e.y >> 16) - c.zlo + 1;
-  }
+  const bool in = (unsigned)cx < (unsigned)w.wbx && (unsigned)cy < (unsigned)w.wby;
+  const int2 e = w.cols[in ? cx * w.wby + cy : 0];
+  Col c;
+  c.off = e.x;
+  c.zlo = e.y & 0xffff;
+  c.zn = in ? (e.y >> 16) - c.zlo + 1 : 0;
   return c;
 }
 
@@ -314,6 +315,7 @@ __device__ void walk_ray(const Geo& G, const float* ray, const Window& w, int* o
   // (the largest of the axes' lo), so it is carried as one value; the cell
   // whose exit parameter reaches a_out is the last before the grid's exit.
   float amin = a_start;
+  int n_out = 0;  // hits outside the window (none expected)
   int cx = X.idx - w.bx0, cy = Y.idx - w.by0;  // column relative to the box
   Col col = load_col(w, cx, cy);
   const float scale = G.fx_scale;
@@ -326,21 +328,25 @@ __device__ void walk_ray(const Geo& G, const float* ray, const Window& w, int* o
     const bool my = !mx && Y.hi <= Z.hi;
     const bool mz = !mx && !my;
     const float amax = mx ? X.hi : (my ? Y.hi : Z.hi);
-    if (amin < amax && amin >= a_lo) {  // cells entered before a_lo: previous piece
+    {
+      // Branch-free add: a step with nothing to add (a zero-length cell, a
+      // cell of the previous piece) adds zero to the trash cell.
+      const bool add = amin < amax && amin >= a_lo;  // before a_lo: previous piece
       const unsigned dz = (unsigned)(Z.idx - col.zlo);
-      if (dz < (unsigned)col.zn) {
-        const int c = col.off + (int)dz;
-        // units = RN(len * scale) split as hi * 2^split + lo; for a product
-        // >= 2^split the float is an integer and both parts are exact
-        const float v = fmul(fmul(fsub(amax, amin), L), scale);
-        const uint32_t h = __float2uint_rz(fmul(v, inv_two_s));
-        uint32_t l = __float2uint_rn(__fmaf_rn(-__uint2float_rn(h), two_s, v));
-        if ((h | l) == 0u) l = 1u;  // a positive chord counts at least one unit
-        atomicAdd(&w.lo[c], l);
-        if (h) atomicAdd(&w.hi[c], h);
-      } else {
-        atomicAdd(outside, 1);
-      }
+      const bool inwin = dz < (unsigned)col.zn;
+      n_out += (add && !inwin) ? 1 : 0;
+      const bool ok = add && inwin;
+      const int c = ok ? col.off + (int)dz : w.trash;
+      // units = RN(len * scale) split as hi * 2^split + lo; for a product
+      // >= 2^split the float is an integer and both parts are exact
+      const float v = fmul(fmul(fsub(amax, amin), L), scale);
+      uint32_t h = __float2uint_rz(fmul(v, inv_two_s));
+      uint32_t l = __float2uint_rn(__fmaf_rn(-__uint2float_rn(h), two_s, v));
+      l = (h | l) == 0u ? 1u : l;  // a positive chord counts at least one unit
+      h = ok ? h : 0u;
+      l = ok ? l : 0u;
+      atomicAdd(&w.lo[c], l);
+      atomicAdd(&w.hi[c], h);
     }
     if (amax >= a_out) {
       // last cell: the part before the starting cell, if any
@@ -367,12 +373,11 @@ __device__ void walk_ray(const Geo& G, const float* ray, const Window& w, int* o
     Y.hi = my ? h : Y.hi; Y.kh = my ? kh : Y.kh; Y.idx += my ? st : 0;
     Z.hi = mz ? h : Z.hi; Z.kh = mz ? kh : Z.kh; Z.idx += mz ? st : 0;
     amin = amax;
-    if (!mz) {  // x or y moved: another column
-      cx += mx ? st : 0;
-      cy += my ? st : 0;
-      col = load_col(w, cx, cy);
-    }
+    cx += mx ? st : 0;  // x or y moved: another column
+    cy += my ? st : 0;
+    col = load_col(w, cx, cy);
   }
+  if (n_out) atomicAdd(outside, n_out);
 }
 
 // Per-channel geometry for the walk, one thread per channel: the 16 crystal
@@ -572,7 +577,7 @@ k_walk(WalkArgs args) {
       if (zhi >= zlo) n += zhi - zlo + 1;
     }
     block_excl_scan(n, warp_tot, &s_total);
-    if (threadIdx.x == 0) args.win_cells[row] = A + s_total;
+    if (threadIdx.x == 0) args.win_cells[row] = A + s_total + 1;  // + the trash cell
     return;
   }
   int2* cols = reinterpret_cast<int2*>(smem + lay.pool);
@@ -625,7 +630,7 @@ k_walk(WalkArgs args) {
       if (cols[k].y >= cols[k].x) n_mine += cols[k].y - cols[k].x + 1;
   const int cexcl = block_excl_scan(n_mine, warp_tot, &s_total);
   const int W = s_total;  // window cells
-  if (!table_fits || A + W > args.cap_cells) {
+  if (!table_fits || A + W + 1 > args.cap_cells) {
     if (threadIdx.x == 0) {
       int k = atomicAdd(args.overflow_count, 1);
       args.overflow_rows[k] = (int32_t)row;
@@ -646,10 +651,11 @@ k_walk(WalkArgs args) {
     }
   }
   win.cols = cols;
-  win.lo = reinterpret_cast<uint32_t*>(smem + lay.pool + (size_t)A * 8);  // 8A + 8W <= pool
-  win.hi = win.lo + W;
+  win.lo = reinterpret_cast<uint32_t*>(smem + lay.pool + (size_t)A * 8);  // 8A + 8(W+1) <= pool
+  win.hi = win.lo + W + 1;
+  win.trash = W;
   // ---- zero the window, walk the rays
-  for (int i = threadIdx.x; i < W; i += kWalkThreads) {
+  for (int i = threadIdx.x; i <= W; i += kWalkThreads) {  // the window and the trash cell
     win.lo[i] = 0u;
     win.hi[i] = 0u;
   }
