@@ -737,27 +737,28 @@ k_walk(WalkArgs args) {
   const ChannelLine L = line;
   const float fR = (float)R;
   // pass 1: candidate filter, count, projections
+  // (every cell takes the same instructions: the candidate test and the
+  // value are computed for all of them and the result selected)
   int cnt = 0;
   float fsum = 0.f;
+  const float inv_fR = __frcp_rn(fR);
   for_cells([&](int cidx, int ix, int iy, int iz) {
     const unsigned long long u =
         ((unsigned long long)win.hi[cidx] << win.split) + (unsigned long long)win.lo[cidx];
-    if (u == 0ull) return;
-    if (!is_candidate(G, L, ix, iy, iz)) {
-      win.lo[cidx] = 0u;  // not a candidate of this channel: drop
-      win.hi[cidx] = 0u;
-      return;
+    const bool cand = is_candidate(G, L, ix, iy, iz);  // not a candidate: dropped
+    const bool keep = (u != 0ull) & cand;
+    const float v = div_cr(fmul(__ull2float_rn(u), G.fx_inv), fR, inv_fR);
+    cnt += keep ? 1 : 0;
+    if (kMode == kModeCsr) win.lo[cidx] = keep ? __float_as_uint(v) : 0u;  // read by pass 2
+    if (kMode != kModeCsr && keep) {
+      const int vox = ix * G.nyz + iy * g.n[2] + iz;
+      if (kMode == kModeForward) fsum = fadd(fsum, fmul(v, args.x[vox]));
+      if (kMode == kModeBack) {
+        const float ev = args.e[row];
+        if (ev != 0.f) atomicAdd(&args.c[vox], fmul(v, ev));
+      }
+      if (kMode == kModeColSum) atomicAdd(&args.s64[vox], (double)v);
     }
-    const float v = fdiv(fmul(__ull2float_rn(u), G.fx_inv), fR);
-    const int vox = ix * G.nyz + iy * g.n[2] + iz;
-    cnt++;
-    if (kMode == kModeCsr) win.lo[cidx] = __float_as_uint(v);  // > 0: read by pass 2
-    if (kMode == kModeForward) fsum = fadd(fsum, fmul(v, args.x[vox]));
-    if (kMode == kModeBack) {
-      const float ev = args.e[row];
-      if (ev != 0.f) atomicAdd(&args.c[vox], fmul(v, ev));
-    }
-    if (kMode == kModeColSum) atomicAdd(&args.s64[vox], (double)v);
   });
   if (kMode == kModeCsr) {
     const int pos = block_excl_scan(cnt, warp_tot, &s_total);
