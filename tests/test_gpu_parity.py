@@ -199,3 +199,22 @@ def test_rays_every_row_any_order(gpu_lib, oracle):
     for i in range(len(rows)):
         want = oracle.rays(p, rows[i], rnd[i], trig=trig)
         assert (bits(got[i]) == bits(want)).all(), i
+
+
+def test_windows_over_capacity_are_redone(case):
+    """With a window capacity (600 cells) below the channels' windows but
+    above their non-zeros, nearly every row is measured again and rebuilt in
+    the second launch with its exact window: the matrix must equal the
+    default build bit for bit, and the matrix-free projections through the
+    same path must agree."""
+    p, rows = case["p"], case["rows"]
+    cap = 600
+    A = api.systemMatrixCalculation(p, dev(rows))
+    B = api.systemMatrixCalculation(p, dev(rows), max_row_nnz=cap)
+    assert torch.equal(A.row_ptr, B.row_ptr)
+    assert torch.equal(A.col, B.col)
+    assert torch.equal(A.val, B.val)
+    x = torch.rand(p.nvoxels, device="cuda")
+    y0 = api.project_forward(p, dev(rows), x)
+    y1 = api.project_forward(p, dev(rows), x, max_row_nnz=cap)
+    assert torch.equal(y0, y1)
