@@ -149,62 +149,69 @@ __device__ __forceinline__ float ld_x(const uint16_t* __restrict__ x, int32_t i)
 
 // Product over the 16-bit layout: a group of G lanes per row; lane l takes
 // the entry pairs l, l + G, ... of the row (32-bit loads of offsets and
-// values), so the lanes of a warp gather x at consecutive entries of the row
-// (neighbouring columns share cache sectors); four pairs per round, and the
-// next round's loads are issued before this round's gathers.
-template <int G, int FMT, class Epi, class XT>
+// values), so the lanes of a group gather x at consecutive entries of the
+// row (neighbouring columns share cache sectors); P pairs per round, and the
+// next round's loads are issued before this round's gathers.  Indices are
+// 32-bit and relative to the row's first stored entry (a row holds fewer
+// than 2^31 entries).
+template <int G, int P, int FMT, class Epi, class XT>
 __global__ void __launch_bounds__(kSpmvThreads)
 k_rows16(const int64_t* __restrict__ ptr, const int32_t* __restrict__ cbase,
          const float* __restrict__ scale, const uint16_t* __restrict__ off,
          const uint16_t* __restrict__ q, const XT* __restrict__ x, int64_t nrows, Epi epi,
          double* __restrict__ partial) {
-  constexpr int RPT = kSpmvThreads / G, P = 4;
+  constexpr int RPT = kSpmvThreads / G;
   __shared__ double red[kSpmvThreads / 32];
   const int lg = threadIdx.x % G;
   const int64_t row = (int64_t)blockIdx.x * RPT + threadIdx.x / G;
   const unsigned gmask = G == 32 ? 0xffffffffu : (((1u << G) - 1u) << (threadIdx.x & 31 & ~(G - 1)));
   double part = 0.0;
   const bool live = row < nrows;
-  const int64_t p0 = live ? ptr[row] >> 1 : 0, p1 = live ? ptr[row + 1] >> 1 : 0;  // pairs
-  const uint32_t* __restrict__ o2 = reinterpret_cast<const uint32_t*>(off);
-  const uint32_t* __restrict__ q2 = reinterpret_cast<const uint32_t*>(q);
+  const int64_t s0 = live ? ptr[row] : 0;                      // a multiple of 8
+  const int n = live ? (int)((ptr[row + 1] - s0) >> 1) : 0;    // pairs
+  const uint32_t* __restrict__ o2 = reinterpret_cast<const uint32_t*>(off + s0);
+  const uint32_t* __restrict__ q2 = reinterpret_cast<const uint32_t*>(q + s0);
+  const int32_t* __restrict__ cb = cbase + (s0 >> 3);          // 4 pairs per chunk
   float acc[P];
   uint32_t oc[P], vc[P];
   int32_t bc[P];
 #pragma unroll
   for (int u = 0; u < P; u++) {
     acc[u] = 0.f;
-    const int64_t pp = p0 + lg + u * G;
+    const int i = lg + u * G;
     oc[u] = 0u; vc[u] = 0u; bc[u] = 0;
-    if (pp < p1) {
-      oc[u] = __ldcs(o2 + pp);
-      vc[u] = __ldcs(q2 + pp);
-      bc[u] = __ldg(cbase + (pp >> 2));
+    if (i < n) {
+      oc[u] = __ldcs(o2 + i);
+      vc[u] = __ldcs(q2 + i);
+      bc[u] = __ldg(cb + (i >> 2));
     }
   }
-  for (int64_t pb = p0 + lg; pb < p1; pb += P * G) {
+  for (int i0 = lg; i0 < n; i0 += P * G) {
     uint32_t on[P], vn[P];
     int32_t bn[P];
 #pragma unroll
     for (int u = 0; u < P; u++) {
-      const int64_t pp = pb + (P + u) * G;
+      const int i = i0 + (P + u) * G;
       on[u] = 0u; vn[u] = 0u; bn[u] = 0;
-      if (pp < p1) {
-        on[u] = __ldcs(o2 + pp);
-        vn[u] = __ldcs(q2 + pp);
-        bn[u] = __ldg(cbase + (pp >> 2));
+      if (i < n) {
+        on[u] = __ldcs(o2 + i);
+        vn[u] = __ldcs(q2 + i);
+        bn[u] = __ldg(cb + (i >> 2));
       }
     }
 #pragma unroll
     for (int u = 0; u < P; u++) {
-      if (pb + u * G < p1) {
-        acc[u] = fmaf(from_q<FMT>(vc[u] & 0xffffu), ld_x(x, bc[u] + (int32_t)(oc[u] & 0xffffu)), acc[u]);
-        acc[u] = fmaf(from_q<FMT>(vc[u] >> 16), ld_x(x, bc[u] + (int32_t)(oc[u] >> 16)), acc[u]);
+      if (i0 + u * G < n) {
+        const XT* xb = x + bc[u];
+        acc[u] = fmaf(from_q<FMT>(vc[u] & 0xffffu), ld_x(xb, (int32_t)(oc[u] & 0xffffu)), acc[u]);
+        acc[u] = fmaf(from_q<FMT>(vc[u] >> 16), ld_x(xb, (int32_t)(oc[u] >> 16)), acc[u]);
       }
       oc[u] = on[u]; vc[u] = vn[u]; bc[u] = bn[u];
     }
   }
-  float a = (acc[0] + acc[1]) + (acc[2] + acc[3]);
+  float a = 0.f;
+#pragma unroll
+  for (int u = 0; u < P; u++) a += acc[u];
 #pragma unroll
   for (int o = G / 2; o > 0; o >>= 1) a += __shfl_xor_sync(gmask, a, o, G);
   if (live && lg == 0) part = epi(row, a * scale[row]);
@@ -225,20 +232,22 @@ static epet_status launch16_fmt(int G, const epet_csr16* a, const XT* x, Epi epi
                                 double* partial, cudaStream_t st) {
   const int rpb = kSpmvThreads / G;
   const unsigned nb = (unsigned)((a->m + rpb - 1) / rpb);
-  switch (G) {
-    case 32: k_rows16<32, FMT, Epi, XT><<<nb, kSpmvThreads, 0, st>>>(a->row_ptr, a->base, a->scale, a->delta, a->q, x, a->m, epi, partial); break;
-    case 16: k_rows16<16, FMT, Epi, XT><<<nb, kSpmvThreads, 0, st>>>(a->row_ptr, a->base, a->scale, a->delta, a->q, x, a->m, epi, partial); break;
-    case 8: k_rows16<8, FMT, Epi, XT><<<nb, kSpmvThreads, 0, st>>>(a->row_ptr, a->base, a->scale, a->delta, a->q, x, a->m, epi, partial); break;
-    default: k_rows16<4, FMT, Epi, XT><<<nb, kSpmvThreads, 0, st>>>(a->row_ptr, a->base, a->scale, a->delta, a->q, x, a->m, epi, partial); break;
+  switch (G) {  // pairs in flight per lane: 8 with whole warps (long rows), else 4
+    case 32: k_rows16<32, 8, FMT, Epi, XT><<<nb, kSpmvThreads, 0, st>>>(a->row_ptr, a->base, a->scale, a->delta, a->q, x, a->m, epi, partial); break;
+    case 16: k_rows16<16, 4, FMT, Epi, XT><<<nb, kSpmvThreads, 0, st>>>(a->row_ptr, a->base, a->scale, a->delta, a->q, x, a->m, epi, partial); break;
+    case 8: k_rows16<8, 4, FMT, Epi, XT><<<nb, kSpmvThreads, 0, st>>>(a->row_ptr, a->base, a->scale, a->delta, a->q, x, a->m, epi, partial); break;
+    default: k_rows16<4, 4, FMT, Epi, XT><<<nb, kSpmvThreads, 0, st>>>(a->row_ptr, a->base, a->scale, a->delta, a->q, x, a->m, epi, partial); break;
   }
   EPET_LAUNCHED();
   return EPET_OK;
 }
 
 // Lanes per row from the mean stored entries per row (a lane takes two
-// entries per step, four steps per round).
+// entries per step): whole warps with 8 pairs in flight for rows of
+// thousands of entries (the transpose), else groups with 4 pairs in flight
+// (measured at 52^3 voxels: rows of ~390 entries run fastest with 16 lanes).
 int pick_group16(double avg_len) {
-  if (avg_len >= 256) return 32;
+  if (avg_len >= 2048) return 32;
   if (avg_len >= 96) return 16;
   if (avg_len >= 32) return 8;
   return 4;

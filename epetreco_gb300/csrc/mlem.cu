@@ -1,7 +1,7 @@
 // mlem.cu -- the reconstruction driver (reco.cu:32-332 without MPI/HDF5).
 //
 // One epet_mlem holds a reconstruction on the device: the measured rows and
-// their counts, the system matrix built once by the fused kernel (it is
+// their counts (reordered by crystal pairs, see order_rows), the system matrix built once by the fused kernel (it is
 // deterministic, so the reference's rebuild in every iteration is not
 // needed), its column-major copy, the normalised sensitivity and the image.
 // An iteration is four kernels: forward product fused with e = y/(Ax);
@@ -12,6 +12,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <vector>
 
 #include "common.cuh"
 #include "internal.h"
@@ -52,6 +53,176 @@ static epet_status mlem_iteration(epet_mlem* h, cudaStream_t st) {
                          EpiMlemUpdate{h->x, h->s, h->xnew, nullptr}, h->part_x, st));
   EPET_CHECK(launch_sum_partials(h->part_x, h->nb_bwd, h->sums + 1, st));
   EPET_CHECK(launch_normalise(h->xnew, h->sums + 1, h->V, h->x, st));
+  return EPET_OK;
+}
+
+// Order of the measured rows inside a reconstruction.  A line through a
+// voxel joins crystals of the two heads whose y indices, and whose z indices,
+// add up to about twice the voxel's position on that axis (the heads face
+// each other with parallel y and z axes), so keys ordered by angle, then by
+// the two index sums, then by the first crystal, make the channels through
+// one voxel a few contiguous runs.  Each column of the column-major copy
+// lists its rows in this order, so the transpose product's gathers of
+// e = y / (A x) read far fewer cache sectors; each column sum has the same
+// terms in another order.  Channels outside the setup get the largest key
+// (the build reports them as before).
+__global__ void k_pair_keys(epet_setup s, const int32_t* __restrict__ rows, int64_t m,
+                            int32_t nch, int32_t kmax, int32_t* __restrict__ key,
+                            int32_t* __restrict__ idx) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= m) return;
+  const int32_t c = rows[i];
+  int32_t k = kmax;
+  if (c >= 0 && c < nch) {
+    int id[5];  // angle, crystal 0 (z, y), crystal 1 (z, y)
+    channel_decode(s, c, id);
+    const int SY = s.n0y + s.n1y - 1, SZ = s.n0z + s.n1z - 1;
+    k = (((id[0] * SY + id[2] + id[4]) * SZ + id[1] + id[3]) * s.n0y + id[2]) * s.n0z + id[1];
+  }
+  key[i] = k;
+  idx[i] = (int32_t)i;
+}
+
+__global__ void k_gather_i32(const int32_t* __restrict__ src, const int32_t* __restrict__ idx,
+                             int64_t m, int32_t* __restrict__ dst) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < m) dst[i] = src[idx[i]];
+}
+
+// h->rows / h->y = the measured rows and counts in the order above (a
+// stable sort of the keys, which carries y along); list order when the keys
+// do not fit 31 bits.  *idx_out (caller frees; null in list order) = the
+// list index of each row in the new order.
+static epet_status order_rows(const epet_problem* p, const int32_t* rows_d, int64_t m,
+                              epet_mlem* h, cudaStream_t st, int32_t** idx_out) {
+  *idx_out = nullptr;
+  const epet_setup& s = p->setup;
+  const int64_t SY = (int64_t)s.n0y + s.n1y - 1, SZ = (int64_t)s.n0z + s.n1z - 1;
+  const int64_t kmax = (int64_t)s.na * SY * SZ * s.n0y * s.n0z;
+  const int64_t nch = (int64_t)s.na * s.n0z * s.n0y * s.n1z * s.n1y;
+  if (m < 2 || m > INT32_MAX || kmax >= INT32_MAX || nch > INT32_MAX) {
+    if (m > 0)
+      EPET_CUDA(cudaMemcpyAsync(h->rows, rows_d, m * 4, cudaMemcpyDeviceToDevice, st));
+    return EPET_OK;
+  }
+  int32_t *key = nullptr, *idx = nullptr;
+  EPET_CUDA(dev_alloc((void**)&key, m * 4, st));
+  cudaError_t e = dev_alloc((void**)&idx, m * 4, st);
+  if (e != cudaSuccess) {
+    dev_free(key, st);
+    return cuda_status(e, "allocation of the row order");
+  }
+  k_pair_keys<<<ceil_div(m, 256), 256, 0, st>>>(s, rows_d, m, (int32_t)nch, (int32_t)kmax, key,
+                                                idx);
+  note_launch();
+  epet_status rc = cudaGetLastError() == cudaSuccess
+                       ? epet_coo_sort(h->y, key, idx, m, nullptr, 0, st)
+                       : set_error(EPET_ERR_CUDA, "row order keys");
+  if (rc == EPET_OK) {
+    k_gather_i32<<<ceil_div(m, 256), 256, 0, st>>>(rows_d, idx, m, h->rows);
+    note_launch();
+    if (cudaGetLastError() != cudaSuccess) rc = set_error(EPET_ERR_CUDA, "row order gather");
+  }
+  dev_free(key, st);
+  if (rc == EPET_OK) *idx_out = idx;
+  else dev_free(idx, st);
+  return rc;
+}
+
+struct SegDev {
+  const int32_t* col;
+  const float* val;
+  int64_t e0;
+};
+
+__global__ void k_perm_len(const int64_t* __restrict__ rp0, const int32_t* __restrict__ idx,
+                           int64_t m, int64_t* __restrict__ len) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < m) len[i] = rp0[idx[i] + 1] - rp0[idx[i]];
+}
+
+// Row i of the CSR = built row idx[i], read from the segment of its chunk
+// (chunks of ch rows); a warp per row.
+__global__ void k_perm_rows(const int64_t* __restrict__ rp0, const SegDev* __restrict__ seg,
+                            int64_t ch, const int32_t* __restrict__ idx, int64_t m,
+                            const int64_t* __restrict__ rp, int32_t* __restrict__ col,
+                            float* __restrict__ val) {
+  const int64_t i = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (i >= m) return;
+  const int64_t j = idx[i];
+  const SegDev sg = seg[j / ch];
+  const int64_t b = rp0[j] - sg.e0, n = rp0[j + 1] - rp0[j], d = rp[i];
+  for (int64_t k = lane; k < n; k += 32) {
+    col[d + k] = sg.col[b + k];
+    val[d + k] = sg.val[b + k];
+  }
+}
+
+// The system matrix of the rows h->rows (the crystal-pair order), built
+// over the rows in list order (rows_d: neighbouring rows are near-parallel
+// lines, which the walk handles faster) into one allocation per chunk, then
+// moved row by row into h->A (exact size; no growth copies).
+static epet_status build_in_pair_order(const epet_problem* p, const int32_t* rows_d,
+                                       const int32_t* idx, int32_t max_row_nnz, epet_mlem* h,
+                                       cudaStream_t st) {
+  const int64_t m = h->m;
+  std::vector<CsrSegment> segs;
+  int64_t *rp0 = nullptr, *len = nullptr, *tmp = nullptr;
+  SegDev* segd = nullptr;
+  int64_t nnz = 0;
+  epet_csr B{m, h->V, 0, nullptr, nullptr, nullptr};
+  epet_status rc = EPET_OK;
+  auto cu = [&](cudaError_t e, const char* what) {
+    if (rc == EPET_OK && e != cudaSuccess) rc = cuda_status(e, what);
+  };
+  cu(dev_alloc((void**)&rp0, (m + 1) * 8, st), "allocation of the row pointers");
+  if (rc == EPET_OK) rc = build_csr_segments(p, rows_d, m, rp0, &segs, &nnz, max_row_nnz, st);
+  const int64_t ch = segs.empty() ? 1 : segs[0].nr;
+  for (size_t k = 0; rc == EPET_OK && k < segs.size(); k++)
+    if (segs[k].r0 != (int64_t)k * ch || (k + 1 < segs.size() && segs[k].nr != ch))
+      rc = set_error(EPET_ERR_INVALID, "internal: uneven build chunks");
+  if (rc == EPET_OK && m > 0) {
+    std::vector<SegDev> hs;
+    for (const CsrSegment& sg : segs) hs.push_back({sg.col, sg.val, sg.e0});
+    cu(dev_alloc((void**)&segd, std::max<size_t>(hs.size(), 1) * sizeof(SegDev), st),
+       "allocation of the chunk table");
+    if (rc == EPET_OK && !hs.empty())
+      cu(cudaMemcpyAsync(segd, hs.data(), hs.size() * sizeof(SegDev), cudaMemcpyHostToDevice, st),
+         "chunk table");
+    cu(dev_alloc((void**)&B.row_ptr, (m + 1) * 8, st), "allocation of A");
+    cu(dev_alloc((void**)&B.col, std::max<int64_t>(nnz, 1) * 4, st), "allocation of A");
+    cu(dev_alloc((void**)&B.val, std::max<int64_t>(nnz, 1) * 4, st), "allocation of A");
+    cu(dev_alloc((void**)&len, m * 8, st), "allocation of the row move");
+    cu(dev_alloc((void**)&tmp, scan_tmp_elems(m) * 8, st), "allocation of the row move");
+    if (rc == EPET_OK) {
+      k_perm_len<<<ceil_div(m, 256), 256, 0, st>>>(rp0, idx, m, len);
+      note_launch();
+      rc = exclusive_scan_i64(len, B.row_ptr, m, tmp, st);
+    }
+    if (rc == EPET_OK) {
+      k_perm_rows<<<ceil_div(m * 32, 256), 256, 0, st>>>(rp0, segd, ch, idx, m, B.row_ptr,
+                                                       B.col, B.val);
+      note_launch();
+      cu(cudaGetLastError(), "row move");
+    }
+    // the copies above must finish before the segments are released
+    cu(cudaStreamSynchronize(st), "row move");
+  }
+  for (const CsrSegment& sg : segs) {
+    dev_free(sg.col, st);
+    dev_free(sg.val, st);
+  }
+  for (void* q : {(void*)rp0, (void*)len, (void*)tmp, (void*)segd})
+    if (q) dev_free(q, st);
+  if (rc != EPET_OK) {
+    for (void* q : {(void*)B.row_ptr, (void*)B.col, (void*)B.val})
+      if (q) dev_free(q, st);
+    return rc;
+  }
+  B.nnz = nnz;
+  h->A = B;
+  h->capA = nnz;
   return EPET_OK;
 }
 
@@ -103,10 +274,7 @@ epet_status epet_mlem_create(const epet_problem* p, const int32_t* rows_d, const
   ALLOC(h->x, V * 4);
   ALLOC(h->xnew, V * 4);
   ALLOC(h->sums, 64);
-  if (m > 0) {
-    cudaMemcpyAsync(h->rows, rows_d, m * 4, cudaMemcpyDeviceToDevice, st);
-    cudaMemcpyAsync(h->y, y_d, m * 4, cudaMemcpyDeviceToDevice, st);
-  }
+  if (m > 0) cudaMemcpyAsync(h->y, y_d, m * 4, cudaMemcpyDeviceToDevice, st);
   cudaMemcpyAsync(h->s, s_d, V * 4, cudaMemcpyDeviceToDevice, st);
   // sensitivity normalised to sum 1 (reco.cu:181-183)
   {
@@ -123,8 +291,15 @@ epet_status epet_mlem_create(const epet_problem* p, const int32_t* rows_d, const
   note_launch();
   if (cudaGetLastError() != cudaSuccess) return fail(set_error(EPET_ERR_CUDA, "fill"));
 
-  // system matrix (rows in list order) and its column-major copy
-  epet_status rc = build_csr_growable(p, h->rows, m, &h->A, &h->capA, o.max_row_nnz, st);
+  int32_t* idx = nullptr;  // list index of each row in the new order
+  {
+    epet_status rc = order_rows(p, rows_d, m, h, st, &idx);
+    if (rc != EPET_OK) return fail(rc);
+  }
+  // system matrix (rows in the crystal-pair order) and its column-major copy
+  epet_status rc = idx ? build_in_pair_order(p, rows_d, idx, o.max_row_nnz, h, st)
+                       : build_csr_growable(p, h->rows, m, &h->A, &h->capA, o.max_row_nnz, st);
+  if (idx) dev_free(idx, st);
   if (rc != EPET_OK) return fail(rc);
   const int64_t nnz = h->A.nnz;
   ALLOC(h->At.col_ptr, (V + 1) * 8);

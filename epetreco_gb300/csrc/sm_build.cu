@@ -34,6 +34,7 @@
 
 #include "common.cuh"
 #include "internal.h"
+#include "mlem_internal.h"
 
 namespace epet {
 
@@ -948,6 +949,12 @@ struct BuildOut {
   const float* e = nullptr;
   float* c = nullptr;
   double* s64 = nullptr;
+  // optional destination of each chunk's entries instead of csr->col/val
+  // (rows c0 .. c0+mc-1, n entries in row order from index 0); returns false
+  // on failure.  csr->row_ptr still receives the global row pointers.
+  bool (*chunk_dst)(BuildOut* self, int64_t c0, int64_t mc, int64_t n, int32_t** col,
+                    float** val) = nullptr;
+  std::vector<CsrSegment>* segs = nullptr;
 };
 
 size_t walk_workspace_size(const Geo& G, int64_t m, int cap_cells, bool csr) {
@@ -1108,12 +1115,22 @@ static epet_status run_walk(const Geo& G, const int32_t* rows, int64_t m,
       int64_t chunk_total = 0;
       EPET_CUDA(cudaMemcpyAsync(&chunk_total, rp_chunk + mc, 8, cudaMemcpyDeviceToHost, st));
       EPET_CUDA(cudaStreamSynchronize(st));
-      if (total_nnz + chunk_total > out->cap && out->grow &&
-          !out->grow(out, total_nnz + chunk_total, total_nnz, c0 + mc, m))
-        return set_error(EPET_ERR_CUDA, "could not grow the system-matrix buffers");
-      k_gather_rows<<<ceil_div(mc * 32, T), T, 0, st>>>(
-          stage_col, stage_val, cap_cells, ovf_idx, stage2_col, stage2_val, cap2, rp, mc,
-          out->csr->col, out->csr->val, out->cap);
+      if (out->chunk_dst) {
+        int32_t* dcol = nullptr;
+        float* dval = nullptr;
+        if (!out->chunk_dst(out, c0, mc, chunk_total, &dcol, &dval))
+          return set_error(EPET_ERR_CUDA, "could not allocate a system-matrix chunk");
+        k_gather_rows<<<ceil_div(mc * 32, T), T, 0, st>>>(
+            stage_col, stage_val, cap_cells, ovf_idx, stage2_col, stage2_val, cap2, rp_chunk,
+            mc, dcol, dval, chunk_total);
+      } else {
+        if (total_nnz + chunk_total > out->cap && out->grow &&
+            !out->grow(out, total_nnz + chunk_total, total_nnz, c0 + mc, m))
+          return set_error(EPET_ERR_CUDA, "could not grow the system-matrix buffers");
+        k_gather_rows<<<ceil_div(mc * 32, T), T, 0, st>>>(
+            stage_col, stage_val, cap_cells, ovf_idx, stage2_col, stage2_val, cap2, rp, mc,
+            out->csr->col, out->csr->val, out->cap);
+      }
       EPET_LAUNCHED();
       total_nnz += chunk_total;
     }
@@ -1155,6 +1172,22 @@ static bool grow_device(BuildOut* self, int64_t need, int64_t keep, int64_t rows
   self->csr->col = col;
   self->csr->val = val;
   self->cap = ncap;
+  return true;
+}
+
+static bool segment_device(BuildOut* self, int64_t c0, int64_t mc, int64_t n, int32_t** col,
+                           float** val) {
+  CsrSegment sg{c0, mc, self->segs->empty() ? 0 : self->segs->back().e0 + self->segs->back().n,
+                n, nullptr, nullptr};
+  const cudaStream_t st = self->stream;
+  if (dev_alloc((void**)&sg.col, std::max<int64_t>(n, 1) * 4, st) != cudaSuccess) return false;
+  if (dev_alloc((void**)&sg.val, std::max<int64_t>(n, 1) * 4, st) != cudaSuccess) {
+    dev_free(sg.col, st);
+    return false;
+  }
+  self->segs->push_back(sg);
+  *col = sg.col;
+  *val = sg.val;
   return true;
 }
 
@@ -1274,6 +1307,23 @@ epet_status build_csr_growable(const epet_problem* p, const int32_t* rows, int64
   out->m = m;
   out->n = G.V;
   out->nnz = bo.nnz;
+  return EPET_OK;
+}
+
+epet_status build_csr_segments(const epet_problem* p, const int32_t* rows, int64_t m,
+                               int64_t* row_ptr, std::vector<CsrSegment>* segs, int64_t* nnz,
+                               int32_t max_row_nnz, cudaStream_t st) {
+  Geo G = make_geo(*p);
+  int capc = 0;
+  EPET_CHECK(resolve_capacity(G, max_row_nnz, st, &capc));
+  epet_csr csr{m, G.V, 0, row_ptr, nullptr, nullptr};
+  BuildOut bo;
+  bo.csr = &csr;
+  bo.stream = st;
+  bo.chunk_dst = segment_device;
+  bo.segs = segs;
+  EPET_CHECK(run_walk<kModeCsr>(G, rows, m, capc, &bo, nullptr, 0, st));
+  *nnz = bo.nnz;
   return EPET_OK;
 }
 
