@@ -3,14 +3,15 @@
 // and the products over it.
 //
 // A row is stored as chunks of 8 entries: chunk c has a 32-bit column base
-// cbase[c] (the column of its first entry), 16-bit offsets
+// cbase[c] (the smallest column of its entries), 16-bit offsets
 // (col = cbase[c] + offset) and 16-bit values (value = scale[r] * q, q the
 // 16-bit float of value / scale[r], scale[r] = the row's largest value).
 // Rows are padded to whole chunks with zero-valued entries of offset 0, so a
 // chunk never mixes rows and a lane decodes its chunk alone: no scan over
-// steps, no masks.  A chunk ends early (and is padded) before an entry
-// 65536 or more columns past its first, so every matrix is representable;
-// at 52^3 voxels 8 consecutive entries of a row span far less.  The same
+// steps, no masks.  Columns need not ascend within a row; a chunk ends early
+// (and is padded) before an entry that would widen its column range to
+// 65536 or more, so every matrix is representable; at 52^3 voxels 8
+// consecutive entries of a row span far less.  The same
 // layout over the column-major copy stores A^T, so one kernel serves both
 // products.  The products accumulate in FP32.
 #include <cuda_bf16.h>
@@ -28,19 +29,24 @@ constexpr int kChunk = 8;
 constexpr int32_t kMaxSpan = 65535;
 
 // True (warp-uniform) when the fixed chunks [b + 8c, b + 8c + 8) of row
-// [b, e) all span at most kMaxSpan columns.
+// [b, e) all span at most kMaxSpan columns (largest - smallest).
 __device__ __forceinline__ bool fixed_chunks(const int32_t* __restrict__ idx, int64_t b,
                                              int64_t e, int lane) {
   bool ok = true;
   for (int64_t k = b + (int64_t)kChunk * lane; k < e; k += 32 * kChunk) {
     const int64_t last = k + kChunk - 1 < e ? k + kChunk - 1 : e - 1;
-    if (idx[last] - idx[k] > kMaxSpan) ok = false;
+    int32_t mn = idx[k], mx = mn;
+    for (int64_t j = k + 1; j <= last; j++) {
+      mn = min(mn, idx[j]);
+      mx = max(mx, idx[j]);
+    }
+    if (mx - mn > kMaxSpan) ok = false;
   }
   return __all_sync(0xffffffffu, ok);
 }
 
 // Greedy chunks of row [b, e) (one thread): a chunk takes up to 8 entries
-// within kMaxSpan columns of its first.  Returns the number of chunks; with
+// whose columns span at most kMaxSpan.  Returns the number of chunks; with
 // out pointers given, writes them.
 template <int FMT>
 __device__ int64_t greedy_chunks(const int32_t* __restrict__ idx, const float* __restrict__ val,
@@ -80,16 +86,20 @@ __device__ int64_t greedy_chunks(const int32_t* __restrict__ idx, const float* _
   int64_t n = 0;
   int64_t k = b;
   while (k < e) {
-    const int32_t c0 = idx[k];
-    int j = 0;
-    for (; j < kChunk && k + j < e && idx[k + j] - c0 <= kMaxSpan; j++) {
-      if (out >= 0) {
-        off[out + n * kChunk + j] = (uint16_t)(idx[k + j] - c0);
-        q[out + n * kChunk + j] = to_q<FMT>(__fdiv_rn(val[k + j], sc));
-      }
+    int32_t mn = idx[k], mx = idx[k];
+    int j = 1;
+    for (; j < kChunk && k + j < e; j++) {
+      const int32_t c = idx[k + j];
+      if (max(mx, c) - min(mn, c) > kMaxSpan) break;
+      mn = min(mn, c);
+      mx = max(mx, c);
     }
     if (out >= 0) {
-      cbase[(out >> 3) + n] = c0;
+      for (int t = 0; t < j; t++) {
+        off[out + n * kChunk + t] = (uint16_t)(idx[k + t] - mn);
+        q[out + n * kChunk + t] = to_q<FMT>(__fdiv_rn(val[k + t], sc));
+      }
+      cbase[(out >> 3) + n] = mn;
       for (int p = j; p < kChunk; p++) {
         off[out + n * kChunk + p] = 0;
         q[out + n * kChunk + p] = 0;
@@ -124,9 +134,11 @@ __global__ void k_c16_fill(const int64_t* __restrict__ ptr, const int32_t* __res
     for (int64_t p0 = 0; p0 < padded; p0 += 32) {
       const int64_t p = p0 + lane;
       const bool real = p < len;
-      const int32_t col = real ? idx[b + p] : 0;
-      // column of the chunk's first entry (lane & ~7 holds it)
-      const int32_t base = __shfl_sync(0xffffffffu, col, lane & ~(kChunk - 1));
+      const int32_t col = real ? idx[b + p] : INT32_MAX;
+      // smallest column of the chunk (lanes lane & ~7 .. +7; a chunk's first
+      // entry is real, padding lanes hold INT32_MAX)
+      int32_t base = col;
+      for (int o = 1; o < kChunk; o <<= 1) base = min(base, __shfl_xor_sync(0xffffffffu, base, o));
       if (p < padded) {
         off[out + p] = real ? (uint16_t)(col - base) : (uint16_t)0;
         q[out + p] = real ? to_q<FMT>(__fdiv_rn(val[b + p], sc)) : (uint16_t)0;

@@ -82,10 +82,11 @@ typedef struct {
 
 /* 16-bit storage of a CSR (value_format 1 = BF16, 2 = FP16): about 4.5 bytes
  * per entry.  A row is stored as chunks of 8 entries (rows padded with
- * zero-valued entries of offset 0): chunk c has a column base base[c], the
- * entries' 16-bit offsets delta (col = base[c] + delta_k) and 16-bit values
- * q (value = scale[r] * q_k, scale = the row's largest value).  A chunk ends
- * early before an entry 65536 or more columns past its first.  row_ptr
+ * zero-valued entries of offset 0): chunk c has a column base base[c] (its
+ * smallest column), the entries' 16-bit offsets delta (col = base[c] +
+ * delta_k) and 16-bit values q (value = scale[r] * q_k, scale = the row's
+ * largest value).  Columns need not ascend within a row; a chunk ends early
+ * before an entry that would widen its column range to 65536.  row_ptr
  * counts stored entries (multiples of 8).  delta and q are read with 16-byte
  * loads: 16-byte aligned; nnz = their capacity in entries, base holds nnz/8
  * chunks, scale m rows. */
@@ -243,7 +244,7 @@ epet_status epet_csrmv(int trans, const epet_csr* a, const epet_csc* csc,
                        epet_stream_t stream);
 
 /* 16-bit layout: per-row stored-entry counts (row_len16_d[m]) and their
- * total; the CSR must have ascending columns within rows. */
+ * total. */
 epet_status epet_csr16_count(const epet_csr* a, int64_t* row_len16_d,
                              int64_t* nnz16_h, epet_stream_t stream);
 /* Converts a CSR (or, given a column-major copy viewed as the CSR of A^T,
@@ -323,9 +324,11 @@ typedef struct {
                           inputs, not on timings).  FP32 values only. */
 } epet_mlem_options;
 
-/* Builds the system matrix for the measured rows (rows_d ascending channel
- * ids with y_d > 0), keeps y, s (normalised here) and x = ones/V.
- * Synchronous. */
+/* Builds the system matrix for the measured rows (rows_d channel ids, in
+ * any order, with y_d > 0), keeps y, s (normalised here) and x = ones/V.
+ * Internally the rows are stored in crystal-pair order (angle, then the sums
+ * of the two crystals' y and z indices, then the first crystal), so a
+ * shuffled row list gives the same object.  Synchronous. */
 epet_status epet_mlem_create(const epet_problem* p, const int32_t* rows_d,
                              const float* y_d, int64_t m, const float* s_d,
                              const epet_mlem_options* opt, epet_mlem** out,

@@ -211,6 +211,20 @@ def test_mlem_graph_equals_eager(small_recon):
     assert la == lb
 
 
+def test_mlem_row_order_does_not_matter(small_recon):
+    """The reconstruction stores its rows in crystal-pair order (a bijective
+    key of the channel), so a shuffled measurement list gives the same
+    matrices and the bit-identical image and log-likelihood."""
+    p, rows, y, s = small_recon
+    perm = np.random.default_rng(5).permutation(len(rows))
+    a = api.Mlem(p, dev(rows), y, s)
+    b = api.Mlem(p, dev(rows[perm]), y[dev(perm)].contiguous(), s)
+    la = a.iterate(4, loglik=True)
+    lb = b.iterate(4, loglik=True)
+    assert torch.equal(a.image(), b.image())
+    assert la == lb
+
+
 def test_mlem_loglik_increases(small_recon):
     p, rows, y, s = small_recon
     R = api.Mlem(p, dev(rows), y, s)

@@ -125,6 +125,36 @@ def test_fixed_chunks_and_padding(gpu_lib):
         assert cols[r].tolist() == col[rp[r]:rp[r + 1]].tolist()
 
 
+def test_unordered_columns(mat, oracle):
+    """Columns in any order within a row (as a reconstruction stores them):
+    each chunk's base is its smallest column, entries keep their places, and
+    a chunk ends before its column range would reach 65536."""
+    p, rows, A, (rp, col, val) = mat
+    rng = np.random.default_rng(6)
+    col2, val2 = col.copy(), val.copy()
+    for r in range(len(rp) - 1):
+        k = rng.permutation(rp[r + 1] - rp[r]) + rp[r]
+        col2[rp[r]:rp[r + 1]], val2[rp[r]:rp[r + 1]] = col[k], val[k]
+    c16, out, keep_alive = compress(rp, col2, val2, p.nvoxels, 1)
+    cols, vals = decode(out, 1)
+    for r in range(len(rp) - 1):
+        assert cols[r].tolist() == col2[rp[r]:rp[r + 1]].tolist()
+    x = np.random.default_rng(2).random(p.nvoxels).astype(np.float32)
+    y = torch.zeros(len(rows), device="cuda")
+    check(lib().epet_csr16_mv(C.byref(c16), 1.0, C.c_void_p(dev(x).data_ptr()), 0.0,
+                              C.c_void_p(y.data_ptr()), stream()))
+    yo = oracle.csrmv_f64(0, rp, col, val, x.astype(np.float64), p.nvoxels)
+    assert (np.abs(y.cpu().numpy() - yo) / np.abs(yo)).max() < 3e-3
+    # a descending row whose range exceeds 65535: chunks split, offsets >= 0
+    rp3 = np.array([0, 5], np.int64)
+    col3 = np.array([200000, 150000, 140000, 100000, 3], np.int32)
+    val3 = np.array([1.0, 2.0, 3.0, 4.0, 5.0], np.float32)
+    c16, out, _ = compress(rp3, col3, val3, 300000, 1)
+    cols, vals = decode(out, 1)
+    assert cols[0].tolist() == col3.tolist()
+    assert np.allclose(vals[0], val3, rtol=4e-3)
+
+
 @pytest.mark.parametrize("fmt", ["bf16", "fp16"])
 def test_product_against_oracle(mat, oracle, fmt):
     p, rows, A, (rp, col, val) = mat
