@@ -285,12 +285,6 @@ template epet_status launch_rows16<EpiMlemForward16, float>(const epet_csr16*, c
 template epet_status launch_rows16<EpiMlemUpdate, uint16_t>(const epet_csr16*, const uint16_t*,
                                                             EpiMlemUpdate, double*, cudaStream_t);
 
-int64_t rows16_blocks(const epet_csr16* a) {
-  const int G = pick_group16(a->m ? (double)a->nnz / a->m : 0.0);
-  const int rpb = kSpmvThreads / G;
-  return (a->m + rpb - 1) / rpb;
-}
-
 }  // namespace epet
 
 using namespace epet;

@@ -5,8 +5,8 @@
 // deterministic, so the reference's rebuild in every iteration is not
 // needed), its column-major copy, the normalised sensitivity and the image.
 // An iteration is four kernels: forward product fused with e = y/(Ax);
-// transpose product fused with x*c/s and the image sum; the fixed-order sum;
-// the normalisation.  With use_graph the four are captured once in a CUDA
+// transpose product fused with x*c/s; the fixed-order image sum (block
+// partials); the normalisation (which reduces the partials itself).  With use_graph the four are captured once in a CUDA
 // graph and replayed.  The Poisson log-likelihood of the last forward
 // projection is reduced in fp64 on request.
 #include <algorithm>
@@ -42,18 +42,14 @@ static epet_status mlem_iteration(epet_mlem* h, cudaStream_t st) {
     EPET_CHECK((launch_rows16<EpiMlemForward16, float>(
         &h->A16, h->x, EpiMlemForward16{h->y, h->e16, h->ybar}, nullptr, st)));
     EPET_CHECK((launch_rows16<EpiMlemUpdate, uint16_t>(
-        &h->At16, h->e16, EpiMlemUpdate{h->x, h->s, h->xnew, nullptr}, h->part_x, st)));
-    EPET_CHECK(launch_sum_partials(h->part_x, h->nb_bwd, h->sums + 1, st));
-    EPET_CHECK(launch_normalise(h->xnew, h->sums + 1, h->V, h->x, st));
-    return EPET_OK;
+        &h->At16, h->e16, EpiMlemUpdate{h->x, h->s, h->xnew, nullptr}, nullptr, st)));
+    return launch_sum_normalise(h->xnew, h->V, h->part_x, h->x, st);
   }
   EPET_CHECK(launch_rows(h->plan_fwd, h->A.row_ptr, h->A.col, h->A.val, h->x, h->m,
                          EpiMlemForward{h->y, h->e, h->ybar}, nullptr, st));
   EPET_CHECK(launch_rows(h->plan_bwd, h->At.col_ptr, h->At.row, h->At.val, h->e, h->V,
-                         EpiMlemUpdate{h->x, h->s, h->xnew, nullptr}, h->part_x, st));
-  EPET_CHECK(launch_sum_partials(h->part_x, h->nb_bwd, h->sums + 1, st));
-  EPET_CHECK(launch_normalise(h->xnew, h->sums + 1, h->V, h->x, st));
-  return EPET_OK;
+                         EpiMlemUpdate{h->x, h->s, h->xnew, nullptr}, nullptr, st));
+  return launch_sum_normalise(h->xnew, h->V, h->part_x, h->x, st);
 }
 
 // Order of the measured rows inside a reconstruction.  A line through a
@@ -340,10 +336,8 @@ epet_status epet_mlem_create(const epet_problem* p, const int32_t* rows_d, const
   }
   h->plan_fwd = default_plan(m ? (double)nnz / m : 0.0);
   h->plan_bwd = default_plan(V ? (double)nnz / V : 0.0);
-  if (o.value_format != EPET_VALUES_FP32) h->nb_bwd = rows16_blocks(&h->At16);
-  else h->nb_bwd = ceil_div(V, kSpmvThreads / 32);  // the most tiles of any plan
   ALLOC(h->part_ll, 1024 * 8);
-  ALLOC(h->part_x, std::max<int64_t>(h->nb_bwd, 1) * 8);
+  ALLOC(h->part_x, sum_blocks(V) * 8);
   if (o.autotune && o.value_format == EPET_VALUES_FP32) {
     // both products are idempotent (they write e / ybar and xnew / partials
     // from x, y, s): the candidates run the real epilogues
@@ -359,12 +353,11 @@ epet_status epet_mlem_create(const epet_problem* p, const int32_t* rows_d, const
           1, V, nnz, m, V ? (double)nnz / V : 0.0,
           [&](const RowPlan& pl) {
             return launch_rows(pl, h->At.col_ptr, h->At.row, h->At.val, h->e, h->V,
-                               EpiMlemUpdate{h->x, h->s, h->xnew, nullptr}, h->part_x, st);
+                               EpiMlemUpdate{h->x, h->s, h->xnew, nullptr}, nullptr, st);
           },
           st, &h->plan_bwd);
     if (rc != EPET_OK) return fail(rc);
   }
-  if (o.value_format == EPET_VALUES_FP32) h->nb_bwd = plan_tiles(h->plan_bwd, V);
 #undef ALLOC
   cudaError_t e = cudaStreamSynchronize(st);
   if (e != cudaSuccess) return fail(cuda_status(e, "mlem create"));

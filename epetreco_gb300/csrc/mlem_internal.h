@@ -18,7 +18,6 @@ struct epet_mlem {
   epet_csr16 A16{}, At16{};  // 16-bit forms (value_format != FP32)
   int64_t capA = 0;
   double *part_ll = nullptr, *part_x = nullptr, *sums = nullptr;
-  int64_t nb_bwd = 0;  // tiles of the transpose launch (partial sums)
   epet::RowPlan plan_fwd, plan_bwd;
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t exec = nullptr;

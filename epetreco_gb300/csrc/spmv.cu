@@ -180,6 +180,43 @@ epet_status launch_normalise(const float* xnew, const double* sum, int64_t n, fl
   return EPET_OK;
 }
 
+// x = xnew * float(1/sum) with sum = the fixed-order sum of nb partials
+// (every block reduces them in the same order, so all see the same value).
+__global__ void k_normalise_parts(const float* __restrict__ xnew,
+                                  const double* __restrict__ part, int nb, int64_t n,
+                                  float* __restrict__ x) {
+  __shared__ double red[8];
+  __shared__ double tot;
+  double s = 0.0;
+  for (int i = threadIdx.x; i < nb; i += blockDim.x) s += part[i];
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = s;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t = 0.0;
+    for (int w = 0; w < (int)(blockDim.x / 32); w++) t += red[w];
+    tot = t;
+  }
+  __syncthreads();
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) x[i] = fmul((float)(1.0 / tot), xnew[i]);
+}
+
+int sum_blocks(int64_t n) {
+  return (int)std::max<int64_t>(1, std::min<int64_t>(ceil_div(n, 4096), 1024));
+}
+
+epet_status launch_sum_normalise(const float* xnew, int64_t n, double* part, float* x,
+                                 cudaStream_t st) {
+  const int nb = sum_blocks(n);
+  k_sum_f64_part<<<nb, 256, 0, st>>>(xnew, n, part);
+  EPET_LAUNCHED();
+  k_normalise_parts<<<ceil_div(n, 256), 256, 0, st>>>(xnew, part, nb, n, x);
+  EPET_LAUNCHED();
+  return EPET_OK;
+}
+
 __global__ void k_loglik_part(const float* __restrict__ y, const float* __restrict__ yb,
                               int64_t m, double* __restrict__ partial) {
   __shared__ double red[8];

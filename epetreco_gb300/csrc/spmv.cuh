@@ -75,9 +75,13 @@ epet_status tune_rows(int kind, int64_t nrows, int64_t nnz, int64_t ncols, doubl
 template <class Epi, class XT>
 epet_status launch_rows16(const epet_csr16* a, const XT* x, Epi epi, double* partial,
                           cudaStream_t st);
-int64_t rows16_blocks(const epet_csr16* a);
 inline int64_t csr16_capacity(int64_t nnz16) { return nnz16; }
 epet_status launch_sum_partials(const double* p, int64_t n, double* out, cudaStream_t st);
+// x = xnew / sum(xnew), the sum in fp64 and in a fixed order: block
+// partials (part holds sum_blocks(n) doubles), then the scaling launch.
+int sum_blocks(int64_t n);
+epet_status launch_sum_normalise(const float* xnew, int64_t n, double* part, float* x,
+                                 cudaStream_t st);
 epet_status launch_normalise(const float* xnew, const double* sum, int64_t n, float* x,
                              cudaStream_t st);
 epet_status sum_f64(const float* x, int64_t n, double* partial, int nblocks, double* out,
