@@ -67,7 +67,7 @@ struct WalkArgs {
   int32_t* win_cells;      // per row window cells
   int32_t* overflow_rows;  // list of rows whose window exceeded cap_cells
   int32_t* overflow_count;
-  int32_t* hit_outside;    // count of hits outside the window (must stay 0)
+  int32_t* hit_outside;    // rows with hits outside the window (must stay 0)
   int32_t* exact_rows;     // rows left to the per-candidate path
   int32_t* exact_count;
   // redo launch over rows whose window exceeded the first launch's capacity:
@@ -185,7 +185,8 @@ struct Window {
   const int2* cols;  // per column: {first cell, zlo | zhi << 16}; empty: zlo 1, zhi 0
   int bx0, by0, wbx, wby;
   int split;
-  int trash;  // cell W past the window: absorbs the (zero) adds of steps with nothing to add
+  int trash;      // cell W: absorbs the adds of steps with nothing to add (never read)
+  int trash_out;  // cell W + 1: counts (in lo) hits outside the window (must stay 0)
 };
 
 // A lane's cached column: first cell, first z, number of z cells.
@@ -245,12 +246,13 @@ struct WalkAxis {
 // is branch-free: the axis whose plane comes first is selected and advanced
 // with one division.
 //
-// With npieces > 1 the lane walks only piece `piece` of the ray: the cells
-// entered in [a_lo, a_hi), the piece's share of the grid range (no wrap).
-// The pieces of a ray compute their common bounds with the same expression,
-// so every cell belongs to exactly one piece.
-__device__ void walk_ray(const Geo& G, const float* ray, const Window& w, int* outside,
-                         int* needs_exact, float frac, int piece, int npieces) {
+// With PIECES the lane walks only piece `piece` of npieces of the ray: the
+// cells entered in [a_lo, a_hi), the piece's share of the grid range (no
+// wrap).  The pieces of a ray compute their common bounds with the same
+// expression, so every cell belongs to exactly one piece.
+template <bool PIECES>
+__device__ void walk_ray(const Geo& G, const float* ray, const Window& w, int* needs_exact,
+                         float frac, int piece, int npieces) {
   const epet_grid& g = G.p.grid;
   if (ray[0] == ray[3] && ray[1] == ray[4] && ray[2] == ray[5]) return;
   if (ray[0] == ray[3] || ray[1] == ray[4] || ray[2] == ray[5]) {
@@ -288,7 +290,7 @@ __device__ void walk_ray(const Geo& G, const float* ray, const Window& w, int* o
   float exl = 0.f, exh = 0.f, exk = 0.f, eyl = 0.f, eyh = 0.f, eyk = 0.f;
   float ezl = 0.f, ezh = 0.f, ezk = 0.f;
   bool second;
-  if (npieces > 1) {
+  if (PIECES) {
     if (piece > 0) a_lo = fadd(a_in, fmul(span, (float)piece / (float)npieces));
     if (piece + 1 < npieces) a_stop = fadd(a_in, fmul(span, (float)(piece + 1) / (float)npieces));
     a_s = piece > 0 ? a_lo : a_in;
@@ -316,10 +318,11 @@ __device__ void walk_ray(const Geo& G, const float* ray, const Window& w, int* o
   // (the largest of the axes' lo), so it is carried as one value; the cell
   // whose exit parameter reaches a_out is the last before the grid's exit.
   float amin = a_start;
-  int n_out = 0;  // hits outside the window (none expected)
   int cx = X.idx - w.bx0, cy = Y.idx - w.by0;  // column relative to the box
   Col col = load_col(w, cx, cy);
-  const float scale = G.fx_scale;
+  // chord units = RN((amax - amin) * L) * 2^s = RN((amax - amin) * (L * 2^s)):
+  // scaling by a power of two is exact
+  const float Ls = fmul(L, G.fx_scale);
   const float two_s = __int_as_float((127 + w.split) << 23);   // 2^split
   const float inv_two_s = __int_as_float((127 - w.split) << 23);
   const int budget = g.n[0] + g.n[1] + g.n[2] + 4;
@@ -331,21 +334,20 @@ __device__ void walk_ray(const Geo& G, const float* ray, const Window& w, int* o
     const float amax = mx ? X.hi : (my ? Y.hi : Z.hi);
     {
       // Branch-free add: a step with nothing to add (a zero-length cell, a
-      // cell of the previous piece) adds zero to the trash cell.
-      const bool add = amin < amax && amin >= a_lo;  // before a_lo: previous piece
+      // cell of the previous piece) adds to the trash cell, a hit outside
+      // the window adds one to the outside cell's count.
+      const bool add = PIECES ? (amin < amax && amin >= a_lo)  // before a_lo: previous piece
+                              : amin < amax;
       const unsigned dz = (unsigned)(Z.idx - col.zlo);
       const bool inwin = dz < (unsigned)col.zn;
-      n_out += (add && !inwin) ? 1 : 0;
-      const bool ok = add && inwin;
-      const int c = ok ? col.off + (int)dz : w.trash;
+      const int c = add ? (inwin ? col.off + (int)dz : w.trash_out) : w.trash;
       // units = RN(len * scale) split as hi * 2^split + lo; for a product
       // >= 2^split the float is an integer and both parts are exact
-      const float v = fmul(fmul(fsub(amax, amin), L), scale);
-      uint32_t h = __float2uint_rz(fmul(v, inv_two_s));
+      const float v = fmul(fsub(amax, amin), Ls);
+      const uint32_t h = __float2uint_rz(fmul(v, inv_two_s));
       uint32_t l = __float2uint_rn(__fmaf_rn(-__uint2float_rn(h), two_s, v));
       l = (h | l) == 0u ? 1u : l;  // a positive chord counts at least one unit
-      h = ok ? h : 0u;
-      l = ok ? l : 0u;
+      l = inwin ? l : 1u;
       atomicAdd(&w.lo[c], l);
       atomicAdd(&w.hi[c], h);
     }
@@ -378,7 +380,6 @@ __device__ void walk_ray(const Geo& G, const float* ray, const Window& w, int* o
     cy += my ? st : 0;
     col = load_col(w, cx, cy);
   }
-  if (n_out) atomicAdd(outside, n_out);
 }
 
 // Per-channel geometry for the walk, one thread per channel: the 16 crystal
@@ -436,7 +437,7 @@ k_walk(WalkArgs args) {
   const float(*c1)[3] = reinterpret_cast<const float(*)[3]>(s_geom + 24);
   const ChannelLine& line = *reinterpret_cast<const ChannelLine*>(s_geom + 48);
   __shared__ int warp_tot[kWalkThreads / 32];
-  __shared__ int s_total, s_outside, s_exact, s_box[4];
+  __shared__ int s_total, s_exact, s_box[4];
   __shared__ double red_d[kWalkThreads / 32];
   __shared__ float red_f[kWalkThreads / 32];
 
@@ -449,7 +450,6 @@ k_walk(WalkArgs args) {
     reinterpret_cast<float4*>(s_geom)[threadIdx.x] =
         reinterpret_cast<const float4*>(args.geom + row * kGeomFloats)[threadIdx.x];
   if (threadIdx.x == 0) {
-    s_outside = 0;
     s_exact = 0;
     s_box[0] = INT_MAX; s_box[1] = INT_MIN; s_box[2] = INT_MAX; s_box[3] = INT_MIN;
   }
@@ -578,7 +578,7 @@ k_walk(WalkArgs args) {
       if (zhi >= zlo) n += zhi - zlo + 1;
     }
     block_excl_scan(n, warp_tot, &s_total);
-    if (threadIdx.x == 0) args.win_cells[row] = A + s_total + 1;  // + the trash cell
+    if (threadIdx.x == 0) args.win_cells[row] = A + s_total + 2;  // + the two trash cells
     return;
   }
   int2* cols = reinterpret_cast<int2*>(smem + lay.pool);
@@ -631,7 +631,7 @@ k_walk(WalkArgs args) {
       if (cols[k].y >= cols[k].x) n_mine += cols[k].y - cols[k].x + 1;
   const int cexcl = block_excl_scan(n_mine, warp_tot, &s_total);
   const int W = s_total;  // window cells
-  if (!table_fits || A + W + 1 > args.cap_cells) {
+  if (!table_fits || A + W + 2 > args.cap_cells) {
     if (threadIdx.x == 0) {
       int k = atomicAdd(args.overflow_count, 1);
       args.overflow_rows[k] = (int32_t)row;
@@ -652,11 +652,12 @@ k_walk(WalkArgs args) {
     }
   }
   win.cols = cols;
-  win.lo = reinterpret_cast<uint32_t*>(smem + lay.pool + (size_t)A * 8);  // 8A + 8(W+1) <= pool
-  win.hi = win.lo + W + 1;
+  win.lo = reinterpret_cast<uint32_t*>(smem + lay.pool + (size_t)A * 8);  // 8A + 8(W+2) <= pool
+  win.hi = win.lo + W + 2;
   win.trash = W;
+  win.trash_out = W + 1;
   // ---- zero the window, walk the rays
-  for (int i = threadIdx.x; i <= W; i += kWalkThreads) {  // the window and the trash cell
+  for (int i = threadIdx.x; i <= W + 1; i += kWalkThreads) {  // the window and the trash cells
     win.lo[i] = 0u;
     win.hi[i] = 0u;
   }
@@ -675,7 +676,8 @@ k_walk(WalkArgs args) {
       ray[0] = a.x; ray[1] = a.y; ray[2] = b.x; ray[3] = b.y; ray[4] = c.x; ray[5] = c.y;
       // golden-ratio spread of the starting points of whole rays
       const float frac = (float)r * 0.6180339887f - floorf((float)r * 0.6180339887f);
-      walk_ray(G, ray, win, &s_outside, &s_exact, frac, piece, np);
+      if (np > 1) walk_ray<true>(G, ray, win, &s_exact, frac, piece, np);
+      else walk_ray<false>(G, ray, win, &s_exact, frac, piece, np);
     };
     const int t = threadIdx.x;
     const int rounds = R / kWalkThreads;
@@ -691,7 +693,7 @@ k_walk(WalkArgs args) {
     }
   }
   __syncthreads();
-  if (threadIdx.x == 0 && s_outside) atomicAdd(args.hit_outside, s_outside);
+  if (threadIdx.x == 0 && win.lo[win.trash_out] != 0u) atomicAdd(args.hit_outside, 1);
   if (s_exact) {  // uniform across the block
     if (threadIdx.x == 0) {
       int k = atomicAdd(args.exact_count, 1);
@@ -1144,7 +1146,7 @@ static epet_status run_walk(const Geo& G, const int32_t* rows, int64_t m,
   EPET_CUDA(cudaStreamSynchronize(st));
   if (outside)
     return set_error(EPET_ERR_UNSUPPORTED,
-                     "%d ray-voxel hits fell outside the crystal-hull window (ray "
+                     "%d rows had ray-voxel hits outside the crystal-hull window (ray "
                      "endpoints inside the grid are not supported)", outside);
   out->nnz = total_nnz;
   return EPET_OK;
