@@ -82,12 +82,14 @@ struct WalkArgs {
 // two 32-bit sum words of every window cell (8 bytes per cell): a channel
 // needs columns + cells <= cap_cells.
 struct WalkLayout {
-  size_t pext, pool, total;
+  size_t pext, planes, pool, total;
 };
-__host__ __device__ inline WalkLayout walk_layout(int nslab, int cap_cells) {
+// nplanes: grid planes of all three axes (n0 + n1 + n2 + 3)
+__host__ __device__ inline WalkLayout walk_layout(int nslab, int nplanes, int cap_cells) {
   WalkLayout L;
   L.pext = align256((size_t)20 * nslab);  // Slab[nslab]
-  L.pool = L.pext + align256((size_t)(nslab + 1) * 16);
+  L.planes = L.pext + align256((size_t)(nslab + 1) * 16);
+  L.pool = L.planes + align256((size_t)nplanes * 4);
   L.total = L.pool + align256((size_t)cap_cells * 8);
   return L;
 }
@@ -171,8 +173,8 @@ __device__ void slab_window(const Geo& G, const float (*c0)[3], const float (*c1
 }
 
 // The window: the cells of a channel's hull, as a table over the columns
-// (ix, iy) of its (x, y) bounding box, each column a run of consecutive z
-// cells [zlo, zhi]; cells are stored column after column (x major, then y,
+// (ix, iy) of its (x, y) bounding box, each column a run of zn consecutive
+// z cells from zlo; cells are stored column after column (x major, then y,
 // then z), which is voxel-id order.  Each cell holds its exact fixed-point
 // sum as two 32-bit words: every chord's units are split as
 // hi * 2^fx_split + lo and the halves are summed separately with
@@ -182,7 +184,11 @@ __device__ void slab_window(const Geo& G, const float (*c0)[3], const float (*c1
 struct Window {
   uint32_t* lo;
   uint32_t* hi;
-  const int2* cols;  // per column: {first cell, zlo | zhi << 16}; empty: zlo 1, zhi 0
+  // per column: {first cell, zlo | zn << 16}; empty: zn 0; entry wbx * wby
+  // is an empty column that stands for every column outside the box
+  const int2* cols;
+  const float* planes;  // grid planes: x at [0, n0], y at poff1 + [0, n1], z at poff2 + ...
+  int poff1, poff2, nplanes;
   int bx0, by0, wbx, wby;
   int split;
   int trash;      // cell W: absorbs the adds of steps with nothing to add (never read)
@@ -193,15 +199,15 @@ struct Window {
 struct Col {
   int off, zlo, zn;
 };
-// Column (cx, cy) relative to the box corner; outside the box: no cells.
-// Branch-free: an index outside the box reads entry 0 and gets zn = 0.
+// Column (cx, cy) relative to the box corner; outside the box: the empty
+// entry past the table (branch-free).
 __device__ __forceinline__ Col load_col(const Window& w, int cx, int cy) {
   const bool in = (unsigned)cx < (unsigned)w.wbx && (unsigned)cy < (unsigned)w.wby;
-  const int2 e = w.cols[in ? cx * w.wby + cy : 0];
+  const int2 e = w.cols[in ? cx * w.wby + cy : w.wbx * w.wby];
   Col c;
   c.off = e.x;
   c.zlo = e.y & 0xffff;
-  c.zn = in ? (e.y >> 16) - c.zlo + 1 : 0;
+  c.zn = e.y >> 16;
   return c;
 }
 
@@ -211,7 +217,7 @@ struct WalkAxis {
   float o, d, r0, dr, inv;  // plane k at o + k*d; ray at r0 + a*dr; inv = RN(1/dr)
   int n, step, idx;
   float lo, hi;  // parameter interval of the current cell along this axis
-  float kh;      // index (as a float) of the plane at hi
+  int kn;        // index of the plane at hi (idx + 1 ascending, idx descending)
   __device__ __forceinline__ float alpha(float k) const {
     return div_cr(fsub(fadd(o, fmul(k, d)), r0), dr, inv);
   }
@@ -223,13 +229,13 @@ struct WalkAxis {
       while (i < n - 1 && alpha((float)(i + 1)) <= a) i++;
       lo = alpha((float)i);
       hi = alpha((float)(i + 1));
-      kh = (float)(i + 1);
+      kn = i + 1;
     } else {         // interval of cell i: [alpha(i+1), alpha(i)]
       while (i < n - 1 && alpha((float)(i + 1)) > a) i++;
       while (i > 0 && alpha((float)i) <= a) i--;
       lo = alpha((float)(i + 1));
       hi = alpha((float)i);
-      kh = (float)i;
+      kn = i;
     }
     idx = i;
   }
@@ -286,9 +292,10 @@ __device__ void walk_ray(const Geo& G, const float* ray, const Window& w, int* n
   if (!(a_in < a_out)) return;
   const float span = fsub(a_out, a_in);
   float a_s, a_lo = -INFINITY, a_stop = INFINITY;
-  int ex = 0, ey = 0, ez = 0;
-  float exl = 0.f, exh = 0.f, exk = 0.f, eyl = 0.f, eyh = 0.f, eyk = 0.f;
-  float ezl = 0.f, ezh = 0.f, ezk = 0.f;
+  // entry state of the second part: plane indices, their parameters, and
+  // the entry parameter of the grid's first cell
+  int eknx = 0, ekny = 0, eknz = 0;
+  float ehx = 0.f, ehy = 0.f, ehz = 0.f, eamin = 0.f;
   bool second;
   if (PIECES) {
     if (piece > 0) a_lo = fadd(a_in, fmul(span, (float)piece / (float)npieces));
@@ -305,49 +312,54 @@ __device__ void walk_ray(const Geo& G, const float* ray, const Window& w, int* n
     X.enter(a_in);
     Y.enter(a_in);
     Z.enter(a_in);
-    ex = X.idx; ey = Y.idx; ez = Z.idx;
-    exl = X.lo; exh = X.hi; exk = X.kh; eyl = Y.lo; eyh = Y.hi; eyk = Y.kh;
-    ezl = Z.lo; ezh = Z.hi; ezk = Z.kh;
+    eknx = X.kn; ekny = Y.kn; eknz = Z.kn;
+    ehx = X.hi; ehy = Y.hi; ehz = Z.hi;
+    eamin = fmaxf(fmaxf(X.lo, Y.lo), Z.lo);
     second = !(a_s > a_in);  // nothing before the starting cell
   }
   X.enter(a_s);
   Y.enter(a_s);
   Z.enter(a_s);
   const float a_start = fmaxf(fmaxf(X.lo, Y.lo), Z.lo);  // entry of the starting cell
-  // The entry parameter of the current cell is always the latest crossing
-  // (the largest of the axes' lo), so it is carried as one value; the cell
-  // whose exit parameter reaches a_out is the last before the grid's exit.
+  // Per axis the walk keeps kn, the index of the plane at which it leaves
+  // the current cell along that axis, and h, that plane's parameter; the cell
+  // index is kn - 1 (ascending) or kn (descending).  The entry parameter of
+  // the current cell is always the latest crossing (the largest of the
+  // axes' lo), so it is carried as one value; the cell whose exit parameter
+  // reaches a_out is the last before the grid's exit.
+  int knx = X.kn, kny = Y.kn, knz = Z.kn;
+  float hx = X.hi, hy = Y.hi, hz = Z.hi;
   float amin = a_start;
-  int cx = X.idx - w.bx0, cy = Y.idx - w.by0;  // column relative to the box
-  Col col = load_col(w, cx, cy);
+  const int ox = (X.step > 0 ? 1 : 0) + w.bx0;  // column = (kn_x - ox, kn_y - oy)
+  const int oy = (Y.step > 0 ? 1 : 0) + w.by0;
+  const int oz = Z.step > 0 ? 1 : 0;            // z cell = kn_z - oz
+  Col col = load_col(w, knx - ox, kny - oy);
   // chord units = RN((amax - amin) * L) * 2^s = RN((amax - amin) * (L * 2^s)):
   // scaling by a power of two is exact
   const float Ls = fmul(L, G.fx_scale);
-  const float two_s = __int_as_float((127 + w.split) << 23);   // 2^split
-  const float inv_two_s = __int_as_float((127 - w.split) << 23);
+  const uint32_t lo_mask = (1u << w.split) - 1u;
   const int budget = g.n[0] + g.n[1] + g.n[2] + 4;
   for (int steps = 0; steps < budget; steps++) {
     if (!(amin < a_stop)) break;
-    const bool mx = X.hi <= Y.hi && X.hi <= Z.hi;
-    const bool my = !mx && Y.hi <= Z.hi;
+    const bool mx = hx <= hy && hx <= hz;
+    const bool my = !mx && hy <= hz;
     const bool mz = !mx && !my;
-    const float amax = mx ? X.hi : (my ? Y.hi : Z.hi);
+    const float amax = mx ? hx : (my ? hy : hz);
     {
       // Branch-free add: a step with nothing to add (a zero-length cell, a
       // cell of the previous piece) adds to the trash cell, a hit outside
       // the window adds one to the outside cell's count.
       const bool add = PIECES ? (amin < amax && amin >= a_lo)  // before a_lo: previous piece
                               : amin < amax;
-      const unsigned dz = (unsigned)(Z.idx - col.zlo);
+      const unsigned dz = (unsigned)(knz - oz - col.zlo);
       const bool inwin = dz < (unsigned)col.zn;
       const int c = add ? (inwin ? col.off + (int)dz : w.trash_out) : w.trash;
-      // units = RN(len * scale) split as hi * 2^split + lo; for a product
-      // >= 2^split the float is an integer and both parts are exact
-      const float v = fmul(fsub(amax, amin), Ls);
-      const uint32_t h = __float2uint_rz(fmul(v, inv_two_s));
-      uint32_t l = __float2uint_rn(__fmaf_rn(-__uint2float_rn(h), two_s, v));
-      l = (h | l) == 0u ? 1u : l;  // a positive chord counts at least one unit
-      l = inwin ? l : 1u;
+      // units = RN_int(len * scale) (< 2^64 by the choice of scale), split as
+      // hi * 2^split + lo
+      const unsigned long long u = __float2ull_rn(fmul(fsub(amax, amin), Ls));
+      const uint32_t h = (uint32_t)(u >> w.split);
+      uint32_t l = (uint32_t)u & lo_mask;
+      l = (u == 0ull || !inwin) ? 1u : l;  // a positive chord counts at least one unit
       atomicAdd(&w.lo[c], l);
       atomicAdd(&w.hi[c], h);
     }
@@ -356,29 +368,26 @@ __device__ void walk_ray(const Geo& G, const float* ray, const Window& w, int* n
       if (second) break;
       second = true;
       a_stop = a_start;
-      X.idx = ex; X.hi = exh; X.kh = exk;
-      Y.idx = ey; Y.hi = eyh; Y.kh = eyk;
-      Z.idx = ez; Z.hi = ezh; Z.kh = ezk;
-      amin = fmaxf(fmaxf(exl, eyl), ezl);
-      cx = ex - w.bx0;
-      cy = ey - w.by0;
-      col = load_col(w, cx, cy);
+      knx = eknx; kny = ekny; knz = eknz;
+      hx = ehx; hy = ehy; hz = ehz;
+      amin = eamin;
+      col = load_col(w, knx - ox, kny - oy);
       continue;
     }
-    // advance the axis whose plane comes first
+    // advance the axis whose plane comes first: its next plane's parameter
+    // is the reference's quotient over the tabulated plane position
     const int st = mx ? X.step : (my ? Y.step : Z.step);
-    const float kh = (mx ? X.kh : (my ? Y.kh : Z.kh)) + (st > 0 ? 1.f : -1.f);
-    const float o = mx ? X.o : (my ? Y.o : Z.o), d = mx ? X.d : (my ? Y.d : Z.d);
+    const int kn = (mx ? knx : (my ? kny : knz)) + st;
+    const int pb = mx ? 0 : (my ? w.poff1 : w.poff2);
+    const float P = w.planes[min((unsigned)(pb + kn), (unsigned)(w.nplanes - 1))];
     const float r0 = mx ? X.r0 : (my ? Y.r0 : Z.r0), dr = mx ? X.dr : (my ? Y.dr : Z.dr);
     const float inv = mx ? X.inv : (my ? Y.inv : Z.inv);
-    const float h = div_cr(fsub(fadd(o, fmul(kh, d)), r0), dr, inv);
-    X.hi = mx ? h : X.hi; X.kh = mx ? kh : X.kh; X.idx += mx ? st : 0;
-    Y.hi = my ? h : Y.hi; Y.kh = my ? kh : Y.kh; Y.idx += my ? st : 0;
-    Z.hi = mz ? h : Z.hi; Z.kh = mz ? kh : Z.kh; Z.idx += mz ? st : 0;
+    const float h = div_cr(fsub(P, r0), dr, inv);
+    hx = mx ? h : hx; knx = mx ? kn : knx;
+    hy = my ? h : hy; kny = my ? kn : kny;
+    hz = mz ? h : hz; knz = mz ? kn : knz;
     amin = amax;
-    cx += mx ? st : 0;  // x or y moved: another column
-    cy += my ? st : 0;
-    col = load_col(w, cx, cy);
+    col = load_col(w, knx - ox, kny - oy);
   }
 }
 
@@ -429,7 +438,8 @@ k_walk(WalkArgs args) {
   const epet_grid& g = G.p.grid;
   const int nx = g.n[0];
   Slab* slabs = reinterpret_cast<Slab*>(smem);
-  const WalkLayout lay = walk_layout(max(g.n[0], g.n[2]), args.cap_cells);
+  const int nplanes = g.n[0] + g.n[1] + g.n[2] + 3;
+  const WalkLayout lay = walk_layout(max(g.n[0], g.n[2]), nplanes, args.cap_cells);
   Window win;
   win.split = G.fx_split;
   __shared__ __align__(16) float s_geom[kGeomFloats];
@@ -578,11 +588,12 @@ k_walk(WalkArgs args) {
       if (zhi >= zlo) n += zhi - zlo + 1;
     }
     block_excl_scan(n, warp_tot, &s_total);
-    if (threadIdx.x == 0) args.win_cells[row] = A + s_total + 2;  // + the two trash cells
+    // + the empty column past the table and the two trash cells
+    if (threadIdx.x == 0) args.win_cells[row] = A + s_total + 3;
     return;
   }
   int2* cols = reinterpret_cast<int2*>(smem + lay.pool);
-  const bool table_fits = A <= args.cap_cells;
+  const bool table_fits = A + 1 <= args.cap_cells;
   if (table_fits) {
     if (sa == 0) {
       for (int k = kbeg; k < kend; k++) {
@@ -631,7 +642,7 @@ k_walk(WalkArgs args) {
       if (cols[k].y >= cols[k].x) n_mine += cols[k].y - cols[k].x + 1;
   const int cexcl = block_excl_scan(n_mine, warp_tot, &s_total);
   const int W = s_total;  // window cells
-  if (!table_fits || A + W + 2 > args.cap_cells) {
+  if (!table_fits || A + W + 3 > args.cap_cells) {
     if (threadIdx.x == 0) {
       int k = atomicAdd(args.overflow_count, 1);
       args.overflow_rows[k] = (int32_t)row;
@@ -644,18 +655,30 @@ k_walk(WalkArgs args) {
     for (int k = kbeg; k < kend; k++) {
       const int2 r = cols[k];
       if (r.y >= r.x) {
-        cols[k] = make_int2(o, r.x | (r.y << 16));
+        cols[k] = make_int2(o, r.x | ((r.y - r.x + 1) << 16));
         o += r.y - r.x + 1;
       } else {
-        cols[k] = make_int2(o, 1);  // empty: zlo 1, zhi 0
+        cols[k] = make_int2(o, 0);  // empty: zn 0
       }
     }
   }
+  if (threadIdx.x == 0) cols[A] = make_int2(0, 0);  // stands for the columns outside the box
   win.cols = cols;
-  win.lo = reinterpret_cast<uint32_t*>(smem + lay.pool + (size_t)A * 8);  // 8A + 8(W+2) <= pool
+  // 8(A + 1) + 8(W + 2) <= pool
+  win.lo = reinterpret_cast<uint32_t*>(smem + lay.pool + (size_t)(A + 1) * 8);
   win.hi = win.lo + W + 2;
   win.trash = W;
   win.trash_out = W + 1;
+  // grid planes o + k d of the three axes (the walk's quotients read them)
+  float* planes = reinterpret_cast<float*>(smem + lay.planes);
+  win.planes = planes;
+  win.poff1 = g.n[0] + 1;
+  win.poff2 = g.n[0] + g.n[1] + 2;
+  win.nplanes = nplanes;
+  for (int i = threadIdx.x; i < nplanes; i += kWalkThreads) {
+    const int a = i < win.poff1 ? 0 : (i < win.poff2 ? 1 : 2);
+    planes[i] = voxel_plane(g, a, i - (a == 0 ? 0 : (a == 1 ? win.poff1 : win.poff2)));
+  }
   // ---- zero the window, walk the rays
   for (int i = threadIdx.x; i <= W + 1; i += kWalkThreads) {  // the window and the trash cells
     win.lo[i] = 0u;
@@ -719,7 +742,7 @@ k_walk(WalkArgs args) {
     }
     int k = lo_k;
     int2 e = cols[k];
-    int zhi = e.y >> 16;
+    int zhi = (e.y & 0xffff) + (e.y >> 16) - 1;
     int cx = k / win.wby, cy = k - cx * win.wby;
     int iz = (e.y & 0xffff) + (cbeg - e.x);
     for (int cidx = cbeg; cidx < cend; cidx++) {
@@ -731,7 +754,7 @@ k_walk(WalkArgs args) {
         }
         e = cols[k];
         iz = e.y & 0xffff;
-        zhi = e.y >> 16;
+        zhi = iz + (e.y >> 16) - 1;
       }
       f(cidx, win.bx0 + cx, win.by0 + cy, iz);
       ++iz;
@@ -836,7 +859,9 @@ __global__ void k_offset_rowptr(int64_t* rp, int64_t n, const int64_t* base) {
 
 static size_t walk_smem(const Geo& G, int cap_cells) {
   static_assert(sizeof(Slab) == 20, "walk_layout assumes 20-byte slabs");
-  return walk_layout(std::max(G.p.grid.n[0], G.p.grid.n[2]), cap_cells).total;
+  return walk_layout(std::max(G.p.grid.n[0], G.p.grid.n[2]),
+                     G.p.grid.n[0] + G.p.grid.n[1] + G.p.grid.n[2] + 3, cap_cells)
+      .total;
 }
 
 static int g_max_smem = 0;
