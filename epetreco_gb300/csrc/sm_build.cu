@@ -82,14 +82,15 @@ struct WalkArgs {
 // two 32-bit sum words of every window cell (8 bytes per cell): a channel
 // needs columns + cells <= cap_cells.
 struct WalkLayout {
-  size_t pext, planes, pool, total;
+  size_t pext, planes, ztab, pool, total;
 };
-// nplanes: grid planes of all three axes (n0 + n1 + n2 + 3)
-__host__ __device__ inline WalkLayout walk_layout(int nslab, int nplanes, int cap_cells) {
+// nplanes: grid planes of all three axes (n0 + n1 + n2 + 3); nz: z cells
+__host__ __device__ inline WalkLayout walk_layout(int nslab, int nplanes, int nz, int cap_cells) {
   WalkLayout L;
   L.pext = align256((size_t)20 * nslab);  // Slab[nslab]
   L.planes = L.pext + align256((size_t)(nslab + 1) * 16);
-  L.pool = L.planes + align256((size_t)nplanes * 4);
+  L.ztab = L.planes + align256((size_t)nplanes * 4);
+  L.pool = L.ztab + align256((size_t)nz * 8);
   L.total = L.pool + align256((size_t)cap_cells * 8);
   return L;
 }
@@ -439,7 +440,7 @@ k_walk(WalkArgs args) {
   const int nx = g.n[0];
   Slab* slabs = reinterpret_cast<Slab*>(smem);
   const int nplanes = g.n[0] + g.n[1] + g.n[2] + 3;
-  const WalkLayout lay = walk_layout(max(g.n[0], g.n[2]), nplanes, args.cap_cells);
+  const WalkLayout lay = walk_layout(max(g.n[0], g.n[2]), nplanes, g.n[2], args.cap_cells);
   Window win;
   win.split = G.fx_split;
   __shared__ __align__(16) float s_geom[kGeomFloats];
@@ -679,6 +680,13 @@ k_walk(WalkArgs args) {
     const int a = i < win.poff1 ? 0 : (i < win.poff2 ? 1 : 2);
     planes[i] = voxel_plane(g, a, i - (a == 0 ? 0 : (a == 1 ? win.poff1 : win.poff2)));
   }
+  // per z cell the candidate test's z terms ab1 * ap2 and ab0 * ap2
+  // (ap = voxel centre - a; the other terms are constant along a column)
+  float2* ztab = reinterpret_cast<float2*>(smem + lay.ztab);
+  for (int iz = threadIdx.x; iz < g.n[2]; iz += kWalkThreads) {
+    const float ap2 = fsub(voxel_centre(g, 2, iz), line.a[2]);
+    ztab[iz] = make_float2(fmul(line.ab[1], ap2), fmul(line.ab[0], ap2));
+  }
   // ---- zero the window, walk the rays
   for (int i = threadIdx.x; i <= W + 1; i += kWalkThreads) {  // the window and the trash cells
     win.lo[i] = 0u;
@@ -731,8 +739,9 @@ k_walk(WalkArgs args) {
   // reads fall in distinct shared-memory banks)
   const int cpt = ((W + kWalkThreads - 1) / kWalkThreads) | 1;
   const int cbeg = min(W, (int)threadIdx.x * cpt), cend = min(W, cbeg + cpt);
-  // Visits the thread's range in order; f(cell, ix, iy, iz).
-  auto for_cells = [&](auto&& f) {
+  // Visits the thread's range in order: fcol(ix, iy) on entering a column,
+  // f(cell, ix, iy, iz) per cell.
+  auto for_cells = [&](auto&& fcol, auto&& f) {
     if (cbeg >= cend) return;
     int lo_k = 0, hi_k = A - 1;  // last column with first cell <= cbeg
     while (lo_k < hi_k) {
@@ -745,16 +754,20 @@ k_walk(WalkArgs args) {
     int zhi = (e.y & 0xffff) + (e.y >> 16) - 1;
     int cx = k / win.wby, cy = k - cx * win.wby;
     int iz = (e.y & 0xffff) + (cbeg - e.x);
+    fcol(win.bx0 + cx, win.by0 + cy);
     for (int cidx = cbeg; cidx < cend; cidx++) {
-      while (iz > zhi) {  // next non-empty column
-        ++k;
-        if (++cy == win.wby) {
-          cy = 0;
-          ++cx;
-        }
-        e = cols[k];
-        iz = e.y & 0xffff;
-        zhi = iz + (e.y >> 16) - 1;
+      if (iz > zhi) {
+        do {  // next non-empty column
+          ++k;
+          if (++cy == win.wby) {
+            cy = 0;
+            ++cx;
+          }
+          e = cols[k];
+          iz = e.y & 0xffff;
+          zhi = iz + (e.y >> 16) - 1;
+        } while (iz > zhi);
+        fcol(win.bx0 + cx, win.by0 + cy);
       }
       f(cidx, win.bx0 + cx, win.by0 + cy, iz);
       ++iz;
@@ -764,20 +777,42 @@ k_walk(WalkArgs args) {
   const float fR = (float)R;
   // pass 1: candidate filter, count, projections
   // (every cell takes the same instructions: the candidate test and the
-  // value are computed for all of them and the result selected)
+  // value are computed for all of them and the result selected).  The
+  // candidate test is the reference's |ab x ap|^2 with the same operations:
+  // its x and y terms come per column, its z terms from the table.
   int cnt = 0;
   float fsum = 0.f;
   const float inv_fR = __frcp_rn(fR);
-  for_cells([&](int cidx, int ix, int iy, int iz) {
+  float K0 = 0.f, K1 = 0.f, c2sq = 0.f;
+  int colvox = 0;
+  for_cells(
+      [&](int ix, int iy) {
+        const float ap0 = fsub(voxel_centre(g, 0, ix), L.a[0]);
+        const float ap1 = fsub(voxel_centre(g, 1, iy), L.a[1]);
+        K0 = fmul(L.ab[2], ap1);
+        K1 = fmul(L.ab[2], ap0);
+        const float c2 = fsub(fmul(L.ab[0], ap1), fmul(L.ab[1], ap0));
+        c2sq = fmul(c2, c2);
+        colvox = ix * G.nyz + iy * g.n[2];
+      },
+      [&](int cidx, int ix, int iy, int iz) {
     const unsigned long long u =
         ((unsigned long long)win.hi[cidx] << win.split) + (unsigned long long)win.lo[cidx];
-    const bool cand = is_candidate(G, L, ix, iy, iz);  // not a candidate: dropped
+    const float2 zt = ztab[iz];
+    const float c0 = fsub(zt.x, K0), c1 = fsub(K1, zt.y);
+    // not a candidate: dropped
+    const bool cand = fadd(fadd(fmul(c0, c0), fmul(c1, c1)), c2sq) < L.s_max;
     const bool keep = (u != 0ull) & cand;
     const float v = div_cr(fmul(__ull2float_rn(u), G.fx_inv), fR, inv_fR);
+    if (kMode == kModeCsr) {
+      // kept entries compacted at the start of the thread's range: the slot
+      // written is this cell's or an earlier one, already read
+      win.hi[cbeg + cnt] = (uint32_t)(colvox + iz);
+      win.lo[cbeg + cnt] = __float_as_uint(v);
+    }
     cnt += keep ? 1 : 0;
-    if (kMode == kModeCsr) win.lo[cidx] = keep ? __float_as_uint(v) : 0u;  // read by pass 2
     if (kMode != kModeCsr && keep) {
-      const int vox = ix * G.nyz + iy * g.n[2] + iz;
+      const int vox = colvox + iz;
       if (kMode == kModeForward) fsum = fadd(fsum, fmul(v, args.x[vox]));
       if (kMode == kModeBack) {
         const float ev = args.e[row];
@@ -788,14 +823,11 @@ k_walk(WalkArgs args) {
   });
   if (kMode == kModeCsr) {
     const int pos = block_excl_scan(cnt, warp_tot, &s_total);
-    int64_t o = slot * args.stride + pos;
-    for_cells([&](int cidx, int ix, int iy, int iz) {
-      const uint32_t vb = win.lo[cidx];  // the value's bits, 0 when dropped
-      if (vb == 0u) return;
-      args.stage_col[o] = ix * G.nyz + iy * g.n[2] + iz;
-      args.stage_val[o] = __uint_as_float(vb);
-      o++;
-    });
+    const int64_t o = slot * args.stride + pos;
+    for (int j = 0; j < cnt; j++) {
+      args.stage_col[o + j] = (int32_t)win.hi[cbeg + j];
+      args.stage_val[o + j] = __uint_as_float(win.lo[cbeg + j]);
+    }
     if (threadIdx.x == 0) {
       args.row_len[row] = s_total;
       if (args.sel) args.ovf_idx[row] = (int32_t)slot;
@@ -860,7 +892,7 @@ __global__ void k_offset_rowptr(int64_t* rp, int64_t n, const int64_t* base) {
 static size_t walk_smem(const Geo& G, int cap_cells) {
   static_assert(sizeof(Slab) == 20, "walk_layout assumes 20-byte slabs");
   return walk_layout(std::max(G.p.grid.n[0], G.p.grid.n[2]),
-                     G.p.grid.n[0] + G.p.grid.n[1] + G.p.grid.n[2] + 3, cap_cells)
+                     G.p.grid.n[0] + G.p.grid.n[1] + G.p.grid.n[2] + 3, G.p.grid.n[2], cap_cells)
       .total;
 }
 
