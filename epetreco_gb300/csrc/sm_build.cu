@@ -710,17 +710,27 @@ k_walk(WalkArgs args) {
       if (np > 1) walk_ray<true>(G, ray, win, &s_exact, frac, piece, np);
       else walk_ray<false>(G, ray, win, &s_exact, frac, piece, np);
     };
+    // one call site, so each form of the walk loop is compiled once
     const int t = threadIdx.x;
     const int rounds = R / kWalkThreads;
-    for (int k = 0; k < rounds; k++) walk(k * kWalkThreads + t, 0, 1);
     const int rr = R - rounds * kWalkThreads, r0 = rounds * kWalkThreads;
-    const int fw = rr / 32;  // warps of whole rays
-    if (t < fw * 32) {
-      walk(r0 + t, 0, 1);
-    } else if (rr > fw * 32) {
-      const int rem = rr - fw * 32, lanes = kWalkThreads - fw * 32;
-      const int np = lanes / rem, l = t - fw * 32;
-      if (l < rem * np) walk(r0 + fw * 32 + l / np, l % np, np);
+    const int fw = rr / 32;  // warps of whole rays in the last round
+    for (int k = 0; k <= rounds; k++) {
+      int r = k * kWalkThreads + t, piece = 0, np = 1;
+      bool act = true;
+      if (k == rounds) {
+        if (t < fw * 32) {
+          r = r0 + t;
+        } else {
+          const int rem = rr - fw * 32, lanes = kWalkThreads - fw * 32;
+          np = rem > 0 ? lanes / rem : 1;
+          const int l = t - fw * 32;
+          act = rem > 0 && l < rem * np;
+          r = r0 + fw * 32 + l / np;
+          piece = l % np;
+        }
+      }
+      if (act) walk(r, piece, np);
     }
   }
   __syncthreads();
