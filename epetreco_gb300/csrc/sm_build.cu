@@ -253,12 +253,12 @@ struct WalkAxis {
 // is branch-free: the axis whose plane comes first is selected and advanced
 // with one division.
 //
-// With PIECES the lane walks only piece `piece` of npieces of the ray: the
-// cells entered in [a_lo, a_hi), the piece's share of the grid range (no
-// wrap).  The pieces of a ray compute their common bounds with the same
-// expression, so every cell belongs to exactly one piece.
-template <bool PIECES>
-__device__ void walk_ray(const Geo& G, const float* ray, const Window& w, int* needs_exact,
+// With npieces > 1 the lane walks only piece `piece` of the ray: the cells
+// entered in [a_lo, a_hi), the piece's share of the grid range (no wrap).
+// The pieces of a ray compute their common bounds with the same expression,
+// so every cell belongs to exactly one piece.  Whole rays and pieces share
+// one loop (one copy of its code).
+__device__ __forceinline__ void walk_ray(const Geo& G, const float* ray, const Window& w, int* needs_exact,
                          float frac, int piece, int npieces) {
   const epet_grid& g = G.p.grid;
   if (ray[0] == ray[3] && ray[1] == ray[4] && ray[2] == ray[5]) return;
@@ -298,7 +298,7 @@ __device__ void walk_ray(const Geo& G, const float* ray, const Window& w, int* n
   int eknx = 0, ekny = 0, eknz = 0;
   float ehx = 0.f, ehy = 0.f, ehz = 0.f, eamin = 0.f;
   bool second;
-  if (PIECES) {
+  if (npieces > 1) {
     if (piece > 0) a_lo = fadd(a_in, fmul(span, (float)piece / (float)npieces));
     if (piece + 1 < npieces) a_stop = fadd(a_in, fmul(span, (float)(piece + 1) / (float)npieces));
     a_s = piece > 0 ? a_lo : a_in;
@@ -350,8 +350,7 @@ __device__ void walk_ray(const Geo& G, const float* ray, const Window& w, int* n
       // Branch-free add: a step with nothing to add (a zero-length cell, a
       // cell of the previous piece) adds to the trash cell, a hit outside
       // the window adds one to the outside cell's count.
-      const bool add = PIECES ? (amin < amax && amin >= a_lo)  // before a_lo: previous piece
-                              : amin < amax;
+      const bool add = amin < amax && amin >= a_lo;  // before a_lo: previous piece
       const unsigned dz = (unsigned)(knz - oz - col.zlo);
       const bool inwin = dz < (unsigned)col.zn;
       const int c = add ? (inwin ? col.off + (int)dz : w.trash_out) : w.trash;
@@ -707,8 +706,7 @@ k_walk(WalkArgs args) {
       ray[0] = a.x; ray[1] = a.y; ray[2] = b.x; ray[3] = b.y; ray[4] = c.x; ray[5] = c.y;
       // golden-ratio spread of the starting points of whole rays
       const float frac = (float)r * 0.6180339887f - floorf((float)r * 0.6180339887f);
-      if (np > 1) walk_ray<true>(G, ray, win, &s_exact, frac, piece, np);
-      else walk_ray<false>(G, ray, win, &s_exact, frac, piece, np);
+      walk_ray(G, ray, win, &s_exact, frac, piece, np);
     };
     // one call site, so each form of the walk loop is compiled once
     const int t = threadIdx.x;
