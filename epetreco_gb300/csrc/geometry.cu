@@ -28,21 +28,41 @@ __device__ __forceinline__ void emit_rays(const Geo& G, int cnl, curandState st,
   angle_sincos(G.p.setup, id[0], &sn, &cs);
   const CrystalMat m0 = crystal_matrix(G.p.setup, sn, cs, 0, id[1], id[2]);
   const CrystalMat m1 = crystal_matrix(G.p.setup, sn, cs, 1, id[3], id[4]);
+  // rays in pairs: 48 bytes as three 16-byte stores when the row's block is
+  // 16-byte aligned (half as many scattered stores as 8-byte ones)
+  const bool wide = (reinterpret_cast<uintptr_t>(o) & 15) == 0;
   for (int r = 0; r < G.p.nrays; r++) {
     float u[6];
 #pragma unroll
     for (int k = 0; k < 6; k++) u[k] = curand_uniform(&st);
+    float w[6];
     if (uniforms) {
-      o[3 * r + 0] = make_float2(u[0], u[1]);
-      o[3 * r + 1] = make_float2(u[2], u[3]);
-      o[3 * r + 2] = make_float2(u[4], u[5]);
+#pragma unroll
+      for (int k = 0; k < 6; k++) w[k] = u[k];
     } else {
-      float p0[3], p1[3];
-      crystal_apply(m0, u[0], u[1], u[2], p0);
-      crystal_apply(m1, u[3], u[4], u[5], p1);
-      o[3 * r + 0] = make_float2(p0[0], p0[1]);
-      o[3 * r + 1] = make_float2(p0[2], p1[0]);
-      o[3 * r + 2] = make_float2(p1[1], p1[2]);
+      crystal_apply(m0, u[0], u[1], u[2], w);
+      crystal_apply(m1, u[3], u[4], u[5], w + 3);
+    }
+    if (wide && r + 1 < G.p.nrays) {
+      float u2[6], w2[6];
+#pragma unroll
+      for (int k = 0; k < 6; k++) u2[k] = curand_uniform(&st);
+      if (uniforms) {
+#pragma unroll
+        for (int k = 0; k < 6; k++) w2[k] = u2[k];
+      } else {
+        crystal_apply(m0, u2[0], u2[1], u2[2], w2);
+        crystal_apply(m1, u2[3], u2[4], u2[5], w2 + 3);
+      }
+      float4* q = reinterpret_cast<float4*>(o + 3 * r);
+      q[0] = make_float4(w[0], w[1], w[2], w[3]);
+      q[1] = make_float4(w[4], w[5], w2[0], w2[1]);
+      q[2] = make_float4(w2[2], w2[3], w2[4], w2[5]);
+      r++;
+    } else {
+      o[3 * r + 0] = make_float2(w[0], w[1]);
+      o[3 * r + 1] = make_float2(w[2], w[3]);
+      o[3 * r + 2] = make_float2(w[4], w[5]);
     }
   }
 }
@@ -64,7 +84,7 @@ __global__ void __launch_bounds__(128) k_uniforms(Geo G, const int32_t* __restri
 // state advanced c subsequences, so this yields the same states while a
 // typical step (consecutive channel ids) applies one jump matrix instead of
 // one per set bit of the channel id.
-constexpr int kRaysPerThread = 8;
+constexpr int kRaysPerThread = 4;
 __global__ void __launch_bounds__(128) k_rays(Geo G, const int32_t* __restrict__ rows,
                                               int64_t m, float* __restrict__ out) {
   const int64_t i0 = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) * kRaysPerThread;
