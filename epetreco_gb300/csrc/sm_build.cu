@@ -1026,8 +1026,8 @@ struct BuildOut {
 
 size_t walk_workspace_size(const Geo& G, int64_t m, int cap_cells, bool csr) {
   const int64_t ch = std::min<int64_t>(std::max<int64_t>(m, 1), chunk_rows(G, cap_cells));
-  size_t b = align256((size_t)ch * G.p.nrays * 24);         // rays
-  b += align256((size_t)ch * kGeomFloats * 4);              // channel geometry
+  size_t b = 2 * align256((size_t)ch * G.p.nrays * 24);     // rays (two chunks)
+  b += 2 * align256((size_t)ch * kGeomFloats * 4);          // channel geometry (two chunks)
   if (csr) {
     b += 2 * align256((size_t)ch * cap_cells * 4);          // staging col/val
     b += align256((size_t)ch * 4);                          // row_len
@@ -1100,8 +1100,12 @@ static epet_status run_walk(const Geo& G, const int32_t* rows, int64_t m,
   const int64_t ch = std::min<int64_t>(std::max<int64_t>(m, 1), chunk_rows(G, cap_cells));
   Scratch scr;
   EPET_CHECK(scr.init(ws, ws_bytes, walk_workspace_size(G, m, cap_cells, csr), st));
-  float* rays = scr.take<float>((size_t)ch * G.p.nrays * 6);
-  float* geom = scr.take<float>((size_t)ch * kGeomFloats);
+  // rays and geometry of two chunks: the next chunk's are generated on a
+  // side stream while the current chunk is walked
+  float* rays_b[2] = {scr.take<float>((size_t)ch * G.p.nrays * 6),
+                      scr.take<float>((size_t)ch * G.p.nrays * 6)};
+  float* geom_b[2] = {scr.take<float>((size_t)ch * kGeomFloats),
+                      scr.take<float>((size_t)ch * kGeomFloats)};
   int32_t *stage_col = nullptr, *row_len = nullptr;
   float* stage_val = nullptr;
   int64_t *cnt = nullptr, *rp_chunk = nullptr, *scan_tmp = nullptr;
@@ -1121,11 +1125,41 @@ static epet_status run_walk(const Geo& G, const int32_t* rows, int64_t m,
 
   EPET_CUDA(cudaMemsetAsync(flags, 0, 64 * 4, st));
   if (csr) EPET_CUDA(cudaMemsetAsync(out->csr->row_ptr, 0, 8, st));
-  int64_t total_nnz = 0;
-  for (int64_t c0 = 0; c0 < m; c0 += ch) {
+  // ready[b]: buffer b holds its chunk's rays; done[b]: the last kernel that
+  // reads buffer b has run (recorded on st).  The side stream is drained
+  // before the scratch memory is released, on every return path.
+  struct Side {
+    cudaStream_t s = nullptr;
+    cudaEvent_t start = nullptr, ready[2] = {nullptr, nullptr}, done[2] = {nullptr, nullptr};
+    ~Side() {
+      if (s) cudaStreamSynchronize(s);
+      for (cudaEvent_t e : {start, ready[0], ready[1], done[0], done[1]})
+        if (e) cudaEventDestroy(e);
+      if (s) cudaStreamDestroy(s);
+    }
+  } side;
+  EPET_CUDA(cudaStreamCreateWithFlags(&side.s, cudaStreamNonBlocking));
+  for (cudaEvent_t* e : {&side.start, &side.ready[0], &side.ready[1], &side.done[0], &side.done[1]})
+    EPET_CUDA(cudaEventCreateWithFlags(e, cudaEventDisableTiming));
+  EPET_CUDA(cudaEventRecord(side.start, st));  // the scratch memory is ready
+  EPET_CUDA(cudaStreamWaitEvent(side.s, side.start, 0));
+  auto prepare = [&](int64_t c0, int b) -> epet_status {
     const int64_t mc = std::min(ch, m - c0);
-    EPET_CHECK(launch_rays(G, rows + c0, mc, rays, false, st));
-    EPET_CHECK(launch_channel_geom(G, rows + c0, mc, geom, st));
+    EPET_CUDA(cudaStreamWaitEvent(side.s, side.done[b], 0));
+    EPET_CHECK(launch_rays(G, rows + c0, mc, rays_b[b], false, side.s));
+    EPET_CHECK(launch_channel_geom(G, rows + c0, mc, geom_b[b], side.s));
+    EPET_CUDA(cudaEventRecord(side.ready[b], side.s));
+    return EPET_OK;
+  };
+  if (m > 0) EPET_CHECK(prepare(0, 0));
+  int64_t total_nnz = 0;
+  for (int64_t c0 = 0, k = 0; c0 < m; c0 += ch, k++) {
+    const int64_t mc = std::min(ch, m - c0);
+    const int b = (int)(k & 1);
+    EPET_CUDA(cudaStreamWaitEvent(st, side.ready[b], 0));
+    if (c0 + ch < m) EPET_CHECK(prepare(c0 + ch, b ^ 1));
+    float* rays = rays_b[b];
+    float* geom = geom_b[b];
     WalkArgs a{};
     a.G = G;
     a.rows = rows + c0;
@@ -1205,6 +1239,7 @@ static epet_status run_walk(const Geo& G, const int32_t* rows, int64_t m,
       dev_free(stage2_col, st);
       dev_free(stage2_val, st);
     }
+    EPET_CUDA(cudaEventRecord(side.done[b], st));  // buffer b free for chunk k + 2
   }
   int32_t outside = 0;
   EPET_CUDA(cudaMemcpyAsync(&outside, flags + 1, 4, cudaMemcpyDeviceToHost, st));
