@@ -377,7 +377,9 @@ def trim_memory(keep_bytes: int = 0) -> None:
 
 class Mlem:
     """One reconstruction on the device (reco.cu's loop): the system matrix
-    of the measured rows is built once at construction."""
+    of the measured rows is built once at construction.  The rows may come in
+    any order; they are stored in crystal-pair order (a bijective key of the
+    channel), so a shuffled list gives the same object."""
 
     def __init__(self, p, rows, y, s, use_graph: bool = True, max_row_nnz: int = 0,
                  value_format: int = 0, autotune: bool = False):
