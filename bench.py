@@ -456,7 +456,7 @@ def gb300_arm(args):
     achieved = bytes_it / t_it_live / 1e9
     traffic = None
     tp = os.path.join(ROOT, "profiles", "traffic_full.json")
-    if os.path.exists(tp):
+    if args.config == "full" and os.path.exists(tp):  # measured for the full workload
         try:
             traffic = json.load(open(tp)).get("mlem_iteration")
         except Exception:
@@ -465,14 +465,17 @@ def gb300_arm(args):
     # ---- 16-bit value forms: iteration speed and image error vs FP32
     forms = None
     if not args.no_forms:
-        R.iterate(nit - 6)  # 1 + 5 iterations ran in timeit
+        # images after the same number of iterations in both forms (1 + 5 ran
+        # in timeit; at least the workload's count)
+        n_cmp = max(nit, 6)
+        R.iterate(n_cmp - 6)
         x32 = R.image()
         forms = {"fp32": {"iteration_ms": 1000 * t_iter, "it_per_s": 1.0 / t_iter},
-                 "iterations": nit}
+                 "iterations": n_cmp}
         for name, fmt in (("bf16", 1), ("fp16", 2)):
             R16 = api.Mlem(p, rows, y, s, use_graph=True, value_format=fmt)
             t16 = timeit(lambda: R16.iterate(1), reps=5)
-            R16.iterate(nit - 6)
+            R16.iterate(n_cmp - 6)
             x16 = R16.image()
             err = float(((x16 - x32).double().norm() / x32.double().norm()).item())
             st16 = R16.stats()

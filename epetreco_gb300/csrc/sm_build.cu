@@ -216,7 +216,7 @@ __device__ __forceinline__ Col load_col(const Window& w, int cx, int cy) {
 // reference's quotient (plane_k - r0)/(r1 - r0), correctly rounded.
 struct WalkAxis {
   float o, d, r0, dr, inv;  // plane k at o + k*d; ray at r0 + a*dr; inv = RN(1/dr)
-  int n, step, idx;
+  int n, step;
   float lo, hi;  // parameter interval of the current cell along this axis
   int kn;        // index of the plane at hi (idx + 1 ascending, idx descending)
   __device__ __forceinline__ float alpha(float k) const {
@@ -238,7 +238,6 @@ struct WalkAxis {
       hi = alpha((float)i);
       kn = i;
     }
-    idx = i;
   }
 };
 
