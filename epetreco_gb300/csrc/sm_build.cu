@@ -89,7 +89,7 @@ __host__ __device__ inline WalkLayout walk_layout(int nslab, int nplanes, int nz
   WalkLayout L;
   L.pext = align256((size_t)20 * nslab);  // Slab[nslab]
   L.planes = L.pext + align256((size_t)(nslab + 1) * 16);
-  L.ztab = L.planes + align256((size_t)nplanes * 4);
+  L.ztab = L.planes + align256((size_t)(nplanes + 2) * 4);  // + a guard entry at each end
   L.pool = L.ztab + align256((size_t)nz * 8);
   L.total = L.pool + align256((size_t)cap_cells * 8);
   return L;
@@ -185,12 +185,14 @@ __device__ void slab_window(const Geo& G, const float (*c0)[3], const float (*c1
 struct Window {
   uint32_t* lo;
   uint32_t* hi;
-  // per column: {first cell, zlo | zn << 16}; empty: zn 0; entry wbx * wby
-  // is an empty column that stands for every column outside the box
+  // per column: {first cell, zlo | zn << 16}; empty: zn 0.  The table has
+  // (wbx + 1) x (wby + 1) entries (row stride wbyp = wby + 1): the last
+  // column of each row and the last row are empty and stand for every
+  // column outside the box.
   const int2* cols;
   const float* planes;  // grid planes: x at [0, n0], y at poff1 + [0, n1], z at poff2 + ...
-  int poff1, poff2, nplanes;
-  int bx0, by0, wbx, wby;
+  int poff1, poff2;
+  int bx0, by0, wbx, wby, wbyp;
   int split;
   int trash;      // cell W: absorbs the adds of steps with nothing to add (never read)
   int trash_out;  // cell W + 1: counts (in lo) hits outside the window (must stay 0)
@@ -200,11 +202,11 @@ struct Window {
 struct Col {
   int off, zlo, zn;
 };
-// Column (cx, cy) relative to the box corner; outside the box: the empty
-// entry past the table (branch-free).
+// Column (cx, cy) relative to the box corner; outside the box: an empty
+// border entry (both indices clamped, unsigned, to the border).
 __device__ __forceinline__ Col load_col(const Window& w, int cx, int cy) {
-  const bool in = (unsigned)cx < (unsigned)w.wbx && (unsigned)cy < (unsigned)w.wby;
-  const int2 e = w.cols[in ? cx * w.wby + cy : w.wbx * w.wby];
+  const unsigned ux = min((unsigned)cx, (unsigned)w.wbx), uy = min((unsigned)cy, (unsigned)w.wby);
+  const int2 e = w.cols[ux * w.wbyp + uy];
   Col c;
   c.off = e.x;
   c.zlo = e.y & 0xffff;
@@ -294,7 +296,7 @@ __device__ __forceinline__ void walk_ray(const Geo& G, const float* ray, const W
   float a_s, a_lo = -INFINITY, a_stop = INFINITY;
   // entry state of the second part: plane indices, their parameters, and
   // the entry parameter of the grid's first cell
-  int eknx = 0, ekny = 0, eknz = 0;
+  int ekpx = 0, ekpy = 0, ekpz = 0;
   float ehx = 0.f, ehy = 0.f, ehz = 0.f, eamin = 0.f;
   bool second;
   if (npieces > 1) {
@@ -312,7 +314,7 @@ __device__ __forceinline__ void walk_ray(const Geo& G, const float* ray, const W
     X.enter(a_in);
     Y.enter(a_in);
     Z.enter(a_in);
-    eknx = X.kn; ekny = Y.kn; eknz = Z.kn;
+    ekpx = X.kn; ekpy = w.poff1 + Y.kn; ekpz = w.poff2 + Z.kn;
     ehx = X.hi; ehy = Y.hi; ehz = Z.hi;
     eamin = fmaxf(fmaxf(X.lo, Y.lo), Z.lo);
     second = !(a_s > a_in);  // nothing before the starting cell
@@ -321,19 +323,21 @@ __device__ __forceinline__ void walk_ray(const Geo& G, const float* ray, const W
   Y.enter(a_s);
   Z.enter(a_s);
   const float a_start = fmaxf(fmaxf(X.lo, Y.lo), Z.lo);  // entry of the starting cell
-  // Per axis the walk keeps kn, the index of the plane at which it leaves
-  // the current cell along that axis, and h, that plane's parameter; the cell
-  // index is kn - 1 (ascending) or kn (descending).  The entry parameter of
-  // the current cell is always the latest crossing (the largest of the
-  // axes' lo), so it is carried as one value; the cell whose exit parameter
-  // reaches a_out is the last before the grid's exit.
-  int knx = X.kn, kny = Y.kn, knz = Z.kn;
+  // Per axis the walk keeps kp, the plane table index of the plane at which
+  // it leaves the current cell along that axis (the axis' table offset plus
+  // the plane index kn), and h, that plane's parameter; the cell index is
+  // kn - 1 (ascending) or kn (descending).  The entry parameter of the
+  // current cell is always the latest crossing (the largest of the axes'
+  // lo), so it is carried as one value; the cell whose exit parameter reaches
+  // a_out is the last before the grid's exit, so no axis steps past its last
+  // plane.
+  int kpx = X.kn, kpy = w.poff1 + Y.kn, kpz = w.poff2 + Z.kn;
   float hx = X.hi, hy = Y.hi, hz = Z.hi;
   float amin = a_start;
-  const int ox = (X.step > 0 ? 1 : 0) + w.bx0;  // column = (kn_x - ox, kn_y - oy)
-  const int oy = (Y.step > 0 ? 1 : 0) + w.by0;
-  const int oz = Z.step > 0 ? 1 : 0;            // z cell = kn_z - oz
-  Col col = load_col(w, knx - ox, kny - oy);
+  const int ox = (X.step > 0 ? 1 : 0) + w.bx0;  // column = (kp_x - ox, kp_y - oy)
+  const int oy = w.poff1 + (Y.step > 0 ? 1 : 0) + w.by0;
+  const int oz = w.poff2 + (Z.step > 0 ? 1 : 0);  // z cell = kp_z - oz
+  Col col = load_col(w, kpx - ox, kpy - oy);
   // chord units = RN((amax - amin) * L) * 2^s = RN((amax - amin) * (L * 2^s)):
   // scaling by a power of two is exact
   const float Ls = fmul(L, G.fx_scale);
@@ -350,7 +354,7 @@ __device__ __forceinline__ void walk_ray(const Geo& G, const float* ray, const W
       // cell of the previous piece) adds to the trash cell, a hit outside
       // the window adds one to the outside cell's count.
       const bool add = amin < amax && amin >= a_lo;  // before a_lo: previous piece
-      const unsigned dz = (unsigned)(knz - oz - col.zlo);
+      const unsigned dz = (unsigned)(kpz - oz - col.zlo);
       const bool inwin = dz < (unsigned)col.zn;
       const int c = add ? (inwin ? col.off + (int)dz : w.trash_out) : w.trash;
       // units = RN_int(len * scale) (< 2^64 by the choice of scale), split as
@@ -367,26 +371,25 @@ __device__ __forceinline__ void walk_ray(const Geo& G, const float* ray, const W
       if (second) break;
       second = true;
       a_stop = a_start;
-      knx = eknx; kny = ekny; knz = eknz;
+      kpx = ekpx; kpy = ekpy; kpz = ekpz;
       hx = ehx; hy = ehy; hz = ehz;
       amin = eamin;
-      col = load_col(w, knx - ox, kny - oy);
+      col = load_col(w, kpx - ox, kpy - oy);
       continue;
     }
     // advance the axis whose plane comes first: its next plane's parameter
     // is the reference's quotient over the tabulated plane position
     const int st = mx ? X.step : (my ? Y.step : Z.step);
-    const int kn = (mx ? knx : (my ? kny : knz)) + st;
-    const int pb = mx ? 0 : (my ? w.poff1 : w.poff2);
-    const float P = w.planes[min((unsigned)(pb + kn), (unsigned)(w.nplanes - 1))];
+    const int kp = (mx ? kpx : (my ? kpy : kpz)) + st;
+    const float P = w.planes[kp];  // in the table or a guard entry
     const float r0 = mx ? X.r0 : (my ? Y.r0 : Z.r0), dr = mx ? X.dr : (my ? Y.dr : Z.dr);
     const float inv = mx ? X.inv : (my ? Y.inv : Z.inv);
     const float h = div_cr(fsub(P, r0), dr, inv);
-    hx = mx ? h : hx; knx = mx ? kn : knx;
-    hy = my ? h : hy; kny = my ? kn : kny;
-    hz = mz ? h : hz; knz = mz ? kn : knz;
+    hx = mx ? h : hx; kpx = mx ? kp : kpx;
+    hy = my ? h : hy; kpy = my ? kp : kpy;
+    hz = mz ? h : hz; kpz = mz ? kp : kpz;
     amin = amax;
-    col = load_col(w, knx - ox, kny - oy);
+    col = load_col(w, kpx - ox, kpy - oy);
   }
 }
 
@@ -547,12 +550,13 @@ k_walk(WalkArgs args) {
   win.by0 = s_box[2];
   win.wbx = s_box[1] >= s_box[0] ? s_box[1] - s_box[0] + 1 : 0;
   win.wby = s_box[3] >= s_box[2] ? s_box[3] - s_box[2] + 1 : 0;
-  const int A = win.wbx * win.wby;  // columns of the table
+  win.wbyp = win.wby + 1;
+  const int A = (win.wbx + 1) * win.wbyp;  // table entries (with the empty border)
   // z range of column k = (ix, iy): for x slabs the range of slab ix's
   // rectangle at iy; for z slabs the first and last slab whose rectangle
   // holds (ix, iy)
   auto col_range_scan = [&](int k, int* zlo, int* zhi) {  // z slabs, no storage
-    const int ix = win.bx0 + k / win.wby, iy = win.by0 + k % win.wby;
+    const int ix = win.bx0 + k / win.wbyp, iy = win.by0 + k % win.wbyp;
     int lo = INT_MAX, hi = INT_MIN;
     for (int iz = 0; iz < ns; iz++) {
       const Slab sl = slabs[iz];
@@ -565,9 +569,10 @@ k_walk(WalkArgs args) {
     *zhi = hi;
   };
   auto col_range_x = [&](int k, int* zlo, int* zhi) {  // x slabs
-    const int ix = win.bx0 + k / win.wby, iy = win.by0 + k % win.wby;
-    const Slab sl = slabs[ix];
-    if ((unsigned)(iy - sl.p0) < (unsigned)sl.wp) {
+    const int cx = k / win.wbyp, cy = k % win.wbyp;
+    const int ix = win.bx0 + cx, iy = win.by0 + cy;
+    const Slab sl = slabs[cx < win.wbx ? ix : win.bx0];  // the border column is empty
+    if (cx < win.wbx && cy < win.wby && (unsigned)(iy - sl.p0) < (unsigned)sl.wp) {
       *zlo = sl.q0;
       *zhi = sl.q0 + sl.wq - 1;
     } else {
@@ -587,12 +592,12 @@ k_walk(WalkArgs args) {
       if (zhi >= zlo) n += zhi - zlo + 1;
     }
     block_excl_scan(n, warp_tot, &s_total);
-    // + the empty column past the table and the two trash cells
-    if (threadIdx.x == 0) args.win_cells[row] = A + s_total + 3;
+    // + the two trash cells
+    if (threadIdx.x == 0) args.win_cells[row] = A + s_total + 2;
     return;
   }
   int2* cols = reinterpret_cast<int2*>(smem + lay.pool);
-  const bool table_fits = A + 1 <= args.cap_cells;
+  const bool table_fits = A <= args.cap_cells;
   if (table_fits) {
     if (sa == 0) {
       for (int k = kbeg; k < kend; k++) {
@@ -622,7 +627,7 @@ k_walk(WalkArgs args) {
             jp = 0;
             jq = 0;
           }
-          const int k = (sl.p0 + jp - win.bx0) * win.wby + (sl.q0 + jq - win.by0);
+          const int k = (sl.p0 + jp - win.bx0) * win.wbyp + (sl.q0 + jq - win.by0);
           atomicMin(&cols[k].x, iz);
           atomicMax(&cols[k].y, iz);
           if (++jq == sl.wq) {
@@ -641,7 +646,7 @@ k_walk(WalkArgs args) {
       if (cols[k].y >= cols[k].x) n_mine += cols[k].y - cols[k].x + 1;
   const int cexcl = block_excl_scan(n_mine, warp_tot, &s_total);
   const int W = s_total;  // window cells
-  if (!table_fits || A + W + 3 > args.cap_cells) {
+  if (!table_fits || A + W + 2 > args.cap_cells) {
     if (threadIdx.x == 0) {
       int k = atomicAdd(args.overflow_count, 1);
       args.overflow_rows[k] = (int32_t)row;
@@ -661,19 +666,18 @@ k_walk(WalkArgs args) {
       }
     }
   }
-  if (threadIdx.x == 0) cols[A] = make_int2(0, 0);  // stands for the columns outside the box
   win.cols = cols;
-  // 8(A + 1) + 8(W + 2) <= pool
-  win.lo = reinterpret_cast<uint32_t*>(smem + lay.pool + (size_t)(A + 1) * 8);
+  // 8A + 8(W + 2) <= pool
+  win.lo = reinterpret_cast<uint32_t*>(smem + lay.pool + (size_t)A * 8);
   win.hi = win.lo + W + 2;
   win.trash = W;
   win.trash_out = W + 1;
   // grid planes o + k d of the three axes (the walk's quotients read them)
-  float* planes = reinterpret_cast<float*>(smem + lay.planes);
+  float* planes = reinterpret_cast<float*>(smem + lay.planes) + 1;  // guards at -1 and nplanes
   win.planes = planes;
   win.poff1 = g.n[0] + 1;
   win.poff2 = g.n[0] + g.n[1] + 2;
-  win.nplanes = nplanes;
+  if (threadIdx.x == 0) planes[-1] = planes[nplanes] = 0.f;
   for (int i = threadIdx.x; i < nplanes; i += kWalkThreads) {
     const int a = i < win.poff1 ? 0 : (i < win.poff2 ? 1 : 2);
     planes[i] = voxel_plane(g, a, i - (a == 0 ? 0 : (a == 1 ? win.poff1 : win.poff2)));
@@ -759,14 +763,14 @@ k_walk(WalkArgs args) {
     int k = lo_k;
     int2 e = cols[k];
     int zhi = (e.y & 0xffff) + (e.y >> 16) - 1;
-    int cx = k / win.wby, cy = k - cx * win.wby;
+    int cx = k / win.wbyp, cy = k - cx * win.wbyp;
     int iz = (e.y & 0xffff) + (cbeg - e.x);
     fcol(win.bx0 + cx, win.by0 + cy);
     for (int cidx = cbeg; cidx < cend; cidx++) {
       if (iz > zhi) {
         do {  // next non-empty column
           ++k;
-          if (++cy == win.wby) {
+          if (++cy == win.wbyp) {
             cy = 0;
             ++cx;
           }
