@@ -183,8 +183,7 @@ __device__ void slab_window(const Geo& G, const float (*c0)[3], const float (*c1
 // neither half can overflow.  The total (hi_sum << fx_split) + lo_sum is
 // exact and independent of the order of the adds.
 struct Window {
-  uint32_t* lo;
-  uint32_t* hi;
+  uint2* cell;  // per cell {lo, hi} sum words
   // per column: {first cell, zlo | zn << 16}; empty: zn 0.  The table has
   // (wbx + 1) x (wby + 1) entries (row stride wbyp = wby + 1): the last
   // column of each row and the last row are empty and stand for every
@@ -345,10 +344,11 @@ __device__ __forceinline__ void walk_ray(const Geo& G, const float* ray, const W
   const int budget = g.n[0] + g.n[1] + g.n[2] + 4;
   for (int steps = 0; steps < budget; steps++) {
     if (!(amin < a_stop)) break;
-    const bool mx = hx <= hy && hx <= hz;
-    const bool my = !mx && hy <= hz;
+    // the axis whose plane comes first (ties: x, then y, then z)
+    const float amax = fminf(fminf(hx, hy), hz);
+    const bool mx = hx == amax;
+    const bool my = !mx && hy == amax;
     const bool mz = !mx && !my;
-    const float amax = mx ? hx : (my ? hy : hz);
     {
       // Branch-free add: a step with nothing to add (a zero-length cell, a
       // cell of the previous piece) adds to the trash cell, a hit outside
@@ -357,14 +357,13 @@ __device__ __forceinline__ void walk_ray(const Geo& G, const float* ray, const W
       const unsigned dz = (unsigned)(kpz - oz - col.zlo);
       const bool inwin = dz < (unsigned)col.zn;
       const int c = add ? (inwin ? col.off + (int)dz : w.trash_out) : w.trash;
-      // units = RN_int(len * scale) (< 2^64 by the choice of scale), split as
-      // hi * 2^split + lo
-      const unsigned long long u = __float2ull_rn(fmul(fsub(amax, amin), Ls));
+      // units = RN_int(max(len * scale, 1)) (< 2^64 by the choice of scale:
+      // a positive chord counts at least one unit), split as hi * 2^split + lo
+      const unsigned long long u = __float2ull_rn(fmaxf(fmul(fsub(amax, amin), Ls), 1.f));
       const uint32_t h = (uint32_t)(u >> w.split);
-      uint32_t l = (uint32_t)u & lo_mask;
-      l = (u == 0ull || !inwin) ? 1u : l;  // a positive chord counts at least one unit
-      atomicAdd(&w.lo[c], l);
-      atomicAdd(&w.hi[c], h);
+      const uint32_t l = inwin ? (uint32_t)u & lo_mask : 1u;
+      atomicAdd(&w.cell[c].x, l);
+      atomicAdd(&w.cell[c].y, h);
     }
     if (amax >= a_out) {
       // last cell: the part before the starting cell, if any
@@ -668,8 +667,7 @@ k_walk(WalkArgs args) {
   }
   win.cols = cols;
   // 8A + 8(W + 2) <= pool
-  win.lo = reinterpret_cast<uint32_t*>(smem + lay.pool + (size_t)A * 8);
-  win.hi = win.lo + W + 2;
+  win.cell = reinterpret_cast<uint2*>(smem + lay.pool + (size_t)A * 8);
   win.trash = W;
   win.trash_out = W + 1;
   // grid planes o + k d of the three axes (the walk's quotients read them)
@@ -691,8 +689,7 @@ k_walk(WalkArgs args) {
   }
   // ---- zero the window, walk the rays
   for (int i = threadIdx.x; i <= W + 1; i += kWalkThreads) {  // the window and the trash cells
-    win.lo[i] = 0u;
-    win.hi[i] = 0u;
+    win.cell[i] = make_uint2(0u, 0u);
   }
   __syncthreads();
   const int R = G.p.nrays;
@@ -735,7 +732,7 @@ k_walk(WalkArgs args) {
     }
   }
   __syncthreads();
-  if (threadIdx.x == 0 && win.lo[win.trash_out] != 0u) atomicAdd(args.hit_outside, 1);
+  if (threadIdx.x == 0 && win.cell[win.trash_out].x != 0u) atomicAdd(args.hit_outside, 1);
   if (s_exact) {  // uniform across the block
     if (threadIdx.x == 0) {
       int k = atomicAdd(args.exact_count, 1);
@@ -807,8 +804,8 @@ k_walk(WalkArgs args) {
         colvox = ix * G.nyz + iy * g.n[2];
       },
       [&](int cidx, int ix, int iy, int iz) {
-    const unsigned long long u =
-        ((unsigned long long)win.hi[cidx] << win.split) + (unsigned long long)win.lo[cidx];
+    const uint2 cu = win.cell[cidx];
+    const unsigned long long u = ((unsigned long long)cu.y << win.split) + (unsigned long long)cu.x;
     const float2 zt = ztab[iz];
     const float c0 = fsub(zt.x, K0), c1 = fsub(K1, zt.y);
     // not a candidate: dropped
@@ -818,8 +815,7 @@ k_walk(WalkArgs args) {
     if (kMode == kModeCsr) {
       // kept entries compacted at the start of the thread's range: the slot
       // written is this cell's or an earlier one, already read
-      win.hi[cbeg + cnt] = (uint32_t)(colvox + iz);
-      win.lo[cbeg + cnt] = __float_as_uint(v);
+      win.cell[cbeg + cnt] = make_uint2(__float_as_uint(v), (uint32_t)(colvox + iz));
     }
     cnt += keep ? 1 : 0;
     if (kMode != kModeCsr && keep) {
@@ -836,8 +832,9 @@ k_walk(WalkArgs args) {
     const int pos = block_excl_scan(cnt, warp_tot, &s_total);
     const int64_t o = slot * args.stride + pos;
     for (int j = 0; j < cnt; j++) {
-      args.stage_col[o + j] = (int32_t)win.hi[cbeg + j];
-      args.stage_val[o + j] = __uint_as_float(win.lo[cbeg + j]);
+      const uint2 e = win.cell[cbeg + j];
+      args.stage_col[o + j] = (int32_t)e.y;
+      args.stage_val[o + j] = __uint_as_float(e.x);
     }
     if (threadIdx.x == 0) {
       args.row_len[row] = s_total;
