@@ -292,7 +292,10 @@ __device__ __forceinline__ void walk_ray(const Geo& G, const float* ray, const W
   }
   if (!(a_in < a_out)) return;
   const float span = fsub(a_out, a_in);
-  float a_s, a_lo = -INFINITY, a_stop = INFINITY;
+  // a_lim: the walk stops after the cell whose exit parameter reaches it
+  // (the grid's exit, the piece's end, or after the wrap the start cell's
+  // entry)
+  float a_s, a_lo = -INFINITY, a_lim = a_out;
   // entry state of the second part: plane indices, their parameters, and
   // the entry parameter of the grid's first cell
   int ekpx = 0, ekpy = 0, ekpz = 0;
@@ -300,9 +303,9 @@ __device__ __forceinline__ void walk_ray(const Geo& G, const float* ray, const W
   bool second;
   if (npieces > 1) {
     if (piece > 0) a_lo = fadd(a_in, fmul(span, (float)piece / (float)npieces));
-    if (piece + 1 < npieces) a_stop = fadd(a_in, fmul(span, (float)(piece + 1) / (float)npieces));
+    if (piece + 1 < npieces) a_lim = fadd(a_in, fmul(span, (float)(piece + 1) / (float)npieces));
     a_s = piece > 0 ? a_lo : a_in;
-    if (!(a_s < a_out)) return;
+    if (!(a_s < a_out) || !(a_lo < a_lim)) return;  // an empty piece (rounding)
     second = true;  // no wrap
   } else {
     a_s = a_in + span * frac;
@@ -343,7 +346,6 @@ __device__ __forceinline__ void walk_ray(const Geo& G, const float* ray, const W
   const uint32_t lo_mask = (1u << w.split) - 1u;
   const int budget = g.n[0] + g.n[1] + g.n[2] + 4;
   for (int steps = 0; steps < budget; steps++) {
-    if (!(amin < a_stop)) break;
     // the axis whose plane comes first (ties: x, then y, then z)
     const float amax = fminf(fminf(hx, hy), hz);
     const bool mx = hx == amax;
@@ -365,11 +367,11 @@ __device__ __forceinline__ void walk_ray(const Geo& G, const float* ray, const W
       atomicAdd(&w.cell[c].x, l);
       atomicAdd(&w.cell[c].y, h);
     }
-    if (amax >= a_out) {
+    if (amax >= a_lim) {
       // last cell: the part before the starting cell, if any
-      if (second) break;
+      if (second || !(eamin < a_start)) break;
       second = true;
-      a_stop = a_start;
+      a_lim = a_start;
       kpx = ekpx; kpy = ekpy; kpz = ekpz;
       hx = ehx; hy = ehy; hz = ehz;
       amin = eamin;
