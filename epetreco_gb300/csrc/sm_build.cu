@@ -223,9 +223,10 @@ struct WalkAxis {
   __device__ __forceinline__ float alpha(float k) const {
     return div_cr(fsub(fadd(o, fmul(k, d)), r0), dr, inv);
   }
-  // cell with lo <= a < hi (a inside the axis' grid range)
+  // cell with lo <= a < hi (a inside the axis' grid range); the first
+  // guess only starts the search, which corrects it either way
   __device__ __forceinline__ void enter(float a) {
-    int i = clampi((int)floorf((r0 + a * dr - o) / d), 0, n - 1);
+    int i = clampi((int)floorf(__fdividef(r0 + a * dr - o, d)), 0, n - 1);
     if (step > 0) {  // interval of cell i: [alpha(i), alpha(i+1)]
       while (i > 0 && alpha((float)i) > a) i--;
       while (i < n - 1 && alpha((float)(i + 1)) <= a) i++;
