@@ -375,6 +375,14 @@ def trim_memory(keep_bytes: int = 0) -> None:
     check(lib().epet_trim_memory(int(keep_bytes)))
 
 
+def build_counters() -> dict:
+    """Rows of system-matrix builds since load that were redone with their
+    exact window size, and rows on the per-candidate path."""
+    o, e = C.c_int64(0), C.c_int64(0)
+    check(lib().epet_build_counters(C.byref(o), C.byref(e)))
+    return {"overflow_rows": o.value, "exact_rows": e.value}
+
+
 class Mlem:
     """One reconstruction on the device (reco.cu's loop): the system matrix
     of the measured rows is built once at construction.  The rows may come in

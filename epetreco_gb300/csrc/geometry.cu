@@ -185,6 +185,12 @@ using namespace epet;
 
 extern "C" {
 
+epet_status epet_build_counters(int64_t* overflow_rows_h, int64_t* exact_rows_h) {
+  if (overflow_rows_h) *overflow_rows_h = overflow_rows_total();
+  if (exact_rows_h) *exact_rows_h = exact_rows_total();
+  return EPET_OK;
+}
+
 epet_status epet_selftest_division(int64_t n, uint64_t seed, int64_t* mismatches_h,
                                    epet_stream_t stream) {
   if (n < 0 || !mismatches_h) return set_error(EPET_ERR_INVALID, "bad arguments");

@@ -20,6 +20,7 @@ size_t radix_hist_elems(int64_t n);
 // Row walk configuration chosen for a problem (per-row accumulator size).
 int auto_row_capacity(const epet_problem& p);
 int64_t exact_rows_total();
+int64_t overflow_rows_total();
 
 // Candidate compaction and per-candidate values (workqueue.cu).
 epet_status launch_workqueue_count(const Geo& G, const int32_t* rows, int64_t m,

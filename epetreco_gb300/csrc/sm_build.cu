@@ -1002,6 +1002,7 @@ int auto_row_capacity(const epet_problem& p) {
 static int64_t n_exact_rows_ = 0;
 static int64_t n_overflow_rows_ = 0;
 int64_t exact_rows_total() { return n_exact_rows_; }
+int64_t overflow_rows_total() { return n_overflow_rows_; }
 
 // Generic driver: runs mode kMode over all rows in chunks.  For kModeCsr the
 // rows are staged and gathered into out (capacity cap).

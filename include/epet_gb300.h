@@ -132,6 +132,11 @@ epet_status epet_trig_table(const epet_problem* p, float* sc_d,
  * getSystemMatrixFromWorkqueue.cu:189-204). */
 epet_status epet_dump_uniforms(const epet_problem* p, const int32_t* rows_d,
                                int64_t m, float* out_d, epet_stream_t stream);
+/* Diagnostics (no counterpart in the reference): rows of system-matrix builds
+ * since the library was loaded whose window exceeded the shared-memory
+ * capacity and were redone with their exact size, and rows handed to the
+ * per-candidate path (a ray with two equal coordinates). */
+epet_status epet_build_counters(int64_t* overflow_rows_h, int64_t* exact_rows_h);
 /* Library self-test (no counterpart in the reference): compares the walk
  * kernel's reciprocal-based correctly rounded division with the hardware's
  * IEEE division on n seeded operand pairs; *mismatches_h counts differing
