@@ -337,6 +337,9 @@ __device__ __forceinline__ void walk_ray(const Geo& G, const float* ray, const W
   int kpx = X.kn, kpy = w.poff1 + Y.kn, kpz = w.poff2 + Z.kn;
   float hx = X.hi, hy = Y.hi, hz = Z.hi;
   float amin = a_start;
+  // a piece's first cell entered before a_lo is the previous piece's: walked
+  // as a zero-length cell (every later cell is entered at or after a_lo)
+  if (amin < a_lo) amin = fminf(fminf(hx, hy), hz);
   const int ox = (X.step > 0 ? 1 : 0) + w.bx0;  // column = (kp_x - ox, kp_y - oy)
   const int oy = w.poff1 + (Y.step > 0 ? 1 : 0) + w.by0;
   const int oz = w.poff2 + (Z.step > 0 ? 1 : 0);  // z cell = kp_z - oz
@@ -353,10 +356,10 @@ __device__ __forceinline__ void walk_ray(const Geo& G, const float* ray, const W
     const bool my = !mx && hy == amax;
     const bool mz = !mx && !my;
     {
-      // Branch-free add: a step with nothing to add (a zero-length cell, a
-      // cell of the previous piece) adds to the trash cell, a hit outside
-      // the window adds one to the outside cell's count.
-      const bool add = amin < amax && amin >= a_lo;  // before a_lo: previous piece
+      // Branch-free add: a step with nothing to add (a zero-length cell, the
+      // previous piece's cell) adds to the trash cell, a hit outside the
+      // window adds one to the outside cell's count.
+      const bool add = amin < amax;
       const unsigned dz = (unsigned)(kpz - oz - col.zlo);
       const bool inwin = dz < (unsigned)col.zn;
       const int c = add ? (inwin ? col.off + (int)dz : w.trash_out) : w.trash;
