@@ -216,28 +216,29 @@ __device__ __forceinline__ Col load_col(const Window& w, int cx, int cy) {
 // One axis of a ray walk: the ray's parameter at grid plane k is the
 // reference's quotient (plane_k - r0)/(r1 - r0), correctly rounded.
 struct WalkAxis {
-  float o, d, r0, dr, inv;  // plane k at o + k*d; ray at r0 + a*dr; inv = RN(1/dr)
+  const float* P;           // plane positions o + k*d, k = 0..n (the shared table)
+  float o, d, r0, dr, inv;  // ray at r0 + a*dr; inv = RN(1/dr)
   int n, step;
   float lo, hi;  // parameter interval of the current cell along this axis
-  int kn;        // index of the plane at hi (idx + 1 ascending, idx descending)
-  __device__ __forceinline__ float alpha(float k) const {
-    return div_cr(fsub(fadd(o, fmul(k, d)), r0), dr, inv);
-  }
+  int kn;        // index of the plane at hi (cell + 1 ascending, cell descending)
+  __device__ __forceinline__ float alpha(int k) const { return div_cr(fsub(P[k], r0), dr, inv); }
   // cell with lo <= a < hi (a inside the axis' grid range); the first
-  // guess only starts the search, which corrects it either way
+  // guess only starts the search, which corrects it either way; the
+  // parameters of the cell's two planes are carried along the search
   __device__ __forceinline__ void enter(float a) {
     int i = clampi((int)floorf(__fdividef(r0 + a * dr - o, d)), 0, n - 1);
+    float ai = alpha(i), ai1 = alpha(i + 1);
     if (step > 0) {  // interval of cell i: [alpha(i), alpha(i+1)]
-      while (i > 0 && alpha((float)i) > a) i--;
-      while (i < n - 1 && alpha((float)(i + 1)) <= a) i++;
-      lo = alpha((float)i);
-      hi = alpha((float)(i + 1));
+      while (i > 0 && ai > a) { i--; ai1 = ai; ai = alpha(i); }
+      while (i < n - 1 && ai1 <= a) { i++; ai = ai1; ai1 = alpha(i + 1); }
+      lo = ai;
+      hi = ai1;
       kn = i + 1;
     } else {         // interval of cell i: [alpha(i+1), alpha(i)]
-      while (i < n - 1 && alpha((float)(i + 1)) > a) i++;
-      while (i > 0 && alpha((float)i) <= a) i--;
-      lo = alpha((float)(i + 1));
-      hi = alpha((float)i);
+      while (i < n - 1 && ai1 > a) { i++; ai = ai1; ai1 = alpha(i + 1); }
+      while (i > 0 && ai <= a) { i--; ai1 = ai; ai = alpha(i); }
+      lo = ai1;
+      hi = ai;
       kn = i;
     }
   }
@@ -272,6 +273,7 @@ __device__ __forceinline__ void walk_ray(const Geo& G, const float* ray, const W
     return;
   }
   WalkAxis X, Y, Z;
+  X.P = w.planes; Y.P = w.planes + w.poff1; Z.P = w.planes + w.poff2;
   X.o = g.o[0]; X.d = g.d[0]; X.r0 = ray[0]; X.dr = fsub(ray[3], ray[0]); X.n = g.n[0];
   Y.o = g.o[1]; Y.d = g.d[1]; Y.r0 = ray[1]; Y.dr = fsub(ray[4], ray[1]); Y.n = g.n[1];
   Z.o = g.o[2]; Z.d = g.d[2]; Z.r0 = ray[2]; Z.dr = fsub(ray[5], ray[2]); Z.n = g.n[2];
@@ -285,9 +287,9 @@ __device__ __forceinline__ void walk_ray(const Geo& G, const float* ray, const W
   // grid parameter range
   float a_in, a_out;
   {
-    const float x0 = X.alpha(0.f), x1 = X.alpha((float)X.n);
-    const float y0 = Y.alpha(0.f), y1 = Y.alpha((float)Y.n);
-    const float z0 = Z.alpha(0.f), z1 = Z.alpha((float)Z.n);
+    const float x0 = X.alpha(0), x1 = X.alpha(X.n);
+    const float y0 = Y.alpha(0), y1 = Y.alpha(Y.n);
+    const float z0 = Z.alpha(0), z1 = Z.alpha(Z.n);
     a_in = fmaxf(fmaxf(fminf(x0, x1), fminf(y0, y1)), fminf(z0, z1));
     a_out = fminf(fminf(fmaxf(x0, x1), fmaxf(y0, y1)), fmaxf(z0, z1));
   }
