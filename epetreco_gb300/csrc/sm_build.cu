@@ -84,14 +84,19 @@ struct WalkArgs {
 struct WalkLayout {
   size_t pext, planes, ztab, pool, total;
 };
-// nplanes: grid planes of all three axes (n0 + n1 + n2 + 3); nz: z cells
+// nplanes: grid planes of all three axes (n0 + n1 + n2 + 3); nz: z cells.
+// The hull extents at the slab planes (pext) are read only while the slab
+// windows are built, before the column table and the cells are written, so
+// they share the start of the pool.
 __host__ __device__ inline WalkLayout walk_layout(int nslab, int nplanes, int nz, int cap_cells) {
   WalkLayout L;
-  L.pext = align256((size_t)20 * nslab);  // Slab[nslab]
-  L.planes = L.pext + align256((size_t)(nslab + 1) * 16);
+  L.planes = align256((size_t)20 * nslab);  // Slab[nslab] first
   L.ztab = L.planes + align256((size_t)(nplanes + 2) * 4);  // + a guard entry at each end
   L.pool = L.ztab + align256((size_t)nz * 8);
-  L.total = L.pool + align256((size_t)cap_cells * 8);
+  L.pext = L.pool;
+  const size_t pool = (size_t)cap_cells * 8 > (size_t)(nslab + 1) * 16 ? (size_t)cap_cells * 8
+                                                                       : (size_t)(nslab + 1) * 16;
+  L.total = L.pool + align256(pool);
   return L;
 }
 
@@ -994,7 +999,28 @@ static epet_status sample_capacity(const Geo& G, cudaStream_t st, int* cap_out) 
   // exact size (redo_overflow).
   std::sort(cells.begin(), cells.end());
   const int p90 = cells.empty() ? 0 : cells[(cells.size() * 9) / 10];
-  *cap_out = std::max(256, (int)(p90 * 1.10) + 64);
+  int cap = std::max(256, (int)(p90 * 1.10) + 64);
+  // If a capacity at most 15 % smaller keeps one more CTA resident per SM,
+  // take the largest such: the occupancy gain outweighs the few more rows
+  // redone.
+  auto resident = [&](int c) {
+    int n = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_walk<kModeCsr>, kWalkThreads,
+                                                      walk_smem(G, c)) != cudaSuccess)
+      n = 0;
+    return n;
+  };
+  const int n0 = resident(cap), lo = std::max(256, (int)(cap * 0.85));
+  if (n0 > 0 && resident(lo) > n0) {
+    int a = lo, b = cap;  // resident(a) > n0 >= resident(b)
+    while (b - a > 1) {
+      const int mid = (a + b) / 2;
+      if (resident(mid) > n0) a = mid;
+      else b = mid;
+    }
+    cap = a;
+  }
+  *cap_out = cap;
   return EPET_OK;
 }
 
