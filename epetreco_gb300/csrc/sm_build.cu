@@ -500,15 +500,36 @@ k_walk(WalkArgs args) {
       dy[q] = c1[b][pa] - ay[q];
       dz[q] = c1[b][qa] - az[q];
     }
+    // t is monotone in the plane position: when every line meets the first
+    // and the last plane within its segment it meets all of them (the usual
+    // case, the grid lying between the heads), and the per-plane tests drop
+    bool span = true;
+    {
+      const float X0 = voxel_plane(g, sa, 0), X1 = voxel_plane(g, sa, ns);
+      for (int q = 0; q < 2; q++) {
+        const float t0 = (X0 - ax[q]) * inv[q], t1 = (X1 - ax[q]) * inv[q];
+        span = span && ok[q] && t0 >= 0.f && t0 <= 1.f && t1 >= 0.f && t1 <= 1.f;
+      }
+    }
+    const bool all_span = __all_sync(0xffffffffu, span);
     for (int k = w; k <= ns; k += kWalkThreads / 32) {
       const float X = voxel_plane(g, sa, k);
       int ylo = INT_MAX, yhi = INT_MIN, zlo = INT_MAX, zhi = INT_MIN;
-      for (int q = 0; q < 2; q++) {
-        const float t = (X - ax[q]) * inv[q];
-        if (ok[q] && t >= 0.f && t <= 1.f) {
+      if (all_span) {
+        for (int q = 0; q < 2; q++) {
+          const float t = (X - ax[q]) * inv[q];
           const int ky = fkey(ay[q] + t * dy[q]), kz = fkey(az[q] + t * dz[q]);
           ylo = min(ylo, ky); yhi = max(yhi, ky);
           zlo = min(zlo, kz); zhi = max(zhi, kz);
+        }
+      } else {
+        for (int q = 0; q < 2; q++) {
+          const float t = (X - ax[q]) * inv[q];
+          if (ok[q] && t >= 0.f && t <= 1.f) {
+            const int ky = fkey(ay[q] + t * dy[q]), kz = fkey(az[q] + t * dz[q]);
+            ylo = min(ylo, ky); yhi = max(yhi, ky);
+            zlo = min(zlo, kz); zhi = max(zhi, kz);
+          }
         }
       }
       ylo = __reduce_min_sync(0xffffffffu, ylo);
