@@ -82,21 +82,27 @@ struct WalkArgs {
 // two 32-bit sum words of every window cell (8 bytes per cell): a channel
 // needs columns + cells <= cap_cells.
 struct WalkLayout {
-  size_t pext, planes, ztab, pool, total;
+  size_t planes, ztab, pool, pext, slabs, total;
 };
 // nplanes: grid planes of all three axes (n0 + n1 + n2 + 3); nz: z cells.
-// The hull extents at the slab planes (pext) are read only while the slab
-// windows are built, before the column table and the cells are written, so
-// they share the start of the pool.
+// The pool holds the column table and the cells.  Two arrays that die early
+// share it: the hull extents at the slab planes (pext, at its start) are
+// read only while the slab windows are built, and the slab windows (slabs,
+// at its end) only until the column table is built, so the table must end
+// before them and the cells, written afterwards, may run over them.
 __host__ __device__ inline WalkLayout walk_layout(int nslab, int nplanes, int nz, int cap_cells) {
   WalkLayout L;
-  L.planes = align256((size_t)20 * nslab);  // Slab[nslab] first
+  L.planes = 0;
   L.ztab = L.planes + align256((size_t)(nplanes + 2) * 4);  // + a guard entry at each end
   L.pool = L.ztab + align256((size_t)nz * 8);
+  const size_t pext_b = ((size_t)(nslab + 1) * 16 + 15) & ~size_t(15);
+  const size_t slab_b = ((size_t)20 * nslab + 15) & ~size_t(15);
+  size_t pool_b = (size_t)cap_cells * 8;
+  if (pool_b < pext_b + slab_b) pool_b = pext_b + slab_b;
+  pool_b = (pool_b + 15) & ~size_t(15);
   L.pext = L.pool;
-  const size_t pool = (size_t)cap_cells * 8 > (size_t)(nslab + 1) * 16 ? (size_t)cap_cells * 8
-                                                                       : (size_t)(nslab + 1) * 16;
-  L.total = L.pool + align256(pool);
+  L.slabs = L.pool + pool_b - slab_b;
+  L.total = L.pool + align256(pool_b);
   return L;
 }
 
@@ -451,9 +457,9 @@ k_walk(WalkArgs args) {
   const Geo& G = args.G;
   const epet_grid& g = G.p.grid;
   const int nx = g.n[0];
-  Slab* slabs = reinterpret_cast<Slab*>(smem);
   const int nplanes = g.n[0] + g.n[1] + g.n[2] + 3;
   const WalkLayout lay = walk_layout(max(g.n[0], g.n[2]), nplanes, g.n[2], args.cap_cells);
+  Slab* slabs = reinterpret_cast<Slab*>(smem + lay.slabs);
   Window win;
   win.split = G.fx_split;
   __shared__ __align__(16) float s_geom[kGeomFloats];
@@ -630,7 +636,7 @@ k_walk(WalkArgs args) {
     return;
   }
   int2* cols = reinterpret_cast<int2*>(smem + lay.pool);
-  const bool table_fits = A <= args.cap_cells;
+  const bool table_fits = (size_t)A * 8 <= lay.slabs - lay.pool;  // ends before the slabs
   if (table_fits) {
     if (sa == 0) {
       for (int k = kbeg; k < kend; k++) {
