@@ -76,11 +76,12 @@ struct WalkArgs {
   int32_t* ovf_idx;
 };
 
-// Dynamic shared memory of the walk kernel; every section starts on a
-// 256-byte boundary (the plane extents are int4).  The pool holds, per
-// channel, the window's column table (8 bytes per column) followed by the
-// two 32-bit sum words of every window cell (8 bytes per cell): a channel
-// needs columns + cells <= cap_cells.
+// Dynamic shared memory of the walk kernel: the grid-plane table, the per-row
+// z terms of the candidate test and the pool, each on a 256-byte boundary.
+// The pool holds, per channel, the window's column table (8 bytes per
+// column, border included) followed by the two 32-bit sum words of every
+// window cell and of the two trash cells (8 bytes per cell): a channel needs
+// columns + cells + 2 <= cap_cells.
 struct WalkLayout {
   size_t planes, ztab, pool, pext, slabs, total;
 };
