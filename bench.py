@@ -158,6 +158,17 @@ def cpu_baseline(cfg_name: str, sample: int, seed: int = 0):
             "sample_seconds": dt}
 
 
+def aggregate_replicas(times, nit, world, dist, device):
+    """Replicas (every rank ran the same workload): each time is the max over
+    ranks, and the whole-job rate is world * nit / that time."""
+    import torch
+    vals = torch.tensor([float(t) for t in times], device=device, dtype=torch.float64)
+    if dist is not None:
+        dist.all_reduce(vals, op=dist.ReduceOp.MAX)
+    tmax = [float(v) for v in vals]
+    return tmax, [world * nit / t for t in tmax]
+
+
 def reference_arm(args):
     """--impl reference: the reference's CPU work for the path (oracle port;
     the reference's own sources do not exist on the GPU machine)."""
@@ -497,15 +508,12 @@ def gb300_arm(args):
         batched_small = batch_measure(args, api, torch, st, grids=(24, 32), angles=(8,))
 
     # ---- aggregate over ranks
-    vals = torch.tensor([t_step, t_e2e], device="cuda", dtype=torch.float64)
-    if dist is not None:
-        dist.all_reduce(vals, op=dist.ReduceOp.MAX)
-    t_step, t_e2e = float(vals[0]), float(vals[1])
+    (t_step, t_e2e), (value, value_e2e) = aggregate_replicas((t_step, t_e2e), nit, world, dist,
+                                                            "cuda")
     if rank != 0:
         if dist is not None:
             dist.destroy_process_group()
         return
-    value = world * nit / t_step
     cpu = None
     if not args.no_cpu_baseline and world == 1:
         cpu = cpu_baseline(args.config, args.cpu_sample)
@@ -521,7 +529,7 @@ def gb300_arm(args):
                                 f"matrix built once per step"),
                    "measured_rows": m, "nnz": nnz, "parallelism": f"replicas{world}",
                    "l2": "inputs larger than L2 (matrix streams of GBs per pass)"},
-        "e2e": {"value": world * nit / t_e2e, "unit": UNIT, "h2d_bytes_per_step": h2d,
+        "e2e": {"value": value_e2e, "unit": UNIT, "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h},
         "gpu_launches": int(launches),
         "clocks": clocks,
