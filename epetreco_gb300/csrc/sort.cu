@@ -8,6 +8,7 @@
 // packed (row, col) key, stable within each tile by warp-ordered ranking
 // (__match_any_sync), a histogram+scan row pointer, and one gather kernel.
 #include <algorithm>
+#include <type_traits>
 #include <mutex>
 
 #include "common.cuh"
@@ -257,7 +258,21 @@ k_radix_scatter(In in, Out out, int64_t n, int shift, int64_t tpc, int nchunks,
       const int64_t i = wbase + r * 32 + lane;
       const bool ok = i < n;
       const unsigned dig = ok ? ((unsigned)(kk[r] >> shift) & (BINS - 1)) : BINS + lane;
-      const unsigned peers = __match_any_sync(0xffffffffu, dig);
+      unsigned peers;
+      if constexpr (std::is_same<In, CsrIn>::value) {
+        // rows of a CSR: consecutive columns, up to 32 distinct digits per
+        // round, where one ballot per digit bit is cheaper than a match
+        peers = __ballot_sync(0xffffffffu, ok);
+        peers = ok ? peers : (1u << lane);
+#pragma unroll
+        for (int b = 0; b < BITS; b++) {
+          const bool bit = (dig >> b) & 1u;
+          const unsigned bal = __ballot_sync(0xffffffffu, bit);
+          peers &= bit ? bal : ~bal;
+        }
+      } else {
+        peers = __match_any_sync(0xffffffffu, dig);
+      }
       unsigned before = 0;
       if (ok) before = wcnt[w][dig];
       rank[r] = before + __popc(peers & lt);
