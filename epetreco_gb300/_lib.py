@@ -34,7 +34,8 @@ class Grid(C.Structure):
 
 
 class ProblemC(C.Structure):
-    _fields_ = [("setup", Setup), ("grid", Grid), ("nrays", C.c_int32), ("seed", C.c_uint64)]
+    _fields_ = [("setup", Setup), ("grid", Grid), ("nrays", C.c_int32),
+                ("ray_mode", C.c_int32), ("seed", C.c_uint64)]
 
 
 class CsrC(C.Structure):
@@ -163,4 +164,4 @@ def problem_struct(p) -> ProblemC:
                           s.segy, s.segz),
                     Grid((C.c_float * 3)(*g.origin), (C.c_float * 3)(*g.pitch),
                          (C.c_int32 * 3)(*g.n)),
-                    int(p.nrays), int(p.seed))
+                    int(p.nrays), int(p.ray_mode), int(p.seed))

@@ -32,7 +32,7 @@ def problem_vector(p: Problem) -> list:
     s, g = p.setup, p.grid
     return [float(v) for v in (s.pos0x, s.pos1x, s.na, s.n0z, s.n0y, s.n1z, s.n1y, s.da,
                                s.segx, s.segy, s.segz, *g.origin, *g.pitch, *g.n, p.nrays,
-                               p.seed)]
+                               p.seed, p.ray_mode)]
 
 
 class Projector:

@@ -82,8 +82,8 @@ class StoredProjection : public torch::autograd::Function<StoredProjection> {
 
 // Matrix-free: the problem as a flat float64 vector of its fields.
 epet_problem unpack(const std::vector<double>& f) {
-  TORCH_CHECK(f.size() == 22, "problem vector must hold 22 numbers");
-  epet_problem p;
+  TORCH_CHECK(f.size() == 23, "problem vector must hold 23 numbers");
+  epet_problem p{};
   p.setup = epet_setup{(float)f[0], (float)f[1], (int)f[2], (int)f[3], (int)f[4], (int)f[5],
                        (int)f[6], (float)f[7], (float)f[8], (float)f[9], (float)f[10]};
   p.grid = epet_grid{{(float)f[11], (float)f[12], (float)f[13]},
@@ -91,6 +91,7 @@ epet_problem unpack(const std::vector<double>& f) {
                      {(int)f[17], (int)f[18], (int)f[19]}};
   p.nrays = (int)f[20];
   p.seed = (uint64_t)f[21];
+  p.ray_mode = (int32_t)f[22];
   return p;
 }
 

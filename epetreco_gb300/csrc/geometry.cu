@@ -4,6 +4,9 @@
 // kernel: curand_init(seed, channel, 0) and six curand_uniform draws per ray,
 // the first three placing the start point in crystal 0 and the last three
 // the end point in crystal 1 (getSystemMatrixFromWorkqueue.cu:189-230).
+// With EPET_RAYS_REGULAR they follow ReguRayGen (RayGenerators.hpp:46-66):
+// the six box coordinates are 0.5, so every ray joins the crystal centres,
+// and no generator is seeded.
 #include <curand_kernel.h>
 
 #include "common.cuh"
@@ -16,12 +19,19 @@ __global__ void k_trig(epet_setup s, float* sc) {
   if (a < s.na) angle_sincos(s, a, &sc[2 * a], &sc[2 * a + 1]);
 }
 
+// Six box coordinates of one ray: cuRAND uniforms, or 0.5 each for regular rays.
+__device__ __forceinline__ void draw6(curandState& st, bool regular, float* u) {
+#pragma unroll
+  for (int k = 0; k < 6; k++) u[k] = regular ? 0.5f : curand_uniform(&st);
+}
+
 // One thread per channel: the cuRAND stream of a channel is sequential, so a
 // channel's 6*nrays draws stay on one thread; channels spread over threads.
 // The uniforms-only form (a test and debugging interface) seeds every
 // channel with curand_init(seed, channel, 0) directly.
 __device__ __forceinline__ void emit_rays(const Geo& G, int cnl, curandState st, bool uniforms,
                                           float2* o) {
+  const bool regular = G.p.ray_mode == EPET_RAYS_REGULAR;
   int id[5];
   channel_decode(G.p.setup, cnl, id);
   float sn, cs;
@@ -33,8 +43,7 @@ __device__ __forceinline__ void emit_rays(const Geo& G, int cnl, curandState st,
   const bool wide = (reinterpret_cast<uintptr_t>(o) & 15) == 0;
   for (int r = 0; r < G.p.nrays; r++) {
     float u[6];
-#pragma unroll
-    for (int k = 0; k < 6; k++) u[k] = curand_uniform(&st);
+    draw6(st, regular, u);
     float w[6];
     if (uniforms) {
 #pragma unroll
@@ -45,8 +54,7 @@ __device__ __forceinline__ void emit_rays(const Geo& G, int cnl, curandState st,
     }
     if (wide && r + 1 < G.p.nrays) {
       float u2[6], w2[6];
-#pragma unroll
-      for (int k = 0; k < 6; k++) u2[k] = curand_uniform(&st);
+      draw6(st, regular, u2);
       if (uniforms) {
 #pragma unroll
         for (int k = 0; k < 6; k++) w2[k] = u2[k];
@@ -71,8 +79,9 @@ __global__ void __launch_bounds__(128) k_uniforms(Geo G, const int32_t* __restri
                                                   int64_t m, float* __restrict__ out) {
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= m) return;
-  curandState st;
-  curand_init(G.p.seed, (unsigned long long)rows[i], 0ull, &st);
+  curandState st = {};
+  if (G.p.ray_mode != EPET_RAYS_REGULAR)
+    curand_init(G.p.seed, (unsigned long long)rows[i], 0ull, &st);
   emit_rays(G, rows[i], st, true,
             reinterpret_cast<float2*>(out + i * (int64_t)G.p.nrays * 6));
 }
@@ -90,12 +99,13 @@ __global__ void __launch_bounds__(128) k_rays(Geo G, const int32_t* __restrict__
   const int64_t i0 = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) * kRaysPerThread;
   if (i0 >= m) return;
   const int64_t i1 = i0 + kRaysPerThread < m ? i0 + kRaysPerThread : m;
-  curandState base;
+  const bool regular = G.p.ray_mode == EPET_RAYS_REGULAR;
+  curandState base = {};
   int prev = rows[i0];
-  curand_init(G.p.seed, (unsigned long long)prev, 0ull, &base);
+  if (!regular) curand_init(G.p.seed, (unsigned long long)prev, 0ull, &base);
   for (int64_t i = i0; i < i1; i++) {
     const int cnl = rows[i];
-    if (i > i0) {
+    if (i > i0 && !regular) {
       if (cnl > prev) skipahead_sequence((unsigned long long)(cnl - prev), &base);
       else if (cnl != prev) curand_init(G.p.seed, (unsigned long long)cnl, 0ull, &base);
       prev = cnl;

@@ -30,11 +30,21 @@ epet_status launch_workqueue_fill(const Geo& G, const int32_t* rows, int64_t m,
                                   cudaStream_t st);
 epet_status launch_values(const Geo& G, const float* rays, int64_t m,
                           const int64_t* row_ptr, const int32_t* col, float* val,
-                          cudaStream_t st);
+                          bool exact, cudaStream_t st);
+// Rows left to the per-candidate path: in CSR mode (mode 0) each row's kept
+// entries go to compact buffers (row i of the list at off[i], any length),
+// row_len[row] is set and src_idx[row] = -2 - i tells the row gather to read
+// them there; the caller frees the buffers (release()) after that gather.
+struct ExactRows {
+  int64_t* off = nullptr;
+  int32_t* col = nullptr;
+  float* val = nullptr;
+  void release(cudaStream_t st);
+};
 epet_status exact_rows_apply(const Geo& G, const int32_t* rows, const int32_t* ex_rows,
-                             int64_t n_ex, int mode, int64_t stride, int32_t* stage_col,
-                             float* stage_val, int32_t* row_len, const float* x, float* y,
-                             const float* e, float* c, double* s64, cudaStream_t st);
+                             int64_t n_ex, int mode, int32_t* row_len, int32_t* src_idx,
+                             ExactRows* keep, const float* x, float* y, const float* e,
+                             float* c, double* s64, cudaStream_t st);
 epet_status column_sums(const epet_problem* p, const int32_t* rows_d, int64_t m,
                         double* s64, int32_t max_row_nnz, void* ws, size_t ws_bytes,
                         cudaStream_t st);

@@ -138,6 +138,8 @@ epet_status epet_problem_validate(const epet_problem* p) {
   const epet_setup& s = p->setup;
   const epet_grid& g = p->grid;
   if (p->nrays < 1) return set_error(EPET_ERR_INVALID, "nrays must be >= 1");
+  if (p->ray_mode != EPET_RAYS_RANDOM && p->ray_mode != EPET_RAYS_REGULAR)
+    return set_error(EPET_ERR_INVALID, "ray_mode must be EPET_RAYS_RANDOM or EPET_RAYS_REGULAR");
   if (s.na < 1 || s.n0z < 1 || s.n0y < 1 || s.n1z < 1 || s.n1y < 1)
     return set_error(EPET_ERR_INVALID, "detector counts must be >= 1");
   double nch = (double)s.na * s.n0z * s.n0y * s.n1z * s.n1y;

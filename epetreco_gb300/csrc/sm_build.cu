@@ -901,12 +901,15 @@ k_walk(WalkArgs args) {
 // Gather staged rows into their final CSR positions (warp per row).
 // Rows redone with a larger window (ovf_idx[row] >= 0) come from the second
 // staging area.
+// Row sources: ovf_idx[row] = -1: the walk's stage (row * stride);
+// >= 0: the redo's stage (slot * stride2); <= -2: row -2 - ovf_idx[row] of
+// the per-candidate path's compact buffers (at ex.off[i]).
 __global__ void k_gather_rows(const int32_t* __restrict__ stage_col,
                               const float* __restrict__ stage_val, int64_t stride,
                               const int32_t* __restrict__ ovf_idx,
                               const int32_t* __restrict__ stage2_col,
                               const float* __restrict__ stage2_val, int64_t stride2,
-                              const int64_t* __restrict__ row_ptr, int64_t m,
+                              ExactRows ex, const int64_t* __restrict__ row_ptr, int64_t m,
                               int32_t* __restrict__ col, float* __restrict__ val,
                               int64_t cap) {
   const int64_t row = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -915,8 +918,16 @@ __global__ void k_gather_rows(const int32_t* __restrict__ stage_col,
   const int64_t b = row_ptr[row], n = row_ptr[row + 1] - b;
   if (b + n > cap) return;
   const int32_t oi = ovf_idx ? ovf_idx[row] : -1;
-  const int32_t* sc = oi >= 0 ? stage2_col + oi * stride2 : stage_col + row * stride;
-  const float* sv = oi >= 0 ? stage2_val + oi * stride2 : stage_val + row * stride;
+  const int32_t* sc;
+  const float* sv;
+  if (oi <= -2) {
+    const int64_t o = ex.off[-2 - oi];
+    sc = ex.col + o;
+    sv = ex.val + o;
+  } else {
+    sc = oi >= 0 ? stage2_col + oi * stride2 : stage_col + row * stride;
+    sv = oi >= 0 ? stage2_val + oi * stride2 : stage_val + row * stride;
+  }
   for (int64_t k = lane; k < n; k += 32) {
     col[b + k] = sc[k];
     val[b + k] = sv[k];
@@ -1259,11 +1270,20 @@ static epet_status run_walk(const Geo& G, const int32_t* rows, int64_t m,
       EPET_CHECK(redo_overflow<kMode>(a, ovf_rows, fl[0], &cap2, &stage2_col, &stage2_val, ovf_idx,
                                       st));
       n_overflow_rows_ += fl[0];
+      // the redone rows can add to the list of rows with an axis-parallel ray
+      EPET_CUDA(cudaMemcpyAsync(&fl[2], flags + 2, 4, cudaMemcpyDeviceToHost, st));
+      EPET_CUDA(cudaStreamSynchronize(st));
     }
+    ExactRows exr;
+    struct ReleaseExact {
+      ExactRows* e;
+      cudaStream_t s;
+      ~ReleaseExact() { e->release(s); }
+    } release_exact{&exr, st};
     if (fl[2] > 0) {
       // rows with an axis-parallel ray: per-candidate path
-      EPET_CHECK(exact_rows_apply(G, rows + c0, ex_rows, fl[2], kMode, cap_cells, stage_col,
-                                  stage_val, row_len, a.x, a.y, a.e, a.c, a.s64, st));
+      EPET_CHECK(exact_rows_apply(G, rows + c0, ex_rows, fl[2], kMode, row_len,
+                                  csr ? ovf_idx : nullptr, &exr, a.x, a.y, a.e, a.c, a.s64, st));
       n_exact_rows_ += fl[2];
     }
     if (csr) {
@@ -1285,14 +1305,14 @@ static epet_status run_walk(const Geo& G, const int32_t* rows, int64_t m,
         if (!out->chunk_dst(out, c0, mc, chunk_total, &dcol, &dval))
           return set_error(EPET_ERR_CUDA, "could not allocate a system-matrix chunk");
         k_gather_rows<<<ceil_div(mc * 32, T), T, 0, st>>>(
-            stage_col, stage_val, cap_cells, ovf_idx, stage2_col, stage2_val, cap2, rp_chunk,
+            stage_col, stage_val, cap_cells, ovf_idx, stage2_col, stage2_val, cap2, exr, rp_chunk,
             mc, dcol, dval, chunk_total);
       } else {
         if (total_nnz + chunk_total > out->cap && out->grow &&
             !out->grow(out, total_nnz + chunk_total, total_nnz, c0 + mc, m))
           return set_error(EPET_ERR_CUDA, "could not grow the system-matrix buffers");
         k_gather_rows<<<ceil_div(mc * 32, T), T, 0, st>>>(
-            stage_col, stage_val, cap_cells, ovf_idx, stage2_col, stage2_val, cap2, rp, mc,
+            stage_col, stage_val, cap_cells, ovf_idx, stage2_col, stage2_val, cap2, exr, rp, mc,
             out->csr->col, out->csr->val, out->cap);
       }
       EPET_LAUNCHED();

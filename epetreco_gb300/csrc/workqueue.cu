@@ -156,6 +156,12 @@ constexpr int kValThreads = 128;
 // CTA (row, slice): the row's rays in shared memory, the slice's threads
 // over every gridDim.y-th group of kValThreads elements (few rows get many
 // slices, so a short list of long rows still fills the device).
+// Exact = false: the fp32 sum in ray order of getSystemMatrixFromWorkqueue.
+// Exact = true: the fused build's exact sum -- each positive chord as
+// max(1, round(chord * 2^s)) fixed-point units, the 64-bit total scaled back
+// and divided by nrays with the same operations as the ray walk -- so rows
+// the walk hands to this path get values of the same definition.
+template <bool Exact>
 __global__ void __launch_bounds__(kValThreads)
 k_values(Geo G, const float* __restrict__ rays, int64_t m,
          const int64_t* __restrict__ row_ptr, const int32_t* __restrict__ col,
@@ -175,9 +181,19 @@ k_values(Geo G, const float* __restrict__ rays, int64_t m,
     const int v = col[k];
     const int ix = v / G.nyz, rem = v - ix * G.nyz;
     const int iy = rem / g.n[2], iz = rem - iy * g.n[2];
-    float a = 0.f;
-    for (int r = 0; r < R; r++) a = fadd(a, isect_len(g, ix, iy, iz, &sray[6 * r]));
-    val[k] = fdiv(a, (float)R);
+    if (Exact) {
+      unsigned long long u = 0ull;
+      for (int r = 0; r < R; r++) {
+        const float c = isect_len(g, ix, iy, iz, &sray[6 * r]);
+        if (c > 0.f) u += __float2ull_rn(fmaxf(fmul(c, G.fx_scale), 1.f));
+      }
+      const float fR = (float)R;
+      val[k] = div_cr(fmul(__ull2float_rn(u), G.fx_inv), fR, __frcp_rn(fR));
+    } else {
+      float a = 0.f;
+      for (int r = 0; r < R; r++) a = fadd(a, isect_len(g, ix, iy, iz, &sray[6 * r]));
+      val[k] = fdiv(a, (float)R);
+    }
   }
 }
 
@@ -188,10 +204,10 @@ template <int kMode>
 __global__ void k_apply_exact(int64_t n_ex, const int32_t* __restrict__ ex_rows,
                               const int64_t* __restrict__ wq_off,
                               const int32_t* __restrict__ wq_vxl,
-                              const float* __restrict__ wq_val, int64_t stride,
-                              int32_t* stage_col, float* stage_val, int32_t* row_len,
+                              const float* __restrict__ wq_val, int32_t* out_col,
+                              float* out_val, int32_t* row_len, int32_t* src_idx,
                               const float* x, float* y, const float* e, float* c,
-                              double* s64, int32_t* too_long) {
+                              double* s64) {
   const int64_t i = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int lane = threadIdx.x & 31;
   if (i >= n_ex) return;
@@ -206,11 +222,9 @@ __global__ void k_apply_exact(int64_t n_ex, const int32_t* __restrict__ ex_rows,
     if (v != 0.f) {
       const int vox = wq_vxl[b + k];
       const int64_t pos = o + __popc(nzm & ((1u << lane) - 1u));
-      if (kMode == 0) {
-        if (pos < stride) {
-          stage_col[row * stride + pos] = vox;
-          stage_val[row * stride + pos] = v;
-        }
+      if (kMode == 0) {  // kept entries compacted in place (at most the candidates)
+        out_col[b + pos] = vox;
+        out_val[b + pos] = v;
       }
       if (kMode == 2 && e[row] != 0.f) atomicAdd(&c[vox], fmul(v, e[row]));
       if (kMode == 3) atomicAdd(&s64[vox], (double)v);
@@ -224,8 +238,8 @@ __global__ void k_apply_exact(int64_t n_ex, const int32_t* __restrict__ ex_rows,
   }
   if (lane == 0) {
     if (kMode == 0) {
-      row_len[row] = (int32_t)(o < stride ? o : stride);
-      if (o > stride) atomicAdd(too_long, 1);
+      row_len[row] = (int32_t)o;
+      src_idx[row] = (int32_t)(-2 - i);
     }
     if (kMode == 1) y[row] = fsum;
   }
@@ -266,34 +280,48 @@ epet_status launch_workqueue_fill(const Geo& G, const int32_t* rows, int64_t m,
 
 epet_status launch_values(const Geo& G, const float* rays, int64_t m,
                           const int64_t* row_ptr, const int32_t* col, float* val,
-                          cudaStream_t st) {
+                          bool exact, cudaStream_t st) {
   if (m == 0) return EPET_OK;
   const size_t smem = (size_t)G.p.nrays * 6 * sizeof(float);
   if (smem > 200 * 1024)
     return set_error(EPET_ERR_UNSUPPORTED, "nrays too large for the values kernel");
-  EPET_CUDA(cudaFuncSetAttribute(k_values, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 (int)smem));
   const unsigned slices = (unsigned)std::min<int64_t>(64, std::max<int64_t>(1, 4096 / m));
-  k_values<<<dim3((unsigned)m, slices), kValThreads, smem, st>>>(G, rays, m, row_ptr, col, val);
+  const dim3 grid((unsigned)m, slices);
+  if (exact) {
+    EPET_CUDA(cudaFuncSetAttribute(k_values<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   (int)smem));
+    k_values<true><<<grid, kValThreads, smem, st>>>(G, rays, m, row_ptr, col, val);
+  } else {
+    EPET_CUDA(cudaFuncSetAttribute(k_values<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   (int)smem));
+    k_values<false><<<grid, kValThreads, smem, st>>>(G, rays, m, row_ptr, col, val);
+  }
   EPET_LAUNCHED();
   return EPET_OK;
 }
 
+void ExactRows::release(cudaStream_t st) {
+  if (off) dev_free(off, st);
+  if (col) dev_free(col, st);
+  if (val) dev_free(val, st);
+  off = nullptr;
+  col = nullptr;
+  val = nullptr;
+}
+
 // Per-candidate path for a few rows (list ex_rows of indices into rows).
 epet_status exact_rows_apply(const Geo& G, const int32_t* rows, const int32_t* ex_rows,
-                             int64_t n_ex, int mode, int64_t stride, int32_t* stage_col,
-                             float* stage_val, int32_t* row_len, const float* x, float* y,
-                             const float* e, float* c, double* s64, cudaStream_t st) {
+                             int64_t n_ex, int mode, int32_t* row_len, int32_t* src_idx,
+                             ExactRows* keep, const float* x, float* y, const float* e,
+                             float* c, double* s64, cudaStream_t st) {
   if (n_ex == 0) return EPET_OK;
+  if (mode == 0 && (!keep || keep->off)) return set_error(EPET_ERR_INVALID, "internal: exact rows");
   int32_t* cnl = nullptr;
   int64_t *cnt = nullptr, *off = nullptr, *tmp = nullptr;
-  int32_t* flag = nullptr;
   EPET_CUDA(dev_alloc((void**)&cnl, n_ex * 4, st));
   EPET_CUDA(dev_alloc((void**)&cnt, (n_ex + 1) * 8, st));
   EPET_CUDA(dev_alloc((void**)&off, (n_ex + 1) * 8, st));
   EPET_CUDA(dev_alloc((void**)&tmp, scan_tmp_elems(n_ex + 1) * 8, st));
-  EPET_CUDA(dev_alloc((void**)&flag, 4, st));
-  EPET_CUDA(cudaMemsetAsync(flag, 0, 4, st));
   k_gather_i32<<<ceil_div(n_ex, 256), 256, 0, st>>>(rows, ex_rows, n_ex, cnl);
   EPET_LAUNCHED();
   EPET_CHECK(launch_workqueue_count(G, cnl, n_ex, cnt, st));
@@ -310,29 +338,34 @@ epet_status exact_rows_apply(const Geo& G, const int32_t* rows, const int32_t* e
   EPET_CUDA(dev_alloc((void**)&rays, n_ex * (int64_t)G.p.nrays * 24, st));
   EPET_CHECK(launch_workqueue_fill(G, cnl, n_ex, off, wc, wv, st));
   EPET_CHECK(launch_rays(G, cnl, n_ex, rays, false, st));
-  EPET_CHECK(launch_values(G, rays, n_ex, off, wv, wval, st));
+  EPET_CHECK(launch_values(G, rays, n_ex, off, wv, wval, true, st));
   const int T = 128;
   const int nb = ceil_div(n_ex * 32, T);
+  // CSR mode: the kept entries overwrite the candidate columns (wc) and a
+  // buffer of values, which the caller's gather reads
+  float* kval = nullptr;
+  if (mode == 0) EPET_CUDA(dev_alloc((void**)&kval, tt * 4, st));
   switch (mode) {
-    case 0: k_apply_exact<0><<<nb, T, 0, st>>>(n_ex, ex_rows, off, wv, wval, stride, stage_col,
-                                               stage_val, row_len, x, y, e, c, s64, flag); break;
-    case 1: k_apply_exact<1><<<nb, T, 0, st>>>(n_ex, ex_rows, off, wv, wval, stride, stage_col,
-                                               stage_val, row_len, x, y, e, c, s64, flag); break;
-    case 2: k_apply_exact<2><<<nb, T, 0, st>>>(n_ex, ex_rows, off, wv, wval, stride, stage_col,
-                                               stage_val, row_len, x, y, e, c, s64, flag); break;
-    default: k_apply_exact<3><<<nb, T, 0, st>>>(n_ex, ex_rows, off, wv, wval, stride, stage_col,
-                                                 stage_val, row_len, x, y, e, c, s64, flag); break;
+    case 0: k_apply_exact<0><<<nb, T, 0, st>>>(n_ex, ex_rows, off, wv, wval, wc, kval, row_len,
+                                               src_idx, x, y, e, c, s64); break;
+    case 1: k_apply_exact<1><<<nb, T, 0, st>>>(n_ex, ex_rows, off, wv, wval, wc, kval, row_len,
+                                               src_idx, x, y, e, c, s64); break;
+    case 2: k_apply_exact<2><<<nb, T, 0, st>>>(n_ex, ex_rows, off, wv, wval, wc, kval, row_len,
+                                               src_idx, x, y, e, c, s64); break;
+    default: k_apply_exact<3><<<nb, T, 0, st>>>(n_ex, ex_rows, off, wv, wval, wc, kval, row_len,
+                                                 src_idx, x, y, e, c, s64); break;
   }
   EPET_LAUNCHED();
-  int32_t too_long = 0;
-  EPET_CUDA(cudaMemcpyAsync(&too_long, flag, 4, cudaMemcpyDeviceToHost, st));
-  EPET_CUDA(cudaStreamSynchronize(st));
-  dev_free(cnl, st); dev_free(cnt, st); dev_free(off, st);
-  dev_free(tmp, st); dev_free(flag, st); dev_free(wc, st);
+  dev_free(cnl, st); dev_free(cnt, st); dev_free(tmp, st);
   dev_free(wv, st); dev_free(wval, st); dev_free(rays, st);
-  if (too_long)
-    return set_error(EPET_ERR_OVERFLOW, "%d exact-path rows exceed the row capacity %lld",
-                     too_long, (long long)stride);
+  if (mode == 0) {
+    keep->off = off;
+    keep->col = wc;
+    keep->val = kval;
+  } else {
+    dev_free(off, st);
+    dev_free(wc, st);
+  }
   return EPET_OK;
 }
 
@@ -404,7 +437,7 @@ epet_status epet_sm_values(const epet_problem* p, const int32_t* rows_d,
   for (int64_t c0 = 0; c0 < m; c0 += ch) {
     const int64_t mc = std::min(ch, m - c0);
     EPET_CHECK(launch_rays(G, rows_d + c0, mc, rays, false, st));
-    EPET_CHECK(launch_values(G, rays, mc, row_ptr_d + c0, col_d, val_d, st));
+    EPET_CHECK(launch_values(G, rays, mc, row_ptr_d + c0, col_d, val_d, false, st));
   }
   return EPET_OK;
 }

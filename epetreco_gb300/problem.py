@@ -86,13 +86,31 @@ class VoxelGrid:
         return (o + (i + np.float32(0.5)) * d).astype(np.float32)
 
 
+RAY_GENERATORS = ("random", "regular")
+
+
 @dataclass(frozen=True)
 class Problem:
-    """One reconstruction geometry plus its Monte-Carlo ray settings."""
+    """One reconstruction geometry plus its Monte-Carlo ray settings.
+
+    ``rays`` picks the ray generator (RayGenerators.hpp): "random" is
+    ``RandRayGen`` (six cuRAND uniforms per ray, generator seeded per channel
+    with ``seed``), "regular" is ``ReguRayGen`` (every ray joins the two
+    crystal centres; the seed is unused)."""
     setup: MeasurementSetup
     grid: VoxelGrid
     nrays: int
     seed: int = 1251  # RANDOM_SEED (getSystemMatrixFromWorkqueue.cu:22)
+    rays: str = "random"
+
+    def __post_init__(self):
+        if self.rays not in RAY_GENERATORS:
+            raise ValueError(f"rays must be one of {RAY_GENERATORS}")
+
+    @property
+    def ray_mode(self) -> int:
+        """EPET_RAYS_RANDOM (0) or EPET_RAYS_REGULAR (1)."""
+        return RAY_GENERATORS.index(self.rays)
 
     @property
     def nchannels(self) -> int:
@@ -104,6 +122,9 @@ class Problem:
 
     def with_seed(self, seed: int) -> "Problem":
         return replace(self, seed=seed)
+
+    def with_rays(self, rays: str) -> "Problem":
+        return replace(self, rays=rays)
 
 
 def two_head_setup(na: int, da: float, pos: float = 0.25, n: int = 13,

@@ -59,13 +59,25 @@ typedef struct {
   int32_t n[3];
 } epet_grid;
 
+/* Ray generators (RayGenerators.hpp): EPET_RAYS_RANDOM is RandRayGen (:15-40),
+ * six cuRAND uniforms per ray from the channel's generator; EPET_RAYS_REGULAR
+ * is ReguRayGen (:46-66), every coordinate 0.5, i.e. each of the nrays rays is
+ * the line between the two crystal centres (nrays = 1 gives the same matrix up
+ * to the rounding of the mean, at 1/nrays of the cost). */
+enum { EPET_RAYS_RANDOM = 0, EPET_RAYS_REGULAR = 1 };
+
 /* Replaces the process-global __constant__ grid_const / setup_const /
  * nrays_const (device_constant_memory.hpp:14-26) with a value passed to each
- * call; seed is RANDOM_SEED (1251 in getSystemMatrixFromWorkqueue.cu:22). */
+ * call; seed is RANDOM_SEED (1251 in getSystemMatrixFromWorkqueue.cu:22).
+ * ray_mode (EPET_RAYS_*) picks the generator the reference selects with the
+ * RayGen template argument of systemMatrixCalculation (wrappers.hpp:172); it
+ * fills what would otherwise be padding, and 0 (a zero-initialised struct)
+ * is the random generator. */
 typedef struct {
   epet_setup setup;
   epet_grid grid;
   int32_t nrays;
+  int32_t ray_mode;
   uint64_t seed;
 } epet_problem;
 

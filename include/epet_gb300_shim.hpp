@@ -13,7 +13,9 @@
  *    stores zero-valued candidates); nnz_devi grows by the non-zeros;
  *  - rays are seeded per channel (curand_init(1251, channel, 0), as the
  *    reference's getSystemMatrixFromWorkqueue), so values are reproducible;
- *    the reference's production kernel seeds per thread and is not;
+ *    the reference's production kernel seeds per thread and is not; the
+ *    RayGen argument of systemMatrixCalculation selects the generator
+ *    (ReguRayGen: regular rays, anything else: RandRayGen);
  *  - errors throw cudaException after printing the library's message, like
  *    HANDLE_ERROR (CUDA_HandleError.hpp:17-31).
  * Operations are synchronous where the reference's are (it synchronises after
@@ -41,7 +43,24 @@
 class cudaException : public std::exception {};
 #endif
 
+/* The regular generator of RayGenerators.hpp:46-66, declared so that the
+ * generator a driver names can be told apart; the reference header defines it
+ * with the same three parameters. */
+template <typename T, typename MSTrafo0_inplace, typename MSTrafo1_inplace>
+struct ReguRayGen;
+
 namespace epet_shim {
+
+/* epet_problem::ray_mode of the RayGen argument: ReguRayGen is
+ * EPET_RAYS_REGULAR, every other generator (RandRayGen) EPET_RAYS_RANDOM. */
+template <typename RayGen>
+struct ray_mode_of {
+  static constexpr int value = EPET_RAYS_RANDOM;
+};
+template <typename T, typename A, typename B>
+struct ray_mode_of<ReguRayGen<T, A, B>> {
+  static constexpr int value = EPET_RAYS_REGULAR;
+};
 
 inline void check(epet_status s, const char* what) {
   if (s != EPET_OK) {
@@ -99,7 +118,8 @@ void systemMatrixCalculation(int* const aEcsrCnlPtr_devi, GridSizeType* const aV
   static_assert(sizeof(T) == 4 && sizeof(GridSizeType) == 4, "float values, int voxel ids");
   (void)handle;
   using namespace epet_shim;
-  const epet_problem p = constant_problem();
+  epet_problem p = constant_problem();
+  p.ray_mode = ray_mode_of<RayGen>::value;
   const int64_t m = (int64_t)nY_host[0];
   const int64_t V = (int64_t)p.grid.n[0] * p.grid.n[1] * p.grid.n[2];
   MemArrSizeType nnz0 = 0;

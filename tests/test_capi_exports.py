@@ -54,3 +54,71 @@ def test_error_without_gpu_is_reported_not_raised():
     assert b"nrays" in L.epet_last_error()
     ps.nrays = 10
     assert L.epet_problem_validate(ctypes.byref(ps)) == 0
+
+
+STRUCTS = {"epet_setup": "Setup", "epet_grid": "Grid", "epet_problem": "ProblemC",
+           "epet_csr": "CsrC", "epet_csc": "CscC", "epet_csr16": "Csr16C",
+           "epet_mlem_options": "MlemOptions"}
+
+
+def test_struct_layout_matches_header(tmp_path):
+    """The ctypes mirrors have the size and field offsets the C compiler
+    gives the header's structs (a C program built with gcc prints them)."""
+    import shutil
+    import subprocess
+    from epetreco_gb300 import _lib
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if cc is None:
+        pytest.skip("no C compiler")
+    lines = ['#include <stddef.h>', '#include <stdio.h>', '#include "epet_gb300.h"',
+             "int main(void) {"]
+    for cname, pyname in STRUCTS.items():
+        lines.append(f'  printf("{pyname} size %zu\\n", sizeof({cname}));')
+        for f, _ in getattr(_lib, pyname)._fields_:
+            lines.append(f'  printf("{pyname} {f} %zu\\n", offsetof({cname}, {f}));')
+    lines += ["  return 0;", "}"]
+    src = tmp_path / "layout.c"
+    src.write_text("\n".join(lines) + "\n")
+    exe = tmp_path / "layout"
+    subprocess.run([cc, "-std=c99", "-I", os.path.join(ROOT, "include"), str(src), "-o",
+                    str(exe)], check=True)
+    got = {}
+    for ln in subprocess.run([str(exe)], check=True, capture_output=True,
+                             text=True).stdout.splitlines():
+        k, v = ln.rsplit(" ", 1)
+        got[k] = int(v)
+    for pyname in STRUCTS.values():
+        T = getattr(_lib, pyname)
+        assert got[f"{pyname} size"] == ctypes.sizeof(T), pyname
+        for f, _ in T._fields_:
+            assert got[f"{pyname} {f}"] == getattr(T, f).offset, (pyname, f)
+
+
+def test_problem_layout_keeps_ray_mode_in_padding():
+    """ray_mode sits between nrays and the 8-byte seed, where a struct without
+    it has padding: the size and the seed's offset are those of the
+    four-field struct, and a zero-initialised problem is the random generator."""
+    from epetreco_gb300 import _lib
+
+    class Four(ctypes.Structure):
+        _fields_ = [("setup", _lib.Setup), ("grid", _lib.Grid), ("nrays", ctypes.c_int32),
+                    ("seed", ctypes.c_uint64)]
+    assert ctypes.sizeof(_lib.ProblemC) == ctypes.sizeof(Four)
+    assert _lib.ProblemC.seed.offset == Four.seed.offset
+    assert _lib.ProblemC().ray_mode == 0
+
+
+def test_ray_mode_validation():
+    from epetreco_gb300 import _lib
+    from epetreco_gb300.problem import Problem, config
+    L = _lib.lib()
+    p = config("small")["problem"]
+    assert p.ray_mode == 0 and p.with_rays("regular").ray_mode == 1
+    ps = _lib.problem_struct(p.with_rays("regular"))
+    assert ps.ray_mode == 1
+    assert L.epet_problem_validate(ctypes.byref(ps)) == 0
+    ps.ray_mode = 2
+    assert L.epet_problem_validate(ctypes.byref(ps)) == 1
+    assert b"ray_mode" in L.epet_last_error()
+    with pytest.raises(ValueError):
+        Problem(p.setup, p.grid, p.nrays, rays="uniform")
