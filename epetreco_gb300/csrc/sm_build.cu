@@ -1119,15 +1119,18 @@ template <int kMode>
 static epet_status redo_overflow(WalkArgs a, const int32_t* ovf_rows, int n, int* cap2,
                                  int32_t** s2c, float** s2v, int32_t* ovf_idx,
                                  cudaStream_t st) {
-  int32_t *sel = nullptr, *cnl = nullptr, *cells = nullptr;
-  EPET_CUDA(dev_alloc((void**)&sel, n * 4, st));
-  EPET_CUDA(dev_alloc((void**)&cnl, n * 4, st));
-  EPET_CUDA(dev_alloc((void**)&cells, n * 4, st));
+  // temporaries in one owned block, released on every return path
+  Scratch tmp;
+  EPET_CHECK(tmp.init(nullptr, 0, 3 * align256((size_t)n * 4) +
+                                      align256((size_t)n * kGeomFloats * 4), st));
+  int32_t* sel = tmp.take<int32_t>(n);
+  int32_t* cnl = tmp.take<int32_t>(n);
+  int32_t* cells = tmp.take<int32_t>(n);
+  float* geom = tmp.take<float>((size_t)n * kGeomFloats);
+  if (tmp.overrun) return set_error(EPET_ERR_INVALID, "internal: redo workspace size");
   EPET_CUDA(cudaMemcpyAsync(sel, ovf_rows, n * 4, cudaMemcpyDeviceToDevice, st));
   k_gather_i32<<<ceil_div(n, 256), 256, 0, st>>>(a.rows, sel, n, cnl);
   EPET_LAUNCHED();
-  float* geom = nullptr;
-  EPET_CUDA(dev_alloc((void**)&geom, (size_t)n * kGeomFloats * 4, st));
   EPET_CHECK(launch_channel_geom(a.G, cnl, n, geom, st));
   WalkArgs w{};
   w.G = a.G;
@@ -1159,10 +1162,6 @@ static epet_status redo_overflow(WalkArgs a, const int32_t* ovf_rows, int n, int
   }
   EPET_CUDA(cudaMemsetAsync(a.overflow_count, 0, 4, st));
   EPET_CHECK(launch_walk<kMode>(b, walk_smem(a.G, *cap2), st));
-  dev_free(sel, st);
-  dev_free(cnl, st);
-  dev_free(cells, st);
-  dev_free(geom, st);
   return EPET_OK;
 }
 
@@ -1261,9 +1260,23 @@ static epet_status run_walk(const Geo& G, const int32_t* rows, int64_t m,
     int32_t fl[3] = {0, 0, 0};
     EPET_CUDA(cudaMemcpyAsync(fl, flags, 12, cudaMemcpyDeviceToHost, st));
     EPET_CUDA(cudaStreamSynchronize(st));
+    // the chunk's second-stage buffers (redone rows, axis-parallel rows),
+    // released on every return path
+    struct ChunkExtra {
+      cudaStream_t s;
+      int32_t* stage2_col = nullptr;
+      float* stage2_val = nullptr;
+      ExactRows exr;
+      ~ChunkExtra() {
+        if (stage2_col) dev_free(stage2_col, s);
+        if (stage2_val) dev_free(stage2_val, s);
+        exr.release(s);
+      }
+    } extra{st};
+    int32_t*& stage2_col = extra.stage2_col;
+    float*& stage2_val = extra.stage2_val;
+    ExactRows& exr = extra.exr;
     // rows whose window exceeded the capacity: redo them with their exact size
-    int32_t* stage2_col = nullptr;
-    float* stage2_val = nullptr;
     int cap2 = 0;
     if (csr) EPET_CUDA(cudaMemsetAsync(ovf_idx, 0xff, mc * 4, st));
     if (fl[0] > 0) {
@@ -1274,12 +1287,6 @@ static epet_status run_walk(const Geo& G, const int32_t* rows, int64_t m,
       EPET_CUDA(cudaMemcpyAsync(&fl[2], flags + 2, 4, cudaMemcpyDeviceToHost, st));
       EPET_CUDA(cudaStreamSynchronize(st));
     }
-    ExactRows exr;
-    struct ReleaseExact {
-      ExactRows* e;
-      cudaStream_t s;
-      ~ReleaseExact() { e->release(s); }
-    } release_exact{&exr, st};
     if (fl[2] > 0) {
       // rows with an axis-parallel ray: per-candidate path
       EPET_CHECK(exact_rows_apply(G, rows + c0, ex_rows, fl[2], kMode, row_len,
@@ -1317,10 +1324,6 @@ static epet_status run_walk(const Geo& G, const int32_t* rows, int64_t m,
       }
       EPET_LAUNCHED();
       total_nnz += chunk_total;
-    }
-    if (stage2_col) {
-      dev_free(stage2_col, st);
-      dev_free(stage2_val, st);
     }
     EPET_CUDA(cudaEventRecord(side.done[b], st));  // buffer b free for chunk k + 2
   }

@@ -316,56 +316,56 @@ epet_status exact_rows_apply(const Geo& G, const int32_t* rows, const int32_t* e
                              float* c, double* s64, cudaStream_t st) {
   if (n_ex == 0) return EPET_OK;
   if (mode == 0 && (!keep || keep->off)) return set_error(EPET_ERR_INVALID, "internal: exact rows");
-  int32_t* cnl = nullptr;
-  int64_t *cnt = nullptr, *off = nullptr, *tmp = nullptr;
-  EPET_CUDA(dev_alloc((void**)&cnl, n_ex * 4, st));
-  EPET_CUDA(dev_alloc((void**)&cnt, (n_ex + 1) * 8, st));
-  EPET_CUDA(dev_alloc((void**)&off, (n_ex + 1) * 8, st));
-  EPET_CUDA(dev_alloc((void**)&tmp, scan_tmp_elems(n_ex + 1) * 8, st));
+  // off/col/val: handed to the caller in CSR mode, else released here; the
+  // temporaries live in owned scratch blocks; all freed on every return path
+  struct Local {
+    ExactRows bufs;
+    cudaStream_t s;
+    ~Local() { bufs.release(s); }
+  } local{ExactRows{}, st};
+  ExactRows& out = mode == 0 ? *keep : local.bufs;
+  Scratch t1;
+  EPET_CHECK(t1.init(nullptr, 0, align256((size_t)n_ex * 4) + align256((size_t)(n_ex + 1) * 8) +
+                                     align256(scan_tmp_elems(n_ex + 1) * 8), st));
+  int32_t* cnl = t1.take<int32_t>(n_ex);
+  int64_t* cnt = t1.take<int64_t>(n_ex + 1);
+  int64_t* tmp = t1.take<int64_t>(scan_tmp_elems(n_ex + 1));
+  if (t1.overrun) return set_error(EPET_ERR_INVALID, "internal: exact-row workspace size");
+  EPET_CUDA(dev_alloc((void**)&out.off, (n_ex + 1) * 8, st));
   k_gather_i32<<<ceil_div(n_ex, 256), 256, 0, st>>>(rows, ex_rows, n_ex, cnl);
   EPET_LAUNCHED();
   EPET_CHECK(launch_workqueue_count(G, cnl, n_ex, cnt, st));
-  EPET_CHECK(exclusive_scan_i64(cnt, off, n_ex, tmp, st));
+  EPET_CHECK(exclusive_scan_i64(cnt, out.off, n_ex, tmp, st));
   int64_t total = 0;
-  EPET_CUDA(cudaMemcpyAsync(&total, off + n_ex, 8, cudaMemcpyDeviceToHost, st));
+  EPET_CUDA(cudaMemcpyAsync(&total, out.off + n_ex, 8, cudaMemcpyDeviceToHost, st));
   EPET_CUDA(cudaStreamSynchronize(st));
-  int32_t *wc = nullptr, *wv = nullptr;
-  float *wval = nullptr, *rays = nullptr;
   const int64_t tt = std::max<int64_t>(total, 1);
-  EPET_CUDA(dev_alloc((void**)&wc, tt * 4, st));
-  EPET_CUDA(dev_alloc((void**)&wv, tt * 4, st));
-  EPET_CUDA(dev_alloc((void**)&wval, tt * 4, st));
-  EPET_CUDA(dev_alloc((void**)&rays, n_ex * (int64_t)G.p.nrays * 24, st));
-  EPET_CHECK(launch_workqueue_fill(G, cnl, n_ex, off, wc, wv, st));
+  Scratch t2;
+  EPET_CHECK(t2.init(nullptr, 0, 2 * align256((size_t)tt * 4) +
+                                     align256((size_t)n_ex * G.p.nrays * 24), st));
+  int32_t* wv = t2.take<int32_t>(tt);
+  float* wval = t2.take<float>(tt);
+  float* rays = t2.take<float>((size_t)n_ex * G.p.nrays * 6);
+  if (t2.overrun) return set_error(EPET_ERR_INVALID, "internal: exact-row workspace size");
+  // candidate channels; in CSR mode the kept columns then overwrite them
+  EPET_CUDA(dev_alloc((void**)&out.col, tt * 4, st));
+  if (mode == 0) EPET_CUDA(dev_alloc((void**)&out.val, tt * 4, st));
+  EPET_CHECK(launch_workqueue_fill(G, cnl, n_ex, out.off, out.col, wv, st));
   EPET_CHECK(launch_rays(G, cnl, n_ex, rays, false, st));
-  EPET_CHECK(launch_values(G, rays, n_ex, off, wv, wval, true, st));
+  EPET_CHECK(launch_values(G, rays, n_ex, out.off, wv, wval, true, st));
   const int T = 128;
   const int nb = ceil_div(n_ex * 32, T);
-  // CSR mode: the kept entries overwrite the candidate columns (wc) and a
-  // buffer of values, which the caller's gather reads
-  float* kval = nullptr;
-  if (mode == 0) EPET_CUDA(dev_alloc((void**)&kval, tt * 4, st));
   switch (mode) {
-    case 0: k_apply_exact<0><<<nb, T, 0, st>>>(n_ex, ex_rows, off, wv, wval, wc, kval, row_len,
-                                               src_idx, x, y, e, c, s64); break;
-    case 1: k_apply_exact<1><<<nb, T, 0, st>>>(n_ex, ex_rows, off, wv, wval, wc, kval, row_len,
-                                               src_idx, x, y, e, c, s64); break;
-    case 2: k_apply_exact<2><<<nb, T, 0, st>>>(n_ex, ex_rows, off, wv, wval, wc, kval, row_len,
-                                               src_idx, x, y, e, c, s64); break;
-    default: k_apply_exact<3><<<nb, T, 0, st>>>(n_ex, ex_rows, off, wv, wval, wc, kval, row_len,
-                                                 src_idx, x, y, e, c, s64); break;
+    case 0: k_apply_exact<0><<<nb, T, 0, st>>>(n_ex, ex_rows, out.off, wv, wval, out.col, out.val,
+                                               row_len, src_idx, x, y, e, c, s64); break;
+    case 1: k_apply_exact<1><<<nb, T, 0, st>>>(n_ex, ex_rows, out.off, wv, wval, out.col, out.val,
+                                               row_len, src_idx, x, y, e, c, s64); break;
+    case 2: k_apply_exact<2><<<nb, T, 0, st>>>(n_ex, ex_rows, out.off, wv, wval, out.col, out.val,
+                                               row_len, src_idx, x, y, e, c, s64); break;
+    default: k_apply_exact<3><<<nb, T, 0, st>>>(n_ex, ex_rows, out.off, wv, wval, out.col,
+                                                 out.val, row_len, src_idx, x, y, e, c, s64); break;
   }
   EPET_LAUNCHED();
-  dev_free(cnl, st); dev_free(cnt, st); dev_free(tmp, st);
-  dev_free(wv, st); dev_free(wval, st); dev_free(rays, st);
-  if (mode == 0) {
-    keep->off = off;
-    keep->col = wc;
-    keep->val = kval;
-  } else {
-    dev_free(off, st);
-    dev_free(wc, st);
-  }
   return EPET_OK;
 }
 
