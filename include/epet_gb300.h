@@ -40,7 +40,8 @@ typedef enum {
   EPET_ERR_CUDA = 3,        /* CUDA runtime error */
   EPET_ERR_UNSUPPORTED = 4, /* geometry/format outside the supported range */
   EPET_ERR_TIMEOUT = 5,     /* a bounded device wait gave up */
-  EPET_ERR_OVERFLOW = 6     /* a row exceeded the per-row accumulator */
+  EPET_ERR_OVERFLOW = 6     /* reserved: no call returns it (rows over the
+                               window capacity are redone at their size) */
 } epet_status;
 
 /* DefaultMeasurementSetup<float> (MeasurementSetup.hpp:124-164): two planar
@@ -131,7 +132,8 @@ const char* epet_version(void);
 /* Number of kernels this library has launched in the process (CUDA-graph
  * replays count the kernels they contain); for launch accounting. */
 long long epet_launch_count(void);
-/* Problem checks: index ranges fit int32, nrays >= 1, positive pitches. */
+/* Problem checks: index ranges fit int32, nrays >= 1, positive pitches,
+ * ray_mode one of EPET_RAYS_*. */
 epet_status epet_problem_validate(const epet_problem* p);
 
 /* ------------------------------------------------------------- geometry */
@@ -141,7 +143,8 @@ epet_status epet_trig_table(const epet_problem* p, float* sc_d,
                             epet_stream_t stream);
 /* The cuRAND uniforms of each listed channel, out_d[m][nrays][6]
  * (curand_init(seed, channel, 0) then 6 curand_uniform per ray, as in
- * getSystemMatrixFromWorkqueue.cu:189-204). */
+ * getSystemMatrixFromWorkqueue.cu:189-204); 0.5 everywhere for
+ * EPET_RAYS_REGULAR. */
 epet_status epet_dump_uniforms(const epet_problem* p, const int32_t* rows_d,
                                int64_t m, float* out_d, epet_stream_t stream);
 /* Diagnostics (no counterpart in the reference): rows of system-matrix builds
@@ -156,7 +159,8 @@ epet_status epet_build_counters(int64_t* overflow_rows_h, int64_t* exact_rows_h)
 epet_status epet_selftest_division(int64_t n, uint64_t seed, int64_t* mismatches_h,
                                    epet_stream_t stream);
 /* World-coordinate rays out_d[m][nrays][6] (RandRayGen, RayGenerators.hpp:
- * 15-40 with the per-channel seeding of getSystemMatrixFromWorkqueue.cu). */
+ * 15-40 with the per-channel seeding of getSystemMatrixFromWorkqueue.cu;
+ * ReguRayGen, :46-66, for EPET_RAYS_REGULAR). */
 epet_status epet_rays(const epet_problem* p, const int32_t* rows_d, int64_t m,
                       float* out_d, epet_stream_t stream);
 
@@ -192,8 +196,10 @@ size_t epet_sm_values_workspace_size(const epet_problem* p, int64_t m);
  * CSR (rows = rows_d, in order).  Stored zeros of the reference are dropped.
  * out->row_ptr/col/val are caller buffers; cap = capacity of col/val.
  * Synchronous.  On EPET_ERR_CAPACITY *nnz_h holds the required nnz and
- * row_ptr is complete.  max_row_nnz: per-row accumulator capacity (0 = auto);
- * EPET_ERR_OVERFLOW if a row exceeds it. */
+ * row_ptr is complete.  max_row_nnz: the walk's per-row window capacity in
+ * cells (0 = sized from a sample of the rows); rows with a larger window are
+ * redone with their own size, so it changes speed and memory, not results
+ * (EPET_ERR_UNSUPPORTED if a window does not fit in shared memory). */
 epet_status epet_sm_build(const epet_problem* p, const int32_t* rows_d,
                           int64_t m, epet_csr* out, int64_t cap,
                           int64_t* nnz_h, int32_t max_row_nnz, void* ws,
