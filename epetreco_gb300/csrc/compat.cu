@@ -2,6 +2,7 @@
 // that hold the reference's int row pointers (ECSR int[m+1], wrappers.hpp:
 // 64-74), and the constant-geometry slot of the C++ drop-in header.
 #include <algorithm>
+#include <mutex>
 
 #include "common.cuh"
 #include "internal.h"
@@ -53,6 +54,9 @@ __global__ void k_expand_channels(const int64_t* __restrict__ ptr, int64_t m,
 
 using namespace epet;
 
+// The process-global geometry of epet_set_constant_geometry (the reference's
+// __constant__ symbols are process-global too); read and written under a lock.
+static std::mutex g_const_mu;
 static epet_problem g_const_problem;
 static bool g_const_set = false;
 
@@ -122,6 +126,7 @@ epet_status epet_set_constant_geometry(const epet_setup* setup, const epet_grid*
   p.nrays = nrays;
   p.seed = 1251;
   EPET_CHECK(epet_problem_validate(&p));
+  std::lock_guard<std::mutex> lock(g_const_mu);
   g_const_problem = p;
   g_const_set = true;
   return EPET_OK;
@@ -129,6 +134,7 @@ epet_status epet_set_constant_geometry(const epet_setup* setup, const epet_grid*
 
 epet_status epet_get_constant_geometry(epet_problem* out) {
   if (!out) return set_error(EPET_ERR_INVALID, "bad arguments");
+  std::lock_guard<std::mutex> lock(g_const_mu);
   if (!g_const_set)
     return set_error(EPET_ERR_INVALID, "no constant geometry set (epet_set_constant_geometry)");
   *out = g_const_problem;

@@ -111,13 +111,16 @@ static std::atomic<long long> g_launches{0};
 void note_launch(int n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
 long long launches() { return g_launches.load(); }
 
-int num_sms() {
-  static int n = 0;
+int num_sms() {  // of the current device, cached per device (any thread)
+  static std::atomic<int> cache[64] = {};
+  int dev = 0;
+  cudaGetDevice(&dev);
+  std::atomic<int>* slot = dev >= 0 && dev < 64 ? &cache[dev] : nullptr;
+  int n = slot ? slot->load(std::memory_order_relaxed) : 0;
   if (n == 0) {
-    int dev = 0;
-    cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
     if (n <= 0) n = 1;
+    if (slot) slot->store(n, std::memory_order_relaxed);
   }
   return n;
 }

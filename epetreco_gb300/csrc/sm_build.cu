@@ -29,6 +29,7 @@
 #include <curand_kernel.h>
 
 #include <algorithm>
+#include <atomic>
 #include <climits>
 #include <vector>
 
@@ -956,15 +957,20 @@ static size_t walk_smem(const Geo& G, int cap_cells) {
       .total;
 }
 
-static int g_max_smem = 0;
+// Dynamic shared memory a walk CTA may use on the current device (cached per
+// device; any thread).
 static int max_dyn_smem() {
-  if (g_max_smem == 0) {
-    int dev = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&g_max_smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
-    g_max_smem -= 4096;  // static shared memory of the kernel
+  static std::atomic<int> cache[64] = {};
+  int dev = 0;
+  cudaGetDevice(&dev);
+  std::atomic<int>* slot = dev >= 0 && dev < 64 ? &cache[dev] : nullptr;
+  int v = slot ? slot->load(std::memory_order_relaxed) : 0;
+  if (v == 0) {
+    cudaDeviceGetAttribute(&v, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+    v -= 4096;  // static shared memory of the kernel
+    if (slot) slot->store(v, std::memory_order_relaxed);
   }
-  return g_max_smem;
+  return v;
 }
 
 template <int kMode>
@@ -1069,10 +1075,10 @@ int auto_row_capacity(const epet_problem& p) {
 }
 
 // Rows redone by the per-candidate path / with a larger window since load.
-static int64_t n_exact_rows_ = 0;
-static int64_t n_overflow_rows_ = 0;
-int64_t exact_rows_total() { return n_exact_rows_; }
-int64_t overflow_rows_total() { return n_overflow_rows_; }
+static std::atomic<int64_t> n_exact_rows_{0};
+static std::atomic<int64_t> n_overflow_rows_{0};
+int64_t exact_rows_total() { return n_exact_rows_.load(); }
+int64_t overflow_rows_total() { return n_overflow_rows_.load(); }
 
 // Generic driver: runs mode kMode over all rows in chunks.  For kModeCsr the
 // rows are staged and gathered into out (capacity cap).
