@@ -17,7 +17,11 @@
  *  - Functions taking (void* ws, size_t ws_bytes) need device scratch: pass
  *    a caller buffer of at least the size reported by the matching
  *    *_workspace_size(), or ws = NULL to let the library allocate it
- *    stream-ordered (cudaMallocAsync) and free it before returning.
+ *    stream-ordered (cudaMallocAsync) and free it before returning.  The
+ *    system-matrix calls take extra stream-ordered memory from the library's
+ *    pool for the rows they redo (a window over capacity, an axis-parallel
+ *    ray), whose count is known only during the call; epet_coo_sort_noalloc
+ *    allocates nothing.
  *  - Index types: channel and voxel ids int32, element counts and row
  *    pointers int64 (the reference's int counts overflow at the full 52^3 x
  *    5.1M-channel size). */
