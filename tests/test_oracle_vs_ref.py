@@ -61,3 +61,33 @@ def test_bounded_workqueue_is_prefix(ref, oracle):
     n = ref.lib.ref_workqueue_bounded(rows, 3, C.byref(lid), C.byref(vid), 777, oc, ov)
     assert n == 777
     assert (oc == full_c[:777]).all() and (ov == full_v[:777]).all()
+
+
+@pytest.mark.parametrize("name", ["small", "full"])
+def test_regular_ray_values(oracle, ref, name):
+    """ReguRayGen (RayGenerators.hpp:46-66) is every box coordinate 0.5; its
+    operator() is device-only, so the reference's host-built transforms and
+    value loop get those uniforms.  Rows whose centre line has equal end
+    coordinates on an axis (crystals at equal height) are included: there the
+    reference's slab test leaves that axis out, a case random rays never
+    reach."""
+    p = PROBLEMS[name]
+    ref.setup(p)
+    rng = np.random.default_rng(5)
+    pool = np.sort(rng.choice(p.nchannels, 400, replace=False)).astype(np.int32)
+    half = np.full(p.nrays * 6, 0.5, np.float32)
+    par = [c for c in pool
+           if (lambda r: r[1] == r[4] or r[2] == r[5])(oracle.rays(p, c, half[:6])[0])]
+    assert len(par) >= 3
+    rows = np.array(sorted(set(pool[:6].tolist()) | set(par[:4])), np.int32)
+    oc, ov, _ = oracle.workqueue(p, rows)
+    row_of = np.searchsorted(rows, oc).astype(np.int32)
+    sel = rng.choice(len(oc), min(1200, len(oc)), replace=False)
+    rnd = np.broadcast_to(half, (len(rows), p.nrays * 6))
+    v = oracle.sm_values_wq(p, rows, p.nrays, rnd, row_of[sel], ov[sel])
+    r = np.array([ref.lib.ref_sm_value(int(oc[i]), int(ov[i]), p.nrays, half) for i in sel],
+                 np.float32)
+    assert (v.view(np.uint32) == r.view(np.uint32)).all()
+    # the axis-parallel rows reach candidates the centre line misses
+    on_par = np.isin(oc[sel], par[:4])
+    assert (v[on_par] > 0).mean() > (v[~on_par] > 0).mean()
