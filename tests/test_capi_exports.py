@@ -122,3 +122,37 @@ def test_ray_mode_validation():
     assert b"ray_mode" in L.epet_last_error()
     with pytest.raises(ValueError):
         Problem(p.setup, p.grid, p.nrays, rays="uniform")
+
+
+def test_constant_geometry_threads():
+    """epet_set/get_constant_geometry (the shim's stand-in for the reference's
+    cudaMemcpyToSymbol of grid_const/setup_const/nrays_const) from several
+    threads at once: every read returns one whole problem that some thread
+    wrote (no CUDA call is involved)."""
+    import threading
+    from epetreco_gb300 import _lib
+    from epetreco_gb300.problem import config
+    L = _lib.lib()
+    base = _lib.problem_struct(config("small")["problem"])
+    errors = []
+
+    def run(k):
+        s, g = _lib.Setup(), _lib.Grid()
+        ctypes.pointer(s)[0] = base.setup
+        ctypes.pointer(g)[0] = base.grid
+        s.na = 1 + k  # na and nrays tie each write together
+        for it in range(2000):
+            if L.epet_set_constant_geometry(ctypes.byref(s), ctypes.byref(g), 100 + k) != 0:
+                errors.append("set")
+            out = _lib.ProblemC()
+            if L.epet_get_constant_geometry(ctypes.byref(out)) != 0:
+                errors.append("get")
+            elif out.nrays - 100 != out.setup.na - 1 or out.seed != 1251 or out.ray_mode != 0:
+                errors.append((out.nrays, out.setup.na))
+
+    ts = [threading.Thread(target=run, args=(k,)) for k in range(4)]
+    for t in ts:
+        t.start()
+    for t in ts:
+        t.join()
+    assert not errors, errors[:5]
