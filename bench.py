@@ -169,6 +169,15 @@ def aggregate_replicas(times, nit, world, dist, device):
     return tmax, [world * nit / t for t in tmax]
 
 
+def workload_name(cfg_name: str) -> str:
+    """The workload as both arms name it in `config`."""
+    from epetreco_gb300.problem import config
+    cfg = config(cfg_name)
+    p = cfg["problem"]
+    return (f"{cfg_name}: {p.grid.n[0]}^3 voxels x {p.nchannels} channels, {p.nrays} rays, "
+            f"{cfg['iterations']} iterations per step")
+
+
 def reference_arm(args):
     """--impl reference: the reference's CPU work for the path (oracle port;
     the reference's own sources do not exist on the GPU machine)."""
@@ -183,12 +192,15 @@ def reference_arm(args):
         info = cpu_baseline(args.config, args.cpu_sample, seed=k)
         per.append(info["value"])
     v = sorted(per)[len(per) // 2]
+    from epetreco_gb300.problem import config
+    nit = config(args.config)["iterations"]
     out = {"metric": METRIC, "value": v, "unit": UNIT, "impl": "reference",
            "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
-           "ms_per_step": 1000.0 * 20 / v if v else None, "higher_is_better": True,
+           "ms_per_step": 1000.0 * nit / v if v else None, "higher_is_better": True,
            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-           "config": {"workload": "full: 52^3 voxels x 5,140,980 channels, 100 rays, "
-                                  "20 iterations (matrix rebuilt every iteration)"},
+           "config": {"workload": workload_name(args.config),
+                      "schedule": "the reference's loop: the system matrix of the measured "
+                                  "rows rebuilt in every iteration (reco.cu:216-254)"},
            "cpu_baseline": {"value": v, "unit": UNIT, "cores": info["cores"],
                             "kind": info["kind"], "sample": info["sample"]},
            "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
@@ -524,9 +536,8 @@ def gb300_arm(args):
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": 1000.0 * t_step, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": (f"{args.config}: {p.grid.n[0]}^3 voxels x {p.nchannels} "
-                                f"channels, {p.nrays} rays, {nit} iterations per step, "
-                                f"matrix built once per step"),
+        "config": {"workload": workload_name(args.config),
+                   "schedule": "system matrix of the measured rows built once per step",
                    "measured_rows": m, "nnz": nnz, "parallelism": f"replicas{world}",
                    "l2": "inputs larger than L2 (matrix streams of GBs per pass)"},
         "e2e": {"value": value_e2e, "unit": UNIT, "h2d_bytes_per_step": h2d,
