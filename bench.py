@@ -76,7 +76,10 @@ class ClockSampler:
     def __init__(self, index: int):
         self.index = index
         self.proc = None
-        self.path = os.path.join(ROOT, "gpurun_out", f"clocks_rank{index}.csv")
+        # the raw samples (EPET_CLOCKS_DIR keeps them; the line carries the summary)
+        import tempfile
+        d = os.environ.get("EPET_CLOCKS_DIR") or tempfile.gettempdir()
+        self.path = os.path.join(d, f"epet_clocks_rank{index}.csv")
 
     def start(self):
         try:
@@ -180,7 +183,7 @@ def workload_name(cfg_name: str) -> str:
 
 def reference_arm(args):
     """--impl reference: the reference's CPU work for the path (oracle port;
-    the reference's own sources do not exist on the GPU machine)."""
+    the reference's own sources are not available where the bench runs)."""
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
