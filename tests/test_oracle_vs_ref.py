@@ -91,3 +91,73 @@ def test_regular_ray_values(oracle, ref, name):
     # the axis-parallel rows reach candidates the centre line misses
     on_par = np.isin(oc[sel], par[:4])
     assert (v[on_par] > 0).mean() > (v[~on_par] > 0).mean()
+
+
+from epetreco_gb300.problem import MeasurementSetup, VoxelGrid  # noqa: E402
+
+# Geometries off the two workloads: heads of different crystal counts at
+# uneven distances, an angle step that is not a divisor of 360, a grid that is
+# neither cubic nor centred nor of equal pitches, and quarter turns (lines along
+# z at 90 and 270 degrees).
+ODD = {
+    "asymmetric": Problem(MeasurementSetup(-0.31, 0.19, 7, 5, 7, 9, 3, 13.0, 0.02, 0.004, 0.005),
+                          VoxelGrid((-0.041, -0.023, -0.017), (0.003, 0.002, 0.0025),
+                                    (24, 18, 14)), 9),
+    "quarter_turns": Problem(MeasurementSetup(-0.2, 0.2, 4, 6, 4, 6, 4, 90.0, 0.01, 0.003, 0.003),
+                             VoxelGrid((-0.02, -0.01, -0.015), (0.002, 0.002, 0.002),
+                                       (20, 10, 15)), 5),
+}
+
+
+@pytest.mark.parametrize("name", list(ODD))
+def test_odd_geometry_indices_and_transforms(oracle, ref, name):
+    p = ODD[name]
+    ref.setup(p)
+    rng = np.random.default_rng(11)
+    out5 = np.zeros(5, np.int32)
+    for c in rng.choice(p.nchannels, 200, replace=False):
+        ref.lib.ref_channel_decode(int(c), out5)
+        assert (oracle.channel_decode(p, int(c)) == out5).all()
+        assert ref.lib.ref_channel_encode(*[int(v) for v in out5]) == c
+        assert p.setup.channel_id(*[int(v) for v in out5]) == c
+    out3 = np.zeros(3, np.int32)
+    for v in rng.choice(p.nvoxels, 200, replace=False):
+        ref.lib.ref_voxel_decode(int(v), out3)
+        assert (oracle.voxel_decode(p, int(v)) == out3).all()
+        assert p.grid.voxel_id(*[int(x) for x in out3]) == v
+    trig = oracle.trig_table(p)
+    w_ref = np.zeros(3, np.float32)
+    for c in rng.choice(p.nchannels, 100, replace=False):
+        ida, i0z, i0y, i1z, i1y = (int(v) for v in oracle.channel_decode(p, int(c)))
+        box = rng.random(3).astype(np.float32)
+        sc = trig[2 * ida:2 * ida + 2]
+        ref.lib.ref_trafo0(box, i0z, i0y, ida, w_ref)
+        assert (oracle.trafo(p, sc, 0, i0z, i0y, box).view(np.uint32) == w_ref.view(np.uint32)).all()
+        ref.lib.ref_trafo1(box, i1z, i1y, ida, w_ref)
+        assert (oracle.trafo(p, sc, 1, i1z, i1y, box).view(np.uint32) == w_ref.view(np.uint32)).all()
+
+
+@pytest.mark.parametrize("name", list(ODD))
+@pytest.mark.parametrize("rays", ["random", "regular"])
+def test_odd_geometry_workqueue_and_values(oracle, ref, name, rays):
+    p = ODD[name]
+    ref.setup(p)
+    rng = np.random.default_rng(13)
+    rows = np.sort(rng.choice(p.nchannels, 16, replace=False)).astype(np.int32)
+    oc, ov, _ = oracle.workqueue(p, rows)
+    rc, rv = ref.workqueue(rows)
+    assert len(oc) > 0
+    assert len(oc) == len(rc) and (oc == rc).all() and (ov == rv).all()
+    if rays == "regular":
+        rnd = np.full((len(rows), p.nrays * 6), 0.5, np.float32)
+    else:
+        rnd = rng.random((len(rows), p.nrays * 6)).astype(np.float32)
+        rnd[rnd == 0] = 1
+    row_of = np.searchsorted(rows, oc).astype(np.int32)
+    sel = rng.choice(len(oc), min(1000, len(oc)), replace=False)
+    v = oracle.sm_values_wq(p, rows, p.nrays, rnd, row_of[sel], ov[sel])
+    r = np.array([ref.lib.ref_sm_value(int(oc[i]), int(ov[i]), p.nrays,
+                                       np.ascontiguousarray(rnd[row_of[i]]))
+                  for i in sel], np.float32)
+    assert (v.view(np.uint32) == r.view(np.uint32)).all()
+    assert (v > 0).any()
