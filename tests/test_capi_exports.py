@@ -156,3 +156,30 @@ def test_constant_geometry_threads():
     for t in ts:
         t.join()
     assert not errors, errors[:5]
+
+
+def test_shim_maps_ray_generators(tmp_path):
+    """The shim's RayGen argument mapping, compiled (no run): a generator
+    template shaped like the reference's ReguRayGen, defined after the shim
+    as a driver including RayGenerators.hpp would, maps to EPET_RAYS_REGULAR;
+    any other type (RandRayGen) to EPET_RAYS_RANDOM."""
+    import shutil
+    import subprocess
+    cxx = shutil.which("g++")
+    nvcc = shutil.which("nvcc") or "/usr/local/cuda/bin/nvcc"
+    cuda_inc = os.path.join(os.path.dirname(os.path.dirname(os.path.realpath(nvcc))), "include")
+    if cxx is None or not os.path.exists(os.path.join(cuda_inc, "cusparse.h")):
+        pytest.skip("no C++ compiler or CUDA headers")
+    src = tmp_path / "shim_rays.cpp"
+    src.write_text(
+        '#include "epet_gb300_shim.hpp"\n'
+        "template <typename T, typename MSTrafo0_inplace, typename MSTrafo1_inplace>\n"
+        "struct ReguRayGen { int unused; };\n"
+        "template <typename T, typename A, typename B> struct RandRayGen { int unused; };\n"
+        "static_assert(epet_shim::ray_mode_of<ReguRayGen<float, int, long>>::value ==\n"
+        "              EPET_RAYS_REGULAR, \"regular\");\n"
+        "static_assert(epet_shim::ray_mode_of<RandRayGen<float, int, long>>::value ==\n"
+        "              EPET_RAYS_RANDOM, \"random\");\n"
+        "int main() { return 0; }\n")
+    subprocess.run([cxx, "-std=c++17", "-fsyntax-only", "-I", os.path.join(ROOT, "include"),
+                    "-I", cuda_inc, str(src)], check=True)
