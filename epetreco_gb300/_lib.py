@@ -67,6 +67,7 @@ SIGNATURES = {
     "epet_last_error": [],
     "epet_version": [],
     "epet_launch_count": [],
+    "epet_device_allocations": [],
     "epet_problem_validate": [P],
     "epet_trig_table": [P, VP, VP],
     "epet_dump_uniforms": [P, VP, I64, VP, VP],
@@ -125,6 +126,7 @@ _RESTYPES = {
     "epet_last_error": C.c_char_p,
     "epet_version": C.c_char_p,
     "epet_launch_count": C.c_longlong,
+    "epet_device_allocations": C.c_longlong,
     "epet_sm_values_workspace_size": SZ,
     "epet_sm_build_workspace_size": SZ,
     "epet_coo_sort_workspace_size": SZ,

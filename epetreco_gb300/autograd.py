@@ -29,10 +29,12 @@ def _ext():
 
 
 def problem_vector(p: Problem) -> list:
+    """The problem's float and int32 fields (exact in float64); the 64-bit
+    seed travels as its own integer argument."""
     s, g = p.setup, p.grid
     return [float(v) for v in (s.pos0x, s.pos1x, s.na, s.n0z, s.n0y, s.n1z, s.n1y, s.da,
                                s.segx, s.segy, s.segz, *g.origin, *g.pitch, *g.n, p.nrays,
-                               p.seed, p.ray_mode)]
+                               p.ray_mode)]
 
 
 class Projector:
@@ -58,7 +60,10 @@ class Projector:
             return self.ext.project_stored(x, A.row_ptr, A.col.contiguous(), A.val.contiguous(),
                                            At.col_ptr, At.row.contiguous(),
                                            At.val.contiguous(), A.n)
-        return self.ext.project_free(x, self.rows, self.pvec)
+        # the seed as a signed 64-bit value with the same bits (libtorch ints are int64)
+        seed = int(self.p.seed) & (2**64 - 1)
+        seed = seed - 2**64 if seed >= 2**63 else seed
+        return self.ext.project_free(x, self.rows, self.pvec, seed)
 
 
 def poisson_nll(ybar: torch.Tensor, y: torch.Tensor, eps: float = 1e-12) -> torch.Tensor:

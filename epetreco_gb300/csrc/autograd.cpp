@@ -80,9 +80,10 @@ class StoredProjection : public torch::autograd::Function<StoredProjection> {
   }
 };
 
-// Matrix-free: the problem as a flat float64 vector of its fields.
-epet_problem unpack(const std::vector<double>& f) {
-  TORCH_CHECK(f.size() == 23, "problem vector must hold 23 numbers");
+// Matrix-free: the problem as a flat float64 vector of its float and int32
+// fields (each exactly representable) and the 64-bit seed on its own.
+epet_problem unpack(const std::vector<double>& f, int64_t seed) {
+  TORCH_CHECK(f.size() == 22, "problem vector must hold 22 numbers");
   epet_problem p{};
   p.setup = epet_setup{(float)f[0], (float)f[1], (int)f[2], (int)f[3], (int)f[4], (int)f[5],
                        (int)f[6], (float)f[7], (float)f[8], (float)f[9], (float)f[10]};
@@ -90,14 +91,14 @@ epet_problem unpack(const std::vector<double>& f) {
                      {(float)f[14], (float)f[15], (float)f[16]},
                      {(int)f[17], (int)f[18], (int)f[19]}};
   p.nrays = (int)f[20];
-  p.seed = (uint64_t)f[21];
-  p.ray_mode = (int32_t)f[22];
+  p.seed = (uint64_t)seed;
+  p.ray_mode = (int32_t)f[21];
   return p;
 }
 
-torch::Tensor apply_free(const std::vector<double>& pf, const torch::Tensor& rows,
+torch::Tensor apply_free(const std::vector<double>& pf, int64_t seed, const torch::Tensor& rows,
                          const torch::Tensor& x, bool trans) {
-  const epet_problem p = unpack(pf);
+  const epet_problem p = unpack(pf, seed);
   const int64_t V = (int64_t)p.grid.n[0] * p.grid.n[1] * p.grid.n[2], m = rows.numel();
   const int64_t in = trans ? m : V, out = trans ? V : m;
   TORCH_CHECK(x.size(-1) == in, "projector: last dimension ", x.size(-1), " != ", in);
@@ -120,16 +121,19 @@ torch::Tensor apply_free(const std::vector<double>& pf, const torch::Tensor& row
 class FreeProjection : public torch::autograd::Function<FreeProjection> {
  public:
   static torch::Tensor forward(torch::autograd::AutogradContext* ctx, torch::Tensor x,
-                               torch::Tensor rows, std::vector<double> problem) {
+                               torch::Tensor rows, std::vector<double> problem, int64_t seed) {
     ctx->save_for_backward({rows});
     ctx->saved_data["problem"] = problem;
-    return apply_free(problem, rows, x, false);
+    ctx->saved_data["seed"] = seed;
+    return apply_free(problem, seed, rows, x, false);
   }
   static torch::autograd::tensor_list backward(torch::autograd::AutogradContext* ctx,
                                                torch::autograd::tensor_list g) {
     auto rows = ctx->get_saved_variables()[0];
     auto pf = ctx->saved_data["problem"].toDoubleVector();
-    return {apply_free(pf, rows, g[0], true), torch::Tensor(), torch::Tensor()};
+    const int64_t seed = ctx->saved_data["seed"].toInt();
+    return {apply_free(pf, seed, rows, g[0], true), torch::Tensor(), torch::Tensor(),
+            torch::Tensor()};
   }
 };
 
@@ -146,10 +150,11 @@ torch::Tensor project_stored(torch::Tensor x, torch::Tensor row_ptr, torch::Tens
   return StoredProjection::apply(x, row_ptr, col, val, col_ptr, row, cval, n);
 }
 
-torch::Tensor project_free(torch::Tensor x, torch::Tensor rows, std::vector<double> problem) {
+torch::Tensor project_free(torch::Tensor x, torch::Tensor rows, std::vector<double> problem,
+                           int64_t seed) {
   check_vec(rows, torch::kInt32, "rows");
   TORCH_CHECK(x.is_cuda(), "x must be a CUDA tensor");
-  return FreeProjection::apply(x, rows, problem);
+  return FreeProjection::apply(x, rows, problem, seed);
 }
 
 }  // namespace

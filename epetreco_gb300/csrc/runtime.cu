@@ -39,7 +39,10 @@ static cudaMemPool_t lib_pool(cudaError_t* err) {
   return g_pool[dev];
 }
 
+static std::atomic<long long> g_allocs{0};
+
 cudaError_t dev_alloc(void** p, size_t bytes, cudaStream_t st) {
+  g_allocs.fetch_add(1, std::memory_order_relaxed);
   cudaError_t e = cudaSuccess;
   cudaMemPool_t pool = lib_pool(&e);
   if (!pool) return e != cudaSuccess ? e : cudaErrorInvalidDevice;
@@ -134,6 +137,8 @@ const char* epet_last_error(void) { return epet::g_err; }
 const char* epet_version(void) { return "epet_gb300 1.0 (sm_103a)"; }
 
 long long epet_launch_count(void) { return epet::launches(); }
+
+long long epet_device_allocations(void) { return epet::g_allocs.load(); }
 
 epet_status epet_problem_validate(const epet_problem* p) {
   using epet::set_error;

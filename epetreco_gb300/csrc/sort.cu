@@ -11,6 +11,8 @@
 #include <type_traits>
 #include <mutex>
 
+#include <cuda.h>
+
 #include "common.cuh"
 #include "internal.h"
 
@@ -151,10 +153,22 @@ static RsGrid rs_grid(int64_t n) {
   return g;
 }
 
+// A pass whose digit is the same in every key is the identity permutation.
+// `vary` (device, optional) holds the OR and the AND of all keys; where
+// given, a pass over a digit with no varying bit only copies its input.
+__device__ __forceinline__ bool pass_active(const uint64_t* vary, int shift, unsigned mask) {
+  return !vary || ((unsigned)((vary[0] ^ vary[1]) >> shift) & mask) != 0u;
+}
+
 template <int BITS, typename In>
 __global__ void __launch_bounds__(kRsThreads)
-k_radix_hist(In in, int64_t n, int shift, int64_t tpc, int nchunks, int64_t* __restrict__ hist) {
+k_radix_hist(In in, int64_t n, int shift, int64_t tpc, int nchunks, int64_t* __restrict__ hist,
+             const uint64_t* __restrict__ vary) {
   constexpr int BINS = 1 << BITS;
+  if (!pass_active(vary, shift, BINS - 1)) {
+    for (int d = threadIdx.x; d < BINS; d += kRsThreads) hist[(int64_t)d * nchunks + blockIdx.x] = 0;
+    return;
+  }
   __shared__ unsigned cnt[BINS];
   for (int d = threadIdx.x; d < BINS; d += kRsThreads) cnt[d] = 0;
   __syncthreads();
@@ -225,8 +239,15 @@ struct CscOut {
 template <int BITS, typename K, typename V, typename In, typename Out>
 __global__ void __launch_bounds__(kRsThreads, 3)
 k_radix_scatter(In in, Out out, int64_t n, int shift, int64_t tpc, int nchunks,
-                const int64_t* __restrict__ offs) {
+                const int64_t* __restrict__ offs, const uint64_t* __restrict__ vary) {
   constexpr int BINS = 1 << BITS;
+  if (!pass_active(vary, shift, BINS - 1)) {
+    const int64_t beg = (int64_t)blockIdx.x * tpc * kRsTile;
+    const int64_t end = min(n, beg + tpc * kRsTile);
+    for (int64_t i = beg + threadIdx.x; i < end; i += kRsThreads)
+      out.put(i, in.key(i), in.val(i), false);
+    return;
+  }
   __shared__ unsigned wcnt[kRsWarps][BINS];
   __shared__ unsigned dstart[BINS + 1];
   __shared__ unsigned warp_tot[kRsWarps];
@@ -363,17 +384,17 @@ size_t radix_hist_elems(int64_t n) {
 // One pass: histogram of `in`'s keys, scan, scatter from `in` to `out`.
 template <int BITS, typename K, typename V, typename In, typename Out>
 epet_status radix_pass(In in, Out out, int64_t n, int shift, int64_t* hist, int64_t* hist_scan,
-                       int64_t* scan_tmp, cudaStream_t st) {
+                       int64_t* scan_tmp, cudaStream_t st, const uint64_t* vary = nullptr) {
   const RsGrid g = rs_grid(n);
   k_radix_hist<BITS, In><<<(unsigned)g.nchunks, kRsThreads, 0, st>>>(in, n, shift, g.tpc,
-                                                                     g.nchunks, hist);
+                                                                     g.nchunks, hist, vary);
   EPET_LAUNCHED();
   EPET_CHECK(exclusive_scan_i64(hist, hist_scan, (int64_t)(1 << BITS) * g.nchunks, scan_tmp, st));
   const size_t dyn = (sizeof(K) + sizeof(V)) * (size_t)kRsTile;
   EPET_CUDA(cudaFuncSetAttribute(k_radix_scatter<BITS, K, V, In, Out>,
                                  cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn));
   k_radix_scatter<BITS, K, V, In, Out><<<(unsigned)g.nchunks, kRsThreads, dyn, st>>>(
-      in, out, n, shift, g.tpc, g.nchunks, hist_scan);
+      in, out, n, shift, g.tpc, g.nchunks, hist_scan, vary);
   EPET_LAUNCHED();
   return EPET_OK;
 }
@@ -578,18 +599,29 @@ epet_status epet_csr2ecsr(int64_t* ecsr_d, const int32_t* yrow_d, int64_t nnzr,
   return EPET_OK;
 }
 
+// Radix passes of the column-major copy: one 9-bit pass up to 2^9 columns,
+// an 8/9-bit and a 9-bit pass up to 2^18, then 9-bit passes (ping-pong
+// through a second key/value pair) up to the int32 column range.
+static int csc_passes(int64_t n) {
+  const int bits = std::max(1, bits_for(n - 1));
+  return bits <= 18 ? (bits <= 9 ? 1 : 2) : (bits + 8) / 9;
+}
+
 size_t epet_csr_to_csc_workspace_size(int64_t m, int64_t n, int64_t nnz) {
   (void)m;
-  (void)n;
   const size_t hist = radix_hist_elems(nnz);
-  return 2 * align256(nnz * 4) + align256(nnz * 8) + align256(hist * 8) +
-         align256((hist + 1) * 8) + align256(scan_tmp_elems(hist) * 8) + 256;
+  const size_t pair = csc_passes(n) > 2 ? 2 : 1;  // key/value pairs between passes
+  return 2 * align256(nnz * 4) + align256(nnz * 8) + (pair - 1) * (align256(nnz * 4) +
+         align256(nnz * 8)) + align256(hist * 8) + align256((hist + 1) * 8) +
+         align256(scan_tmp_elems(hist) * 8) + 256;
 }
 
 epet_status epet_csr_to_csc(const epet_csr* a, epet_csc* out, void* ws, size_t ws_bytes,
                             epet_stream_t stream) {
   if (!a || !out || !out->col_ptr || (a->nnz > 0 && (!out->row || !out->val)))
     return set_error(EPET_ERR_INVALID, "bad arguments");
+  if (a->n < 0 || a->n > (int64_t)INT32_MAX + 1)
+    return set_error(EPET_ERR_INVALID, "column count %lld", (long long)a->n);
   cudaStream_t st = (cudaStream_t)stream;
   const int64_t nnz = a->nnz;
   out->m = a->m;
@@ -601,28 +633,28 @@ epet_status epet_csr_to_csc(const epet_csr* a, epet_csc* out, void* ws, size_t w
   }
   Scratch scr;
   EPET_CHECK(scr.init(ws, ws_bytes, epet_csr_to_csc_workspace_size(a->m, a->n, nnz), st));
+  const int passes = csc_passes(a->n);
   uint32_t* key = scr.take<uint32_t>(nnz);
   uint64_t* pv = scr.take<uint64_t>(nnz);
+  uint32_t* key2 = passes > 2 ? scr.take<uint32_t>(nnz) : nullptr;
+  uint64_t* pv2 = passes > 2 ? scr.take<uint64_t>(nnz) : nullptr;
   const size_t hn = radix_hist_elems(nnz);
   int64_t* hist = scr.take<int64_t>(hn);
   int64_t* hist_scan = scr.take<int64_t>(hn + 1);
   int64_t* tmp = scr.take<int64_t>(scan_tmp_elems(hn));
-  if (scr.overrun) return set_error(EPET_ERR_INVALID, "internal: workspace size");
-  const int bits = std::max(1, bits_for(a->n - 1));
-  if (bits > 18)
-    return set_error(EPET_ERR_UNSUPPORTED, "more than 2^18 voxels in the column-major copy");
   int32_t* rid = scr.take<int32_t>(nnz);
   if (scr.overrun) return set_error(EPET_ERR_INVALID, "internal: workspace size");
+  const int bits = std::max(1, bits_for(a->n - 1));
   k_row_ids<<<ceil_div(a->m * 32, 256), 256, 0, st>>>(a->row_ptr, a->m, rid);
   EPET_LAUNCHED();
   CsrIn in{a->col, rid, a->val};
   CscOut co{out->row, out->val, out->col_ptr};
   k_fill_i64<<<ceil_div(a->n + 1, 256), 256, 0, st>>>(out->col_ptr, a->n + 1, nnz);
   EPET_LAUNCHED();
-  if (bits <= 9) {
+  if (passes == 1) {
     // one pass: CSR -> CSC
     EPET_CHECK((radix_pass<9, uint32_t, uint64_t>(in, co, nnz, 0, hist, hist_scan, tmp, st)));
-  } else {
+  } else if (passes == 2) {
     // low digits: CSR -> (key, row|val); high digits -> CSC
     const int b0 = bits - 9;
     ArrOut<uint32_t, uint64_t> mid{key, pv};
@@ -631,6 +663,23 @@ epet_status epet_csr_to_csc(const epet_csr* a, epet_csc* out, void* ws, size_t w
     else EPET_CHECK((radix_pass<9, uint32_t, uint64_t>(in, mid, nnz, 0, hist, hist_scan, tmp, st)));
     EPET_CHECK((radix_pass<9, uint32_t, uint64_t>(mid_in, co, nnz, b0 <= 8 ? 8 : 9, hist,
                                                   hist_scan, tmp, st)));
+  } else {
+    // 9-bit digits from the least significant: CSR -> pair 0, pair k%2 ->
+    // pair (k+1)%2, the last one -> CSC
+    uint32_t* ks[2] = {key, key2};
+    uint64_t* vs[2] = {pv, pv2};
+    EPET_CHECK((radix_pass<9, uint32_t, uint64_t>(in, ArrOut<uint32_t, uint64_t>{ks[0], vs[0]},
+                                                  nnz, 0, hist, hist_scan, tmp, st)));
+    for (int k = 1; k < passes; k++) {
+      ArrIn<uint32_t, uint64_t> src{ks[(k - 1) & 1], vs[(k - 1) & 1]};
+      if (k + 1 < passes)
+        EPET_CHECK((radix_pass<9, uint32_t, uint64_t>(src, ArrOut<uint32_t, uint64_t>{ks[k & 1],
+                                                      vs[k & 1]}, nnz, 9 * k, hist, hist_scan,
+                                                      tmp, st)));
+      else
+        EPET_CHECK((radix_pass<9, uint32_t, uint64_t>(src, co, nnz, 9 * k, hist, hist_scan, tmp,
+                                                      st)));
+    }
   }
   // empty columns start where the next non-empty one does
   k_suffix_min_i64<<<1, 1024, 0, st>>>(out->col_ptr, a->n + 1);
@@ -643,20 +692,96 @@ epet_status epet_csr_to_csc(const epet_csr* a, epet_csc* out, void* ws, size_t w
 // ----------------------------------------------- allocation-free cooSort
 //
 // For callers that must not allocate device memory from inside the library
-// call: code running inside a captured stream region or a real-time loop
-// where cudaMalloc would synchronise the device or fail, a host process whose
-// allocator owns all device memory, or an integration whose memory budget is
-// fixed at start-up.  The sort's scratch lives in a file-scope device array
-// sized for kNoAllocCooSortMax entries (about 6.6 MB), which every GPU that
+// call: a host process whose own allocator owns all device memory, an
+// integration whose memory budget is fixed at start-up, or a loop that must
+// not wait on the allocator.  The sort's scratch lives in a file-scope device
+// array sized for kNoAllocCooSortMax entries (7 MiB), which every GPU that
 // loads this library holds until the process exits.
+//
+// Unlike epet_coo_sort, this path reads nothing back to the host: the keys
+// are (row, col) with the sign bits flipped (so unsigned order is the signed
+// order of the reference's comparator, negative ids included), all eight
+// 8-bit digits get a pass, and a pass over a digit that no key varies in
+// (found on the device from the OR and AND of the keys) only copies.
 
 namespace epet {
 constexpr int64_t kNoAllocCooSortMax = int64_t(1) << 18;  // 262,144 triples
 constexpr size_t kNoAllocScratchBytes = size_t(7) << 20;  // 7 MiB
 static __device__ __align__(256) unsigned char g_coo_sort_scratch[kNoAllocScratchBytes];
 
+__global__ void k_pack_coo_signed(const int32_t* row, const int32_t* col, const float* val,
+                                  int64_t n, uint64_t* key, uint32_t* v, uint64_t* vary) {
+  uint64_t o = 0, a = ~uint64_t(0);
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const uint64_t k = ((uint64_t)((uint32_t)row[i] ^ 0x80000000u) << 32) |
+                       ((uint32_t)col[i] ^ 0x80000000u);
+    key[i] = k;
+    v[i] = __float_as_uint(val[i]);
+    o |= k;
+    a &= k;
+  }
+  for (int s = 16; s > 0; s >>= 1) {
+    o |= __shfl_xor_sync(0xffffffffu, o, s);
+    a &= __shfl_xor_sync(0xffffffffu, a, s);
+  }
+  if ((threadIdx.x & 31) == 0) {
+    atomicOr(reinterpret_cast<unsigned long long*>(vary), (unsigned long long)o);
+    atomicAnd(reinterpret_cast<unsigned long long*>(vary + 1), (unsigned long long)a);
+  }
+}
+
+__global__ void k_unpack_coo_signed(const uint64_t* key, const uint32_t* v, int64_t n,
+                                    int32_t* row, int32_t* col, float* val) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) {
+    row[i] = (int32_t)((uint32_t)(key[i] >> 32) ^ 0x80000000u);
+    col[i] = (int32_t)((uint32_t)key[i] ^ 0x80000000u);
+    val[i] = __uint_as_float(v[i]);
+  }
+}
+
+static size_t noalloc_scratch_need(int64_t n) {
+  const size_t hn = radix_hist_elems(n);
+  return 2 * align256(n * 8) + 2 * align256(n * 4) + align256(hn * 8) + align256((hn + 1) * 8) +
+         align256(scan_tmp_elems(hn) * 8) + align256(16);
+}
+
+// Device address of the array, per device, for the context it was looked up
+// in (a caller that makes another context current gets it looked up again).
+typedef CUresult (*CtxGetCurrentFn)(CUcontext*);
 static std::mutex g_noalloc_mu;
-static void* g_noalloc_ptr[256];  // device address of the array, per device
+static void* g_noalloc_ptr[256];
+static CUcontext g_noalloc_ctx[256];
+
+static epet_status noalloc_scratch(void** out) {
+  static CtxGetCurrentFn ctx_get = [] {
+    void* fn = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &fn, 12000, cudaEnableDefault, &q) !=
+            cudaSuccess ||
+        q != cudaDriverEntryPointSuccess)
+      fn = nullptr;
+    return reinterpret_cast<CtxGetCurrentFn>(fn);
+  }();
+  int dev = 0;
+  EPET_CUDA(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= 256) return set_error(EPET_ERR_UNSUPPORTED, "device index %d", dev);
+  // cudaGetDevice made the device's primary context current if none was
+  CUcontext ctx = nullptr;
+  if (ctx_get) ctx_get(&ctx);
+  std::lock_guard<std::mutex> lk(g_noalloc_mu);
+  if (!g_noalloc_ptr[dev] || g_noalloc_ctx[dev] != ctx) {
+    // the array's host-side name is a stand-in, not a device address
+    void* p = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&p, g_coo_sort_scratch);
+    if (e != cudaSuccess) return cuda_status(e, "cudaGetSymbolAddress(g_coo_sort_scratch)");
+    g_noalloc_ptr[dev] = p;
+    g_noalloc_ctx[dev] = ctx;
+  }
+  *out = g_noalloc_ptr[dev];
+  return EPET_OK;
+}
 }  // namespace epet
 
 extern "C" epet_status epet_coo_sort_noalloc(float* val_d, int32_t* row_d, int32_t* col_d,
@@ -670,27 +795,42 @@ extern "C" epet_status epet_coo_sort_noalloc(float* val_d, int32_t* row_d, int32
                      "epet_coo_sort with a workspace for larger inputs",
                      (long long)kNoAllocCooSortMax, (long long)n);
   if (n <= 1) return EPET_OK;
-  const size_t need = epet_coo_sort_workspace_size(n);
-  if (need > kNoAllocScratchBytes)
-    return set_error(EPET_ERR_INVALID, "internal: static scratch too small (%zu > %zu)", need,
-                     kNoAllocScratchBytes);
-  // The array's host-side name is not a device address: resolve it once per
-  // device, with that device current.
-  int dev = 0;
-  EPET_CUDA(cudaGetDevice(&dev));
-  if (dev < 0 || dev >= 256) return set_error(EPET_ERR_UNSUPPORTED, "device index %d", dev);
+  if (noalloc_scratch_need(n) > kNoAllocScratchBytes)
+    return set_error(EPET_ERR_INVALID, "internal: static scratch too small (%zu > %zu)",
+                     noalloc_scratch_need(n), kNoAllocScratchBytes);
   void* scratch = nullptr;
-  {
-    std::lock_guard<std::mutex> lk(g_noalloc_mu);
-    if (!g_noalloc_ptr[dev]) {
-      void* p = nullptr;
-      cudaError_t e = cudaGetSymbolAddress(&p, g_coo_sort_scratch);
-      if (e != cudaSuccess) return cuda_status(e, "cudaGetSymbolAddress(g_coo_sort_scratch)");
-      g_noalloc_ptr[dev] = p;
-    }
-    scratch = g_noalloc_ptr[dev];
+  EPET_CHECK(noalloc_scratch(&scratch));
+  cudaStream_t st = (cudaStream_t)stream;
+  Scratch scr;  // carves the array; owns nothing
+  EPET_CHECK(scr.init(scratch, kNoAllocScratchBytes, noalloc_scratch_need(n), st));
+  uint64_t* key = scr.take<uint64_t>(n);
+  uint64_t* key2 = scr.take<uint64_t>(n);
+  uint32_t* v = scr.take<uint32_t>(n);
+  uint32_t* v2 = scr.take<uint32_t>(n);
+  const size_t hn = radix_hist_elems(n);
+  int64_t* hist = scr.take<int64_t>(hn);
+  int64_t* hist_scan = scr.take<int64_t>(hn + 1);
+  int64_t* tmp = scr.take<int64_t>(scan_tmp_elems(hn));
+  uint64_t* vary = scr.take<uint64_t>(2);
+  if (scr.overrun) return set_error(EPET_ERR_INVALID, "internal: workspace size");
+  // the array keeps the previous call's contents: the OR starts at 0, the AND at all ones
+  EPET_CUDA(cudaMemsetAsync(vary, 0x00, 8, st));
+  EPET_CUDA(cudaMemsetAsync(vary + 1, 0xff, 8, st));
+  const int T = 256;
+  k_pack_coo_signed<<<std::min(ceil_div(n, T), 1024), T, 0, st>>>(row_d, col_d, val_d, n, key,
+                                                                   v, vary);
+  EPET_LAUNCHED();
+  // eight passes (an even count: the result ends in key / v)
+  uint64_t *sk = key, *dk = key2;
+  uint32_t *sv = v, *dv = v2;
+  for (int shift = 0; shift < 64; shift += 8) {
+    EPET_CHECK((radix_pass<8, uint64_t, uint32_t>(ArrIn<uint64_t, uint32_t>{sk, sv},
+                                                  ArrOut<uint64_t, uint32_t>{dk, dv}, n, shift,
+                                                  hist, hist_scan, tmp, st, vary)));
+    std::swap(sk, dk);
+    std::swap(sv, dv);
   }
-  // The caller-workspace path of epet_coo_sort allocates nothing; every
-  // scratch section it uses is written before it is read.
-  return epet_coo_sort(val_d, row_d, col_d, n, scratch, kNoAllocScratchBytes, stream);
+  k_unpack_coo_signed<<<ceil_div(n, T), T, 0, st>>>(key, v, n, row_d, col_d, val_d);
+  EPET_LAUNCHED();
+  return EPET_OK;
 }

@@ -136,6 +136,10 @@ const char* epet_version(void);
 /* Number of kernels this library has launched in the process (CUDA-graph
  * replays count the kernels they contain); for launch accounting. */
 long long epet_launch_count(void);
+/* Number of device allocations the library has made itself in the process
+ * (from its memory pool; caller workspaces are not counted).  For
+ * accounting and tests; no counterpart in the reference. */
+long long epet_device_allocations(void);
 /* Problem checks: index ranges fit int32, nrays >= 1, positive pitches,
  * ray_mode one of EPET_RAYS_*. */
 epet_status epet_problem_validate(const epet_problem* p);
@@ -236,16 +240,24 @@ epet_status epet_coo_sort(float* val_d, int32_t* row_d, int32_t* col_d,
                           int64_t n, void* ws, size_t ws_bytes,
                           epet_stream_t stream);
 size_t epet_coo_sort_workspace_size(int64_t n);
-/* epet_coo_sort for callers that cannot allocate device memory during the
- * call (inside a stream-capture region, a real-time loop, or an integration
- * whose allocator owns the device memory).  No counterpart in the reference.
- * Allocates nothing: its scratch is a file-scope device array of about 7 MB,
- * held by every GPU that loads the library, so n is limited to 262,144
- * triples (EPET_ERR_CAPACITY above that).  The first call on a device looks
- * up the array's device address with that device current; make that first
- * call before any stream capture.  All calls share the one array: calls that
- * overlap on the GPU (different streams, or several host threads) race on it
- * and must be serialised by the caller. */
+/* epet_coo_sort for callers that cannot let the library allocate device
+ * memory: a host application whose own allocator owns all of the device's
+ * memory, or an integration whose memory budget is fixed at start-up.  No
+ * counterpart in the reference.  Allocates nothing: its scratch is a
+ * file-scope device array of 7 MiB, held by every GPU that loads the library
+ * until the process exits, so n is limited to 262,144 triples
+ * (EPET_ERR_CAPACITY above that).  Stream-ordered, and nothing is read back
+ * to the host: ids sort in signed order (negative ids included, as the
+ * reference's comparator orders them), where epet_coo_sort rejects negative
+ * ids.  The first call on a device looks up the array's device address
+ * (cudaGetSymbolAddress) with that device current, and again when another
+ * context has been made current; make that first call before any stream
+ * capture begins.  The address is not looked up again after cudaDeviceReset
+ * of a device whose context handle stays the same: do not use this call on a
+ * device after resetting it in the same process.  All calls share the one
+ * array, which keeps the last call's contents (the call initialises what it
+ * reads): calls that overlap on the GPU (different streams, or several host
+ * threads) race on it and must be serialised by the caller. */
 epet_status epet_coo_sort_noalloc(float* val_d, int32_t* row_d, int32_t* col_d,
                                   int64_t n, epet_stream_t stream);
 /* convertCoo2Csr (cusparseWrapper.hpp:38-45): row pointer of row-sorted COO. */

@@ -21,7 +21,22 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 ORACLE_SO = os.path.join(HERE, "_build", "libepet_oracle.so")
 REF_SO = os.path.join(HERE, "_ref", "libepet_ref.so")
-REF_SRC = os.environ.get("EPET_REF_SRC", "/root/reference/src")
+
+
+def _ref_src() -> str:
+    """The reference's src/ tree: EPET_REF_SRC, else the recipe's default
+    (``make -C oracle ref-src``)."""
+    env = os.environ.get("EPET_REF_SRC")
+    if env:
+        return env
+    try:
+        return subprocess.run(["make", "-s", "-C", HERE, "ref-src"], capture_output=True,
+                              text=True, check=True).stdout.strip()
+    except (OSError, subprocess.CalledProcessError):
+        return ""
+
+
+REF_SRC = _ref_src()
 
 _f32p = np.ctypeslib.ndpointer(np.float32, flags="C_CONTIGUOUS")
 _f64p = np.ctypeslib.ndpointer(np.float64, flags="C_CONTIGUOUS")

@@ -101,3 +101,18 @@ def test_gradient_reconstruction_decreases_nll(setup):
     x, losses = reconstruct(proj, y, iters=30, lr=0.05)
     assert losses[-1] < losses[0]
     assert torch.isfinite(x).all() and (x > 0).all()
+
+
+def test_matrix_free_keeps_a_64_bit_seed(gpu_lib):
+    """A seed above 2^53 (not exact in float64) reaches the matrix-free
+    projector unchanged: its forward equals the stored product built with
+    the same seed."""
+    from epetreco_gb300.autograd import Projector
+    p = config("small")["problem"].with_seed(2**63 + 12345)
+    rows = torch.arange(20000, 20400, dtype=torch.int32, device="cuda")
+    free = Projector(p, rows, mode="free")
+    A = api.systemMatrixCalculation(p, rows)
+    x = torch.rand(p.nvoxels, device="cuda")
+    assert torch.allclose(free(x), api.CSRmv(0, A, x), rtol=2e-6, atol=0)
+    B = api.systemMatrixCalculation(p.with_seed(2**63 + 12344), rows)
+    assert not torch.equal(A.val, B.val)  # the low bits of the seed matter

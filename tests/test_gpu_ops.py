@@ -54,6 +54,29 @@ def test_coosort_large_matches_numpy(gpu_lib):
     assert (v.cpu().numpy() == val[order]).all()
 
 
+@pytest.mark.parametrize("ncols", [(1 << 18) + 1, (1 << 27) + 3])
+def test_csc_beyond_two_radix_passes(gpu_lib, ncols):
+    """Column-major copies of grids above 2^18 voxels (three and four 9-bit
+    passes): stable transpose against numpy, empty columns included."""
+    rng = np.random.default_rng(ncols & 0xffff)
+    m = 3000
+    lens = rng.integers(0, 300, m)
+    rp = np.concatenate([[0], np.cumsum(lens)]).astype(np.int64)
+    hot = np.unique(rng.integers(0, ncols, 2000))  # columns shared by many rows
+    col = np.concatenate([np.sort(rng.choice(hot, l, replace=False)) for l in lens]).astype(
+        np.int32)
+    val = rng.random(col.size).astype(np.float32)
+    A = api.Csr(dev(rp), dev(col), dev(val), ncols)
+    At = api.csr_to_csc(A)
+    r = np.repeat(np.arange(m), lens)
+    order = np.lexsort((r, col))
+    cnt = np.bincount(col, minlength=ncols)
+    got_ptr = At.col_ptr.cpu().numpy()
+    assert got_ptr[0] == 0 and (np.diff(got_ptr) == cnt).all()
+    assert (At.row.cpu().numpy() == r[order]).all()
+    assert (bits(At.val.cpu().numpy()) == bits(val[order])).all()
+
+
 def test_coo2csr_kat(gpu_lib, golden):
     # test_cusparseWrapper.cu:20-55
     csr = api.convertCoo2Csr(dev(golden["coo2csr_row"]), 9, 4)
