@@ -54,6 +54,10 @@ def parse():
                     help="run only the batched-reconstruction measurement")
     ap.add_argument("--no-forms", action="store_true",
                     help="skip the 16-bit value forms")
+    ap.add_argument("--no-rebuild", action="store_true",
+                    help="skip the matrix-free (rebuild every iteration) schedule")
+    ap.add_argument("--no-parity", action="store_true",
+                    help="skip the per-iteration image error against the FP64 oracle")
     ap.add_argument("--profile", action="store_true",
                     help="one reconstruction with one iteration, nothing else (for ncu)")
     ap.add_argument("--profile-kernels", type=int, default=0, metavar="ROWS",
@@ -125,19 +129,23 @@ class ClockSampler:
 # ------------------------------------------------------------ CPU baseline
 
 def cpu_baseline(cfg_name: str, sample: int, seed: int = 0):
-    """The oracle (plain C restatement of the reference's per-iteration work,
-    OpenMP over host cores): for a seeded sample of channels, the reference's
-    dense candidate scan over all voxels, the nrays-ray values of every
-    candidate, and the forward/transpose products of those rows.  Scaled by
-    the number of measured channels (estimated from the sample); the
-    reference rebuilds the matrix in every iteration (reco.cu:216-254)."""
+    """The oracle (plain C restatement of the reference's work for the path,
+    OpenMP over host cores) on a seeded sample of channels: the reference's
+    dense candidate scan over all voxels plus the nrays-ray values of every
+    candidate (the system-matrix build), and the forward and transpose
+    products over those rows (replicated to a few tens of millions of
+    non-zeros, beyond the caches).  Per-row costs are scaled to the measured
+    rows (estimated from the sample) for two schedules: the matrix built
+    once per step and iterated (the schedule of the GPU arm's `value`), and
+    the reference's own loop, which rebuilds the matrix in every iteration
+    (reco.cu:216-254)."""
     import numpy as np
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     from pyoracle import Oracle
     from epetreco_gb300.phantom import phantom_image
     from epetreco_gb300.problem import config
     cfg = config(cfg_name)
-    p = cfg["problem"]
+    p, nit = cfg["problem"], cfg["iterations"]
     o = Oracle()
     rng = np.random.default_rng(seed)
     rows = np.sort(rng.choice(p.nchannels, sample, replace=False)).astype(np.int32)
@@ -146,19 +154,29 @@ def cpu_baseline(cfg_name: str, sample: int, seed: int = 0):
     x_true = phantom_image(p, 1)
     t0 = time.perf_counter()
     rp, col, val = o.sm_build_csr(p, rows, p.nrays, rnd, exact=False)
-    yb = o.csrmv(0, rp, col, val, x_true, p.nvoxels)
+    t_build = time.perf_counter() - t0
+    reps = max(1, int(2e7 // max(1, len(col))))
+    lens = np.tile(np.diff(rp), reps)
+    rpb = np.concatenate([[0], np.cumsum(lens)]).astype(np.int64)
+    colb, valb = np.tile(col, reps), np.tile(val, reps)
+    t0 = time.perf_counter()
+    yb = o.csrmv(0, rpb, colb, valb, x_true, p.nvoxels)
     e = np.where(yb > 0, 1.0 / np.maximum(yb, 1e-30), 0).astype(np.float32)
-    o.csrmv(1, rp, col, val, e, p.nvoxels)
-    dt = time.perf_counter() - t0
-    measured_frac = max(float((yb > 0).mean()), 1.0 / sample)
+    o.csrmv(1, rpb, colb, valb, e, p.nvoxels)
+    t_prod = (time.perf_counter() - t0) / reps
+    measured_frac = max(float((yb[:sample] > 0).mean()), 1.0 / sample)
     m_est = measured_frac * p.nchannels
-    t_iter = dt / sample * m_est
+    t_once = m_est / sample * (t_build + nit * t_prod)
+    t_rebuild = m_est / sample * nit * (t_build + t_prod)
     cores = int(os.environ.get("OMP_NUM_THREADS", os.cpu_count() or 1))
-    return {"value": 1.0 / t_iter, "unit": UNIT, "cores": cores, "kind": "port",
-            "sample": (f"{sample} seeded channels of the {cfg_name} workload through candidate "
-                       f"scan + {p.nrays}-ray values + forward/transpose products "
-                       f"({dt:.1f} s), scaled to {m_est:.0f} measured rows per iteration"),
-            "sample_seconds": dt}
+    return {"value": nit / t_once, "unit": UNIT, "cores": cores, "kind": "port",
+            "sample": (f"{sample} seeded channels of the {cfg_name} workload: candidate scan + "
+                       f"{p.nrays}-ray values ({t_build:.1f} s), forward/transpose products "
+                       f"({t_prod * 1e3:.1f} ms per pass over the sample, timed on {reps} "
+                       f"copies); scaled to {m_est:.0f} measured rows, matrix built once and "
+                       f"{nit} iterations"),
+            "rebuild_per_iteration": nit / t_rebuild,
+            "sample_seconds": t_build + reps * t_prod}
 
 
 def aggregate_replicas(times, nit, world, dist, device):
@@ -181,19 +199,27 @@ def workload_name(cfg_name: str) -> str:
             f"{cfg['iterations']} iterations per step")
 
 
+SCHEDULE = ("a step = one reconstruction: the system matrix of the measured rows built once, "
+            "then the workload's iterations")
+REBUILD = ("the reference's own loop (reco.cu:216-254): the system matrix recomputed in every "
+           "iteration")
+
+
 def reference_arm(args):
     """--impl reference: the reference's CPU work for the path (oracle port;
-    the reference's own sources are not available where the bench runs)."""
+    the reference's own sources are not available where the bench runs), on
+    the same workload and schedule as the GB300 arm."""
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
-    per = []
+    per, reb = [], []
     if args.warmup > 0:
         cpu_baseline(args.config, max(4, args.cpu_sample // 16), seed=99)
     info = None
     for k in range(args.steps):
         info = cpu_baseline(args.config, args.cpu_sample, seed=k)
         per.append(info["value"])
+        reb.append(info["rebuild_per_iteration"])
     v = sorted(per)[len(per) // 2]
     from epetreco_gb300.problem import config
     nit = config(args.config)["iterations"]
@@ -201,9 +227,10 @@ def reference_arm(args):
            "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
            "ms_per_step": 1000.0 * nit / v if v else None, "higher_is_better": True,
            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-           "config": {"workload": workload_name(args.config),
-                      "schedule": "the reference's loop: the system matrix of the measured "
-                                  "rows rebuilt in every iteration (reco.cu:216-254)"},
+           "config": {"workload": workload_name(args.config)},
+           "schedule": SCHEDULE,
+           "rebuild_per_iteration": {"value": sorted(reb)[len(reb) // 2], "unit": UNIT,
+                                     "schedule": REBUILD},
            "cpu_baseline": {"value": v, "unit": UNIT, "cores": info["cores"],
                             "kind": info["kind"], "sample": info["sample"]},
            "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
@@ -463,6 +490,7 @@ def gb300_arm(args):
     c1 = api.build_counters()
     # rows of one build redone with their exact window size (timeit runs it twice)
     build_rows = {k: (c1[k] - c0[k]) // 2 for k in c0}
+    steps = api.ray_steps(p, rows)
     t_csc = timeit(lambda: api.csr_to_csc(A), reps=1)
     At = api.csr_to_csc(A)
     x = torch.full((p.nvoxels,), 1.0 / p.nvoxels, device="cuda")
@@ -470,7 +498,7 @@ def gb300_arm(args):
     t_fwd = timeit(lambda: api.CSRmv(0, A, x), reps=5)
     t_bwd = timeit(lambda: api.CSRmv(1, A, e, At=At), reps=5)
     t_iter = timeit(lambda: R.iterate(1), reps=5)
-    del A, At
+    del At
     peaks = {}
     try:
         peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
@@ -492,29 +520,62 @@ def gb300_arm(args):
         except Exception:
             traffic = None
 
-    # ---- 16-bit value forms: iteration speed and image error vs FP32
+    # ---- the reference's schedule on the GPU: no matrix stored, the chords
+    # recomputed in every iteration (one walk per row gives A x, the ratio
+    # and the row's share of A^T e)
+    rebuild = None
+    if not args.no_rebuild:
+        Rf = api.Mlem(p, rows, y, s, matrix_free=True)
+        Rf.iterate(1)
+        Rf.close()
+        a_ev, b_ev = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        a_ev.record(st)
+        Rf = api.Mlem(p, rows, y, s, matrix_free=True)
+        Rf.iterate(nit)
+        b_ev.record(st)
+        torch.cuda.synchronize()
+        Rf.close()
+        t_rb = a_ev.elapsed_time(b_ev) / 1000.0
+        rebuild = {"value": nit / t_rb, "unit": UNIT, "ms_per_step": 1000 * t_rb,
+                   "ms_per_iteration": 1000 * t_rb / nit, "schedule": REBUILD,
+                   "how": "matrix-free reconstruction object: one chord walk per row and "
+                          "iteration (A x, e = y / A x, the row's A^T e)"}
+
+    # ---- per-iteration images of the three value forms, for the FP64 oracle
+    x0 = torch.full((p.nvoxels,), 1.0 / p.nvoxels, dtype=torch.float32, device="cuda")
+
+    def trace(Rx):
+        Rx.set_image(x0)
+        imgs = []
+        for _ in range(nit):
+            Rx.iterate(1)
+            imgs.append(Rx.image())
+        return torch.stack(imgs).cpu().numpy()
+
+    traces = {"fp32": trace(R)}
     forms = None
     if not args.no_forms:
-        # images after the same number of iterations in both forms (1 + 5 ran
-        # in timeit; at least the workload's count)
-        n_cmp = max(nit, 6)
-        R.iterate(n_cmp - 6)
-        x32 = R.image()
         forms = {"fp32": {"iteration_ms": 1000 * t_iter, "it_per_s": 1.0 / t_iter},
-                 "iterations": n_cmp}
+                 "iterations": nit}
         for name, fmt in (("bf16", 1), ("fp16", 2)):
             R16 = api.Mlem(p, rows, y, s, use_graph=True, value_format=fmt)
             t16 = timeit(lambda: R16.iterate(1), reps=5)
-            R16.iterate(n_cmp - 6)
-            x16 = R16.image()
-            err = float(((x16 - x32).double().norm() / x32.double().norm()).item())
+            traces[name] = trace(R16)
             st16 = R16.stats()
             forms[name] = {"iteration_ms": 1000 * t16, "it_per_s": 1.0 / t16,
                            "speedup_vs_fp32": t_iter / t16,
                            "bytes_per_iteration": st16["bytes_per_iteration"],
-                           "image_rel_l2_vs_fp32": err}
+                           "image_rel_l2_vs_fp32": float(
+                               np.linalg.norm(traces[name][-1] - traces["fp32"][-1]) /
+                               np.linalg.norm(traces["fp32"][-1]))}
             R16.close()
     R.close()
+    parity = None
+    if not args.no_parity and rank == 0:
+        parity = fp64_parity(p, A, rows, y, s, traces, nit)
+    del A
+    torch.cuda.empty_cache()
     batched = batched_small = None
     if args.batch > 0 and world == 1:
         batched = batch_measure(args, api, torch, st)
@@ -535,14 +596,16 @@ def gb300_arm(args):
         cpu.pop("sample_seconds", None)
     h2d = rows_h.numel() * 4 + y_h.numel() * 4 + s_h.numel() * 4
     d2h = x_h.numel() * 4
+    # the walk's work: grid cells crossed by all rays, per second of the build
+    sms = torch.cuda.get_device_properties(local).multi_processor_count
     out = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": 1000.0 * t_step, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": workload_name(args.config),
-                   "schedule": "system matrix of the measured rows built once per step",
-                   "measured_rows": m, "nnz": nnz, "parallelism": f"replicas{world}",
-                   "l2": "inputs larger than L2 (matrix streams of GBs per pass)"},
+        "config": {"workload": workload_name(args.config)},
+        "schedule": SCHEDULE,
+        "measured_rows": m, "nnz": nnz, "parallelism": f"replicas{world}",
+        "l2": "inputs larger than L2 (matrix streams of GBs per pass)",
         "e2e": {"value": value_e2e, "unit": UNIT, "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h},
         "gpu_launches": int(launches),
@@ -557,9 +620,16 @@ def gb300_arm(args):
                          "iteration": 1000 * t_iter},
         "plan": plan,
         "sm_build_nnz_per_s": nnz / t_build,
+        "sm_build_steps": {"ray_voxel_steps": steps, "per_s": steps / t_build,
+                           "per_sm_cycle": steps / t_build / (sms * 1e6 * (clocks.get("sm_mhz")
+                                                                          or 2070.0))},
         "sm_build_rows_redone": build_rows,
         "spmv_gbs": {"forward": fwd_bytes / t_fwd / 1e9, "transpose": bwd_bytes / t_bwd / 1e9},
     }
+    if rebuild is not None:
+        out["rebuild_per_iteration"] = rebuild
+    if parity is not None:
+        out["parity_fp64"] = parity
     if forms is not None:
         out["forms"] = forms
     if batched is not None:
@@ -571,6 +641,43 @@ def gb300_arm(args):
     print(json.dumps(out), flush=True)
     if dist is not None:
         dist.destroy_process_group()
+
+
+def fp64_parity(p, A, rows, y, s, traces, nit):
+    """Image error of every iteration of each value form against the FP64
+    oracle (the plain C restatement, on the host cores) run on the same
+    system matrix: the matrix of the measured rows copied to the host, the
+    sensitivity as the FP64 column sums of that matrix when every channel is
+    measured (else the library's FP64 sums), MLEM as reco.cu:209-281 in
+    FP64."""
+    import numpy as np
+    import torch
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    from pyoracle import Oracle
+    from epetreco_gb300 import api
+    t0 = time.perf_counter()
+    o = Oracle()
+    rp = A.row_ptr.cpu().numpy()
+    col = A.col.cpu().numpy()
+    val = A.val.cpu().numpy()
+    t_copy = time.perf_counter() - t0
+    m = rows.numel()
+    if m == p.nchannels:
+        s64 = o.csrmv_f64(1, rp, col, val, np.ones(m), p.nvoxels)
+        s_src = "FP64 column sums of the matrix on the host (every channel is measured)"
+    else:
+        s64 = api.sensitivity(p, return_f64=True)[1].cpu().numpy()
+        s_src = "the library's FP64 column sums over all channels"
+    x0 = np.full(p.nvoxels, 1.0 / p.nvoxels)
+    tr = o.mlem_f64_trace(rp, col, val, y.cpu().numpy().astype(np.float64), s64 / s64.sum(), x0,
+                          nit, p.nvoxels)
+    out = {"oracle": "FP64 MLEM of the plain C restatement on the host cores, same matrix",
+           "sensitivity": s_src, "iterations": nit, "nnz": int(len(col))}
+    for name, t in traces.items():
+        err = [float(np.linalg.norm(t[k] - tr[k]) / np.linalg.norm(tr[k])) for k in range(nit)]
+        out[name] = {"image_rel_l2_per_iteration": err, "max": max(err), "last": err[-1]}
+    out["seconds"] = {"copy": t_copy, "oracle": time.perf_counter() - t0 - t_copy}
+    return out
 
 
 def main():

@@ -56,7 +56,8 @@ class Csr16C(C.Structure):
 
 class MlemOptions(C.Structure):
     _fields_ = [("max_row_nnz", C.c_int32), ("use_graph", C.c_int32),
-                ("value_format", C.c_int32), ("autotune", C.c_int32)]
+                ("value_format", C.c_int32), ("autotune", C.c_int32),
+                ("matrix_free", C.c_int32)]
 
 
 P, VP, I64, I32, F, D, SZ = (C.POINTER(ProblemC), C.c_void_p, C.c_int64, C.c_int32, C.c_float,
@@ -80,6 +81,7 @@ SIGNATURES = {
     "epet_sm_build_workspace_size": [P, I64, I32],
     "epet_project_forward": [P, VP, I64, VP, VP, I32, VP, SZ, VP],
     "epet_project_back": [P, VP, I64, VP, VP, I32, VP, SZ, VP],
+    "epet_project_mlem": [P, VP, I64, VP, VP, VP, VP, I32, VP, SZ, VP],
     "epet_sensitivity": [P, VP, I64, VP, VP, I32, VP, SZ, VP],
     "epet_coo_sort": [VP, VP, VP, I64, VP, SZ, VP],
     "epet_coo_sort_workspace_size": [I64],
@@ -114,6 +116,7 @@ SIGNATURES = {
     "epet_trim_memory": [C.c_size_t],
     "epet_selftest_division": [I64, C.c_uint64, C.POINTER(C.c_int64), VP],
     "epet_build_counters": [C.POINTER(C.c_int64), C.POINTER(C.c_int64)],
+    "epet_ray_steps": [P, VP, I64, C.POINTER(C.c_int64), VP],
     "epet_mlem_batch_create": [I32, VP, VP, VP, VP, VP, C.POINTER(MlemOptions), C.POINTER(VP),
                                VP],
     "epet_mlem_batch_destroy": [VP],

@@ -199,6 +199,20 @@ def project_back(p, rows, e, c=None, max_row_nnz: int = 0) -> torch.Tensor:
     return c
 
 
+def project_mlem(p, rows, x, y, c64=None, ybar=None, max_row_nnz: int = 0):
+    """One matrix-free MLEM pass: ybar = A x, c64 += A^T (y / ybar) in fp64.
+    Returns (c64, ybar)."""
+    rows = _i32(rows)
+    if c64 is None:
+        c64 = torch.zeros(p.nvoxels, dtype=torch.float64, device="cuda")
+    if ybar is None:
+        ybar = torch.empty(rows.numel(), dtype=torch.float32, device="cuda")
+    check(lib().epet_project_mlem(C.byref(problem_struct(p)), _ptr(rows), rows.numel(),
+                                  _ptr(x.contiguous()), _ptr(y.to(torch.float32).contiguous()),
+                                  _ptr(ybar), _ptr(c64), int(max_row_nnz), None, 0, _stream()))
+    return c64, ybar
+
+
 def sensitivity(p, rows=None, max_row_nnz: int = 0, return_f64: bool = False):
     """s = column sums of A over the listed channels (all channels by
     default), fp64 accumulation, normalised to sum 1."""
@@ -383,6 +397,16 @@ def build_counters() -> dict:
     return {"overflow_rows": o.value, "exact_rows": e.value}
 
 
+def ray_steps(p, rows) -> int:
+    """Grid cells crossed by all rays of the listed channels (the walk's
+    work)."""
+    rows = _i32(rows)
+    n = C.c_int64(0)
+    check(lib().epet_ray_steps(C.byref(problem_struct(p)), _ptr(rows), rows.numel(), C.byref(n),
+                               _stream()))
+    return n.value
+
+
 class Mlem:
     """One reconstruction on the device (reco.cu's loop): the system matrix
     of the measured rows is built once at construction.  The rows may come in
@@ -390,14 +414,17 @@ class Mlem:
     channel), so a shuffled list gives the same object."""
 
     def __init__(self, p, rows, y, s, use_graph: bool = True, max_row_nnz: int = 0,
-                 value_format: int = 0, autotune: bool = False):
+                 value_format: int = 0, autotune: bool = False, matrix_free: bool = False):
+        """``matrix_free=True`` stores no matrix: every iteration recomputes
+        the chords in one walk per row (the reference's schedule of a matrix
+        rebuilt in every iteration)."""
         self.p = p
         rows = _i32(rows)
         y = y.to(torch.float32).contiguous()
         s = s.to(torch.float32).contiguous()
         self._h = C.c_void_p()
         opt = MlemOptions(int(max_row_nnz), 1 if use_graph else 0, int(value_format),
-                          1 if autotune else 0)
+                          1 if autotune else 0, 1 if matrix_free else 0)
         check(lib().epet_mlem_create(C.byref(problem_struct(p)), _ptr(rows), _ptr(y),
                                      rows.numel(), _ptr(s), C.byref(opt), C.byref(self._h),
                                      _stream()))

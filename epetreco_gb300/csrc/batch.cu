@@ -191,6 +191,9 @@ epet_status epet_mlem_batch_create(int32_t nprob, const epet_problem* problems,
     return set_error(EPET_ERR_INVALID, "bad arguments");
   epet_mlem_options o{};
   if (opt) o = *opt;
+  if (o.matrix_free)
+    return set_error(EPET_ERR_INVALID, "batched reconstructions store their matrices "
+                                       "(matrix_free is not supported)");
   if (o.value_format != EPET_VALUES_FP32)
     return set_error(EPET_ERR_INVALID, "batched reconstructions hold FP32 values");
   cudaStream_t st = (cudaStream_t)stream;

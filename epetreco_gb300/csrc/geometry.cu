@@ -9,6 +9,8 @@
 // and no generator is seeded.
 #include <curand_kernel.h>
 
+#include <algorithm>
+
 #include "common.cuh"
 #include "internal.h"
 
@@ -193,6 +195,46 @@ __global__ void k_selftest_div(int64_t n, uint64_t seed, unsigned long long* bad
 
 using namespace epet;
 
+// Work measure of the walk: the cells a ray crosses inside the grid, i.e. 1
+// + the grid planes it passes between its entry and exit (per axis, the
+// distance between the entry and exit cell indices).  Entry and exit cells
+// are taken a little inside the ray's grid interval, so a ray that only
+// grazes a plane counts the cells on one side of it.
+__global__ void k_ray_steps(Geo G, const float* __restrict__ rays, int64_t n,
+                            unsigned long long* __restrict__ total) {
+  const epet_grid& g = G.p.grid;
+  unsigned long long mine = 0;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const float* r = rays + 6 * i;
+    float a_in = 0.f, a_out = 1.f;
+    bool hit = true;
+    for (int a = 0; a < 3; a++) {
+      const float p0 = r[a], dp = r[a + 3] - r[a];
+      const float lo = g.o[a], hi = g.o[a] + g.n[a] * g.d[a];
+      if (dp == 0.f) {
+        hit = hit && p0 > lo && p0 < hi;
+      } else {
+        const float t0 = (lo - p0) / dp, t1 = (hi - p0) / dp;
+        a_in = fmaxf(a_in, fminf(t0, t1));
+        a_out = fminf(a_out, fmaxf(t0, t1));
+      }
+    }
+    if (!hit || !(a_in < a_out)) continue;
+    const float span = a_out - a_in, t_in = a_in + 1e-6f * span, t_out = a_out - 1e-6f * span;
+    unsigned long long st = 1;
+    for (int a = 0; a < 3; a++) {
+      const float dp = r[a + 3] - r[a];
+      const int c0 = min(max((int)floorf((r[a] + t_in * dp - g.o[a]) / g.d[a]), 0), g.n[a] - 1);
+      const int c1 = min(max((int)floorf((r[a] + t_out * dp - g.o[a]) / g.d[a]), 0), g.n[a] - 1);
+      st += (unsigned long long)abs(c1 - c0);
+    }
+    mine += st;
+  }
+  for (int o = 16; o > 0; o >>= 1) mine += __shfl_xor_sync(0xffffffffu, mine, o);
+  if ((threadIdx.x & 31) == 0 && mine) atomicAdd(total, mine);
+}
+
 extern "C" {
 
 epet_status epet_build_counters(int64_t* overflow_rows_h, int64_t* exact_rows_h) {
@@ -215,6 +257,35 @@ epet_status epet_selftest_division(int64_t n, uint64_t seed, int64_t* mismatches
   EPET_CUDA(dev_free(bad, st));
   EPET_CUDA(cudaStreamSynchronize(st));
   *mismatches_h = (int64_t)h;
+  return EPET_OK;
+}
+
+epet_status epet_ray_steps(const epet_problem* p, const int32_t* rows_d, int64_t m,
+                           int64_t* steps_h, epet_stream_t stream) {
+  EPET_CHECK(epet_problem_validate(p));
+  if (m < 0 || (m > 0 && !rows_d) || !steps_h) return set_error(EPET_ERR_INVALID, "bad arguments");
+  cudaStream_t st = (cudaStream_t)stream;
+  const Geo G = make_geo(*p);
+  // rays of chunks of rows (about 256 MB per chunk)
+  const int64_t ch = std::max<int64_t>(1, std::min<int64_t>(m, (int64_t(256) << 20) /
+                                                                   ((int64_t)p->nrays * 24)));
+  Scratch scr;
+  EPET_CHECK(scr.init(nullptr, 0, align256((size_t)ch * p->nrays * 24) + 256, st));
+  float* rays = scr.take<float>((size_t)ch * p->nrays * 6);
+  unsigned long long* tot = scr.take<unsigned long long>(1);
+  if (scr.overrun) return set_error(EPET_ERR_INVALID, "internal: workspace size");
+  EPET_CUDA(cudaMemsetAsync(tot, 0, 8, st));
+  for (int64_t c0 = 0; c0 < m; c0 += ch) {
+    const int64_t mc = std::min(ch, m - c0);
+    EPET_CHECK(launch_rays(G, rows_d + c0, mc, rays, false, st));
+    const int64_t nr = mc * p->nrays;
+    k_ray_steps<<<std::min<int64_t>(ceil_div(nr, 256), 8 * (int64_t)num_sms()), 256, 0, st>>>(G, rays, nr, tot);
+    EPET_LAUNCHED();
+  }
+  unsigned long long h = 0;
+  EPET_CUDA(cudaMemcpyAsync(&h, tot, 8, cudaMemcpyDeviceToHost, st));
+  EPET_CUDA(cudaStreamSynchronize(st));
+  *steps_h = (int64_t)h;
   return EPET_OK;
 }
 

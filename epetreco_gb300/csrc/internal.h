@@ -44,7 +44,8 @@ struct ExactRows {
 epet_status exact_rows_apply(const Geo& G, const int32_t* rows, const int32_t* ex_rows,
                              int64_t n_ex, int mode, int32_t* row_len, int32_t* src_idx,
                              ExactRows* keep, const float* x, float* y, const float* e,
-                             float* c, double* s64, cudaStream_t st);
+                             float* c, double* s64, const float* ycnt, double* c64,
+                             cudaStream_t st);
 epet_status column_sums(const epet_problem* p, const int32_t* rows_d, int64_t m,
                         double* s64, int32_t max_row_nnz, void* ws, size_t ws_bytes,
                         cudaStream_t st);

@@ -31,13 +31,39 @@ static void mlem_free(epet_mlem* h) {
                   h->At16.row_ptr, h->At16.base, h->At16.scale, h->At16.delta, h->At16.q,
                   h->rows, h->y, h->ybar, h->e16, h->s, h->x, h->xnew, h->e, h->A.row_ptr, h->A.col,
                   h->A.val,
-                  h->At.col_ptr, h->At.row, h->At.val, h->part_ll, h->part_x, h->sums};
+                  h->At.col_ptr, h->At.row, h->At.val, h->part_ll, h->part_x, h->sums, h->c64};
   for (void* b : bufs)
     if (b) dev_free(b, 0);
   delete h;
 }
 
+// x*c/s (dividesMultiplies, mlemOperations.hpp:38-79, with s == 0 -> 1) from
+// the fp64 correction image of the matrix-free schedule, rounded to fp32 as
+// the reference's float c.
+__global__ void k_update_c64(const float* __restrict__ x, const double* __restrict__ c64,
+                             const float* __restrict__ s, int64_t V, float* __restrict__ xnew) {
+  const int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (v >= V) return;
+  const float c = (float)c64[v];
+  float dvs = s[v];
+  dvs = __fadd_rn(dvs, (float)(dvs == 0.f));
+  xnew[v] = __fdiv_rn(__fmul_rn(x[v], c), dvs);
+}
+
+// The reference's schedule: the chords recomputed in every iteration (one
+// walk per row gives A x, e and the row's share of A^T e), then the update
+// and the normalisation.
+static epet_status mlem_iteration_free(epet_mlem* h, cudaStream_t st) {
+  EPET_CUDA(cudaMemsetAsync(h->c64, 0, h->V * 8, st));
+  EPET_CHECK(epet_project_mlem(&h->p, h->rows, h->m, h->x, h->y, h->ybar, h->c64,
+                               h->opt.max_row_nnz, nullptr, 0, st));
+  k_update_c64<<<ceil_div(h->V, 256), 256, 0, st>>>(h->x, h->c64, h->s, h->V, h->xnew);
+  EPET_LAUNCHED();
+  return launch_sum_normalise(h->xnew, h->V, h->part_x, h->x, st);
+}
+
 static epet_status mlem_iteration(epet_mlem* h, cudaStream_t st) {
+  if (h->opt.matrix_free) return mlem_iteration_free(h, st);
   if (h->opt.value_format != EPET_VALUES_FP32) {
     EPET_CHECK((launch_rows16<EpiMlemForward16, float>(
         &h->A16, h->x, EpiMlemForward16{h->y, h->e16, h->ybar}, nullptr, st)));
@@ -287,6 +313,23 @@ epet_status epet_mlem_create(const epet_problem* p, const int32_t* rows_d, const
   note_launch();
   if (cudaGetLastError() != cudaSuccess) return fail(set_error(EPET_ERR_CUDA, "fill"));
 
+  if (o.matrix_free) {
+    // nothing stored: rows and counts in list order, the fp64 correction image
+    if (o.value_format != EPET_VALUES_FP32)
+      return fail(set_error(EPET_ERR_INVALID, "matrix_free needs FP32 values"));
+    h->opt.use_graph = 0;
+    h->opt.autotune = 0;
+    if (m > 0) cudaMemcpyAsync(h->rows, rows_d, m * 4, cudaMemcpyDeviceToDevice, st);
+    ALLOC(h->c64, V * 8);
+    ALLOC(h->part_ll, 1024 * 8);
+    ALLOC(h->part_x, sum_blocks(V) * 8);
+    h->plan_fwd = default_plan(0.0);
+    h->plan_bwd = default_plan(0.0);
+    cudaError_t e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) return fail(cuda_status(e, "mlem create"));
+    *out = h;
+    return EPET_OK;
+  }
   int32_t* idx = nullptr;  // list index of each row in the new order
   {
     epet_status rc = order_rows(p, rows_d, m, h, st, &idx);
@@ -430,7 +473,14 @@ epet_status epet_mlem_set_image(epet_mlem* h, const float* x_d, epet_stream_t st
 epet_status epet_mlem_stats(const epet_mlem* h, int64_t* nnz_h, int64_t* bytes_h) {
   if (!h) return set_error(EPET_ERR_INVALID, "bad arguments");
   if (nnz_h) *nnz_h = h->A.nnz;
-  if (bytes_h && h->opt.value_format != EPET_VALUES_FP32) {
+  if (bytes_h && h->opt.matrix_free) {
+    // no matrix: the pass writes and reads the rays (24 bytes each) and the
+    // channel geometry (224 bytes per row), reads y and writes ybar, reads x
+    // and the fp64 c (zeroed, accumulated), writes xnew, then sums and scales
+    const int64_t m = h->m, V = h->V, R = h->p.nrays;
+    *bytes_h = 2 * 24 * R * m + 2 * 224 * m + 8 * m + 4 * V + 3 * 8 * V + 4 * V + 4 * V +
+               4 * V + 4 * V;
+  } else if (bytes_h && h->opt.value_format != EPET_VALUES_FP32) {
     // per stored entry 4 bytes (offset + value) and a 4-byte base per 8;
     // per row a pointer and a scale (12 bytes); vectors as in FP32
     const int64_t m = h->m, V = h->V;

@@ -18,6 +18,7 @@ struct epet_mlem {
   epet_csr16 A16{}, At16{};  // 16-bit forms (value_format != FP32)
   int64_t capA = 0;
   double *part_ll = nullptr, *part_x = nullptr, *sums = nullptr;
+  double* c64 = nullptr;  // correction image of the matrix-free schedule
   epet::RowPlan plan_fwd, plan_bwd;
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t exec = nullptr;

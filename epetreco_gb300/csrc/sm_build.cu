@@ -44,7 +44,7 @@ constexpr int kGeomFloats = 56;  // per-channel geometry record (k_channel_geom)
 constexpr int kMaxSlabs = 1024;  // nx limit of the walk kernel
 
 enum WalkMode { kModeCsr = 0, kModeForward = 1, kModeBack = 2, kModeColSum = 3,
-                kModeWindow = 4 };
+                kModeWindow = 4, kModeMlem = 5 };
 
 struct WalkArgs {
   Geo G;
@@ -64,6 +64,9 @@ struct WalkArgs {
   const float* e;  // back-projection input (rows)
   float* c;        // back-projection output (voxels)
   double* s64;     // column sums
+  // one MLEM pass (kModeMlem): ybar = A x into y, c64 += A^T (ycnt / ybar)
+  const float* ycnt;  // measured counts (rows)
+  double* c64;        // correction image (voxels), fp64
   // window sizes (kModeWindow) and overflow reporting
   int32_t* win_cells;      // per row window cells
   int32_t* overflow_rows;  // list of rows whose window exceeded cap_cells
@@ -472,6 +475,7 @@ k_walk(WalkArgs args) {
   __shared__ int s_total, s_exact, s_box[4];
   __shared__ double red_d[kWalkThreads / 32];
   __shared__ float red_f[kWalkThreads / 32];
+  __shared__ float s_e;
 
   if ((int64_t)blockIdx.x >= args.m) return;
   const int64_t row = args.sel ? (int64_t)args.sel[blockIdx.x] : (int64_t)blockIdx.x;
@@ -854,7 +858,7 @@ k_walk(WalkArgs args) {
     const bool cand = fadd(fadd(fmul(c0, c0), fmul(c1, c1)), c2sq) < L.s_max;
     const bool keep = (u != 0ull) & cand;
     const float v = div_cr(fmul(__ull2float_rn(u), G.fx_inv), fR, inv_fR);
-    if (kMode == kModeCsr) {
+    if (kMode == kModeCsr || kMode == kModeMlem) {
       // kept entries compacted at the start of the thread's range: the slot
       // written is this cell's or an earlier one, already read
       win.cell[cbeg + cnt] = make_uint2(__float_as_uint(v), (uint32_t)(colvox + iz));
@@ -862,7 +866,7 @@ k_walk(WalkArgs args) {
     cnt += keep ? 1 : 0;
     if (kMode != kModeCsr && keep) {
       const int vox = colvox + iz;
-      if (kMode == kModeForward) fsum = fadd(fsum, fmul(v, args.x[vox]));
+      if (kMode == kModeForward || kMode == kModeMlem) fsum = fadd(fsum, fmul(v, args.x[vox]));
       if (kMode == kModeBack) {
         const float ev = args.e[row];
         if (ev != 0.f) atomicAdd(&args.c[vox], fmul(v, ev));
@@ -882,7 +886,7 @@ k_walk(WalkArgs args) {
       args.row_len[row] = s_total;
       if (args.sel) args.ovf_idx[row] = (int32_t)slot;
     }
-  } else if (kMode == kModeForward) {
+  } else if (kMode == kModeForward || kMode == kModeMlem) {
     // deterministic block reduction in thread order
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     float v = fsum;
@@ -893,7 +897,19 @@ k_walk(WalkArgs args) {
     if (threadIdx.x == 0) {
       float t = 0.f;
       for (int k = 0; k < kWalkThreads / 32; k++) t = fadd(t, red_f[k]);
-      args.y[row] = t;
+      if (args.y) args.y[row] = t;
+      // e = y / (A x) (mlemOperations.hpp:22-32, 0 where A x == 0)
+      if (kMode == kModeMlem) s_e = t > 0.f ? __fdiv_rn(args.ycnt[row], t) : 0.f;
+    }
+    if (kMode == kModeMlem) {
+      // the row's share of A^T e: its kept entries, compacted in pass 1
+      __syncthreads();
+      const float ev = s_e;
+      if (ev != 0.f)
+        for (int j = 0; j < cnt; j++) {
+          const uint2 en = win.cell[cbeg + j];
+          atomicAdd(&args.c64[en.y], (double)fmul(__uint_as_float(en.x), ev));
+        }
     }
   }
   (void)red_d;
@@ -1096,6 +1112,8 @@ struct BuildOut {
   const float* e = nullptr;
   float* c = nullptr;
   double* s64 = nullptr;
+  const float* ycnt = nullptr;  // kModeMlem: counts in; c64 out
+  double* c64 = nullptr;
   // optional destination of each chunk's entries instead of csr->col/val
   // (rows c0 .. c0+mc-1, n entries in row order from index 0); returns false
   // on failure.  csr->row_ptr still receives the global row pointers.
@@ -1255,6 +1273,8 @@ static epet_status run_walk(const Geo& G, const int32_t* rows, int64_t m,
     a.e = out->e ? out->e + c0 : nullptr;
     a.c = out->c;
     a.s64 = out->s64;
+    a.ycnt = out->ycnt ? out->ycnt + c0 : nullptr;
+    a.c64 = out->c64;
     a.overflow_rows = ovf_rows;
     a.overflow_count = flags;
     a.hit_outside = flags + 1;
@@ -1296,7 +1316,8 @@ static epet_status run_walk(const Geo& G, const int32_t* rows, int64_t m,
     if (fl[2] > 0) {
       // rows with an axis-parallel ray: per-candidate path
       EPET_CHECK(exact_rows_apply(G, rows + c0, ex_rows, fl[2], kMode, row_len,
-                                  csr ? ovf_idx : nullptr, &exr, a.x, a.y, a.e, a.c, a.s64, st));
+                                  csr ? ovf_idx : nullptr, &exr, a.x, a.y, a.e, a.c, a.s64,
+                                  a.ycnt, a.c64, st));
       n_exact_rows_ += fl[2];
     }
     if (csr) {
@@ -1476,6 +1497,24 @@ epet_status epet_project_back(const epet_problem* p, const int32_t* rows_d,
   bo.e = e_d;
   bo.c = c_d;
   return run_walk<kModeBack>(G, rows_d, m, capc, &bo, ws, ws_bytes, st);
+}
+
+epet_status epet_project_mlem(const epet_problem* p, const int32_t* rows_d, int64_t m,
+                              const float* x_d, const float* y_d, float* ybar_d,
+                              double* c64_d, int32_t max_row_nnz, void* ws, size_t ws_bytes,
+                              epet_stream_t stream) {
+  EPET_CHECK(check_rows(p, rows_d, m));
+  if (!x_d || (m > 0 && !y_d) || !c64_d) return set_error(EPET_ERR_INVALID, "x/y/c64 NULL");
+  cudaStream_t st = (cudaStream_t)stream;
+  Geo G = make_geo(*p);
+  int capc = 0;
+  EPET_CHECK(resolve_capacity(G, max_row_nnz, st, &capc));
+  BuildOut bo;
+  bo.x = x_d;
+  bo.y = ybar_d;
+  bo.ycnt = y_d;
+  bo.c64 = c64_d;
+  return run_walk<kModeMlem>(G, rows_d, m, capc, &bo, ws, ws_bytes, st);
 }
 
 }  // extern "C"

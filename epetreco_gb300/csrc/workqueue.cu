@@ -199,7 +199,8 @@ k_values(Geo G, const float* __restrict__ rays, int64_t m,
 
 // Per-candidate path for the rows the walk leaves out (see sm_build.cu):
 // candidates -> values in reference order -> drop zeros.
-// kMode as in sm_build.cu: 0 CSR staging, 1 forward, 2 back, 3 column sums.
+// kMode as in sm_build.cu: 0 CSR staging, 1 forward, 2 back, 3 column sums,
+// 5 one MLEM pass (forward into y, then c64 += A^T (ycnt / y)).
 template <int kMode>
 __global__ void k_apply_exact(int64_t n_ex, const int32_t* __restrict__ ex_rows,
                               const int64_t* __restrict__ wq_off,
@@ -207,7 +208,7 @@ __global__ void k_apply_exact(int64_t n_ex, const int32_t* __restrict__ ex_rows,
                               const float* __restrict__ wq_val, int32_t* out_col,
                               float* out_val, int32_t* row_len, int32_t* src_idx,
                               const float* x, float* y, const float* e, float* c,
-                              double* s64) {
+                              double* s64, const float* ycnt, double* c64) {
   const int64_t i = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int lane = threadIdx.x & 31;
   if (i >= n_ex) return;
@@ -229,7 +230,7 @@ __global__ void k_apply_exact(int64_t n_ex, const int32_t* __restrict__ ex_rows,
       if (kMode == 2 && e[row] != 0.f) atomicAdd(&c[vox], fmul(v, e[row]));
       if (kMode == 3) atomicAdd(&s64[vox], (double)v);
     }
-    if (kMode == 1) {
+    if (kMode == 1 || kMode == 5) {
       // ordered: lane contributions in element order via the warp
       float t = v != 0.f ? fmul(v, x[wq_vxl[b + k < b + n ? b + k : b]]) : 0.f;
       for (int l = 0; l < 32; l++) fsum = fadd(fsum, __shfl_sync(0xffffffffu, t, l));
@@ -241,7 +242,16 @@ __global__ void k_apply_exact(int64_t n_ex, const int32_t* __restrict__ ex_rows,
       row_len[row] = (int32_t)o;
       src_idx[row] = (int32_t)(-2 - i);
     }
-    if (kMode == 1) y[row] = fsum;
+    if ((kMode == 1 || kMode == 5) && y) y[row] = fsum;
+  }
+  if (kMode == 5) {
+    // every lane holds the same fsum (the warp-ordered sum)
+    const float ev = fsum > 0.f ? __fdiv_rn(ycnt[row], fsum) : 0.f;
+    if (ev != 0.f)
+      for (int64_t k = lane; k < n; k += 32) {
+        const float v = wq_val[b + k];
+        if (v != 0.f) atomicAdd(&c64[wq_vxl[b + k]], (double)fmul(v, ev));
+      }
   }
 }
 
@@ -313,7 +323,8 @@ void ExactRows::release(cudaStream_t st) {
 epet_status exact_rows_apply(const Geo& G, const int32_t* rows, const int32_t* ex_rows,
                              int64_t n_ex, int mode, int32_t* row_len, int32_t* src_idx,
                              ExactRows* keep, const float* x, float* y, const float* e,
-                             float* c, double* s64, cudaStream_t st) {
+                             float* c, double* s64, const float* ycnt, double* c64,
+                             cudaStream_t st) {
   if (n_ex == 0) return EPET_OK;
   if (mode == 0 && (!keep || keep->off)) return set_error(EPET_ERR_INVALID, "internal: exact rows");
   // off/col/val: handed to the caller in CSR mode, else released here; the
@@ -355,16 +366,17 @@ epet_status exact_rows_apply(const Geo& G, const int32_t* rows, const int32_t* e
   EPET_CHECK(launch_values(G, rays, n_ex, out.off, wv, wval, true, st));
   const int T = 128;
   const int nb = ceil_div(n_ex * 32, T);
+#define EPET_APPLY(K)                                                                    \
+  k_apply_exact<K><<<nb, T, 0, st>>>(n_ex, ex_rows, out.off, wv, wval, out.col, out.val, row_len, \
+                                     src_idx, x, y, e, c, s64, ycnt, c64)
   switch (mode) {
-    case 0: k_apply_exact<0><<<nb, T, 0, st>>>(n_ex, ex_rows, out.off, wv, wval, out.col, out.val,
-                                               row_len, src_idx, x, y, e, c, s64); break;
-    case 1: k_apply_exact<1><<<nb, T, 0, st>>>(n_ex, ex_rows, out.off, wv, wval, out.col, out.val,
-                                               row_len, src_idx, x, y, e, c, s64); break;
-    case 2: k_apply_exact<2><<<nb, T, 0, st>>>(n_ex, ex_rows, out.off, wv, wval, out.col, out.val,
-                                               row_len, src_idx, x, y, e, c, s64); break;
-    default: k_apply_exact<3><<<nb, T, 0, st>>>(n_ex, ex_rows, out.off, wv, wval, out.col,
-                                                 out.val, row_len, src_idx, x, y, e, c, s64); break;
+    case 0: EPET_APPLY(0); break;
+    case 1: EPET_APPLY(1); break;
+    case 2: EPET_APPLY(2); break;
+    case 5: EPET_APPLY(5); break;
+    default: EPET_APPLY(3); break;
   }
+#undef EPET_APPLY
   EPET_LAUNCHED();
   return EPET_OK;
 }

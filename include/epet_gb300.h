@@ -160,6 +160,11 @@ epet_status epet_dump_uniforms(const epet_problem* p, const int32_t* rows_d,
  * capacity and were redone with their exact size, and rows handed to the
  * per-candidate path (a ray with two equal coordinates). */
 epet_status epet_build_counters(int64_t* overflow_rows_h, int64_t* exact_rows_h);
+/* Work measure of the chord walk (no counterpart in the reference): the
+ * total over the listed channels' rays of the grid cells each ray crosses
+ * (1 + the grid planes it passes inside the grid).  Synchronous. */
+epet_status epet_ray_steps(const epet_problem* p, const int32_t* rows_d, int64_t m,
+                           int64_t* steps_h, epet_stream_t stream);
 /* Library self-test (no counterpart in the reference): compares the walk
  * kernel's reciprocal-based correctly rounded division with the hardware's
  * IEEE division on n seeded operand pairs; *mismatches_h counts differing
@@ -225,6 +230,16 @@ epet_status epet_project_back(const epet_problem* p, const int32_t* rows_d,
                               int64_t m, const float* e_d, float* c_d,
                               int32_t max_row_nnz, void* ws, size_t ws_bytes,
                               epet_stream_t stream);
+/* One MLEM pass without a stored matrix, the reference's schedule of a
+ * system matrix rebuilt in every iteration (reco.cu:216-254: the chunk's
+ * matrix, csrmv, divides, transposed csrmv with beta = 1) done by one chord
+ * walk per row: ybar = A x (into ybar_d, may be NULL), e = y / ybar (0 where
+ * ybar == 0), c64_d[V] += A^T e accumulated in fp64 (the caller zeroes it).
+ * Same element values and the same A x as epet_project_forward. */
+epet_status epet_project_mlem(const epet_problem* p, const int32_t* rows_d,
+                              int64_t m, const float* x_d, const float* y_d,
+                              float* ybar_d, double* c64_d, int32_t max_row_nnz,
+                              void* ws, size_t ws_bytes, epet_stream_t stream);
 /* Sensitivity image (backprojection.cu:113-161 fed an all-ones measurement):
  * s_d[V] = column sums of A over the listed channels, accumulated in fp64
  * (s64_d, may be NULL) and normalised to sum 1 in s_d. */
@@ -361,6 +376,10 @@ typedef struct {
                           matrix at create (cached per matrix shape for the process);
                           0: a fixed heuristic shape (results then depend only on the
                           inputs, not on timings).  FP32 values only. */
+  int32_t matrix_free; /* 1: store no matrix; every iteration recomputes the chords
+                          (epet_project_mlem), as the reference rebuilds its matrix in
+                          every iteration.  FP32 values; use_graph and autotune are
+                          ignored (the pass reads per-chunk counters back). */
 } epet_mlem_options;
 
 /* Builds the system matrix for the measured rows (rows_d channel ids, in
@@ -378,7 +397,9 @@ epet_status epet_mlem_destroy(epet_mlem* h);
  * projection is returned (synchronous then). */
 epet_status epet_mlem_iterate(epet_mlem* h, int32_t nit, double* loglik_h,
                               epet_stream_t stream);
-/* Image access (device pointer valid until destroy), copy-out, statistics. */
+/* Image access (device pointer valid until destroy), copy-out, statistics
+ * (with matrix_free: nnz 0, and the bytes of the pass's rays, channel
+ * geometry and vectors). */
 float* epet_mlem_image(epet_mlem* h);
 epet_status epet_mlem_get_image(const epet_mlem* h, float* x_d, epet_stream_t stream);
 epet_status epet_mlem_set_image(epet_mlem* h, const float* x_d,

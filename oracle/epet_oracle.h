@@ -107,6 +107,12 @@ int64_t eo_sm_build_csr(const eo_setup* s, const eo_grid* g, const float* trig,
                         const int32_t* list, int64_t n_list, int nrays,
                         const float* rnd_rows, int sum_mode, int64_t* row_ptr,
                         int32_t* col, float* val, int64_t cap);
+/* One-pass form of eo_sm_build_csr: start returns a handle and the nnz;
+ * finish writes row_ptr[n_list+1], col, val and frees the handle. */
+void* eo_sm_build_start(const eo_setup* s, const eo_grid* g, const float* trig,
+                        const int32_t* list, int64_t n_list, int nrays,
+                        const float* rnd_rows, int sum_mode, int64_t* nnz_out);
+void eo_sm_build_finish(void* h, int64_t* row_ptr, int32_t* col, float* val);
 
 /* ---- sparse format conversions */
 /* Stable lexicographic (row, col) sort carrying values (cooSort.hpp:26-71). */
@@ -143,6 +149,9 @@ void eo_mlem(int64_t m, int64_t V, const int64_t* row_ptr, const int32_t* col,
 void eo_mlem_f64(int64_t m, int64_t V, const int64_t* row_ptr,
                  const int32_t* col, const float* val, const double* y,
                  const double* s, double* x, int nit);
+void eo_mlem_f64_trace(int64_t m, int64_t V, const int64_t* rp, const int32_t* col,
+                       const float* val, const double* y, const double* s, double* x,
+                       int nit, double* trace);
 /* s = A^T 1 normalised to sum 1 (backprojection.cu:113-161 with an all-ones
  * measurement). */
 void eo_sensitivity(int64_t m, int64_t V, const int64_t* row_ptr,

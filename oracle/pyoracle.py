@@ -115,6 +115,12 @@ class Oracle:
         lib.eo_sm_build_csr.argtypes = [S, G, C.c_void_p, _i32p, C.c_int64, C.c_int, _f32p,
                                         C.c_int, _i64p, _i32p, _f32p, C.c_int64]
         lib.eo_sm_build_csr.restype = C.c_int64
+        lib.eo_sm_build_start.argtypes = [S, G, C.c_void_p, _i32p, C.c_int64, C.c_int, _f32p,
+                                          C.c_int, C.POINTER(C.c_int64)]
+        lib.eo_sm_build_start.restype = C.c_void_p
+        lib.eo_sm_build_finish.argtypes = [C.c_void_p, _i64p, _i32p, _f32p]
+        lib.eo_mlem_f64_trace.argtypes = [C.c_int64, C.c_int64, _i64p, _i32p, _f32p, _f64p,
+                                          _f64p, _f64p, C.c_int, _f64p]
         lib.eo_coo_sort.argtypes = [_f32p, _i32p, _i32p, C.c_int64]
         lib.eo_coo2csr.argtypes = [_i32p, C.c_int64, C.c_int64, _i64p]
         lib.eo_csr2ecsr.argtypes = [_i64p, _i32p, C.c_int64, _i64p, C.c_int64]
@@ -217,18 +223,17 @@ class Oracle:
         rows = np.ascontiguousarray(rows, np.int32)
         rnd_rows = np.ascontiguousarray(rnd_rows, np.float32).reshape(-1)
         m = len(rows)
-        rp = np.zeros(m + 1, np.int64)
         tp = self._trig_ptr(trig)
         S, G = C.byref(_setup_struct(p)), C.byref(_grid_struct(p))
-        dummy_i = np.zeros(1, np.int32)
-        dummy_f = np.zeros(1, np.float32)
-        nnz = self.lib.eo_sm_build_csr(S, G, tp[0] if tp else None, rows, m, nrays, rnd_rows,
-                                       1 if exact else 0, rp, dummy_i, dummy_f, 0)
-        col = np.zeros(max(nnz, 1), np.int32)
-        val = np.zeros(max(nnz, 1), np.float32)
-        self.lib.eo_sm_build_csr(S, G, tp[0] if tp else None, rows, m, nrays, rnd_rows,
-                                 1 if exact else 0, rp, col, val, nnz)
-        return rp, col[:nnz], val[:nnz]
+        nnz = C.c_int64(0)
+        h = self.lib.eo_sm_build_start(S, G, tp[0] if tp else None, rows, m, nrays, rnd_rows,
+                                       1 if exact else 0, C.byref(nnz))
+        n = nnz.value
+        rp = np.zeros(m + 1, np.int64)
+        col = np.zeros(max(n, 1), np.int32)
+        val = np.zeros(max(n, 1), np.float32)
+        self.lib.eo_sm_build_finish(h, rp, col, val)
+        return rp, col[:n], val[:n]
 
     def coo_sort(self, val, row, col):
         val = np.array(val, np.float32)
@@ -304,6 +309,17 @@ class Oracle:
                              np.ascontiguousarray(y, np.float64),
                              np.ascontiguousarray(s, np.float64), x, nit)
         return x
+
+    def mlem_f64_trace(self, rp, col, val, y, s, x0, nit, V):
+        """FP64 MLEM; returns the images after each iteration, [nit][V]."""
+        x = np.array(x0, np.float64)
+        tr = np.zeros((nit, V), np.float64)
+        self.lib.eo_mlem_f64_trace(len(rp) - 1, V, np.ascontiguousarray(rp, np.int64),
+                                   np.ascontiguousarray(col, np.int32),
+                                   np.ascontiguousarray(val, np.float32),
+                                   np.ascontiguousarray(y, np.float64),
+                                   np.ascontiguousarray(s, np.float64), x, nit, tr)
+        return tr
 
     def sensitivity(self, rp, col, val, V):
         s = np.zeros(V, np.float32)

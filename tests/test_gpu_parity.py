@@ -222,3 +222,28 @@ def test_windows_over_capacity_are_redone(case):
     y0 = api.project_forward(p, dev(rows), x)
     y1 = api.project_forward(p, dev(rows), x, max_row_nnz=cap)
     assert torch.equal(y0, y1)
+
+
+def test_ray_steps_counts_cells_crossed(case):
+    """epet_ray_steps (the walk's work measure): cells crossed per ray, from
+    the entry and exit cells of each ray's grid interval (numpy, float64);
+    rays that only graze a plane may count differently by one."""
+    p, rows = case["p"], case["rows"]
+    got = api.ray_steps(p, dev(rows))
+    r = api.rays(p, dev(rows)).cpu().numpy().reshape(-1, 6).astype(np.float64)
+    o = np.array(p.grid.origin, np.float64)
+    d = np.array(p.grid.pitch, np.float64)
+    n = np.array(p.grid.n)
+    p0, dp = r[:, :3], r[:, 3:] - r[:, :3]
+    with np.errstate(divide="ignore", invalid="ignore"):
+        t0 = (o - p0) / dp
+        t1 = (o + n * d - p0) / dp
+    a_in = np.maximum(0, np.nanmax(np.minimum(t0, t1), axis=1))
+    a_out = np.minimum(1, np.nanmin(np.maximum(t0, t1), axis=1))
+    hit = a_in < a_out
+    span = a_out - a_in
+    c_in = np.clip(np.floor((p0 + (a_in + 1e-6 * span)[:, None] * dp - o) / d), 0, n - 1)
+    c_out = np.clip(np.floor((p0 + (a_out - 1e-6 * span)[:, None] * dp - o) / d), 0, n - 1)
+    want = int((1 + np.abs(c_out - c_in).sum(1))[hit].sum())
+    assert abs(got - want) <= 1e-3 * want, (got, want)
+    assert want > len(rows) * p.nrays  # every ray crosses several cells
