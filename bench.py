@@ -12,13 +12,23 @@ column-major copy, and 20 MLEM iterations (forward product, ratio,
 transpose product, update, normalisation).  The metric is MLEM iterations
 per second of that step: 20 / step time, the matrix build included.  The
 sensitivity image and the measurement are inputs (the reference reads them
-from files).
+from files).  Beside it the line carries:
+  rebuild_per_iteration  the reference's own schedule (the matrix recomputed
+                         in every iteration) on the GPU, matrix-free;
+  parity_fp64            the image of every iteration of the FP32, BF16 and
+                         FP16 forms against the FP64 oracle on the host;
+  sm_build_steps         ray-voxel steps (grid cells crossed by all rays)
+                         per second of the system-matrix build;
+  forms, batched         the 16-bit value forms and batched reconstructions;
+  cpu_baseline           the oracle on the host cores, same schedule.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
 
 With torchrun (N > 1) every rank reconstructs its own copy of the workload
-(replicas; the path has no cross-GPU exchange in this form), the step time
-is the max over ranks and the value counts all ranks' iterations.
+(replicas): the step time is the max over ranks and the value counts all
+ranks' iterations.  With --sharded the ranks share ONE reconstruction (its
+measured rows split over the ranks, the correction image all-reduced over
+NCCL in every iteration) and the value is that reconstruction's it/s.
 """
 from __future__ import annotations
 
@@ -58,6 +68,10 @@ def parse():
                     help="skip the matrix-free (rebuild every iteration) schedule")
     ap.add_argument("--no-parity", action="store_true",
                     help="skip the per-iteration image error against the FP64 oracle")
+    ap.add_argument("--sharded", action="store_true",
+                    help="with N > 1 ranks: ONE reconstruction whose measured rows are split "
+                         "over the ranks (NCCL all-reduce of the correction image per "
+                         "iteration; strong scaling) instead of N replicas")
     ap.add_argument("--profile", action="store_true",
                     help="one reconstruction with one iteration, nothing else (for ncu)")
     ap.add_argument("--profile-kernels", type=int, default=0, metavar="ROWS",
@@ -179,15 +193,17 @@ def cpu_baseline(cfg_name: str, sample: int, seed: int = 0):
             "sample_seconds": t_build + reps * t_prod}
 
 
-def aggregate_replicas(times, nit, world, dist, device):
-    """Replicas (every rank ran the same workload): each time is the max over
-    ranks, and the whole-job rate is world * nit / that time."""
+def aggregate_replicas(times, nit, world, dist, device, sharded=False):
+    """Each time is the max over ranks.  Replicas (every rank ran the whole
+    workload): the whole-job rate is world * nit / that time; one sharded
+    reconstruction: nit / that time."""
     import torch
     vals = torch.tensor([float(t) for t in times], device=device, dtype=torch.float64)
     if dist is not None:
         dist.all_reduce(vals, op=dist.ReduceOp.MAX)
     tmax = [float(v) for v in vals]
-    return tmax, [world * nit / t for t in tmax]
+    k = 1 if sharded else world
+    return tmax, [k * nit / t for t in tmax]
 
 
 def workload_name(cfg_name: str) -> str:
@@ -397,8 +413,14 @@ def gb300_arm(args):
 
     it_events = []
 
+    sharded = args.sharded and world > 1
+
     def step(r, yy, ss, record=False):
-        R = api.Mlem(p, r, yy, ss, use_graph=True, autotune=True)
+        if sharded:
+            from epetreco_gb300.shard import ShardedMlem
+            R = ShardedMlem(p, r, yy, ss, use_graph=True, autotune=True)
+        else:
+            R = api.Mlem(p, r, yy, ss, use_graph=True, autotune=True)
         if record:
             a = torch.cuda.Event(enable_timing=True)
             b = torch.cuda.Event(enable_timing=True)
@@ -585,7 +607,7 @@ def gb300_arm(args):
 
     # ---- aggregate over ranks
     (t_step, t_e2e), (value, value_e2e) = aggregate_replicas((t_step, t_e2e), nit, world, dist,
-                                                            "cuda")
+                                                            "cuda", sharded=sharded)
     if rank != 0:
         if dist is not None:
             dist.destroy_process_group()
@@ -601,10 +623,12 @@ def gb300_arm(args):
     out = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": 1000.0 * t_step, "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "scaling": "strong" if sharded else "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic",
         "config": {"workload": workload_name(args.config)},
         "schedule": SCHEDULE,
-        "measured_rows": m, "nnz": nnz, "parallelism": f"replicas{world}",
+        "measured_rows": m, "nnz": nnz,
+        "parallelism": f"rows{world}" if sharded else f"replicas{world}",
         "l2": "inputs larger than L2 (matrix streams of GBs per pass)",
         "e2e": {"value": value_e2e, "unit": UNIT, "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h},

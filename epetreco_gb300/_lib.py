@@ -113,10 +113,13 @@ SIGNATURES = {
     "epet_mlem_set_image": [VP, VP, VP],
     "epet_mlem_stats": [VP, C.POINTER(C.c_int64), C.POINTER(C.c_int64)],
     "epet_mlem_plan": [VP, C.POINTER(C.c_int32)],
+    "epet_mlem_correction": [VP, VP, VP],
+    "epet_mlem_update": [VP, VP, VP],
+    "epet_mlem_loglik": [VP, C.POINTER(C.c_double), VP],
     "epet_trim_memory": [C.c_size_t],
     "epet_selftest_division": [I64, C.c_uint64, C.POINTER(C.c_int64), VP],
     "epet_build_counters": [C.POINTER(C.c_int64), C.POINTER(C.c_int64)],
-    "epet_ray_steps": [P, VP, I64, C.POINTER(C.c_int64), VP],
+    "epet_ray_steps": [P, VP, I64, VP, C.POINTER(C.c_int64), VP],
     "epet_mlem_batch_create": [I32, VP, VP, VP, VP, VP, C.POINTER(MlemOptions), C.POINTER(VP),
                                VP],
     "epet_mlem_batch_destroy": [VP],

@@ -397,14 +397,15 @@ def build_counters() -> dict:
     return {"overflow_rows": o.value, "exact_rows": e.value}
 
 
-def ray_steps(p, rows) -> int:
+def ray_steps(p, rows, per_row: bool = False):
     """Grid cells crossed by all rays of the listed channels (the walk's
-    work)."""
+    work); with per_row, also the int64 count of each row."""
     rows = _i32(rows)
     n = C.c_int64(0)
-    check(lib().epet_ray_steps(C.byref(problem_struct(p)), _ptr(rows), rows.numel(), C.byref(n),
-                               _stream()))
-    return n.value
+    rs = torch.empty(rows.numel(), dtype=torch.int64, device="cuda") if per_row else None
+    check(lib().epet_ray_steps(C.byref(problem_struct(p)), _ptr(rows), rows.numel(), _ptr(rs),
+                               C.byref(n), _stream()))
+    return (n.value, rs) if per_row else n.value
 
 
 class Mlem:
@@ -434,6 +435,24 @@ class Mlem:
         check(lib().epet_mlem_iterate(self._h, int(nit), C.byref(ll) if loglik else None,
                                       _stream()))
         return ll.value if loglik else None
+
+    def correction(self, c: torch.Tensor | None = None) -> torch.Tensor:
+        """c = A^T (y / A x) over this object's rows; the image is unchanged
+        (row-sharded reconstructions sum c over the shards, then update)."""
+        if c is None:
+            c = torch.empty(self.p.nvoxels, dtype=torch.float32, device="cuda")
+        check(lib().epet_mlem_correction(self._h, _ptr(c), _stream()))
+        return c
+
+    def update(self, c: torch.Tensor) -> None:
+        """x = x*c/s (s == 0 -> 1), then x /= sum(x)."""
+        check(lib().epet_mlem_update(self._h, _ptr(c.to(torch.float32).contiguous()), _stream()))
+
+    def loglik(self) -> float:
+        """FP64 Poisson log-likelihood of the last forward projection."""
+        ll = C.c_double(0.0)
+        check(lib().epet_mlem_loglik(self._h, C.byref(ll), _stream()))
+        return ll.value
 
     def image(self) -> torch.Tensor:
         """A copy of the current image (float32, V)."""

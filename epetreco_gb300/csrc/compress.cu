@@ -284,6 +284,8 @@ template epet_status launch_rows16<EpiMlemForward16, float>(const epet_csr16*, c
                                                             cudaStream_t);
 template epet_status launch_rows16<EpiMlemUpdate, uint16_t>(const epet_csr16*, const uint16_t*,
                                                             EpiMlemUpdate, double*, cudaStream_t);
+template epet_status launch_rows16<EpiKeep, uint16_t>(const epet_csr16*, const uint16_t*,
+                                                      EpiKeep, double*, cudaStream_t);
 
 }  // namespace epet
 

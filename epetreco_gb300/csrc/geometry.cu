@@ -201,7 +201,8 @@ using namespace epet;
 // are taken a little inside the ray's grid interval, so a ray that only
 // grazes a plane counts the cells on one side of it.
 __global__ void k_ray_steps(Geo G, const float* __restrict__ rays, int64_t n,
-                            unsigned long long* __restrict__ total) {
+                            unsigned long long* __restrict__ total,
+                            unsigned long long* __restrict__ per_row) {
   const epet_grid& g = G.p.grid;
   unsigned long long mine = 0;
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
@@ -230,6 +231,7 @@ __global__ void k_ray_steps(Geo G, const float* __restrict__ rays, int64_t n,
       st += (unsigned long long)abs(c1 - c0);
     }
     mine += st;
+    if (per_row) atomicAdd(per_row + i / G.p.nrays, st);
   }
   for (int o = 16; o > 0; o >>= 1) mine += __shfl_xor_sync(0xffffffffu, mine, o);
   if ((threadIdx.x & 31) == 0 && mine) atomicAdd(total, mine);
@@ -261,7 +263,7 @@ epet_status epet_selftest_division(int64_t n, uint64_t seed, int64_t* mismatches
 }
 
 epet_status epet_ray_steps(const epet_problem* p, const int32_t* rows_d, int64_t m,
-                           int64_t* steps_h, epet_stream_t stream) {
+                           int64_t* row_steps_d, int64_t* steps_h, epet_stream_t stream) {
   EPET_CHECK(epet_problem_validate(p));
   if (m < 0 || (m > 0 && !rows_d) || !steps_h) return set_error(EPET_ERR_INVALID, "bad arguments");
   cudaStream_t st = (cudaStream_t)stream;
@@ -275,11 +277,14 @@ epet_status epet_ray_steps(const epet_problem* p, const int32_t* rows_d, int64_t
   unsigned long long* tot = scr.take<unsigned long long>(1);
   if (scr.overrun) return set_error(EPET_ERR_INVALID, "internal: workspace size");
   EPET_CUDA(cudaMemsetAsync(tot, 0, 8, st));
+  if (row_steps_d && m > 0) EPET_CUDA(cudaMemsetAsync(row_steps_d, 0, m * 8, st));
   for (int64_t c0 = 0; c0 < m; c0 += ch) {
     const int64_t mc = std::min(ch, m - c0);
     EPET_CHECK(launch_rays(G, rows_d + c0, mc, rays, false, st));
     const int64_t nr = mc * p->nrays;
-    k_ray_steps<<<std::min<int64_t>(ceil_div(nr, 256), 8 * (int64_t)num_sms()), 256, 0, st>>>(G, rays, nr, tot);
+    k_ray_steps<<<std::min<int64_t>(ceil_div(nr, 256), 8 * (int64_t)num_sms()), 256, 0, st>>>(
+        G, rays, nr, tot,
+        row_steps_d ? reinterpret_cast<unsigned long long*>(row_steps_d + c0) : nullptr);
     EPET_LAUNCHED();
   }
   unsigned long long h = 0;

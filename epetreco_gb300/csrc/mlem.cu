@@ -37,17 +37,25 @@ static void mlem_free(epet_mlem* h) {
   delete h;
 }
 
-// x*c/s (dividesMultiplies, mlemOperations.hpp:38-79, with s == 0 -> 1) from
-// the fp64 correction image of the matrix-free schedule, rounded to fp32 as
-// the reference's float c.
-__global__ void k_update_c64(const float* __restrict__ x, const double* __restrict__ c64,
-                             const float* __restrict__ s, int64_t V, float* __restrict__ xnew) {
+// x*c/s (dividesMultiplies, mlemOperations.hpp:38-79, with s == 0 -> 1), the
+// arithmetic of EpiMlemUpdate, from a correction image held apart: the fp64
+// one of the matrix-free schedule (rounded to fp32 as the reference's float
+// c) or the fp32 one summed across the shards of a row-sharded
+// reconstruction.
+template <typename CT>
+__global__ void k_update_c(const float* __restrict__ x, const CT* __restrict__ cimg,
+                           const float* __restrict__ s, int64_t V, float* __restrict__ xnew) {
   const int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (v >= V) return;
-  const float c = (float)c64[v];
+  const float c = (float)cimg[v];
   float dvs = s[v];
   dvs = __fadd_rn(dvs, (float)(dvs == 0.f));
   xnew[v] = __fdiv_rn(__fmul_rn(x[v], c), dvs);
+}
+
+__global__ void k_f64_to_f32_vec(const double* __restrict__ a, int64_t n, float* __restrict__ b) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) b[i] = (float)a[i];
 }
 
 // The reference's schedule: the chords recomputed in every iteration (one
@@ -57,9 +65,31 @@ static epet_status mlem_iteration_free(epet_mlem* h, cudaStream_t st) {
   EPET_CUDA(cudaMemsetAsync(h->c64, 0, h->V * 8, st));
   EPET_CHECK(epet_project_mlem(&h->p, h->rows, h->m, h->x, h->y, h->ybar, h->c64,
                                h->opt.max_row_nnz, nullptr, 0, st));
-  k_update_c64<<<ceil_div(h->V, 256), 256, 0, st>>>(h->x, h->c64, h->s, h->V, h->xnew);
+  k_update_c<double><<<ceil_div(h->V, 256), 256, 0, st>>>(h->x, h->c64, h->s, h->V, h->xnew);
   EPET_LAUNCHED();
   return launch_sum_normalise(h->xnew, h->V, h->part_x, h->x, st);
+}
+
+// c = A^T (y / A x) over this object's rows, without the update (the
+// forward product keeps ybar and e as in the iteration).
+static epet_status mlem_correction(epet_mlem* h, float* c, cudaStream_t st) {
+  if (h->opt.matrix_free) {
+    EPET_CUDA(cudaMemsetAsync(h->c64, 0, h->V * 8, st));
+    EPET_CHECK(epet_project_mlem(&h->p, h->rows, h->m, h->x, h->y, h->ybar, h->c64,
+                                 h->opt.max_row_nnz, nullptr, 0, st));
+    k_f64_to_f32_vec<<<ceil_div(h->V, 256), 256, 0, st>>>(h->c64, h->V, c);
+    EPET_LAUNCHED();
+    return EPET_OK;
+  }
+  if (h->opt.value_format != EPET_VALUES_FP32) {
+    EPET_CHECK((launch_rows16<EpiMlemForward16, float>(
+        &h->A16, h->x, EpiMlemForward16{h->y, h->e16, h->ybar}, nullptr, st)));
+    return launch_rows16<EpiKeep, uint16_t>(&h->At16, h->e16, EpiKeep{c}, nullptr, st);
+  }
+  EPET_CHECK(launch_rows(h->plan_fwd, h->A.row_ptr, h->A.col, h->A.val, h->x, h->m,
+                         EpiMlemForward{h->y, h->e, h->ybar}, nullptr, st));
+  return launch_rows(h->plan_bwd, h->At.col_ptr, h->At.row, h->At.val, h->e, h->V, EpiKeep{c},
+                     nullptr, st);
 }
 
 static epet_status mlem_iteration(epet_mlem* h, cudaStream_t st) {
@@ -451,6 +481,35 @@ epet_status epet_mlem_iterate(epet_mlem* h, int32_t nit, double* loglik_h,
     EPET_CUDA(cudaStreamSynchronize(st));
     *loglik_h = s0;
   }
+  return EPET_OK;
+}
+
+epet_status epet_mlem_correction(epet_mlem* h, float* c_d, epet_stream_t stream) {
+  if (!h || !c_d) return set_error(EPET_ERR_INVALID, "bad arguments");
+  return mlem_correction(h, c_d, (cudaStream_t)stream);
+}
+
+epet_status epet_mlem_update(epet_mlem* h, const float* c_d, epet_stream_t stream) {
+  if (!h || !c_d) return set_error(EPET_ERR_INVALID, "bad arguments");
+  cudaStream_t st = (cudaStream_t)stream;
+  k_update_c<float><<<ceil_div(h->V, 256), 256, 0, st>>>(h->x, c_d, h->s, h->V, h->xnew);
+  EPET_LAUNCHED();
+  return launch_sum_normalise(h->xnew, h->V, h->part_x, h->x, st);
+}
+
+epet_status epet_mlem_loglik(epet_mlem* h, double* loglik_h, epet_stream_t stream) {
+  if (!h || !loglik_h) return set_error(EPET_ERR_INVALID, "bad arguments");
+  cudaStream_t st = (cudaStream_t)stream;
+  if (h->m > 0) {
+    const int nb = (int)std::max<int64_t>(1, std::min<int64_t>(ceil_div(h->m, 256), 1024));
+    EPET_CHECK(poisson_loglik(h->y, h->ybar, h->m, h->part_ll, nb, h->sums + 0, st));
+  } else {
+    EPET_CUDA(cudaMemsetAsync(h->sums, 0, 8, st));
+  }
+  double s0 = 0.0;
+  EPET_CUDA(cudaMemcpyAsync(&s0, h->sums, 8, cudaMemcpyDeviceToHost, st));
+  EPET_CUDA(cudaStreamSynchronize(st));
+  *loglik_h = s0;
   return EPET_OK;
 }
 

@@ -105,6 +105,9 @@ template epet_status launch_rows<EpiMlemForward>(const RowPlan&, const int64_t*,
 template epet_status launch_rows<EpiMlemUpdate>(const RowPlan&, const int64_t*, const int32_t*,
                                                 const float*, const float*, int64_t,
                                                 EpiMlemUpdate, double*, cudaStream_t);
+template epet_status launch_rows<EpiKeep>(const RowPlan&, const int64_t*, const int32_t*,
+                                           const float*, const float*, int64_t, EpiKeep,
+                                           double*, cudaStream_t);
 
 epet_status launch_sum_partials(const double* p, int64_t n, double* out, cudaStream_t st) {
   k_sum_partials<<<1, 1024, 0, st>>>(p, n, out);

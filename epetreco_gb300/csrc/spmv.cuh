@@ -56,6 +56,16 @@ struct EpiMlemUpdate {
   }
 };
 
+// Store the product (c = (A^T e)[v] of a row-sharded reconstruction, summed
+// across shards before the update).
+struct EpiKeep {
+  float* out;
+  __device__ double operator()(int64_t r, float d) const {
+    out[r] = d;
+    return 0.0;
+  }
+};
+
 int pick_group(double avg_len);
 RowPlan default_plan(double avg_len);
 

@@ -162,9 +162,10 @@ epet_status epet_dump_uniforms(const epet_problem* p, const int32_t* rows_d,
 epet_status epet_build_counters(int64_t* overflow_rows_h, int64_t* exact_rows_h);
 /* Work measure of the chord walk (no counterpart in the reference): the
  * total over the listed channels' rays of the grid cells each ray crosses
- * (1 + the grid planes it passes inside the grid).  Synchronous. */
+ * (1 + the grid planes it passes inside the grid), in *steps_h and, when
+ * row_steps_d != NULL, per row in row_steps_d[m].  Synchronous. */
 epet_status epet_ray_steps(const epet_problem* p, const int32_t* rows_d, int64_t m,
-                           int64_t* steps_h, epet_stream_t stream);
+                           int64_t* row_steps_d, int64_t* steps_h, epet_stream_t stream);
 /* Library self-test (no counterpart in the reference): compares the walk
  * kernel's reciprocal-based correctly rounded division with the hardware's
  * IEEE division on n seeded operand pairs; *mismatches_h counts differing
@@ -397,6 +398,18 @@ epet_status epet_mlem_destroy(epet_mlem* h);
  * projection is returned (synchronous then). */
 epet_status epet_mlem_iterate(epet_mlem* h, int32_t nit, double* loglik_h,
                               epet_stream_t stream);
+/* Row-sharded reconstructions (reco.cu:216-260: row chunks dealt to the MPI
+ * ranks, the correction image summed with MPI_Allreduce, then the update on
+ * every rank).  epet_mlem_correction runs the forward product (e = y / A x,
+ * ybar kept) and writes c_d[V] = A^T e over this object's rows, leaving the
+ * image unchanged; the caller sums c_d over the shards (e.g. an all-reduce);
+ * epet_mlem_update then applies x = x*c/s (s == 0 -> 1) and x /= sum(x).  On
+ * one shard, correction + update is one iteration, bit for bit.
+ * epet_mlem_loglik: the fp64 Poisson log-likelihood of the last forward
+ * projection over this object's rows (synchronous); shards add theirs. */
+epet_status epet_mlem_correction(epet_mlem* h, float* c_d, epet_stream_t stream);
+epet_status epet_mlem_update(epet_mlem* h, const float* c_d, epet_stream_t stream);
+epet_status epet_mlem_loglik(epet_mlem* h, double* loglik_h, epet_stream_t stream);
 /* Image access (device pointer valid until destroy), copy-out, statistics
  * (with matrix_free: nnz 0, and the bytes of the pass's rays, channel
  * geometry and vectors). */
