@@ -102,6 +102,7 @@ SIGNATURES = {
     "epet_csr2ecsr_i32": [VP, VP, I64, VP, I64, VP],
     "epet_csrmv_i32": [C.c_int, I64, I64, I64, F, VP, VP, VP, VP, F, VP, VP],
     "epet_index_i64_to_i32": [VP, I64, VP, VP],
+    "epet_index_i32_to_i64": [VP, I64, VP, VP],
     "epet_csr_expand_rows": [VP, I64, VP, VP, VP],
     "epet_set_constant_geometry": [C.POINTER(Setup), C.POINTER(Grid), I32],
     "epet_get_constant_geometry": [P],

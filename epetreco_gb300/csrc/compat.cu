@@ -90,6 +90,15 @@ epet_status epet_index_i64_to_i32(const int64_t* a_d, int64_t n, int32_t* b_d,
   return EPET_OK;
 }
 
+epet_status epet_index_i32_to_i64(const int32_t* a_d, int64_t n, int64_t* b_d,
+                                  epet_stream_t stream) {
+  if (n < 0 || (n > 0 && (!a_d || !b_d))) return set_error(EPET_ERR_INVALID, "bad arguments");
+  if (n == 0) return EPET_OK;
+  k_ptr_i32_to_i64<<<ceil_div(n, 256), 256, 0, (cudaStream_t)stream>>>(a_d, n, b_d);
+  EPET_LAUNCHED();
+  return EPET_OK;
+}
+
 epet_status epet_csr_expand_rows(const int64_t* row_ptr_d, int64_t m, const int32_t* rows_d,
                                  int32_t* out_d, epet_stream_t stream) {
   if (m < 0 || (m > 0 && (!row_ptr_d || !rows_d || !out_d)))

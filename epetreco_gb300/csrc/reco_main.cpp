@@ -3,7 +3,8 @@
 // no MPI, raw float32 files instead of HDF5.
 //
 //   epet_reco <measurement.f32> <out> <nrays> <sensitivity.f32> <nIt>
-//             <guess.f32|-> <geometry> [--matrix-once]
+//             <guess.f32|-> <geometry>
+//             [--matrix-once | --matrix-free | --csc-transpose]
 //
 // measurement: dense float[NCHANNELS] (the reference's "messung" dataset);
 // sensitivity, guess, output: float[V] in voxel-id order.  <geometry> is 20
@@ -14,6 +15,10 @@
 // Default: the reference's loop -- the system matrix of each row chunk is
 // rebuilt in every iteration (reco.cu:216-254).  --matrix-once: the library's
 // reconstruction object (matrix built once, iteration in a CUDA graph).
+// --matrix-free: the reconstruction object storing no matrix (the chords
+// recomputed in every iteration by one walk per row).  --csc-transpose: the
+// reference's loop with each chunk's transposed product over its
+// column-major copy (epetBuildTranspose) instead of atomics.
 #include <cstdio>
 #include <cstdlib>
 #include <sstream>
@@ -83,13 +88,16 @@ bool write_f32(const std::string& fn, const std::vector<float>& v) {
 int main(int argc, char** argv) {
   if (argc < 8) {
     fprintf(stderr,
-            "usage: %s measurement out nrays sensitivity nIt guess geometry [--matrix-once]\n",
+            "usage: %s measurement out nrays sensitivity nIt guess geometry "
+            "[--matrix-once | --matrix-free | --csc-transpose]\n",
             argv[0]);
     return EXIT_FAILURE;
   }
   const std::string fn(argv[1]), on(argv[2]), sfn(argv[4]), xfn(argv[6]);
   const int nrays = atoi(argv[3]), nIt = atoi(argv[5]);
-  const bool once = argc > 8 && std::string(argv[8]) == "--matrix-once";
+  const std::string mode = argc > 8 ? std::string(argv[8]) : std::string();
+  const bool once = mode == "--matrix-once", free_ = mode == "--matrix-free";
+  const bool csc_t = mode == "--csc-transpose";
   double g[20];
   {
     std::stringstream ss(argv[7]);
@@ -158,10 +166,10 @@ int main(int argc, char** argv) {
       scales<float>(s_devi, (float)(1. / norm), V);
     }
 
-    if (once) {
+    if (once || free_) {
       epet_problem p;
       epet_shim::check(epet_get_constant_geometry(&p), "geometry");
-      epet_mlem_options o{0, 1, 0, 0};
+      epet_mlem_options o{0, 1, 0, 0, free_ ? 1 : 0};
       epet_mlem* h = nullptr;
       epet_shim::check(epet_mlem_create(&p, yRowId_devi, yVal_devi, effM, s_devi, &o, &h, 0),
                        "epet_mlem_create");
@@ -218,8 +226,12 @@ int main(int argc, char** argv) {
                        val, ecsr, vxl, x_devi, &zero, yt);
         float* yv = &yVal_devi[ptr];
         divides<float>(e, yv, yt, m);
+        // --csc-transpose: the chunk's column-major copy makes the transposed
+        // product scatter-free (deterministic) instead of atomic
+        if (csc_t) epetBuildTranspose(m, V, (int)nnz_host, val, ecsr, vxl);
         CSRmv<float>()(handle, CUSPARSE_OPERATION_TRANSPOSE, m, V, (int)nnz_host, &one, A, val,
                        ecsr, vxl, e, &one, c);
+        if (csc_t) epetReleaseTranspose(val);
       }
       dividesMultiplies<float>(xx, x_devi, c, s_devi, V);
       CK(cudaMemcpy(x_devi, xx, sizeof(float) * V, cudaMemcpyDeviceToDevice));

@@ -12,6 +12,7 @@
 // x*c/s (s == 0 -> 1) and the image sum, both reduced in fp64 with a fixed
 // order (deterministic).
 #include <algorithm>
+#include <cstdlib>
 
 #include "common.cuh"
 #include "internal.h"
@@ -254,6 +255,38 @@ epet_status sum_f64(const float* x, int64_t n, double* partial, int nblocks, dou
   return launch_sum_partials(partial, nblocks, out, st);
 }
 
+// Launch plan of a drop-in product (epet_csrmv): the autotuner's, timed once
+// per matrix shape and process into a scratch output (so y = alpha A x +
+// beta y is only computed once, by the caller's launch); the heuristic plan
+// while the stream is being captured (no timing then) unless one is cached,
+// and always with EPET_AUTOTUNE=0 in the environment (results then depend on
+// the inputs alone).
+static epet_status dropin_plan(int kind, const int64_t* ptr, const int32_t* idx,
+                               const float* val, const float* x, int64_t nrows, int64_t nnz,
+                               int64_t ncols, cudaStream_t st, RowPlan* out) {
+  const double avg = nrows ? (double)nnz / nrows : 0.0;
+  *out = default_plan(avg);
+  static const bool off = [] {
+    const char* e = getenv("EPET_AUTOTUNE");
+    return e && e[0] == '0';
+  }();
+  if (off || nrows <= 0 || nnz <= 0) return EPET_OK;
+  if (tune_lookup(kind, nrows, nnz, ncols, out)) return EPET_OK;
+  cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+  EPET_CUDA(cudaStreamIsCapturing(st, &cs));
+  if (cs != cudaStreamCaptureStatusNone) return EPET_OK;
+  float* scratch = nullptr;
+  EPET_CUDA(dev_alloc((void**)&scratch, nrows * 4, st));
+  epet_status rc = tune_rows(
+      kind, nrows, nnz, ncols, avg,
+      [&](const RowPlan& pl) {
+        return launch_rows(pl, ptr, idx, val, x, nrows, EpiAxpby{1.f, 0.f, scratch}, nullptr, st);
+      },
+      st, out);
+  dev_free(scratch, st);
+  return rc;
+}
+
 }  // namespace epet
 
 using namespace epet;
@@ -269,13 +302,17 @@ epet_status epet_csrmv(int trans, const epet_csr* a, const epet_csc* csc, float 
   if (out_len == 0) return EPET_OK;
   cudaStream_t st = (cudaStream_t)stream;
   if (!trans) {
-    return launch_rows(default_plan(a->m ? (double)a->nnz / a->m : 0.0), a->row_ptr, a->col,
-                       a->val, x_d, a->m, EpiAxpby{alpha, beta, y_d}, nullptr, st);
+    RowPlan pl;
+    EPET_CHECK(dropin_plan(2, a->row_ptr, a->col, a->val, x_d, a->m, a->nnz, a->n, st, &pl));
+    return launch_rows(pl, a->row_ptr, a->col, a->val, x_d, a->m, EpiAxpby{alpha, beta, y_d},
+                       nullptr, st);
   }
   if (csc) {
-    return launch_rows(default_plan(csc->n ? (double)csc->nnz / csc->n : 0.0), csc->col_ptr,
-                       csc->row, csc->val, x_d, csc->n, EpiAxpby{alpha, beta, y_d}, nullptr,
-                       st);
+    RowPlan pl;
+    EPET_CHECK(dropin_plan(3, csc->col_ptr, csc->row, csc->val, x_d, csc->n, csc->nnz, csc->m,
+                           st, &pl));
+    return launch_rows(pl, csc->col_ptr, csc->row, csc->val, x_d, csc->n,
+                       EpiAxpby{alpha, beta, y_d}, nullptr, st);
   }
   if (beta != 1.f) {
     k_scale_vec<<<ceil_div(a->n, 256), 256, 0, st>>>(y_d, a->n, beta);

@@ -82,6 +82,8 @@ epet_status launch_rows(const RowPlan& plan, const int64_t* ptr, const int32_t* 
 epet_status tune_rows(int kind, int64_t nrows, int64_t nnz, int64_t ncols, double avg,
                       const std::function<epet_status(const RowPlan&)>& run, cudaStream_t st,
                       RowPlan* out);
+// The cached plan of (kind, rows, nnz, cols) on the current device, if any.
+bool tune_lookup(int kind, int64_t nrows, int64_t nnz, int64_t ncols, RowPlan* out);
 template <class Epi, class XT>
 epet_status launch_rows16(const epet_csr16* a, const XT* x, Epi epi, double* partial,
                           cudaStream_t st);

@@ -45,6 +45,16 @@ epet_status time_plan(const RowPlan& p, const std::function<epet_status(const Ro
 
 }  // namespace
 
+bool tune_lookup(int kind, int64_t nrows, int64_t nnz, int64_t ncols, RowPlan* out) {
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return false;
+  std::lock_guard<std::mutex> lock(g_tune_mu);
+  auto it = g_tune_cache.find(TuneKey{dev, kind, nrows, nnz, ncols});
+  if (it == g_tune_cache.end()) return false;
+  *out = it->second;
+  return true;
+}
+
 epet_status tune_rows(int kind, int64_t nrows, int64_t nnz, int64_t ncols, double avg,
                       const std::function<epet_status(const RowPlan&)>& run, cudaStream_t st,
                       RowPlan* out) {

@@ -293,7 +293,13 @@ size_t epet_csr_to_csc_workspace_size(int64_t m, int64_t n, int64_t nnz);
 /* CSRmv<float>::operator() (csrmv.hpp:25-36): y = alpha*op(A)*x + beta*y,
  * trans = 0 (NON_TRANSPOSE) or 1 (TRANSPOSE).  The transpose reads the CSC
  * when csc != NULL (scatter-free, deterministic), else scatters with fp32
- * atomics into y. */
+ * atomics into y.  The launch shape of the row products comes from the
+ * autotuner: the first call for a matrix shape (rows, nnz, columns) times
+ * the candidate shapes into scratch memory (y is written once) and the
+ * process keeps the winner; while the stream is being captured, or with
+ * EPET_AUTOTUNE=0 in the environment, a fixed heuristic shape is used
+ * (results then depend on the inputs alone; shapes change fp32 rounding
+ * only). */
 epet_status epet_csrmv(int trans, const epet_csr* a, const epet_csc* csc,
                        float alpha, const float* x_d, float beta, float* y_d,
                        epet_stream_t stream);
@@ -341,6 +347,8 @@ epet_status epet_csrmv_i32(int trans, int64_t m, int64_t n, int64_t nnz,
                            const float* x_d, float beta, float* y_d,
                            epet_stream_t stream);
 epet_status epet_index_i64_to_i32(const int64_t* a_d, int64_t n, int32_t* b_d,
+                                  epet_stream_t stream);
+epet_status epet_index_i32_to_i64(const int32_t* a_d, int64_t n, int64_t* b_d,
                                   epet_stream_t stream);
 /* out_d[k] = rows_d[i] for every entry k of row i (the COO row ids that
  * systemMatrixCalculation leaves in aCnlId_devi, wrappers.hpp:172-247). */

@@ -175,8 +175,77 @@ inline void convertCsr2Ecsr(int* const ecsrRowPtr, int* const yRowId, int const 
   epet_shim::check_cuda(cudaDeviceSynchronize(), "convertCsr2Ecsr");
 }
 
+namespace epet_shim {
+
+/* Column-major copies registered for CSRs (keyed by the CSR's value array):
+ * a transposed CSRmv on a registered matrix reads its copy (scatter-free,
+ * deterministic) instead of scattering with atomics.  One host thread, as
+ * the reference's drivers. */
+struct TransposeEntry {
+  const float* csr_val;
+  int m, n, nnz;
+  epet_csc csc;
+};
+inline TransposeEntry* transposes() {
+  static TransposeEntry table[16];
+  return table;
+}
+inline int& transpose_count() {
+  static int n = 0;
+  return n;
+}
+inline TransposeEntry* find_transpose(const float* val, int m, int n, int nnz) {
+  TransposeEntry* t = transposes();
+  for (int i = 0; i < transpose_count(); i++)
+    if (t[i].csr_val == val && t[i].m == m && t[i].n == n && t[i].nnz == nnz) return &t[i];
+  return nullptr;
+}
+
+}  // namespace epet_shim
+
+/* No counterpart in the reference: builds the column-major copy of an
+ * m x n CSR with int row pointers (device arrays, as CSRmv takes them) and
+ * registers it, so later CSRmv(CUSPARSE_OPERATION_TRANSPOSE) calls on this
+ * matrix (same value array and sizes) use the scatter-free product.  Worth
+ * it when a matrix is transposed in several iterations (a driver that keeps
+ * its matrix); release with epetReleaseTranspose before freeing the CSR. */
+inline void epetBuildTranspose(int m, int n, int nnz, float* const csrValA,
+                               int* const csrRowPtrA, int* const csrColIdA) {
+  using namespace epet_shim;
+  if (find_transpose(csrValA, m, n, nnz)) return;
+  TransposeEntry* t = transposes();
+  if (transpose_count() == 16) check(EPET_ERR_CAPACITY, "epetBuildTranspose: 16 registered");
+  TransposeEntry e{csrValA, m, n, nnz, epet_csc{}};
+  int64_t* rp = nullptr;
+  check_cuda(cudaMalloc((void**)&rp, ((size_t)m + 1) * sizeof(int64_t)), "cudaMalloc");
+  check_cuda(cudaMalloc((void**)&e.csc.col_ptr, ((size_t)n + 1) * sizeof(int64_t)), "cudaMalloc");
+  check_cuda(cudaMalloc((void**)&e.csc.row, ((size_t)nnz + 1) * sizeof(int32_t)), "cudaMalloc");
+  check_cuda(cudaMalloc((void**)&e.csc.val, ((size_t)nnz + 1) * sizeof(float)), "cudaMalloc");
+  epet_status st = epet_index_i32_to_i64(csrRowPtrA, (int64_t)m + 1, rp, 0);
+  epet_csr a{m, n, nnz, rp, csrColIdA, csrValA};
+  if (st == EPET_OK) st = epet_csr_to_csc(&a, &e.csc, nullptr, 0, 0);
+  check_cuda(cudaDeviceSynchronize(), "epetBuildTranspose");
+  cudaFree(rp);
+  check(st, "epetBuildTranspose");
+  t[transpose_count()++] = e;
+}
+
+inline void epetReleaseTranspose(float* const csrValA) {
+  using namespace epet_shim;
+  TransposeEntry* t = transposes();
+  for (int i = 0; i < transpose_count(); i++)
+    if (t[i].csr_val == csrValA) {
+      cudaFree(t[i].csc.col_ptr);
+      cudaFree(t[i].csc.row);
+      cudaFree(t[i].csc.val);
+      t[i] = t[--transpose_count()];
+      return;
+    }
+}
+
 /* CSRmv<float> (csrmv.hpp:18-36); alpha/beta are host pointers as in the
- * reference; the transpose scatters with atomics. */
+ * reference; the transpose reads the column-major copy registered with
+ * epetBuildTranspose for this matrix, else scatters with atomics. */
 template <typename T>
 struct CSRmv;
 
@@ -188,8 +257,17 @@ struct CSRmv<float> {
                   float* const beta, float* const y) {
     (void)handle;
     (void)descrA;
-    epet_shim::check(epet_csrmv_i32(transA == CUSPARSE_OPERATION_NON_TRANSPOSE ? 0 : 1, m, n,
-                                    nnz, *alpha, csrValA, csrRowPtrA, csrColIdA, x, *beta, y, 0),
+    const int trans = transA == CUSPARSE_OPERATION_NON_TRANSPOSE ? 0 : 1;
+    if (trans) {
+      if (const epet_shim::TransposeEntry* e =
+              epet_shim::find_transpose(csrValA, m, n, nnz)) {
+        epet_csr a{m, n, nnz, nullptr, csrColIdA, csrValA};
+        epet_shim::check(epet_csrmv(1, &a, &e->csc, *alpha, x, *beta, y, 0), "CSRmv");
+        return;
+      }
+    }
+    epet_shim::check(epet_csrmv_i32(trans, m, n, nnz, *alpha, csrValA, csrRowPtrA, csrColIdA, x,
+                                    *beta, y, 0),
                      "CSRmv");
   }
 };

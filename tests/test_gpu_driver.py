@@ -62,3 +62,16 @@ def test_driver_reference_loop_matches_library(inputs):
     R.iterate(2)
     x = R.image().cpu().numpy()
     assert np.linalg.norm(x_drv - x) / np.linalg.norm(x) < 1e-5
+
+
+@pytest.mark.parametrize("mode", ["--matrix-free", "--csc-transpose"])
+def test_driver_other_schedules_match_library(inputs, mode):
+    """The reconstruction object without a stored matrix, and the reference's
+    loop whose transposed products read each chunk's column-major copy
+    (epetBuildTranspose) instead of scattering with atomics."""
+    p, rows, y, s, d, exe = inputs
+    x_drv = run_driver(exe, d, p, 2, [mode])
+    R = api.Mlem(p, rows, y, s)
+    R.iterate(2)
+    x = R.image().cpu().numpy()
+    assert np.linalg.norm(x_drv - x) / np.linalg.norm(x) < 1e-5
