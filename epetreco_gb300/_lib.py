@@ -57,7 +57,7 @@ class Csr16C(C.Structure):
 class MlemOptions(C.Structure):
     _fields_ = [("max_row_nnz", C.c_int32), ("use_graph", C.c_int32),
                 ("value_format", C.c_int32), ("autotune", C.c_int32),
-                ("matrix_free", C.c_int32)]
+                ("matrix_free", C.c_int32), ("layout", C.c_int32)]
 
 
 P, VP, I64, I32, F, D, SZ = (C.POINTER(ProblemC), C.c_void_p, C.c_int64, C.c_int32, C.c_float,

@@ -278,6 +278,8 @@ def CSRmv(transA: int, A: Csr, x: torch.Tensor, alpha: float = 1.0, beta: float 
 # ------------------------------------------------------ 16-bit value storage
 
 BF16, FP16 = 1, 2
+# layouts of a reconstruction's stored matrix (epet_mlem_options.layout)
+LAYOUT_AUTO, LAYOUT_GROUPED, LAYOUT_CSC = 0, 1, 2
 
 
 @dataclass
@@ -415,7 +417,8 @@ class Mlem:
     channel), so a shuffled list gives the same object."""
 
     def __init__(self, p, rows, y, s, use_graph: bool = True, max_row_nnz: int = 0,
-                 value_format: int = 0, autotune: bool = False, matrix_free: bool = False):
+                 value_format: int = 0, autotune: bool = False, matrix_free: bool = False,
+                 layout: int = LAYOUT_AUTO):
         """``matrix_free=True`` stores no matrix: every iteration recomputes
         the chords in one walk per row (the reference's schedule of a matrix
         rebuilt in every iteration)."""
@@ -425,7 +428,7 @@ class Mlem:
         s = s.to(torch.float32).contiguous()
         self._h = C.c_void_p()
         opt = MlemOptions(int(max_row_nnz), 1 if use_graph else 0, int(value_format),
-                          1 if autotune else 0, 1 if matrix_free else 0)
+                          1 if autotune else 0, 1 if matrix_free else 0, int(layout))
         check(lib().epet_mlem_create(C.byref(problem_struct(p)), _ptr(rows), _ptr(y),
                                      rows.numel(), _ptr(s), C.byref(opt), C.byref(self._h),
                                      _stream()))

@@ -205,6 +205,7 @@ epet_status epet_mlem_batch_create(int32_t nprob, const epet_problem* problems,
   };
   epet_mlem_options po = o;  // members iterated alone: graph as asked, heuristic shapes
   po.autotune = 0;
+  po.layout = EPET_LAYOUT_CSC;  // the batched launches read each member's CSR and CSC
   for (int i = 0; i < nprob; i++) {
     epet_mlem* p = nullptr;
     epet_status rc = epet_mlem_create(&problems[i], rows_d[i], y_d[i], m[i], s_d[i], &po, &p,

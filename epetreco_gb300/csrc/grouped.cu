@@ -1,0 +1,508 @@
+// grouped.cu -- a reconstruction's system matrix as row groups with
+// group-local column ids, and the one-pass MLEM iteration over it.
+//
+// The rows (in the reconstruction's crystal-pair order) are cut into groups
+// of consecutive rows whose distinct columns fit a per-warp table in shared
+// memory.  Consecutive rows in that order are a fan of lines through nearly
+// one point, so a group touches few voxels: at 52^3 voxels a group of 32
+// rows (~14k entries) touches ~1000.  Each entry keeps only its value and a
+// 2-byte rank of its column among the group's sorted distinct columns (the
+// group's table), 6 bytes per entry in FP32 and 4 in BF16/FP16 instead of a
+// CSR plus a column-major copy (16 bytes).
+//
+// One iteration reads every entry once (k_group_mlem): a warp takes a group,
+// gathers x at the table into shared memory, and row by row forms A x from
+// the shared copy, e = y / (A x) and adds the row times e into the group's
+// shared correction; a row's columns are distinct, so the lanes never write
+// the same word and each column's sum runs in row order.  The group's
+// corrections go to one slot per (group, column); the slots of each column,
+// listed in group order (built once, a column-major copy of the table),
+// are summed in that order by a row kernel whose epilogue applies x*c/s.
+// Every sum has an input-determined order, so results are deterministic.
+#include <cuda_bf16.h>
+#include <cuda_fp16.h>
+
+#include <algorithm>
+#include <vector>
+
+#include "common.cuh"
+#include "internal.h"
+#include "mlem_internal.h"
+#include "spmv.cuh"
+
+namespace epet {
+
+constexpr int kGroupFirstRows = 32;  // rows of a first-cut group (split while too wide)
+constexpr int kGroupThreads = 256;   // threads of the table-building kernels
+
+// Distinct columns of the candidate groups cand[g] = {r0, r1}: a bitmap over
+// the columns in shared memory (nwords 32-bit words).
+__global__ void __launch_bounds__(kGroupThreads)
+k_group_distinct(const int64_t* __restrict__ row_ptr, const int32_t* __restrict__ col,
+                 const int2* __restrict__ cand, int nwords, int32_t* __restrict__ nd) {
+  extern __shared__ unsigned gbm[];
+  __shared__ int wsum[kGroupThreads / 32];
+  for (int i = threadIdx.x; i < nwords; i += kGroupThreads) gbm[i] = 0u;
+  __syncthreads();
+  const int2 c = cand[blockIdx.x];
+  const int64_t b = row_ptr[c.x], e = row_ptr[c.y];
+  for (int64_t k = b + threadIdx.x; k < e; k += kGroupThreads) {
+    const unsigned v = (unsigned)col[k];
+    atomicOr(&gbm[v >> 5], 1u << (v & 31));
+  }
+  __syncthreads();
+  int n = 0;
+  for (int i = threadIdx.x; i < nwords; i += kGroupThreads) n += __popc(gbm[i]);
+  for (int o = 16; o > 0; o >>= 1) n += __shfl_xor_sync(0xffffffffu, n, o);
+  if ((threadIdx.x & 31) == 0) wsum[threadIdx.x >> 5] = n;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int t = 0;
+    for (int w = 0; w < kGroupThreads / 32; w++) t += wsum[w];
+    nd[blockIdx.x] = t;
+  }
+}
+
+// Tables and local ids of the final groups (one block per group): the
+// group's distinct columns, ascending, at table[tb ..]; each entry's rank in
+// them.  A single row wider than the shared tables keeps its own columns as
+// its table (its entries' ranks are their positions in the row).
+__global__ void __launch_bounds__(kGroupThreads)
+k_group_tables(const int64_t* __restrict__ row_ptr, const int32_t* __restrict__ col,
+               const GroupDesc* __restrict__ groups, int nwords, int32_t* __restrict__ table,
+               uint16_t* __restrict__ loc) {
+  extern __shared__ unsigned gsh[];
+  unsigned* bm = gsh;
+  int* pre = reinterpret_cast<int*>(gsh + nwords);
+  __shared__ int wtot[kGroupThreads / 32];
+  const GroupDesc gd = groups[blockIdx.x];
+  const int64_t b = row_ptr[gd.r0], e = row_ptr[gd.r1];
+  if (gd.nd > kGroupCap) {
+    for (int64_t k = b + threadIdx.x; k < e; k += kGroupThreads) table[gd.tb + (k - b)] = col[k];
+    return;
+  }
+  for (int i = threadIdx.x; i < nwords; i += kGroupThreads) bm[i] = 0u;
+  __syncthreads();
+  for (int64_t k = b + threadIdx.x; k < e; k += kGroupThreads) {
+    const unsigned v = (unsigned)col[k];
+    atomicOr(&bm[v >> 5], 1u << (v & 31));
+  }
+  __syncthreads();
+  // exclusive prefix of the words' popcounts: thread t owns a contiguous
+  // range of words
+  const int per = (nwords + kGroupThreads - 1) / kGroupThreads;
+  const int wb = min(nwords, (int)threadIdx.x * per), we = min(nwords, wb + per);
+  int cnt = 0;
+  for (int w = wb; w < we; w++) cnt += __popc(bm[w]);
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  int inc = warp_incl_scan(cnt);
+  if (lane == 31) wtot[wid] = inc;
+  __syncthreads();
+  if (wid == 0) {
+    const int t = lane < kGroupThreads / 32 ? wtot[lane] : 0;
+    const int ti = warp_incl_scan(t);
+    if (lane < kGroupThreads / 32) wtot[lane] = ti - t;
+  }
+  __syncthreads();
+  int run = wtot[wid] + inc - cnt;
+  for (int w = wb; w < we; w++) {
+    pre[w] = run;
+    unsigned word = bm[w];
+    while (word) {
+      const int bit = __ffs(word) - 1;
+      table[gd.tb + run] = w * 32 + bit;
+      run++;
+      word &= word - 1u;
+    }
+  }
+  __syncthreads();
+  for (int64_t k = b + threadIdx.x; k < e; k += kGroupThreads) {
+    const unsigned v = (unsigned)col[k];
+    loc[k] = (uint16_t)(pre[v >> 5] + __popc(bm[v >> 5] & ((1u << (v & 31)) - 1u)));
+  }
+}
+
+__global__ void k_slot_ids(int64_t n, float* __restrict__ out) {  // slot index bits
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) out[i] = __int_as_float((int32_t)i);
+}
+
+__global__ void k_fill_f32(float* __restrict__ p, int64_t n, float v) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) p[i] = v;
+}
+
+// 16-bit values: q = the 16-bit float of value / scale, scale = the row's
+// largest value (the 16-bit forms' quantisation), a warp per row.
+template <int FMT>
+__device__ __forceinline__ uint16_t gq_to(float v) {
+  if (FMT == 1) return __bfloat16_as_ushort(__float2bfloat16_rn(v));
+  return __half_as_ushort(__float2half_rn(v));
+}
+template <int FMT>
+__device__ __forceinline__ float gq_from(uint32_t q) {
+  if (FMT == 1) return __uint_as_float(q << 16);
+  return __half2float(__ushort_as_half((unsigned short)q));
+}
+
+template <int FMT>
+__global__ void k_group_quantise(const int64_t* __restrict__ row_ptr, const float* __restrict__ val,
+                                 int64_t m, float* __restrict__ scale, uint16_t* __restrict__ q) {
+  const int64_t r = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (r >= m) return;
+  const int64_t b = row_ptr[r], e = row_ptr[r + 1];
+  float mx = 0.f;
+  for (int64_t k = b + lane; k < e; k += 32) mx = fmaxf(mx, fabsf(val[k]));
+  for (int o = 16; o > 0; o >>= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+  const float sc = mx > 0.f ? mx : 1.f;
+  if (lane == 0) scale[r] = sc;
+  for (int64_t k = b + lane; k < e; k += 32) q[k] = gq_to<FMT>(__fdiv_rn(val[k], sc));
+}
+
+// Four consecutive values (index k4, a multiple of 4) of the matrix stream.
+template <int FMT>
+__device__ __forceinline__ void gload4(const void* __restrict__ v, int64_t k4, float out[4]) {
+  if constexpr (FMT == 0) {
+    const float4 t = __ldcs(reinterpret_cast<const float4*>(static_cast<const float*>(v) + k4));
+    out[0] = t.x; out[1] = t.y; out[2] = t.z; out[3] = t.w;
+  } else {
+    const uint2 t = __ldcs(reinterpret_cast<const uint2*>(static_cast<const uint16_t*>(v) + k4));
+    out[0] = gq_from<FMT>(t.x & 0xffffu); out[1] = gq_from<FMT>(t.x >> 16);
+    out[2] = gq_from<FMT>(t.y & 0xffffu); out[3] = gq_from<FMT>(t.y >> 16);
+  }
+}
+__device__ __forceinline__ void gloadloc4(const uint16_t* __restrict__ l, int64_t k4, int out[4]) {
+  const uint2 t = __ldcs(reinterpret_cast<const uint2*>(l + k4));
+  out[0] = (int)(t.x & 0xffffu); out[1] = (int)(t.x >> 16);
+  out[2] = (int)(t.y & 0xffffu); out[3] = (int)(t.y >> 16);
+}
+
+struct GroupIterArgs {
+  const GroupDesc* groups;
+  int64_t ngroups;
+  const int64_t* row_ptr;
+  const void* val;       // float (FP32) or 16-bit bits
+  const float* scale;    // per row (16-bit forms)
+  const uint16_t* loc;
+  const int32_t* table;
+  const float* x;
+  const float* y;
+  float* ybar;
+  float* partial;
+};
+
+constexpr int kGroupRounds = 4;  // 4-entry chunks per lane kept in registers (512 entries a row)
+
+// One pass of the MLEM iteration over the grouped matrix: per row ybar =
+// A x, e = y / ybar (0 where ybar == 0, the fused epilogue's guard), and the
+// group's corrections sum_rows A[r, .] * e_r into partial[slot].
+template <int FMT>
+__global__ void __launch_bounds__(kGroupWarps * 32, 1)
+k_group_mlem(GroupIterArgs a) {
+  extern __shared__ __align__(16) float gsm[];
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  float* xs = gsm + (size_t)w * 2 * kGroupCap;
+  float* cs = xs + kGroupCap;
+  for (int64_t g = (int64_t)blockIdx.x * kGroupWarps + w; g < a.ngroups;
+       g += (int64_t)gridDim.x * kGroupWarps) {
+    const GroupDesc gd = a.groups[g];
+    const bool wide = gd.nd > kGroupCap;  // one row, its own columns as table
+    if (!wide) {
+      for (int j = lane; j < gd.nd; j += 32) {
+        xs[j] = __ldg(a.x + a.table[gd.tb + j]);
+        cs[j] = 0.f;
+      }
+      __syncwarp();
+    }
+    for (int r = gd.r0; r < gd.r1; r++) {
+      const int64_t b = a.row_ptr[r], e = a.row_ptr[r + 1];
+      const int64_t a0 = b & ~int64_t(3);
+      const int64_t nq = (e - a0 + 3) >> 2;  // 4-entry chunks over [a0, e)
+      float v[kGroupRounds][4];
+      int l[kGroupRounds][4];
+#pragma unroll
+      for (int u = 0; u < kGroupRounds; u++) {
+        const int64_t q = lane + 32 * u;
+        if (q < nq) {
+          gload4<FMT>(a.val, a0 + 4 * q, v[u]);
+          if (!wide) gloadloc4(a.loc, a0 + 4 * q, l[u]);
+        }
+      }
+      float acc = 0.f;
+      auto dot4 = [&](const float* vv, const int* ll, int64_t k0) {
+#pragma unroll
+        for (int t = 0; t < 4; t++) {
+          const int64_t k = k0 + t;
+          if (k >= b && k < e) {
+            const float xv = wide ? __ldg(a.x + a.table[gd.tb + (k - b)]) : xs[ll[t]];
+            acc = fmaf(vv[t], xv, acc);
+          }
+        }
+      };
+#pragma unroll
+      for (int u = 0; u < kGroupRounds; u++) {
+        const int64_t q = lane + 32 * u;
+        if (q < nq) dot4(v[u], l[u], a0 + 4 * q);
+      }
+      for (int64_t q = lane + 32 * kGroupRounds; q < nq; q += 32) {  // rows over 512 entries
+        float vv[4];
+        int ll[4];
+        gload4<FMT>(a.val, a0 + 4 * q, vv);
+        if (!wide) gloadloc4(a.loc, a0 + 4 * q, ll);
+        dot4(vv, ll, a0 + 4 * q);
+      }
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+      const float sc = FMT == 0 ? 1.f : a.scale[r];
+      const float yb = FMT == 0 ? acc : fmul(acc, sc);
+      if (lane == 0) a.ybar[r] = yb;
+      // e = y / (A x) (mlemOperations.hpp:22-32; 0 where A x == 0)
+      const float er = yb > 0.f ? __fdiv_rn(a.y[r], yb) : 0.f;
+      const float f = FMT == 0 ? er : fmul(er, sc);
+      auto scatter4 = [&](const float* vv, const int* ll, int64_t k0) {
+#pragma unroll
+        for (int t = 0; t < 4; t++) {
+          const int64_t k = k0 + t;
+          if (k >= b && k < e) {
+            if (wide) a.partial[gd.tb + (k - b)] = fmul(vv[t], f);
+            else cs[ll[t]] = fadd(cs[ll[t]], fmul(vv[t], f));
+          }
+        }
+      };
+#pragma unroll
+      for (int u = 0; u < kGroupRounds; u++) {
+        const int64_t q = lane + 32 * u;
+        if (q < nq) scatter4(v[u], l[u], a0 + 4 * q);
+      }
+      for (int64_t q = lane + 32 * kGroupRounds; q < nq; q += 32) {
+        float vv[4];
+        int ll[4];
+        gload4<FMT>(a.val, a0 + 4 * q, vv);
+        if (!wide) gloadloc4(a.loc, a0 + 4 * q, ll);
+        scatter4(vv, ll, a0 + 4 * q);
+      }
+      __syncwarp();
+    }
+    if (!wide) {
+      for (int j = lane; j < gd.nd; j += 32) a.partial[gd.tb + j] = cs[j];
+      __syncwarp();
+    }
+  }
+}
+
+// ---------------------------------------------------------------- host
+
+static int bitmap_words(int64_t V) { return (int)((V + 31) / 32); }
+
+bool grouped_supported(int64_t V, int64_t m) {
+  // two V-bit maps in a table block's shared memory; int32 rows
+  return V > 0 && (size_t)bitmap_words(V) * 8 <= (size_t)200 * 1024 && m < INT32_MAX;
+}
+
+void grouped_free(GroupedMatrix* G, cudaStream_t st) {
+  for (void* p : {(void*)G->groups, (void*)G->table, (void*)G->loc, (void*)G->cg_ptr,
+                  (void*)G->cg_slot, (void*)G->ones, (void*)G->partial, (void*)G->val16,
+                  (void*)G->scale})
+    if (p) dev_free(p, st);
+  *G = GroupedMatrix{};
+}
+
+// Groups of consecutive rows of A (row pointers on the device) whose
+// distinct columns fit kGroupCap: first cuts of kGroupFirstRows rows, halved
+// while too wide; a single row wider than that is a group of its own.
+static epet_status form_groups(const epet_csr& A, std::vector<GroupDesc>* out, cudaStream_t st) {
+  const int64_t m = A.m;
+  const int nwords = bitmap_words(A.n);
+  struct Piece {
+    int32_t r0, r1, nd;  // nd < 0: not measured yet
+  };
+  std::vector<Piece> ps;
+  for (int64_t r = 0; r < m; r += kGroupFirstRows)
+    ps.push_back({(int32_t)r, (int32_t)std::min<int64_t>(m, r + kGroupFirstRows), -1});
+  int2* cand = nullptr;
+  int32_t* nd = nullptr;
+  epet_status rc = EPET_OK;
+  EPET_CUDA(cudaFuncSetAttribute(k_group_distinct, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 nwords * 4));
+  for (int round = 0; round < 40 && rc == EPET_OK; round++) {
+    std::vector<int> todo;
+    for (int i = 0; i < (int)ps.size(); i++)
+      if (ps[i].nd < 0) todo.push_back(i);
+    if (todo.empty()) break;
+    std::vector<int2> hc(todo.size());
+    for (size_t k = 0; k < todo.size(); k++) hc[k] = make_int2(ps[todo[k]].r0, ps[todo[k]].r1);
+    std::vector<int32_t> hn(todo.size());
+    const size_t n = todo.size();
+    cudaError_t e = dev_alloc((void**)&cand, n * sizeof(int2), st);
+    if (e == cudaSuccess) e = dev_alloc((void**)&nd, n * 4, st);
+    if (e == cudaSuccess)
+      e = cudaMemcpyAsync(cand, hc.data(), n * sizeof(int2), cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess) {
+      k_group_distinct<<<(unsigned)n, kGroupThreads, nwords * 4, st>>>(A.row_ptr, A.col, cand,
+                                                                       nwords, nd);
+      note_launch();
+      e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaMemcpyAsync(hn.data(), nd, n * 4, cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (cand) dev_free(cand, st);
+    if (nd) dev_free(nd, st);
+    cand = nullptr;
+    nd = nullptr;
+    if (e != cudaSuccess) {
+      rc = cuda_status(e, "row groups");
+      break;
+    }
+    for (size_t k = 0; k < n; k++) ps[todo[k]].nd = hn[k];
+    std::vector<Piece> next;
+    next.reserve(ps.size() + 64);
+    for (const Piece& p : ps) {
+      if (p.nd > kGroupCap && p.r1 - p.r0 > 1) {
+        const int32_t mid = p.r0 + (p.r1 - p.r0) / 2;
+        next.push_back({p.r0, mid, -1});
+        next.push_back({mid, p.r1, -1});
+      } else {
+        next.push_back(p);
+      }
+    }
+    ps.swap(next);
+  }
+  if (rc != EPET_OK) return rc;
+  out->clear();
+  int64_t tb = 0;
+  for (const Piece& p : ps) {
+    if (p.nd < 0) return set_error(EPET_ERR_INVALID, "internal: row groups unmeasured");
+    if (tb + p.nd > INT32_MAX) return set_error(EPET_ERR_UNSUPPORTED, "row-group tables exceed int32");
+    out->push_back(GroupDesc{p.r0, p.r1, (int32_t)tb, p.nd});
+    tb += p.nd;
+  }
+  return EPET_OK;
+}
+
+epet_status grouped_build(const epet_csr& A, int value_format, GroupedMatrix* G,
+                          cudaStream_t st) {
+  *G = GroupedMatrix{};
+  G->fmt = value_format;
+  if (!grouped_supported(A.n, A.m))
+    return set_error(EPET_ERR_UNSUPPORTED, "grouped layout: %lld columns", (long long)A.n);
+  std::vector<GroupDesc> hg;
+  EPET_CHECK(form_groups(A, &hg, st));
+  G->ngroups = (int64_t)hg.size();
+  G->nslots = hg.empty() ? 0 : (int64_t)hg.back().tb + hg.back().nd;
+  const int64_t ns = std::max<int64_t>(G->nslots, 1);
+  auto fail = [&](epet_status rc) {
+    grouped_free(G, st);
+    return rc;
+  };
+#define GALLOC(ptr, bytes)                                                        \
+  do {                                                                            \
+    cudaError_t e_ = dev_alloc((void**)&(ptr), std::max<size_t>((bytes), 16), st); \
+    if (e_ != cudaSuccess) return fail(cuda_status(e_, "grouped allocation " #ptr)); \
+  } while (0)
+  GALLOC(G->groups, hg.size() * sizeof(GroupDesc));
+  GALLOC(G->table, ns * 4);
+  GALLOC(G->loc, (A.nnz + 8) * 2);  // 4-entry loads may reach 3 entries past the end
+  GALLOC(G->partial, ns * 4);
+  GALLOC(G->ones, ns * 4);
+  GALLOC(G->cg_ptr, (A.n + 1) * 8);
+  if (!hg.empty()) {
+    cudaError_t e = cudaMemcpyAsync(G->groups, hg.data(), hg.size() * sizeof(GroupDesc),
+                                    cudaMemcpyHostToDevice, st);
+    if (e != cudaSuccess) return fail(cuda_status(e, "group table"));
+  }
+  cudaMemsetAsync(G->loc + A.nnz, 0, 16, st);
+  const int nwords = bitmap_words(A.n);
+  cudaError_t e = cudaFuncSetAttribute(k_group_tables, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       nwords * 8);
+  {
+    const int smem = kGroupWarps * 2 * kGroupCap * 4;  // the iteration kernel's tables
+    if (e == cudaSuccess)
+      e = cudaFuncSetAttribute(k_group_mlem<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    if (e == cudaSuccess)
+      e = cudaFuncSetAttribute(k_group_mlem<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    if (e == cudaSuccess)
+      e = cudaFuncSetAttribute(k_group_mlem<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+  }
+  if (e != cudaSuccess) return fail(cuda_status(e, "group tables"));
+  if (!hg.empty()) {
+    k_group_tables<<<(unsigned)hg.size(), kGroupThreads, nwords * 8, st>>>(A.row_ptr, A.col,
+                                                                            G->groups, nwords,
+                                                                            G->table, G->loc);
+    note_launch();
+    if (cudaGetLastError() != cudaSuccess) return fail(set_error(EPET_ERR_CUDA, "group tables"));
+  }
+  // the slots of each column in group order: the column-major copy of the
+  // (group x column) table, its values the slot indices
+  {
+    float* slot_bits = nullptr;
+    int32_t* cg_group = nullptr;
+    GALLOC(slot_bits, ns * 4);
+    GALLOC(cg_group, ns * 4);
+    GALLOC(G->cg_slot, ns * 4);
+    int64_t* gptr = nullptr;
+    GALLOC(gptr, (G->ngroups + 1) * 8);
+    std::vector<int64_t> hp(G->ngroups + 1);
+    for (int64_t i = 0; i < G->ngroups; i++) hp[i] = hg[i].tb;
+    hp[G->ngroups] = G->nslots;
+    epet_status rc = EPET_OK;
+    e = cudaMemcpyAsync(gptr, hp.data(), hp.size() * 8, cudaMemcpyHostToDevice, st);
+    if (e != cudaSuccess) rc = cuda_status(e, "slot lists");
+    if (rc == EPET_OK && G->nslots > 0) {
+      k_slot_ids<<<ceil_div(G->nslots, 256), 256, 0, st>>>(G->nslots, slot_bits);
+      note_launch();
+      k_fill_f32<<<ceil_div(G->nslots, 256), 256, 0, st>>>(G->ones, G->nslots, 1.f);
+      note_launch();
+      epet_csr T{G->ngroups, A.n, G->nslots, gptr, G->table, slot_bits};
+      epet_csc C{G->ngroups, A.n, G->nslots, G->cg_ptr, cg_group,
+                 reinterpret_cast<float*>(G->cg_slot)};
+      rc = epet_csr_to_csc(&T, &C, nullptr, 0, st);
+    } else if (rc == EPET_OK) {
+      cudaMemsetAsync(G->cg_ptr, 0, (A.n + 1) * 8, st);
+    }
+    dev_free(slot_bits, st);
+    dev_free(cg_group, st);
+    dev_free(gptr, st);
+    if (rc != EPET_OK) return fail(rc);
+  }
+  if (value_format != EPET_VALUES_FP32) {
+    GALLOC(G->val16, (A.nnz + 8) * 2);
+    GALLOC(G->scale, std::max<int64_t>(A.m, 1) * 4);
+    cudaMemsetAsync(G->val16 + A.nnz, 0, 16, st);
+    if (A.m > 0) {
+      if (value_format == EPET_VALUES_BF16)
+        k_group_quantise<1><<<ceil_div(A.m * 32, 256), 256, 0, st>>>(A.row_ptr, A.val, A.m,
+                                                                     G->scale, G->val16);
+      else
+        k_group_quantise<2><<<ceil_div(A.m * 32, 256), 256, 0, st>>>(A.row_ptr, A.val, A.m,
+                                                                     G->scale, G->val16);
+      note_launch();
+      if (cudaGetLastError() != cudaSuccess) return fail(set_error(EPET_ERR_CUDA, "quantise"));
+    }
+  }
+#undef GALLOC
+  G->plan_cols = default_plan(A.n ? (double)G->nslots / A.n : 0.0);
+  return EPET_OK;
+}
+
+epet_status grouped_pass(const GroupedMatrix& G, const epet_csr& A, const float* x, const float* y,
+                         float* ybar, cudaStream_t st) {
+  if (G.ngroups == 0) return EPET_OK;
+  GroupIterArgs a{G.groups, G.ngroups, A.row_ptr,
+                  G.fmt == EPET_VALUES_FP32 ? (const void*)A.val : (const void*)G.val16,
+                  G.scale, G.loc, G.table, x, y, ybar, G.partial};
+  const size_t smem = (size_t)kGroupWarps * 2 * kGroupCap * 4;
+  const unsigned grid = (unsigned)std::min<int64_t>(
+      (G.ngroups + kGroupWarps - 1) / kGroupWarps, (int64_t)num_sms());
+  // (the shared-memory size was allowed when the layout was built: this
+  // launch may be captured in a graph)
+  switch (G.fmt) {
+    case EPET_VALUES_BF16: k_group_mlem<1><<<grid, kGroupWarps * 32, smem, st>>>(a); break;
+    case EPET_VALUES_FP16: k_group_mlem<2><<<grid, kGroupWarps * 32, smem, st>>>(a); break;
+    default: k_group_mlem<0><<<grid, kGroupWarps * 32, smem, st>>>(a);
+  }
+  EPET_LAUNCHED();
+  return EPET_OK;
+}
+
+}  // namespace epet

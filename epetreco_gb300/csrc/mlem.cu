@@ -25,6 +25,7 @@ using namespace epet;
 static void mlem_free(epet_mlem* h) {
   if (!h) return;
   cudaDeviceSynchronize();  // nothing in flight uses the arrays
+  grouped_free(&h->G, 0);
   if (h->exec) cudaGraphExecDestroy(h->exec);
   if (h->graph) cudaGraphDestroy(h->graph);
   void* bufs[] = {h->A16.row_ptr, h->A16.base, h->A16.scale, h->A16.delta, h->A16.q,
@@ -73,6 +74,11 @@ static epet_status mlem_iteration_free(epet_mlem* h, cudaStream_t st) {
 // c = A^T (y / A x) over this object's rows, without the update (the
 // forward product keeps ybar and e as in the iteration).
 static epet_status mlem_correction(epet_mlem* h, float* c, cudaStream_t st) {
+  if (h->grouped) {
+    EPET_CHECK(grouped_pass(h->G, h->A, h->x, h->y, h->ybar, st));
+    return launch_rows(h->G.plan_cols, h->G.cg_ptr, h->G.cg_slot, h->G.ones, h->G.partial, h->V,
+                       EpiKeep{c}, nullptr, st);
+  }
   if (h->opt.matrix_free) {
     EPET_CUDA(cudaMemsetAsync(h->c64, 0, h->V * 8, st));
     EPET_CHECK(epet_project_mlem(&h->p, h->rows, h->m, h->x, h->y, h->ybar, h->c64,
@@ -92,8 +98,19 @@ static epet_status mlem_correction(epet_mlem* h, float* c, cudaStream_t st) {
                      nullptr, st);
 }
 
+// The grouped layout: one pass over the entries (A x, e, the groups' shares
+// of A^T e), the fixed-order slot sums per column fused with x*c/s, the
+// image sum and the normalisation.
+static epet_status mlem_iteration_grouped(epet_mlem* h, cudaStream_t st) {
+  EPET_CHECK(grouped_pass(h->G, h->A, h->x, h->y, h->ybar, st));
+  EPET_CHECK(launch_rows(h->G.plan_cols, h->G.cg_ptr, h->G.cg_slot, h->G.ones, h->G.partial,
+                         h->V, EpiMlemUpdate{h->x, h->s, h->xnew, nullptr}, nullptr, st));
+  return launch_sum_normalise(h->xnew, h->V, h->part_x, h->x, st);
+}
+
 static epet_status mlem_iteration(epet_mlem* h, cudaStream_t st) {
   if (h->opt.matrix_free) return mlem_iteration_free(h, st);
+  if (h->grouped) return mlem_iteration_grouped(h, st);
   if (h->opt.value_format != EPET_VALUES_FP32) {
     EPET_CHECK((launch_rows16<EpiMlemForward16, float>(
         &h->A16, h->x, EpiMlemForward16{h->y, h->e16, h->ybar}, nullptr, st)));
@@ -243,8 +260,9 @@ static epet_status build_in_pair_order(const epet_problem* p, const int32_t* row
       cu(cudaMemcpyAsync(segd, hs.data(), hs.size() * sizeof(SegDev), cudaMemcpyHostToDevice, st),
          "chunk table");
     cu(dev_alloc((void**)&B.row_ptr, (m + 1) * 8, st), "allocation of A");
-    cu(dev_alloc((void**)&B.col, std::max<int64_t>(nnz, 1) * 4, st), "allocation of A");
-    cu(dev_alloc((void**)&B.val, std::max<int64_t>(nnz, 1) * 4, st), "allocation of A");
+    // (4 entries of padding: the grouped pass loads 4 entries at a time)
+    cu(dev_alloc((void**)&B.col, (nnz + 4) * 4, st), "allocation of A");
+    cu(dev_alloc((void**)&B.val, (nnz + 4) * 4, st), "allocation of A");
     cu(dev_alloc((void**)&len, m * 8, st), "allocation of the row move");
     cu(dev_alloc((void**)&tmp, scan_tmp_elems(m) * 8, st), "allocation of the row move");
     if (rc == EPET_OK) {
@@ -371,6 +389,51 @@ epet_status epet_mlem_create(const epet_problem* p, const int32_t* rows_d, const
   if (idx) dev_free(idx, st);
   if (rc != EPET_OK) return fail(rc);
   const int64_t nnz = h->A.nnz;
+  if (o.layout != EPET_LAYOUT_AUTO && o.layout != EPET_LAYOUT_GROUPED &&
+      o.layout != EPET_LAYOUT_CSC)
+    return fail(set_error(EPET_ERR_INVALID, "layout %d", o.layout));
+  const bool grouped_ok = grouped_supported(V, m) &&
+                          (reinterpret_cast<uintptr_t>(h->A.val) & 15) == 0;
+  if (o.layout == EPET_LAYOUT_GROUPED && !grouped_ok)
+    return fail(set_error(EPET_ERR_UNSUPPORTED, "grouped layout: %lld voxels (at most 819,200)",
+                          (long long)V));
+  if (o.layout != EPET_LAYOUT_CSC && grouped_ok) {
+    // the grouped layout replaces the column indices (and, for the 16-bit
+    // forms, the FP32 values): the CSR's row pointers stay
+    rc = grouped_build(h->A, o.value_format, &h->G, st);
+    if (rc != EPET_OK) return fail(rc);
+    EPET_CUDA(cudaStreamSynchronize(st));
+    h->grouped = true;
+    dev_free(h->A.col, st);
+    h->A.col = nullptr;
+    if (o.value_format != EPET_VALUES_FP32) {
+      dev_free(h->A.val, st);
+      h->A.val = nullptr;
+    }
+    h->plan_fwd = RowPlan{32, 1, num_sms(), false};  // reported: one warp per group
+    h->plan_bwd = h->G.plan_cols;
+    ALLOC(h->part_ll, 1024 * 8);
+    ALLOC(h->part_x, sum_blocks(V) * 8);
+    if (o.autotune) {
+      // the slot sums' launch shape: one pass fills the slots, then the
+      // candidates run the real (idempotent) epilogue
+      rc = grouped_pass(h->G, h->A, h->x, h->y, h->ybar, st);
+      if (rc == EPET_OK)
+        rc = tune_rows(
+            4, V, h->G.nslots, h->G.ngroups, V ? (double)h->G.nslots / V : 0.0,
+            [&](const RowPlan& pl) {
+              return launch_rows(pl, h->G.cg_ptr, h->G.cg_slot, h->G.ones, h->G.partial, h->V,
+                                 EpiMlemUpdate{h->x, h->s, h->xnew, nullptr}, nullptr, st);
+            },
+            st, &h->G.plan_cols);
+      if (rc != EPET_OK) return fail(rc);
+      h->plan_bwd = h->G.plan_cols;
+    }
+    cudaError_t e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) return fail(cuda_status(e, "mlem create"));
+    *out = h;
+    return EPET_OK;
+  }
   ALLOC(h->At.col_ptr, (V + 1) * 8);
   ALLOC(h->At.row, nnz * 4);
   ALLOC(h->At.val, nnz * 4);
@@ -532,7 +595,17 @@ epet_status epet_mlem_set_image(epet_mlem* h, const float* x_d, epet_stream_t st
 epet_status epet_mlem_stats(const epet_mlem* h, int64_t* nnz_h, int64_t* bytes_h) {
   if (!h) return set_error(EPET_ERR_INVALID, "bad arguments");
   if (nnz_h) *nnz_h = h->A.nnz;
-  if (bytes_h && h->opt.matrix_free) {
+  if (bytes_h && h->grouped) {
+    // pass: values (4 or 2 bytes) and ranks (2) per entry, row pointers,
+    // y, ybar, row scales (16-bit), per slot the table, the x gather and
+    // the correction written; slot sums: column pointers, per slot the slot
+    // index, a one and the correction, x and s read, xnew written; image
+    // sum and normalisation: xnew read twice, x written
+    const int64_t nnz = h->A.nnz, m = h->m, V = h->V, ns = h->G.nslots;
+    const int64_t bv = h->G.fmt == EPET_VALUES_FP32 ? 4 : 2;
+    *bytes_h = (bv + 2) * nnz + 8 * (m + 1) + 8 * m + (bv == 2 ? 4 * m : 0) + 12 * ns +
+               8 * (V + 1) + 12 * ns + 8 * V + 4 * V + 8 * V + 4 * V;
+  } else if (bytes_h && h->opt.matrix_free) {
     // no matrix: the pass writes and reads the rays (24 bytes each) and the
     // channel geometry (224 bytes per row), reads y and writes ybar, reads x
     // and the fp64 c (zeroed, accumulated), writes xnew, then sums and scales

@@ -5,6 +5,37 @@
 #include "common.cuh"
 #include "spmv.cuh"
 
+namespace epet {
+// Grouped layout of a reconstruction's matrix (grouped.cu): consecutive rows
+// in groups whose distinct columns fit a per-warp shared table.
+constexpr int kGroupCap = 1536;  // distinct columns of a group held in shared memory
+constexpr int kGroupWarps = 16;  // warps (groups in flight) per block of the iteration
+struct GroupDesc {
+  int32_t r0, r1;  // rows [r0, r1)
+  int32_t tb, nd;  // table slots [tb, tb + nd)
+};
+struct GroupedMatrix {
+  int fmt = 0;  // EPET_VALUES_*
+  int64_t ngroups = 0, nslots = 0;
+  GroupDesc* groups = nullptr;
+  int32_t* table = nullptr;   // each group's distinct columns, ascending
+  uint16_t* loc = nullptr;    // per entry: rank of its column in its group's table
+  int64_t* cg_ptr = nullptr;  // per column: its slots (group order) at cg_slot[cg_ptr[v] ..]
+  int32_t* cg_slot = nullptr;
+  float* ones = nullptr;      // nslots ones (the slot sums run on the row kernel)
+  float* partial = nullptr;   // per slot: the group's share of c = A^T e
+  uint16_t* val16 = nullptr;  // 16-bit forms: values / row scale
+  float* scale = nullptr;
+  RowPlan plan_cols;
+};
+bool grouped_supported(int64_t V, int64_t m);
+epet_status grouped_build(const epet_csr& A, int value_format, GroupedMatrix* G, cudaStream_t st);
+// ybar = A x, e = y / ybar and the groups' shares of A^T e into G.partial.
+epet_status grouped_pass(const GroupedMatrix& G, const epet_csr& A, const float* x,
+                         const float* y, float* ybar, cudaStream_t st);
+void grouped_free(GroupedMatrix* G, cudaStream_t st);
+}  // namespace epet
+
 struct epet_mlem {
   epet_problem p;
   epet_mlem_options opt;
@@ -19,6 +50,8 @@ struct epet_mlem {
   int64_t capA = 0;
   double *part_ll = nullptr, *part_x = nullptr, *sums = nullptr;
   double* c64 = nullptr;  // correction image of the matrix-free schedule
+  bool grouped = false;   // the matrix in the grouped layout (no column-major copy)
+  epet::GroupedMatrix G;
   epet::RowPlan plan_fwd, plan_bwd;
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t exec = nullptr;

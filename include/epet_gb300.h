@@ -389,7 +389,19 @@ typedef struct {
                           (epet_project_mlem), as the reference rebuilds its matrix in
                           every iteration.  FP32 values; use_graph and autotune are
                           ignored (the pass reads per-chunk counters back). */
+  int32_t layout;      /* EPET_LAYOUT_*: how a stored matrix is held */
 } epet_mlem_options;
+
+/* Layouts of a reconstruction's stored matrix.  GROUPED: rows cut into
+ * groups of consecutive rows (crystal-pair order) whose distinct columns fit
+ * a per-warp table in shared memory; each entry keeps its value and a 2-byte
+ * rank of its column in the group's table (6 bytes per entry in FP32, 4 in
+ * BF16/FP16); one pass over the entries per iteration gives A x, the ratio
+ * and A^T e, the latter summed per column in a fixed order; supported up to
+ * 819,200 voxels.  CSC: the CSR and its column-major copy (16 bytes per entry
+ * in FP32), the transpose product over the copy.  AUTO: GROUPED where
+ * supported, else CSC.  Both are deterministic. */
+enum { EPET_LAYOUT_AUTO = 0, EPET_LAYOUT_GROUPED = 1, EPET_LAYOUT_CSC = 2 };
 
 /* Builds the system matrix for the measured rows (rows_d channel ids, in
  * any order, with y_d > 0), keeps y, s (normalised here) and x = ones/V.

@@ -201,12 +201,13 @@ def small_recon(gpu_lib):
     return p, rows, y, s
 
 
-def test_mlem_matches_oracle(small_recon, oracle):
+@pytest.mark.parametrize("layout", [api.LAYOUT_GROUPED, api.LAYOUT_CSC], ids=["grouped", "csc"])
+def test_mlem_matches_oracle(small_recon, oracle, layout):
     """5 iterations: image within 1e-4 relative L2 of the oracle's fp32
-    sequence (reco.cu:209-281) on the same matrix, and the fp64 oracle error
-    is reported."""
+    sequence (reco.cu:209-281) on the same matrix, and within 1e-4 of the
+    fp64 oracle, in both layouts of the stored matrix."""
     p, rows, y, s = small_recon
-    R = api.Mlem(p, dev(rows), y, s, use_graph=True)
+    R = api.Mlem(p, dev(rows), y, s, use_graph=True, layout=layout)
     R.iterate(5)
     x = R.image().cpu().numpy()
     A = api.systemMatrixCalculation(p, dev(rows))
@@ -293,3 +294,46 @@ def test_csrmv_ragged_rows_any_alignment(gpu_lib, oracle, offset):
     assert (got[lens == 0] == 0).all()
     nz = lens > 0
     assert np.abs(got[nz] - yo[nz]).max() <= 1e-5 * np.abs(yo[nz]).max()
+
+
+@pytest.mark.parametrize("fmt", [0, api.BF16])
+def test_grouped_layout_equals_csc_layout(small_recon, fmt):
+    """The one-pass grouped iteration and the CSR + column-major copy give
+    the same images up to fp32 summation order (both deterministic: the same
+    object iterated twice is bit-equal)."""
+    p, rows, y, s = small_recon
+    a = api.Mlem(p, dev(rows), y, s, layout=api.LAYOUT_GROUPED, value_format=fmt)
+    b = api.Mlem(p, dev(rows), y, s, layout=api.LAYOUT_CSC, value_format=fmt)
+    c = api.Mlem(p, dev(rows), y, s, layout=api.LAYOUT_GROUPED, value_format=fmt)
+    la, lb, lc = (r.iterate(6, loglik=True) for r in (a, b, c))
+    xa, xb = a.image().double(), b.image().double()
+    tol = 1e-6 if fmt == 0 else 2e-4  # the 16-bit layouts round their values differently
+    assert float((xa - xb).norm() / xb.norm()) <= tol
+    assert torch.equal(a.image(), c.image()) and la == lc
+    assert abs(la - lb) <= 1e-6 * abs(lb)
+
+
+def test_grouped_layout_wide_rows(gpu_lib, oracle):
+    """Rows wider than a group's shared table (1 mm voxels along 256 mm of
+    the lines: thousands of entries a row) keep their own columns as their
+    table; against the column-major layout and the FP64 oracle."""
+    s = two_head_setup(2, 90.0, pos=0.25, n=3)
+    g = VoxelGrid((-0.128, -0.004, -0.004), (0.001, 0.001, 0.001), (256, 8, 8))
+    p = Problem(s, g, 4)
+    rows = torch.arange(p.nchannels, dtype=torch.int32, device="cuda")
+    A = api.systemMatrixCalculation(p, rows)
+    lens = torch.diff(A.row_ptr)
+    assert int(lens.max()) > 1536  # wider than the shared table
+    y = torch.full((p.nchannels,), 50.0, device="cuda")
+    sens = api.sensitivity(p)
+    a = api.Mlem(p, rows, y, sens, layout=api.LAYOUT_GROUPED)
+    b = api.Mlem(p, rows, y, sens, layout=api.LAYOUT_CSC)
+    a.iterate(4)
+    b.iterate(4)
+    xa, xb = a.image().double(), b.image().double()
+    assert float((xa - xb).norm() / xb.norm()) <= 1e-6
+    rp, col, val = (t.cpu().numpy() for t in (A.row_ptr, A.col, A.val))
+    s64 = oracle.csrmv_f64(1, rp, col, val, np.ones(p.nchannels), p.nvoxels)
+    x64 = oracle.mlem_f64(rp, col, val, np.full(p.nchannels, 50.0), s64 / s64.sum(),
+                          np.full(p.nvoxels, 1.0 / p.nvoxels), 4, p.nvoxels)
+    assert np.linalg.norm(xa.cpu().numpy() - x64) / np.linalg.norm(x64) <= 1e-4
