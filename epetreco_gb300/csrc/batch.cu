@@ -121,6 +121,12 @@ struct epet_mlem_batch {
   double* sums = nullptr;          // nprob
   RowPlan plan_fwd, plan_bwd;
   int64_t nnz = 0, rows = 0, voxels = 0;
+  // grouped layout: one pass over all problems' row groups replaces the
+  // forward launch; the transpose launch sums each problem's slots
+  bool grouped = false;
+  void* gdesc = nullptr;      // device, nprob descriptors of the pass
+  int64_t* gstart = nullptr;  // device, prefix of the problems' group counts
+  int64_t total_groups = 0;
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t exec = nullptr;
 
@@ -139,7 +145,8 @@ void batch_free(epet_mlem_batch* h) {
   if (h->exec) cudaGraphExecDestroy(h->exec);
   if (h->graph) cudaGraphDestroy(h->graph);
   for (epet_mlem* p : h->probs) epet_mlem_destroy(p);
-  for (void* b : {(void*)h->desc, (void*)h->tiles, (void*)h->partial, (void*)h->sums})
+  for (void* b : {(void*)h->desc, (void*)h->tiles, (void*)h->partial, (void*)h->sums,
+                  h->gdesc, (void*)h->gstart})
     if (b) dev_free(b, 0);
   delete h;
 }
@@ -164,7 +171,10 @@ epet_status launch_batch_rows(const epet_mlem_batch* h, const RowPlan& plan, boo
 }
 
 epet_status batch_iteration(const epet_mlem_batch* h, cudaStream_t st) {
-  EPET_CHECK(launch_batch_rows(h, h->plan_fwd, true, st));
+  if (h->grouped)
+    EPET_CHECK(grouped_pass_batch(h->gdesc, h->gstart, h->np(), h->total_groups, st));
+  else
+    EPET_CHECK(launch_batch_rows(h, h->plan_fwd, true, st));
   EPET_CHECK(launch_batch_rows(h, h->plan_bwd, false, st));
   k_batch_sums<<<h->np(), kSpmvThreads, 0, st>>>(h->partial, h->bwd_tiles(h->plan_bwd.G),
                                                  h->sums);
@@ -205,7 +215,16 @@ epet_status epet_mlem_batch_create(int32_t nprob, const epet_problem* problems,
   };
   epet_mlem_options po = o;  // members iterated alone: graph as asked, heuristic shapes
   po.autotune = 0;
-  po.layout = EPET_LAYOUT_CSC;  // the batched launches read each member's CSR and CSC
+  // every member in the grouped layout where all support it (6 bytes per
+  // entry), else every member with its CSR and column-major copy
+  bool all_grouped = o.layout != EPET_LAYOUT_CSC;
+  for (int i = 0; i < nprob && all_grouped; i++) {
+    const epet_grid& g = problems[i].grid;
+    all_grouped = grouped_supported((int64_t)g.n[0] * g.n[1] * g.n[2], m[i]);
+  }
+  if (o.layout == EPET_LAYOUT_GROUPED && !all_grouped)
+    return set_error(EPET_ERR_UNSUPPORTED, "batch: a problem too large for the grouped layout");
+  po.layout = all_grouped ? EPET_LAYOUT_GROUPED : EPET_LAYOUT_CSC;
   for (int i = 0; i < nprob; i++) {
     epet_mlem* p = nullptr;
     epet_status rc = epet_mlem_create(&problems[i], rows_d[i], y_d[i], m[i], s_d[i], &po, &p,
@@ -219,12 +238,26 @@ epet_status epet_mlem_batch_create(int32_t nprob, const epet_problem* problems,
   const int np = nprob;
   std::vector<BatchDesc> dh(np);
   h->tiles_h.assign(9 * (np + 1), 0);
+  h->grouped = all_grouped;
+  std::vector<unsigned char> gd_h(all_grouped ? np * grouped_batch_desc_bytes() : 0);
+  std::vector<int64_t> gs_h(np + 1, 0);
   for (int i = 0; i < np; i++) {
     const epet_mlem* p = h->probs[i];
-    dh[i] = BatchDesc{p->A.row_ptr, p->A.col, p->A.val, p->At.col_ptr, p->At.row, p->At.val,
-                      p->y, p->e, p->ybar, p->s, p->x, p->xnew, p->m, p->V};
-    if (!aligned16(p->A.col, p->A.val) || !aligned16(p->At.row, p->At.val))
-      return fail(set_error(EPET_ERR_UNSUPPORTED, "batch: matrix streams not 16-byte aligned"));
+    if (all_grouped) {
+      // the transpose launch sums the problem's slots: the slot lists as
+      // "columns", the ones as values, the slots' corrections gathered
+      dh[i] = BatchDesc{p->A.row_ptr, nullptr, nullptr, p->G.cg_ptr, p->G.cg_slot, p->G.ones,
+                        p->y, p->G.partial, p->ybar, p->s, p->x, p->xnew, p->m, p->V};
+      grouped_batch_desc(p->G, p->A, p->x, p->y, p->ybar, gd_h.data() + i * grouped_batch_desc_bytes());
+      gs_h[i + 1] = gs_h[i] + p->G.ngroups;
+      if (!aligned16(p->G.cg_slot, p->G.ones))
+        return fail(set_error(EPET_ERR_UNSUPPORTED, "batch: slot streams not 16-byte aligned"));
+    } else {
+      dh[i] = BatchDesc{p->A.row_ptr, p->A.col, p->A.val, p->At.col_ptr, p->At.row, p->At.val,
+                        p->y, p->e, p->ybar, p->s, p->x, p->xnew, p->m, p->V};
+      if (!aligned16(p->A.col, p->A.val) || !aligned16(p->At.row, p->At.val))
+        return fail(set_error(EPET_ERR_UNSUPPORTED, "batch: matrix streams not 16-byte aligned"));
+    }
     for (int k = 0; k < 4; k++) {
       const int64_t rpt = int64_t(8) << k;
       int64_t* f = &h->tiles_h[k * (np + 1)];
@@ -244,30 +277,53 @@ epet_status epet_mlem_batch_create(int32_t nprob, const epet_problem* problems,
   ALLOC(h->tiles, h->tiles_h.size() * 8);
   ALLOC(h->partial, std::max<int64_t>(h->host_total(4), 1) * 8);  // 8 rows per tile: most
   ALLOC(h->sums, np * 8);
+  if (all_grouped) {
+    ALLOC(h->gdesc, gd_h.size());
+    ALLOC(h->gstart, (np + 1) * 8);
+    h->total_groups = gs_h[np];
+  }
 #undef ALLOC
   cudaError_t e = cudaMemcpyAsync(h->desc, dh.data(), np * sizeof(BatchDesc),
                                   cudaMemcpyHostToDevice, st);
   if (e == cudaSuccess)
     e = cudaMemcpyAsync(h->tiles, h->tiles_h.data(), h->tiles_h.size() * 8,
                         cudaMemcpyHostToDevice, st);
+  if (e == cudaSuccess && all_grouped)
+    e = cudaMemcpyAsync(h->gdesc, gd_h.data(), gd_h.size(), cudaMemcpyHostToDevice, st);
+  if (e == cudaSuccess && all_grouped)
+    e = cudaMemcpyAsync(h->gstart, gs_h.data(), (np + 1) * 8, cudaMemcpyHostToDevice, st);
   if (e == cudaSuccess) e = cudaStreamSynchronize(st);
   if (e != cudaSuccess) return fail(cuda_status(e, "batch descriptors"));
 
   const double avg_row = h->rows ? (double)h->nnz / h->rows : 0.0;
-  const double avg_col = h->voxels ? (double)h->nnz / h->voxels : 0.0;
+  int64_t nslots = 0;
+  for (const epet_mlem* p : h->probs) nslots += p->G.nslots;
+  const double avg_col = h->voxels ? (double)(all_grouped ? nslots : h->nnz) / h->voxels : 0.0;
   h->plan_fwd = default_plan(avg_row);
   h->plan_bwd = default_plan(avg_col);
   if (o.autotune) {
-    // kinds 2 / 3 keep batch plans apart from single-matrix plans
-    epet_status rc = tune_rows(
-        2, h->rows, h->nnz, np, avg_row,
-        [&](const RowPlan& pl) { return launch_batch_rows(h, pl, true, st); }, st,
-        &h->plan_fwd);
-    if (rc == EPET_OK)
+    // kinds 5 / 6 / 7 keep batch plans apart from single-matrix plans
+    epet_status rc = EPET_OK;
+    if (all_grouped) {
+      // one pass fills the slots; the slot sums' candidates rerun the
+      // (idempotent) update epilogue
+      rc = grouped_pass_batch(h->gdesc, h->gstart, np, h->total_groups, st);
+      if (rc == EPET_OK)
+        rc = tune_rows(
+            7, h->voxels, nslots, np, avg_col,
+            [&](const RowPlan& pl) { return launch_batch_rows(h, pl, false, st); }, st,
+            &h->plan_bwd);
+    } else {
       rc = tune_rows(
-          3, h->voxels, h->nnz, np, avg_col,
-          [&](const RowPlan& pl) { return launch_batch_rows(h, pl, false, st); }, st,
-          &h->plan_bwd);
+          5, h->rows, h->nnz, np, avg_row,
+          [&](const RowPlan& pl) { return launch_batch_rows(h, pl, true, st); }, st,
+          &h->plan_fwd);
+      if (rc == EPET_OK)
+        rc = tune_rows(
+            6, h->voxels, h->nnz, np, avg_col,
+            [&](const RowPlan& pl) { return launch_batch_rows(h, pl, false, st); }, st,
+            &h->plan_bwd);
+    }
     if (rc != EPET_OK) return fail(rc);
   }
   *out = h;
@@ -298,9 +354,10 @@ epet_status epet_mlem_batch_iterate(epet_mlem_batch* h, int32_t nit, double* log
       if (e2 != cudaSuccess) return cuda_status(e2, "end capture");
       EPET_CUDA(cudaGraphInstantiate(&h->exec, h->graph, 0));
     }
-    const int per_iter = 3 + (h->host_total(8) > 0 ? 1 : 0) -
-                         (h->host_total(0 + rpt_index(h->plan_fwd.G)) > 0 ? 0 : 1) -
-                         (h->host_total(4 + rpt_index(h->plan_bwd.G)) > 0 ? 0 : 1);
+    const bool fwd = h->grouped ? h->total_groups > 0
+                                : h->host_total(0 + rpt_index(h->plan_fwd.G)) > 0;
+    const int per_iter = 1 + (fwd ? 1 : 0) + (h->host_total(8) > 0 ? 1 : 0) +
+                         (h->host_total(4 + rpt_index(h->plan_bwd.G)) > 0 ? 1 : 0);
     for (int it = 0; it < nit; it++) {
       EPET_CUDA(cudaGraphLaunch(h->exec, st));
       note_launch(per_iter);

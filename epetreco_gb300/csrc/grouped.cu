@@ -23,6 +23,7 @@
 #include <cuda_fp16.h>
 
 #include <algorithm>
+#include <type_traits>
 #include <vector>
 
 #include "common.cuh"
@@ -160,22 +161,41 @@ __global__ void k_group_quantise(const int64_t* __restrict__ row_ptr, const floa
   for (int64_t k = b + lane; k < e; k += 32) q[k] = gq_to<FMT>(__fdiv_rn(val[k], sc));
 }
 
-// Four consecutive values (index k4, a multiple of 4) of the matrix stream.
+// A row's entries as the pass holds them: 4-entry chunks, chunk u of lane l
+// the (l + 32 u)-th chunk of the row's aligned span (the 4-entry boundaries
+// below its first entry); values raw (FP32: float4, 16-bit: 4 x 16 bits)
+// and column ranks as 4 x 16 bits.
+constexpr int kGroupRounds = 4;  // chunks per lane held in registers (512 entries a row)
 template <int FMT>
-__device__ __forceinline__ void gload4(const void* __restrict__ v, int64_t k4, float out[4]) {
-  if constexpr (FMT == 0) {
-    const float4 t = __ldcs(reinterpret_cast<const float4*>(static_cast<const float*>(v) + k4));
-    out[0] = t.x; out[1] = t.y; out[2] = t.z; out[3] = t.w;
-  } else {
-    const uint2 t = __ldcs(reinterpret_cast<const uint2*>(static_cast<const uint16_t*>(v) + k4));
-    out[0] = gq_from<FMT>(t.x & 0xffffu); out[1] = gq_from<FMT>(t.x >> 16);
-    out[2] = gq_from<FMT>(t.y & 0xffffu); out[3] = gq_from<FMT>(t.y >> 16);
-  }
+struct RowBuf {
+  using V = typename std::conditional<FMT == 0, float4, uint2>::type;
+  V v[kGroupRounds];
+  uint2 l[kGroupRounds];
+};
+
+template <int FMT>
+__device__ __forceinline__ float gval(const float4& c, int t) {
+  return t == 0 ? c.x : t == 1 ? c.y : t == 2 ? c.z : c.w;
 }
-__device__ __forceinline__ void gloadloc4(const uint16_t* __restrict__ l, int64_t k4, int out[4]) {
-  const uint2 t = __ldcs(reinterpret_cast<const uint2*>(l + k4));
-  out[0] = (int)(t.x & 0xffffu); out[1] = (int)(t.x >> 16);
-  out[2] = (int)(t.y & 0xffffu); out[3] = (int)(t.y >> 16);
+template <int FMT>
+__device__ __forceinline__ float gval(const uint2& c, int t) {
+  const uint32_t w = t < 2 ? c.x : c.y;
+  return gq_from<FMT>((t & 1) ? (w >> 16) : (w & 0xffffu));
+}
+__device__ __forceinline__ int grank(const uint2& c, int t) {
+  const uint32_t w = t < 2 ? c.x : c.y;
+  return (int)((t & 1) ? (w >> 16) : (w & 0xffffu));
+}
+
+template <int FMT>
+__device__ __forceinline__ void gload_chunk(const void* __restrict__ val,
+                                            const uint16_t* __restrict__ loc, int64_t k4,
+                                            bool ranks, typename RowBuf<FMT>::V* v, uint2* l) {
+  if constexpr (FMT == 0)
+    *v = __ldcs(reinterpret_cast<const float4*>(static_cast<const float*>(val) + k4));
+  else
+    *v = __ldcs(reinterpret_cast<const uint2*>(static_cast<const uint16_t*>(val) + k4));
+  if (ranks) *l = __ldcs(reinterpret_cast<const uint2*>(loc + k4));
 }
 
 struct GroupIterArgs {
@@ -192,11 +212,163 @@ struct GroupIterArgs {
   float* partial;
 };
 
-constexpr int kGroupRounds = 4;  // 4-entry chunks per lane kept in registers (512 entries a row)
+// One group of the MLEM pass (a warp): per row ybar = A x, e = y / ybar (0
+// where ybar == 0, the fused epilogue's guard) and the rows' shares of
+// A^T e summed, row after row, into the group's shared correction, written
+// to partial[slot] at the end.  Software pipeline: the group's row pointers,
+// counts and scales are loaded once (one row per lane; a group has at most
+// 32 rows), and the next row's entries are in flight while a row is reduced
+// and scattered.
+template <int FMT>
+__device__ __forceinline__ void group_pass(const GroupIterArgs& a, int64_t g, float* xs,
+                                           float* cs, int lane) {
+  const GroupDesc gd = a.groups[g];
+  const int nr = gd.r1 - gd.r0;  // <= 32
+  const bool wide = gd.nd > kGroupCap;  // one row, its own columns as table
+  const int64_t rp_l = lane <= nr && lane < 32 ? a.row_ptr[gd.r0 + lane] : 0;
+  const int64_t rp_end = a.row_ptr[gd.r1];
+  const float y_l = lane < nr ? a.y[gd.r0 + lane] : 0.f;
+  const float sc_l = FMT != 0 && lane < nr ? a.scale[gd.r0 + lane] : 1.f;
+  float yb_l = 0.f;
+  auto row_begin = [&](int i) -> int64_t { return __shfl_sync(0xffffffffu, rp_l, i); };
+  auto row_end = [&](int i) -> int64_t {
+    const int64_t t = __shfl_sync(0xffffffffu, rp_l, (i + 1) & 31);
+    return i + 1 < 32 ? t : rp_end;
+  };
+  if (!wide) {
+    for (int j = lane; j < gd.nd; j += 32) {
+      xs[j] = __ldg(a.x + a.table[gd.tb + j]);
+      cs[j] = 0.f;
+    }
+    __syncwarp();
+  }
+  auto load_row = [&](int i, RowBuf<FMT>& B) {
+    const int64_t b = row_begin(i), e = row_end(i);
+    const int64_t a0 = b & ~int64_t(3);
+    const int nq = (int)((e - a0 + 3) >> 2);
+#pragma unroll
+    for (int u = 0; u < kGroupRounds; u++) {
+      const int q = lane + 32 * u;
+      if (q < nq) gload_chunk<FMT>(a.val, a.loc, a0 + 4 * q, !wide, &B.v[u], &B.l[u]);
+    }
+  };
+  auto process_row = [&](int i, const RowBuf<FMT>& B) {
+    const int64_t b = row_begin(i), e = row_end(i);
+    const int64_t a0 = b & ~int64_t(3);
+    const int nq = (int)((e - a0 + 3) >> 2);
+    const int lo = (int)(b - a0), hi = (int)(e - a0);  // valid entries: lo <= 4q + t < hi
+    float acc = 0.f;
+    auto dot = [&](const typename RowBuf<FMT>::V& vv, const uint2& ll, int q) {
+#pragma unroll
+      for (int t = 0; t < 4; t++) {
+        const int k = 4 * q + t;
+        if (k >= lo && k < hi) {
+          const float xv = wide ? __ldg(a.x + a.table[gd.tb + (k - lo)]) : xs[grank(ll, t)];
+          acc = fmaf(gval<FMT>(vv, t), xv, acc);
+        }
+      }
+    };
+#pragma unroll
+    for (int u = 0; u < kGroupRounds; u++) {
+      const int q = lane + 32 * u;
+      if (q < nq) dot(B.v[u], B.l[u], q);
+    }
+    for (int q = lane + 32 * kGroupRounds; q < nq; q += 32) {  // rows over 512 entries
+      typename RowBuf<FMT>::V vv;
+      uint2 ll;
+      gload_chunk<FMT>(a.val, a.loc, a0 + 4 * q, !wide, &vv, &ll);
+      dot(vv, ll, q);
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+    const float sc = __shfl_sync(0xffffffffu, sc_l, i);
+    const float yb = FMT == 0 ? acc : fmul(acc, sc);
+    if (lane == i) yb_l = yb;
+    // e = y / (A x) (mlemOperations.hpp:22-32; 0 where A x == 0)
+    const float yr = __shfl_sync(0xffffffffu, y_l, i);
+    const float er = yb > 0.f ? __fdiv_rn(yr, yb) : 0.f;
+    const float f = FMT == 0 ? er : fmul(er, sc);
+    auto scatter = [&](const typename RowBuf<FMT>::V& vv, const uint2& ll, int q) {
+#pragma unroll
+      for (int t = 0; t < 4; t++) {
+        const int k = 4 * q + t;
+        if (k >= lo && k < hi) {
+          const float p = fmul(gval<FMT>(vv, t), f);
+          if (wide) a.partial[gd.tb + (k - lo)] = p;
+          else cs[grank(ll, t)] = fadd(cs[grank(ll, t)], p);
+        }
+      }
+    };
+#pragma unroll
+    for (int u = 0; u < kGroupRounds; u++) {
+      const int q = lane + 32 * u;
+      if (q < nq) scatter(B.v[u], B.l[u], q);
+    }
+    for (int q = lane + 32 * kGroupRounds; q < nq; q += 32) {
+      typename RowBuf<FMT>::V vv;
+      uint2 ll;
+      gload_chunk<FMT>(a.val, a.loc, a0 + 4 * q, !wide, &vv, &ll);
+      scatter(vv, ll, q);
+    }
+    __syncwarp();
+  };
+  RowBuf<FMT> b0, b1;
+  if (nr > 0) load_row(0, b0);
+  for (int i = 0; i < nr; i += 2) {
+    if (i + 1 < nr) load_row(i + 1, b1);
+    process_row(i, b0);
+    if (i + 1 < nr) {
+      if (i + 2 < nr) load_row(i + 2, b0);
+      process_row(i + 1, b1);
+    }
+  }
+  if (lane < nr) a.ybar[gd.r0 + lane] = yb_l;
+  if (!wide) {
+    for (int j = lane; j < gd.nd; j += 32) a.partial[gd.tb + j] = cs[j];
+    __syncwarp();
+  }
+}
 
-// One pass of the MLEM iteration over the grouped matrix: per row ybar =
-// A x, e = y / ybar (0 where ybar == 0, the fused epilogue's guard), and the
-// group's corrections sum_rows A[r, .] * e_r into partial[slot].
+// Column sums of the grouped matrix's values (the 16-bit forms dequantised)
+// over its rows, by the same group / slot structure as the pass: a warp per
+// group adds its rows' values, row after row, into the group's shared sums
+// (the slots); the slot sums per column then run on the row kernel.
+template <int FMT>
+__global__ void __launch_bounds__(kGroupWarps * 32, 1)
+k_group_colsum(GroupIterArgs a) {
+  extern __shared__ __align__(16) float gsm[];
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  float* cs = gsm + (size_t)w * 2 * kGroupCap;
+  for (int64_t g = (int64_t)blockIdx.x * kGroupWarps + w; g < a.ngroups;
+       g += (int64_t)gridDim.x * kGroupWarps) {
+    const GroupDesc gd = a.groups[g];
+    const bool wide = gd.nd > kGroupCap;
+    if (!wide) {
+      for (int j = lane; j < gd.nd; j += 32) cs[j] = 0.f;
+      __syncwarp();
+    }
+    for (int r = gd.r0; r < gd.r1; r++) {
+      const int64_t b = a.row_ptr[r], e = a.row_ptr[r + 1];
+      const float sc = FMT == 0 ? 1.f : a.scale[r];
+      for (int64_t k = b + lane; k < e; k += 32) {
+        float v;
+        if constexpr (FMT == 0) v = static_cast<const float*>(a.val)[k];
+        else v = fmul(gq_from<FMT>(static_cast<const uint16_t*>(a.val)[k]), sc);
+        if (wide) a.partial[gd.tb + (k - b)] = v;
+        else cs[a.loc[k]] = fadd(cs[a.loc[k]], v);
+      }
+      __syncwarp();
+    }
+    if (!wide) {
+      for (int j = lane; j < gd.nd; j += 32) a.partial[gd.tb + j] = cs[j];
+      __syncwarp();
+    }
+  }
+}
+
+// A warp per group, a persistent grid striding over the groups; each warp
+// holds its group's tables (x and the correction at the distinct columns)
+// in its share of the block's shared memory.
 template <int FMT>
 __global__ void __launch_bounds__(kGroupWarps * 32, 1)
 k_group_mlem(GroupIterArgs a) {
@@ -205,89 +377,29 @@ k_group_mlem(GroupIterArgs a) {
   float* xs = gsm + (size_t)w * 2 * kGroupCap;
   float* cs = xs + kGroupCap;
   for (int64_t g = (int64_t)blockIdx.x * kGroupWarps + w; g < a.ngroups;
+       g += (int64_t)gridDim.x * kGroupWarps)
+    group_pass<FMT>(a, g, xs, cs, lane);
+}
+
+// The same over the groups of many reconstructions (batched form): global
+// group g belongs to problem p with gstart[p] <= g < gstart[p + 1].
+__global__ void __launch_bounds__(kGroupWarps * 32, 1)
+k_group_mlem_batch(const GroupIterArgs* __restrict__ desc, const int64_t* __restrict__ gstart,
+                   int np) {
+  extern __shared__ __align__(16) float gsm[];
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  float* xs = gsm + (size_t)w * 2 * kGroupCap;
+  float* cs = xs + kGroupCap;
+  const int64_t total = gstart[np];
+  for (int64_t g = (int64_t)blockIdx.x * kGroupWarps + w; g < total;
        g += (int64_t)gridDim.x * kGroupWarps) {
-    const GroupDesc gd = a.groups[g];
-    const bool wide = gd.nd > kGroupCap;  // one row, its own columns as table
-    if (!wide) {
-      for (int j = lane; j < gd.nd; j += 32) {
-        xs[j] = __ldg(a.x + a.table[gd.tb + j]);
-        cs[j] = 0.f;
-      }
-      __syncwarp();
+    int lo = 0, hi = np;  // gstart[lo] <= g < gstart[hi]
+    while (hi - lo > 1) {
+      const int mid = (lo + hi) >> 1;
+      if (__ldg(gstart + mid) <= g) lo = mid;
+      else hi = mid;
     }
-    for (int r = gd.r0; r < gd.r1; r++) {
-      const int64_t b = a.row_ptr[r], e = a.row_ptr[r + 1];
-      const int64_t a0 = b & ~int64_t(3);
-      const int64_t nq = (e - a0 + 3) >> 2;  // 4-entry chunks over [a0, e)
-      float v[kGroupRounds][4];
-      int l[kGroupRounds][4];
-#pragma unroll
-      for (int u = 0; u < kGroupRounds; u++) {
-        const int64_t q = lane + 32 * u;
-        if (q < nq) {
-          gload4<FMT>(a.val, a0 + 4 * q, v[u]);
-          if (!wide) gloadloc4(a.loc, a0 + 4 * q, l[u]);
-        }
-      }
-      float acc = 0.f;
-      auto dot4 = [&](const float* vv, const int* ll, int64_t k0) {
-#pragma unroll
-        for (int t = 0; t < 4; t++) {
-          const int64_t k = k0 + t;
-          if (k >= b && k < e) {
-            const float xv = wide ? __ldg(a.x + a.table[gd.tb + (k - b)]) : xs[ll[t]];
-            acc = fmaf(vv[t], xv, acc);
-          }
-        }
-      };
-#pragma unroll
-      for (int u = 0; u < kGroupRounds; u++) {
-        const int64_t q = lane + 32 * u;
-        if (q < nq) dot4(v[u], l[u], a0 + 4 * q);
-      }
-      for (int64_t q = lane + 32 * kGroupRounds; q < nq; q += 32) {  // rows over 512 entries
-        float vv[4];
-        int ll[4];
-        gload4<FMT>(a.val, a0 + 4 * q, vv);
-        if (!wide) gloadloc4(a.loc, a0 + 4 * q, ll);
-        dot4(vv, ll, a0 + 4 * q);
-      }
-#pragma unroll
-      for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
-      const float sc = FMT == 0 ? 1.f : a.scale[r];
-      const float yb = FMT == 0 ? acc : fmul(acc, sc);
-      if (lane == 0) a.ybar[r] = yb;
-      // e = y / (A x) (mlemOperations.hpp:22-32; 0 where A x == 0)
-      const float er = yb > 0.f ? __fdiv_rn(a.y[r], yb) : 0.f;
-      const float f = FMT == 0 ? er : fmul(er, sc);
-      auto scatter4 = [&](const float* vv, const int* ll, int64_t k0) {
-#pragma unroll
-        for (int t = 0; t < 4; t++) {
-          const int64_t k = k0 + t;
-          if (k >= b && k < e) {
-            if (wide) a.partial[gd.tb + (k - b)] = fmul(vv[t], f);
-            else cs[ll[t]] = fadd(cs[ll[t]], fmul(vv[t], f));
-          }
-        }
-      };
-#pragma unroll
-      for (int u = 0; u < kGroupRounds; u++) {
-        const int64_t q = lane + 32 * u;
-        if (q < nq) scatter4(v[u], l[u], a0 + 4 * q);
-      }
-      for (int64_t q = lane + 32 * kGroupRounds; q < nq; q += 32) {
-        float vv[4];
-        int ll[4];
-        gload4<FMT>(a.val, a0 + 4 * q, vv);
-        if (!wide) gloadloc4(a.loc, a0 + 4 * q, ll);
-        scatter4(vv, ll, a0 + 4 * q);
-      }
-      __syncwarp();
-    }
-    if (!wide) {
-      for (int j = lane; j < gd.nd; j += 32) a.partial[gd.tb + j] = cs[j];
-      __syncwarp();
-    }
+    group_pass<0>(desc[lo], g - gstart[lo], xs, cs, lane);
   }
 }
 
@@ -423,6 +535,15 @@ epet_status grouped_build(const epet_csr& A, int value_format, GroupedMatrix* G,
       e = cudaFuncSetAttribute(k_group_mlem<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
     if (e == cudaSuccess)
       e = cudaFuncSetAttribute(k_group_mlem<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    if (e == cudaSuccess)
+      e = cudaFuncSetAttribute(k_group_mlem_batch, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                               smem);
+    if (e == cudaSuccess)
+      e = cudaFuncSetAttribute(k_group_colsum<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    if (e == cudaSuccess)
+      e = cudaFuncSetAttribute(k_group_colsum<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    if (e == cudaSuccess)
+      e = cudaFuncSetAttribute(k_group_colsum<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
   }
   if (e != cudaSuccess) return fail(cuda_status(e, "group tables"));
   if (!hg.empty()) {
@@ -485,12 +606,60 @@ epet_status grouped_build(const epet_csr& A, int value_format, GroupedMatrix* G,
   return EPET_OK;
 }
 
+static GroupIterArgs iter_args(const GroupedMatrix& G, const epet_csr& A, const float* x,
+                               const float* y, float* ybar) {
+  return GroupIterArgs{G.groups, G.ngroups, A.row_ptr,
+                       G.fmt == EPET_VALUES_FP32 ? (const void*)A.val : (const void*)G.val16,
+                       G.scale, G.loc, G.table, x, y, ybar, G.partial};
+}
+
+size_t grouped_batch_desc_bytes() { return sizeof(GroupIterArgs); }
+
+void grouped_batch_desc(const GroupedMatrix& G, const epet_csr& A, const float* x,
+                        const float* y, float* ybar, void* out) {
+  *static_cast<GroupIterArgs*>(out) = iter_args(G, A, x, y, ybar);
+}
+
+epet_status grouped_pass_batch(const void* desc, const int64_t* gstart, int np,
+                               int64_t total_groups, cudaStream_t st) {
+  if (total_groups <= 0) return EPET_OK;
+  const size_t smem = (size_t)kGroupWarps * 2 * kGroupCap * 4;
+  const unsigned grid = (unsigned)std::min<int64_t>((total_groups + kGroupWarps - 1) / kGroupWarps,
+                                                    (int64_t)num_sms());
+  k_group_mlem_batch<<<grid, kGroupWarps * 32, smem, st>>>(
+      static_cast<const GroupIterArgs*>(desc), gstart, np);
+  EPET_LAUNCHED();
+  return EPET_OK;
+}
+
+epet_status grouped_column_sums(const GroupedMatrix& G, const epet_csr& A, bool quantised,
+                                float* out, cudaStream_t st) {
+  const int64_t V = A.n;
+  if (G.ngroups > 0) {
+    GroupIterArgs a = iter_args(G, A, nullptr, nullptr, nullptr);
+    int fmt = G.fmt;
+    if (!quantised) {
+      a.val = A.val;
+      fmt = EPET_VALUES_FP32;
+    }
+    const size_t smem = (size_t)kGroupWarps * 2 * kGroupCap * 4;
+    const unsigned grid = (unsigned)std::min<int64_t>(
+        (G.ngroups + kGroupWarps - 1) / kGroupWarps, (int64_t)num_sms());
+    switch (fmt) {
+      case EPET_VALUES_BF16: k_group_colsum<1><<<grid, kGroupWarps * 32, smem, st>>>(a); break;
+      case EPET_VALUES_FP16: k_group_colsum<2><<<grid, kGroupWarps * 32, smem, st>>>(a); break;
+      default: k_group_colsum<0><<<grid, kGroupWarps * 32, smem, st>>>(a);
+    }
+    EPET_LAUNCHED();
+  }
+  return launch_rows(G.plan_cols, G.cg_ptr, G.cg_slot, G.ones, G.partial, V, EpiKeep{out},
+                     nullptr, st);
+}
+
 epet_status grouped_pass(const GroupedMatrix& G, const epet_csr& A, const float* x, const float* y,
                          float* ybar, cudaStream_t st) {
   if (G.ngroups == 0) return EPET_OK;
-  GroupIterArgs a{G.groups, G.ngroups, A.row_ptr,
-                  G.fmt == EPET_VALUES_FP32 ? (const void*)A.val : (const void*)G.val16,
-                  G.scale, G.loc, G.table, x, y, ybar, G.partial};
+  GroupIterArgs a = iter_args(G, A, x, y, ybar);
   const size_t smem = (size_t)kGroupWarps * 2 * kGroupCap * 4;
   const unsigned grid = (unsigned)std::min<int64_t>(
       (G.ngroups + kGroupWarps - 1) / kGroupWarps, (int64_t)num_sms());

@@ -296,6 +296,13 @@ static epet_status build_in_pair_order(const epet_problem* p, const int32_t* row
   return EPET_OK;
 }
 
+// s *= num / den where den > 0 (the 16-bit forms' sensitivity).
+__global__ void k_scale_by_ratio(float* __restrict__ s, const float* __restrict__ num,
+                                 const float* __restrict__ den, int64_t n) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n && den[i] > 0.f) s[i] = __fmul_rn(s[i], __fdiv_rn(num[i], den[i]));
+}
+
 __global__ void k_fill(float* x, int64_t n, float v) {
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i < n) x[i] = v;
@@ -402,6 +409,27 @@ epet_status epet_mlem_create(const epet_problem* p, const int32_t* rows_d, const
     // forms, the FP32 values): the CSR's row pointers stay
     rc = grouped_build(h->A, o.value_format, &h->G, st);
     if (rc != EPET_OK) return fail(rc);
+    if (o.value_format != EPET_VALUES_FP32 && V > 0) {
+      // The iterations run with the 16-bit values, whose column sums differ
+      // from the FP32 ones by the rounding of the values; an MLEM update
+      // x*c/s with s from the FP32 matrix would then drift by that ratio in
+      // every iteration.  s is scaled per column by (sum of 16-bit values) /
+      // (sum of FP32 values) over the measured rows, the sensitivity of the
+      // matrix the iterations use.
+      float *q = nullptr, *f = nullptr;
+      ALLOC(q, V * 4);
+      ALLOC(f, V * 4);
+      rc = grouped_column_sums(h->G, h->A, true, q, st);
+      if (rc == EPET_OK) rc = grouped_column_sums(h->G, h->A, false, f, st);
+      if (rc == EPET_OK) {
+        k_scale_by_ratio<<<ceil_div(V, 256), 256, 0, st>>>(h->s, q, f, V);
+        note_launch();
+        if (cudaGetLastError() != cudaSuccess) rc = set_error(EPET_ERR_CUDA, "sensitivity ratio");
+      }
+      dev_free(q, st);
+      dev_free(f, st);
+      if (rc != EPET_OK) return fail(rc);
+    }
     EPET_CUDA(cudaStreamSynchronize(st));
     h->grouped = true;
     dev_free(h->A.col, st);

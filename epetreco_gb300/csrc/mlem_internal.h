@@ -34,6 +34,20 @@ epet_status grouped_build(const epet_csr& A, int value_format, GroupedMatrix* G,
 epet_status grouped_pass(const GroupedMatrix& G, const epet_csr& A, const float* x,
                          const float* y, float* ybar, cudaStream_t st);
 void grouped_free(GroupedMatrix* G, cudaStream_t st);
+// Column sums of the values over the matrix's rows into out[V]: the stored
+// 16-bit values dequantised (quantised) or the FP32 values A.val (while
+// they exist); fixed summation order.
+epet_status grouped_column_sums(const GroupedMatrix& G, const epet_csr& A, bool quantised,
+                                float* out, cudaStream_t st);
+// Batched form: a descriptor per problem (grouped_batch_desc_bytes() each,
+// written by grouped_batch_desc into a host buffer and copied to the
+// device) and one pass over all problems' groups (gstart: device prefix of
+// the problems' group counts, np + 1 entries).
+size_t grouped_batch_desc_bytes();
+void grouped_batch_desc(const GroupedMatrix& G, const epet_csr& A, const float* x,
+                        const float* y, float* ybar, void* out);
+epet_status grouped_pass_batch(const void* desc, const int64_t* gstart, int np,
+                               int64_t total_groups, cudaStream_t st);
 }  // namespace epet
 
 struct epet_mlem {

@@ -315,11 +315,11 @@ def test_grouped_layout_equals_csc_layout(small_recon, fmt):
 
 def test_grouped_layout_wide_rows(gpu_lib, oracle):
     """Rows wider than a group's shared table (1 mm voxels along 256 mm of
-    the lines: thousands of entries a row) keep their own columns as their
-    table; against the column-major layout and the FP64 oracle."""
+    the lines, 16 rays: thousands of entries a row) keep their own columns
+    as their table; against the column-major layout and the FP64 oracle."""
     s = two_head_setup(2, 90.0, pos=0.25, n=3)
-    g = VoxelGrid((-0.128, -0.004, -0.004), (0.001, 0.001, 0.001), (256, 8, 8))
-    p = Problem(s, g, 4)
+    g = VoxelGrid((-0.128, -0.008, -0.008), (0.001, 0.001, 0.001), (256, 16, 16))
+    p = Problem(s, g, 16)
     rows = torch.arange(p.nchannels, dtype=torch.int32, device="cuda")
     A = api.systemMatrixCalculation(p, rows)
     lens = torch.diff(A.row_ptr)
