@@ -257,16 +257,21 @@ __device__ __forceinline__ void group_pass(const GroupIterArgs& a, int64_t g, fl
     const int64_t a0 = b & ~int64_t(3);
     const int nq = (int)((e - a0 + 3) >> 2);
     const int lo = (int)(b - a0), hi = (int)(e - a0);  // valid entries: lo <= 4q + t < hi
-    float acc = 0.f;
+    // dot product: four accumulators (entry position t in its chunk), the
+    // shared x loads all independent; entries outside the row count zero
+    float acc[4] = {0.f, 0.f, 0.f, 0.f};
     auto dot = [&](const typename RowBuf<FMT>::V& vv, const uint2& ll, int q) {
+      float xv[4];
 #pragma unroll
       for (int t = 0; t < 4; t++) {
         const int k = 4 * q + t;
-        if (k >= lo && k < hi) {
-          const float xv = wide ? __ldg(a.x + a.table[gd.tb + (k - lo)]) : xs[grank(ll, t)];
-          acc = fmaf(gval<FMT>(vv, t), xv, acc);
-        }
+        const bool ok = k >= lo && k < hi;
+        xv[t] = wide ? (ok ? __ldg(a.x + a.table[gd.tb + (k - lo)]) : 0.f)
+                     : xs[ok ? grank(ll, t) : 0];
+        xv[t] = ok ? xv[t] : 0.f;
       }
+#pragma unroll
+      for (int t = 0; t < 4; t++) acc[t] = fmaf(gval<FMT>(vv, t), xv[t], acc[t]);
     };
 #pragma unroll
     for (int u = 0; u < kGroupRounds; u++) {
@@ -279,25 +284,41 @@ __device__ __forceinline__ void group_pass(const GroupIterArgs& a, int64_t g, fl
       gload_chunk<FMT>(a.val, a.loc, a0 + 4 * q, !wide, &vv, &ll);
       dot(vv, ll, q);
     }
+    float d = fadd(fadd(acc[0], acc[1]), fadd(acc[2], acc[3]));
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+    for (int o = 16; o > 0; o >>= 1) d += __shfl_xor_sync(0xffffffffu, d, o);
     const float sc = __shfl_sync(0xffffffffu, sc_l, i);
-    const float yb = FMT == 0 ? acc : fmul(acc, sc);
+    const float yb = FMT == 0 ? d : fmul(d, sc);
     if (lane == i) yb_l = yb;
     // e = y / (A x) (mlemOperations.hpp:22-32; 0 where A x == 0)
     const float yr = __shfl_sync(0xffffffffu, y_l, i);
     const float er = yb > 0.f ? __fdiv_rn(yr, yb) : 0.f;
     const float f = FMT == 0 ? er : fmul(er, sc);
+    // scatter into the group's correction, a chunk at a time: its four
+    // columns are distinct (as all of a row's), so the four sums are read
+    // before any is written
     auto scatter = [&](const typename RowBuf<FMT>::V& vv, const uint2& ll, int q) {
+      if (wide) {
+#pragma unroll
+        for (int t = 0; t < 4; t++) {
+          const int k = 4 * q + t;
+          if (k >= lo && k < hi) a.partial[gd.tb + (k - lo)] = fmul(gval<FMT>(vv, t), f);
+        }
+        return;
+      }
+      float old[4];
+      int rk[4];
+      bool ok[4];
 #pragma unroll
       for (int t = 0; t < 4; t++) {
         const int k = 4 * q + t;
-        if (k >= lo && k < hi) {
-          const float p = fmul(gval<FMT>(vv, t), f);
-          if (wide) a.partial[gd.tb + (k - lo)] = p;
-          else cs[grank(ll, t)] = fadd(cs[grank(ll, t)], p);
-        }
+        ok[t] = k >= lo && k < hi;
+        rk[t] = grank(ll, t);
+        old[t] = cs[ok[t] ? rk[t] : 0];
       }
+#pragma unroll
+      for (int t = 0; t < 4; t++)
+        if (ok[t]) cs[rk[t]] = fadd(old[t], fmul(gval<FMT>(vv, t), f));
     };
 #pragma unroll
     for (int u = 0; u < kGroupRounds; u++) {

@@ -296,21 +296,21 @@ def test_csrmv_ragged_rows_any_alignment(gpu_lib, oracle, offset):
     assert np.abs(got[nz] - yo[nz]).max() <= 1e-5 * np.abs(yo[nz]).max()
 
 
-@pytest.mark.parametrize("fmt", [0, api.BF16])
+@pytest.mark.parametrize("fmt", [0, api.BF16, api.FP16], ids=["fp32", "bf16", "fp16"])
 def test_grouped_layout_equals_csc_layout(small_recon, fmt):
-    """The one-pass grouped iteration and the CSR + column-major copy give
-    the same images up to fp32 summation order (both deterministic: the same
-    object iterated twice is bit-equal)."""
+    """The one-pass grouped iteration against the CSR + column-major copy:
+    FP32 images equal up to fp32 summation order, the 16-bit forms within
+    1e-3 of FP32; the same grouped object iterated twice is bit-equal."""
     p, rows, y, s = small_recon
     a = api.Mlem(p, dev(rows), y, s, layout=api.LAYOUT_GROUPED, value_format=fmt)
-    b = api.Mlem(p, dev(rows), y, s, layout=api.LAYOUT_CSC, value_format=fmt)
     c = api.Mlem(p, dev(rows), y, s, layout=api.LAYOUT_GROUPED, value_format=fmt)
+    b = api.Mlem(p, dev(rows), y, s, layout=api.LAYOUT_CSC)
     la, lb, lc = (r.iterate(6, loglik=True) for r in (a, b, c))
     xa, xb = a.image().double(), b.image().double()
-    tol = 1e-6 if fmt == 0 else 2e-4  # the 16-bit layouts round their values differently
+    tol = 1e-6 if fmt == 0 else 1e-3
     assert float((xa - xb).norm() / xb.norm()) <= tol
     assert torch.equal(a.image(), c.image()) and la == lc
-    assert abs(la - lb) <= 1e-6 * abs(lb)
+    assert abs(la - lb) <= (1e-6 if fmt == 0 else 1e-4) * abs(lb)
 
 
 def test_grouped_layout_wide_rows(gpu_lib, oracle):
