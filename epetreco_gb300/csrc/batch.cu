@@ -246,9 +246,9 @@ epet_status epet_mlem_batch_create(int32_t nprob, const epet_problem* problems,
     if (all_grouped) {
       // the transpose launch sums the problem's slots: the slot lists as
       // "columns", the ones as values, the slots' corrections gathered
-      dh[i] = BatchDesc{p->A.row_ptr, nullptr, nullptr, p->G.cg_ptr, p->G.cg_slot, p->G.ones,
+      dh[i] = BatchDesc{nullptr, nullptr, nullptr, p->G.cg_ptr, p->G.cg_slot, p->G.ones,
                         p->y, p->G.partial, p->ybar, p->s, p->x, p->xnew, p->m, p->V};
-      grouped_batch_desc(p->G, p->A, p->x, p->y, p->ybar, gd_h.data() + i * grouped_batch_desc_bytes());
+      grouped_batch_desc(p->G, p->x, p->y, p->ybar, gd_h.data() + i * grouped_batch_desc_bytes());
       gs_h[i + 1] = gs_h[i] + p->G.ngroups;
       if (!aligned16(p->G.cg_slot, p->G.ones))
         return fail(set_error(EPET_ERR_UNSUPPORTED, "batch: slot streams not 16-byte aligned"));

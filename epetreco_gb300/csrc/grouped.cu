@@ -8,17 +8,21 @@
 // rows (~14k entries) touches ~1000.  Each entry keeps only its value and a
 // 2-byte rank of its column among the group's sorted distinct columns (the
 // group's table), 6 bytes per entry in FP32 and 4 in BF16/FP16 instead of a
-// CSR plus a column-major copy (16 bytes).
+// CSR plus a column-major copy (16 bytes).  Rows start on 4-entry boundaries
+// and are padded to whole 4-entry chunks with zero values whose rank is a
+// trash slot (past the table), so the pass reads 16-byte chunks with no
+// per-entry bounds tests.
 //
 // One iteration reads every entry once (k_group_mlem): a warp takes a group,
 // gathers x at the table into shared memory, and row by row forms A x from
 // the shared copy, e = y / (A x) and adds the row times e into the group's
 // shared correction; a row's columns are distinct, so the lanes never write
-// the same word and each column's sum runs in row order.  The group's
-// corrections go to one slot per (group, column); the slots of each column,
-// listed in group order (built once, a column-major copy of the table),
-// are summed in that order by a row kernel whose epilogue applies x*c/s.
-// Every sum has an input-determined order, so results are deterministic.
+// the same word (padding goes to the trash slot, which is never read) and
+// each column's sum runs in row order.  The group's corrections go to one
+// slot per (group, column); the slots of each column, listed in group order
+// (built once, a column-major copy of the table), are summed in that order
+// by a row kernel whose epilogue applies x*c/s.  Every sum has an
+// input-determined order, so results are deterministic.
 #include <cuda_bf16.h>
 #include <cuda_fp16.h>
 
@@ -35,6 +39,10 @@ namespace epet {
 
 constexpr int kGroupFirstRows = 32;  // rows of a first-cut group (split while too wide)
 constexpr int kGroupThreads = 256;   // threads of the table-building kernels
+constexpr int kTrash = kGroupCap;    // rank of the padding entries
+constexpr int kGroupStride = kGroupCap + 4;  // floats per shared table (the trash slot included)
+constexpr size_t kGroupSmem = (size_t)kGroupWarps * 2 * kGroupStride * 4;
+static_assert(kGroupSmem <= 227 * 1024, "grouped tables exceed shared memory");
 
 // Distinct columns of the candidate groups cand[g] = {r0, r1}: a bitmap over
 // the columns in shared memory (nwords 32-bit words).
@@ -64,14 +72,15 @@ k_group_distinct(const int64_t* __restrict__ row_ptr, const int32_t* __restrict_
   }
 }
 
-// Tables and local ids of the final groups (one block per group): the
-// group's distinct columns, ascending, at table[tb ..]; each entry's rank in
-// them.  A single row wider than the shared tables keeps its own columns as
-// its table (its entries' ranks are their positions in the row).
+// Tables of the final groups (one block per group): the group's distinct
+// columns, ascending, at table[tb ..], and each entry's rank among them
+// (rank[k] for the CSR's entry k).  A single row wider than the shared
+// tables (a "wide" group) keeps its own columns as its table, padded like
+// the row with column 0 (the padding values are zero).
 __global__ void __launch_bounds__(kGroupThreads)
 k_group_tables(const int64_t* __restrict__ row_ptr, const int32_t* __restrict__ col,
                const GroupDesc* __restrict__ groups, int nwords, int32_t* __restrict__ table,
-               uint16_t* __restrict__ loc) {
+               uint16_t* __restrict__ rank) {
   extern __shared__ unsigned gsh[];
   unsigned* bm = gsh;
   int* pre = reinterpret_cast<int*>(gsh + nwords);
@@ -79,7 +88,8 @@ k_group_tables(const int64_t* __restrict__ row_ptr, const int32_t* __restrict__ 
   const GroupDesc gd = groups[blockIdx.x];
   const int64_t b = row_ptr[gd.r0], e = row_ptr[gd.r1];
   if (gd.nd > kGroupCap) {
-    for (int64_t k = b + threadIdx.x; k < e; k += kGroupThreads) table[gd.tb + (k - b)] = col[k];
+    for (int64_t j = threadIdx.x; j < gd.nd; j += kGroupThreads)
+      table[gd.tb + j] = b + j < e ? col[b + j] : 0;
     return;
   }
   for (int i = threadIdx.x; i < nwords; i += kGroupThreads) bm[i] = 0u;
@@ -96,7 +106,7 @@ k_group_tables(const int64_t* __restrict__ row_ptr, const int32_t* __restrict__ 
   int cnt = 0;
   for (int w = wb; w < we; w++) cnt += __popc(bm[w]);
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-  int inc = warp_incl_scan(cnt);
+  const int inc = warp_incl_scan(cnt);
   if (lane == 31) wtot[wid] = inc;
   __syncthreads();
   if (wid == 0) {
@@ -119,8 +129,30 @@ k_group_tables(const int64_t* __restrict__ row_ptr, const int32_t* __restrict__ 
   __syncthreads();
   for (int64_t k = b + threadIdx.x; k < e; k += kGroupThreads) {
     const unsigned v = (unsigned)col[k];
-    loc[k] = (uint16_t)(pre[v >> 5] + __popc(bm[v >> 5] & ((1u << (v & 31)) - 1u)));
+    rank[k] = (uint16_t)(pre[v >> 5] + __popc(bm[v >> 5] & ((1u << (v & 31)) - 1u)));
   }
+}
+
+// The padded layout, a warp per row: row r's entries at ptr[r] (a multiple
+// of 4) onwards, then zero values up to the next multiple of 4 with the
+// trash rank (a wide group's padding points past its row in its table).
+__global__ void k_group_pad(const int64_t* __restrict__ row_ptr, const float* __restrict__ val,
+                            const uint16_t* __restrict__ rank, const int64_t* __restrict__ ptr,
+                            int64_t m, float* __restrict__ pval, uint16_t* __restrict__ ploc) {
+  const int64_t r = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (r >= m) return;
+  const int64_t b = row_ptr[r], n = row_ptr[r + 1] - b, d = ptr[r], pn = ptr[r + 1] - d;
+  for (int64_t j = lane; j < pn; j += 32) {
+    pval[d + j] = j < n ? val[b + j] : 0.f;
+    ploc[d + j] = j < n ? rank[b + j] : (uint16_t)kTrash;
+  }
+}
+
+__global__ void k_padded_len(const int64_t* __restrict__ row_ptr, int64_t m,
+                             int64_t* __restrict__ len) {
+  const int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (r < m) len[r] = (row_ptr[r + 1] - row_ptr[r] + 3) & ~int64_t(3);
 }
 
 __global__ void k_slot_ids(int64_t n, float* __restrict__ out) {  // slot index bits
@@ -147,12 +179,12 @@ __device__ __forceinline__ float gq_from(uint32_t q) {
 }
 
 template <int FMT>
-__global__ void k_group_quantise(const int64_t* __restrict__ row_ptr, const float* __restrict__ val,
+__global__ void k_group_quantise(const int64_t* __restrict__ ptr, const float* __restrict__ val,
                                  int64_t m, float* __restrict__ scale, uint16_t* __restrict__ q) {
   const int64_t r = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int lane = threadIdx.x & 31;
   if (r >= m) return;
-  const int64_t b = row_ptr[r], e = row_ptr[r + 1];
+  const int64_t b = ptr[r], e = ptr[r + 1];
   float mx = 0.f;
   for (int64_t k = b + lane; k < e; k += 32) mx = fmaxf(mx, fabsf(val[k]));
   for (int o = 16; o > 0; o >>= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
@@ -162,9 +194,8 @@ __global__ void k_group_quantise(const int64_t* __restrict__ row_ptr, const floa
 }
 
 // A row's entries as the pass holds them: 4-entry chunks, chunk u of lane l
-// the (l + 32 u)-th chunk of the row's aligned span (the 4-entry boundaries
-// below its first entry); values raw (FP32: float4, 16-bit: 4 x 16 bits)
-// and column ranks as 4 x 16 bits.
+// the (l + 32 u)-th chunk of the (padded) row; values raw (FP32: float4,
+// 16-bit: 4 x 16 bits) and column ranks as 4 x 16 bits.
 constexpr int kGroupRounds = 4;  // chunks per lane held in registers (512 entries a row)
 template <int FMT>
 struct RowBuf {
@@ -173,14 +204,17 @@ struct RowBuf {
   uint2 l[kGroupRounds];
 };
 
-template <int FMT>
-__device__ __forceinline__ float gval(const float4& c, int t) {
+__device__ __forceinline__ float gval4(const float4& c, int t) {
   return t == 0 ? c.x : t == 1 ? c.y : t == 2 ? c.z : c.w;
 }
 template <int FMT>
-__device__ __forceinline__ float gval(const uint2& c, int t) {
-  const uint32_t w = t < 2 ? c.x : c.y;
-  return gq_from<FMT>((t & 1) ? (w >> 16) : (w & 0xffffu));
+__device__ __forceinline__ float gval(const typename RowBuf<FMT>::V& c, int t) {
+  if constexpr (FMT == 0) {
+    return gval4(c, t);
+  } else {
+    const uint32_t w = t < 2 ? c.x : c.y;
+    return gq_from<FMT>((t & 1) ? (w >> 16) : (w & 0xffffu));
+  }
 }
 __device__ __forceinline__ int grank(const uint2& c, int t) {
   const uint32_t w = t < 2 ? c.x : c.y;
@@ -190,21 +224,21 @@ __device__ __forceinline__ int grank(const uint2& c, int t) {
 template <int FMT>
 __device__ __forceinline__ void gload_chunk(const void* __restrict__ val,
                                             const uint16_t* __restrict__ loc, int64_t k4,
-                                            bool ranks, typename RowBuf<FMT>::V* v, uint2* l) {
+                                            typename RowBuf<FMT>::V* v, uint2* l) {
   if constexpr (FMT == 0)
     *v = __ldcs(reinterpret_cast<const float4*>(static_cast<const float*>(val) + k4));
   else
     *v = __ldcs(reinterpret_cast<const uint2*>(static_cast<const uint16_t*>(val) + k4));
-  if (ranks) *l = __ldcs(reinterpret_cast<const uint2*>(loc + k4));
+  *l = __ldcs(reinterpret_cast<const uint2*>(loc + k4));
 }
 
 struct GroupIterArgs {
   const GroupDesc* groups;
   int64_t ngroups;
-  const int64_t* row_ptr;
-  const void* val;       // float (FP32) or 16-bit bits
-  const float* scale;    // per row (16-bit forms)
-  const uint16_t* loc;
+  const int64_t* row_ptr;  // padded (multiples of 4)
+  const void* val;         // float (FP32) or 16-bit bits, padded
+  const float* scale;      // per row (16-bit forms)
+  const uint16_t* loc;     // padded
   const int32_t* table;
   const float* x;
   const float* y;
@@ -212,64 +246,73 @@ struct GroupIterArgs {
   float* partial;
 };
 
-// One group of the MLEM pass (a warp): per row ybar = A x, e = y / ybar (0
-// where ybar == 0, the fused epilogue's guard) and the rows' shares of
-// A^T e summed, row after row, into the group's shared correction, written
-// to partial[slot] at the end.  Software pipeline: the group's row pointers,
-// counts and scales are loaded once (one row per lane; a group has at most
-// 32 rows), and the next row's entries are in flight while a row is reduced
-// and scattered.
+// What a group's pass needs before its first row: its row pointers, counts
+// and scales, one row per lane (a group has at most 32 rows), loaded one
+// group ahead.
+struct GroupHead {
+  GroupDesc gd;
+  int64_t rp, rp_end;
+  float y, sc;
+};
+
 template <int FMT>
-__device__ __forceinline__ void group_pass(const GroupIterArgs& a, int64_t g, float* xs,
+__device__ __forceinline__ GroupHead group_head(const GroupIterArgs& a, const GroupDesc& gd,
+                                                int lane) {
+  GroupHead h;
+  h.gd = gd;
+  const int nr = gd.r1 - gd.r0;
+  h.rp = lane <= nr ? a.row_ptr[gd.r0 + lane] : 0;
+  h.rp_end = a.row_ptr[gd.r1];
+  h.y = lane < nr ? a.y[gd.r0 + lane] : 0.f;
+  h.sc = FMT != 0 && lane < nr ? a.scale[gd.r0 + lane] : 1.f;
+  return h;
+}
+
+// One group of the MLEM pass (a warp): per row ybar = A x, e = y / ybar (0
+// where ybar == 0, the fused epilogue's guard) and the row's share of A^T e
+// added, row after row, to the group's shared correction, written to
+// partial[slot] at the end.  The next row's entries are in flight while a
+// row is reduced and scattered.
+template <int FMT>
+__device__ __forceinline__ void group_pass(const GroupIterArgs& a, const GroupHead& H, float* xs,
                                            float* cs, int lane) {
-  const GroupDesc gd = a.groups[g];
-  const int nr = gd.r1 - gd.r0;  // <= 32
+  const GroupDesc& gd = H.gd;
+  const int nr = gd.r1 - gd.r0;         // <= 32
   const bool wide = gd.nd > kGroupCap;  // one row, its own columns as table
-  const int64_t rp_l = lane <= nr && lane < 32 ? a.row_ptr[gd.r0 + lane] : 0;
-  const int64_t rp_end = a.row_ptr[gd.r1];
-  const float y_l = lane < nr ? a.y[gd.r0 + lane] : 0.f;
-  const float sc_l = FMT != 0 && lane < nr ? a.scale[gd.r0 + lane] : 1.f;
   float yb_l = 0.f;
-  auto row_begin = [&](int i) -> int64_t { return __shfl_sync(0xffffffffu, rp_l, i); };
+  auto row_begin = [&](int i) -> int64_t { return __shfl_sync(0xffffffffu, H.rp, i); };
   auto row_end = [&](int i) -> int64_t {
-    const int64_t t = __shfl_sync(0xffffffffu, rp_l, (i + 1) & 31);
-    return i + 1 < 32 ? t : rp_end;
+    const int64_t t = __shfl_sync(0xffffffffu, H.rp, (i + 1) & 31);
+    return i + 1 < 32 ? t : H.rp_end;
   };
   if (!wide) {
     for (int j = lane; j < gd.nd; j += 32) {
       xs[j] = __ldg(a.x + a.table[gd.tb + j]);
       cs[j] = 0.f;
     }
+    if (lane == 0) xs[kTrash] = 0.f;
     __syncwarp();
   }
   auto load_row = [&](int i, RowBuf<FMT>& B) {
-    const int64_t b = row_begin(i), e = row_end(i);
-    const int64_t a0 = b & ~int64_t(3);
-    const int nq = (int)((e - a0 + 3) >> 2);
+    const int64_t b = row_begin(i);
+    const int nq = (int)((row_end(i) - b) >> 2);
 #pragma unroll
     for (int u = 0; u < kGroupRounds; u++) {
       const int q = lane + 32 * u;
-      if (q < nq) gload_chunk<FMT>(a.val, a.loc, a0 + 4 * q, !wide, &B.v[u], &B.l[u]);
+      if (q < nq) gload_chunk<FMT>(a.val, a.loc, b + 4 * q, &B.v[u], &B.l[u]);
     }
   };
   auto process_row = [&](int i, const RowBuf<FMT>& B) {
-    const int64_t b = row_begin(i), e = row_end(i);
-    const int64_t a0 = b & ~int64_t(3);
-    const int nq = (int)((e - a0 + 3) >> 2);
-    const int lo = (int)(b - a0), hi = (int)(e - a0);  // valid entries: lo <= 4q + t < hi
+    const int64_t b = row_begin(i);
+    const int nq = (int)((row_end(i) - b) >> 2);
     // dot product: four accumulators (entry position t in its chunk), the
-    // shared x loads all independent; entries outside the row count zero
+    // shared x loads independent; padding entries are zero
     float acc[4] = {0.f, 0.f, 0.f, 0.f};
     auto dot = [&](const typename RowBuf<FMT>::V& vv, const uint2& ll, int q) {
       float xv[4];
 #pragma unroll
-      for (int t = 0; t < 4; t++) {
-        const int k = 4 * q + t;
-        const bool ok = k >= lo && k < hi;
-        xv[t] = wide ? (ok ? __ldg(a.x + a.table[gd.tb + (k - lo)]) : 0.f)
-                     : xs[ok ? grank(ll, t) : 0];
-        xv[t] = ok ? xv[t] : 0.f;
-      }
+      for (int t = 0; t < 4; t++)
+        xv[t] = wide ? __ldg(a.x + a.table[gd.tb + 4 * q + t]) : xs[grank(ll, t)];
 #pragma unroll
       for (int t = 0; t < 4; t++) acc[t] = fmaf(gval<FMT>(vv, t), xv[t], acc[t]);
     };
@@ -281,44 +324,33 @@ __device__ __forceinline__ void group_pass(const GroupIterArgs& a, int64_t g, fl
     for (int q = lane + 32 * kGroupRounds; q < nq; q += 32) {  // rows over 512 entries
       typename RowBuf<FMT>::V vv;
       uint2 ll;
-      gload_chunk<FMT>(a.val, a.loc, a0 + 4 * q, !wide, &vv, &ll);
+      gload_chunk<FMT>(a.val, a.loc, b + 4 * q, &vv, &ll);
       dot(vv, ll, q);
     }
     float d = fadd(fadd(acc[0], acc[1]), fadd(acc[2], acc[3]));
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) d += __shfl_xor_sync(0xffffffffu, d, o);
-    const float sc = __shfl_sync(0xffffffffu, sc_l, i);
+    const float sc = __shfl_sync(0xffffffffu, H.sc, i);
     const float yb = FMT == 0 ? d : fmul(d, sc);
     if (lane == i) yb_l = yb;
     // e = y / (A x) (mlemOperations.hpp:22-32; 0 where A x == 0)
-    const float yr = __shfl_sync(0xffffffffu, y_l, i);
+    const float yr = __shfl_sync(0xffffffffu, H.y, i);
     const float er = yb > 0.f ? __fdiv_rn(yr, yb) : 0.f;
     const float f = FMT == 0 ? er : fmul(er, sc);
     // scatter into the group's correction, a chunk at a time: its four
-    // columns are distinct (as all of a row's), so the four sums are read
-    // before any is written
+    // columns are distinct (as all of a row's; padding goes to the trash
+    // slot), so the four sums are read before any is written
     auto scatter = [&](const typename RowBuf<FMT>::V& vv, const uint2& ll, int q) {
       if (wide) {
 #pragma unroll
-        for (int t = 0; t < 4; t++) {
-          const int k = 4 * q + t;
-          if (k >= lo && k < hi) a.partial[gd.tb + (k - lo)] = fmul(gval<FMT>(vv, t), f);
-        }
+        for (int t = 0; t < 4; t++) a.partial[gd.tb + 4 * q + t] = fmul(gval<FMT>(vv, t), f);
         return;
       }
       float old[4];
-      int rk[4];
-      bool ok[4];
 #pragma unroll
-      for (int t = 0; t < 4; t++) {
-        const int k = 4 * q + t;
-        ok[t] = k >= lo && k < hi;
-        rk[t] = grank(ll, t);
-        old[t] = cs[ok[t] ? rk[t] : 0];
-      }
+      for (int t = 0; t < 4; t++) old[t] = cs[grank(ll, t)];
 #pragma unroll
-      for (int t = 0; t < 4; t++)
-        if (ok[t]) cs[rk[t]] = fadd(old[t], fmul(gval<FMT>(vv, t), f));
+      for (int t = 0; t < 4; t++) cs[grank(ll, t)] = fmaf(gval<FMT>(vv, t), f, old[t]);
     };
 #pragma unroll
     for (int u = 0; u < kGroupRounds; u++) {
@@ -328,7 +360,7 @@ __device__ __forceinline__ void group_pass(const GroupIterArgs& a, int64_t g, fl
     for (int q = lane + 32 * kGroupRounds; q < nq; q += 32) {
       typename RowBuf<FMT>::V vv;
       uint2 ll;
-      gload_chunk<FMT>(a.val, a.loc, a0 + 4 * q, !wide, &vv, &ll);
+      gload_chunk<FMT>(a.val, a.loc, b + 4 * q, &vv, &ll);
       scatter(vv, ll, q);
     }
     __syncwarp();
@@ -350,6 +382,56 @@ __device__ __forceinline__ void group_pass(const GroupIterArgs& a, int64_t g, fl
   }
 }
 
+// A warp per group, a persistent grid striding over the groups; each warp
+// holds its group's tables (x and the correction at the distinct columns)
+// in its share of the block's shared memory.  The next group's head is
+// loaded one group ahead, descriptors two ahead.
+template <int FMT>
+__global__ void __launch_bounds__(kGroupWarps * 32, 1)
+k_group_mlem(GroupIterArgs a) {
+  extern __shared__ __align__(16) float gsm[];
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  float* xs = gsm + (size_t)w * 2 * kGroupStride;
+  float* cs = xs + kGroupStride;
+  const int64_t step = (int64_t)gridDim.x * kGroupWarps;
+  int64_t g = (int64_t)blockIdx.x * kGroupWarps + w;
+  if (g >= a.ngroups) return;
+  GroupHead cur = group_head<FMT>(a, a.groups[g], lane);
+  GroupDesc nxt = g + step < a.ngroups ? a.groups[g + step] : GroupDesc{0, 0, 0, 0};
+  for (; g < a.ngroups; g += step) {
+    const GroupDesc nn =
+        g + 2 * step < a.ngroups ? a.groups[g + 2 * step] : GroupDesc{0, 0, 0, 0};
+    GroupHead head_next{};
+    if (g + step < a.ngroups) head_next = group_head<FMT>(a, nxt, lane);
+    group_pass<FMT>(a, cur, xs, cs, lane);
+    cur = head_next;
+    nxt = nn;
+  }
+}
+
+// The same over the groups of many reconstructions (batched form): global
+// group g belongs to problem p with gstart[p] <= g < gstart[p + 1].
+__global__ void __launch_bounds__(kGroupWarps * 32, 1)
+k_group_mlem_batch(const GroupIterArgs* __restrict__ desc, const int64_t* __restrict__ gstart,
+                   int np) {
+  extern __shared__ __align__(16) float gsm[];
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  float* xs = gsm + (size_t)w * 2 * kGroupStride;
+  float* cs = xs + kGroupStride;
+  const int64_t total = gstart[np];
+  for (int64_t g = (int64_t)blockIdx.x * kGroupWarps + w; g < total;
+       g += (int64_t)gridDim.x * kGroupWarps) {
+    int lo = 0, hi = np;  // gstart[lo] <= g < gstart[hi]
+    while (hi - lo > 1) {
+      const int mid = (lo + hi) >> 1;
+      if (__ldg(gstart + mid) <= g) lo = mid;
+      else hi = mid;
+    }
+    const GroupIterArgs& a = desc[lo];
+    group_pass<0>(a, group_head<0>(a, a.groups[g - gstart[lo]], lane), xs, cs, lane);
+  }
+}
+
 // Column sums of the grouped matrix's values (the 16-bit forms dequantised)
 // over its rows, by the same group / slot structure as the pass: a warp per
 // group adds its rows' values, row after row, into the group's shared sums
@@ -359,7 +441,7 @@ __global__ void __launch_bounds__(kGroupWarps * 32, 1)
 k_group_colsum(GroupIterArgs a) {
   extern __shared__ __align__(16) float gsm[];
   const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  float* cs = gsm + (size_t)w * 2 * kGroupCap;
+  float* cs = gsm + (size_t)w * 2 * kGroupStride;
   for (int64_t g = (int64_t)blockIdx.x * kGroupWarps + w; g < a.ngroups;
        g += (int64_t)gridDim.x * kGroupWarps) {
     const GroupDesc gd = a.groups[g];
@@ -376,7 +458,7 @@ k_group_colsum(GroupIterArgs a) {
         if constexpr (FMT == 0) v = static_cast<const float*>(a.val)[k];
         else v = fmul(gq_from<FMT>(static_cast<const uint16_t*>(a.val)[k]), sc);
         if (wide) a.partial[gd.tb + (k - b)] = v;
-        else cs[a.loc[k]] = fadd(cs[a.loc[k]], v);
+        else cs[a.loc[k]] = fadd(cs[a.loc[k]], v);  // padding: the trash slot
       }
       __syncwarp();
     }
@@ -384,43 +466,6 @@ k_group_colsum(GroupIterArgs a) {
       for (int j = lane; j < gd.nd; j += 32) a.partial[gd.tb + j] = cs[j];
       __syncwarp();
     }
-  }
-}
-
-// A warp per group, a persistent grid striding over the groups; each warp
-// holds its group's tables (x and the correction at the distinct columns)
-// in its share of the block's shared memory.
-template <int FMT>
-__global__ void __launch_bounds__(kGroupWarps * 32, 1)
-k_group_mlem(GroupIterArgs a) {
-  extern __shared__ __align__(16) float gsm[];
-  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  float* xs = gsm + (size_t)w * 2 * kGroupCap;
-  float* cs = xs + kGroupCap;
-  for (int64_t g = (int64_t)blockIdx.x * kGroupWarps + w; g < a.ngroups;
-       g += (int64_t)gridDim.x * kGroupWarps)
-    group_pass<FMT>(a, g, xs, cs, lane);
-}
-
-// The same over the groups of many reconstructions (batched form): global
-// group g belongs to problem p with gstart[p] <= g < gstart[p + 1].
-__global__ void __launch_bounds__(kGroupWarps * 32, 1)
-k_group_mlem_batch(const GroupIterArgs* __restrict__ desc, const int64_t* __restrict__ gstart,
-                   int np) {
-  extern __shared__ __align__(16) float gsm[];
-  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  float* xs = gsm + (size_t)w * 2 * kGroupCap;
-  float* cs = xs + kGroupCap;
-  const int64_t total = gstart[np];
-  for (int64_t g = (int64_t)blockIdx.x * kGroupWarps + w; g < total;
-       g += (int64_t)gridDim.x * kGroupWarps) {
-    int lo = 0, hi = np;  // gstart[lo] <= g < gstart[hi]
-    while (hi - lo > 1) {
-      const int mid = (lo + hi) >> 1;
-      if (__ldg(gstart + mid) <= g) lo = mid;
-      else hi = mid;
-    }
-    group_pass<0>(desc[lo], g - gstart[lo], xs, cs, lane);
   }
 }
 
@@ -436,14 +481,22 @@ bool grouped_supported(int64_t V, int64_t m) {
 void grouped_free(GroupedMatrix* G, cudaStream_t st) {
   for (void* p : {(void*)G->groups, (void*)G->table, (void*)G->loc, (void*)G->cg_ptr,
                   (void*)G->cg_slot, (void*)G->ones, (void*)G->partial, (void*)G->val16,
-                  (void*)G->scale})
+                  (void*)G->val32, (void*)G->row_ptr, (void*)G->scale})
     if (p) dev_free(p, st);
   *G = GroupedMatrix{};
 }
 
+void grouped_drop_fp32(GroupedMatrix* G, cudaStream_t st) {
+  if (G->fmt != EPET_VALUES_FP32 && G->val32) {
+    dev_free(G->val32, st);
+    G->val32 = nullptr;
+  }
+}
+
 // Groups of consecutive rows of A (row pointers on the device) whose
 // distinct columns fit kGroupCap: first cuts of kGroupFirstRows rows, halved
-// while too wide; a single row wider than that is a group of its own.
+// while too wide; a single row wider than that is a group of its own, its
+// table the row's columns padded to whole 4-entry chunks.
 static epet_status form_groups(const epet_csr& A, std::vector<GroupDesc>* out, cudaStream_t st) {
   const int64_t m = A.m;
   const int nwords = bitmap_words(A.n);
@@ -455,10 +508,9 @@ static epet_status form_groups(const epet_csr& A, std::vector<GroupDesc>* out, c
     ps.push_back({(int32_t)r, (int32_t)std::min<int64_t>(m, r + kGroupFirstRows), -1});
   int2* cand = nullptr;
   int32_t* nd = nullptr;
-  epet_status rc = EPET_OK;
   EPET_CUDA(cudaFuncSetAttribute(k_group_distinct, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  nwords * 4));
-  for (int round = 0; round < 40 && rc == EPET_OK; round++) {
+  for (int round = 0; round < 40; round++) {
     std::vector<int> todo;
     for (int i = 0; i < (int)ps.size(); i++)
       if (ps[i].nd < 0) todo.push_back(i);
@@ -483,10 +535,7 @@ static epet_status form_groups(const epet_csr& A, std::vector<GroupDesc>* out, c
     if (nd) dev_free(nd, st);
     cand = nullptr;
     nd = nullptr;
-    if (e != cudaSuccess) {
-      rc = cuda_status(e, "row groups");
-      break;
-    }
+    if (e != cudaSuccess) return cuda_status(e, "row groups");
     for (size_t k = 0; k < n; k++) ps[todo[k]].nd = hn[k];
     std::vector<Piece> next;
     next.reserve(ps.size() + 64);
@@ -501,14 +550,14 @@ static epet_status form_groups(const epet_csr& A, std::vector<GroupDesc>* out, c
     }
     ps.swap(next);
   }
-  if (rc != EPET_OK) return rc;
   out->clear();
   int64_t tb = 0;
   for (const Piece& p : ps) {
     if (p.nd < 0) return set_error(EPET_ERR_INVALID, "internal: row groups unmeasured");
-    if (tb + p.nd > INT32_MAX) return set_error(EPET_ERR_UNSUPPORTED, "row-group tables exceed int32");
-    out->push_back(GroupDesc{p.r0, p.r1, (int32_t)tb, p.nd});
-    tb += p.nd;
+    const int32_t n = p.nd > kGroupCap ? (p.nd + 3) & ~3 : p.nd;  // wide: padded like its row
+    if (tb + n > INT32_MAX) return set_error(EPET_ERR_UNSUPPORTED, "row-group tables exceed int32");
+    out->push_back(GroupDesc{p.r0, p.r1, (int32_t)tb, n});
+    tb += n;
   }
   return EPET_OK;
 }
@@ -517,6 +566,7 @@ epet_status grouped_build(const epet_csr& A, int value_format, GroupedMatrix* G,
                           cudaStream_t st) {
   *G = GroupedMatrix{};
   G->fmt = value_format;
+  G->n = A.n;
   if (!grouped_supported(A.n, A.m))
     return set_error(EPET_ERR_UNSUPPORTED, "grouped layout: %lld columns", (long long)A.n);
   std::vector<GroupDesc> hg;
@@ -535,54 +585,79 @@ epet_status grouped_build(const epet_csr& A, int value_format, GroupedMatrix* G,
   } while (0)
   GALLOC(G->groups, hg.size() * sizeof(GroupDesc));
   GALLOC(G->table, ns * 4);
-  GALLOC(G->loc, (A.nnz + 8) * 2);  // 4-entry loads may reach 3 entries past the end
   GALLOC(G->partial, ns * 4);
   GALLOC(G->ones, ns * 4);
   GALLOC(G->cg_ptr, (A.n + 1) * 8);
+  GALLOC(G->row_ptr, (A.m + 1) * 8);
   if (!hg.empty()) {
     cudaError_t e = cudaMemcpyAsync(G->groups, hg.data(), hg.size() * sizeof(GroupDesc),
                                     cudaMemcpyHostToDevice, st);
     if (e != cudaSuccess) return fail(cuda_status(e, "group table"));
   }
-  cudaMemsetAsync(G->loc + A.nnz, 0, 16, st);
   const int nwords = bitmap_words(A.n);
   cudaError_t e = cudaFuncSetAttribute(k_group_tables, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                        nwords * 8);
+  for (const void* k : {(const void*)k_group_mlem<0>, (const void*)k_group_mlem<1>,
+                        (const void*)k_group_mlem<2>, (const void*)k_group_mlem_batch,
+                        (const void*)k_group_colsum<0>, (const void*)k_group_colsum<1>,
+                        (const void*)k_group_colsum<2>})
+    if (e == cudaSuccess)
+      e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kGroupSmem);
+  if (e != cudaSuccess) return fail(cuda_status(e, "grouped kernels"));
+  // ranks in the CSR's entry order, then the padded layout
   {
-    const int smem = kGroupWarps * 2 * kGroupCap * 4;  // the iteration kernel's tables
-    if (e == cudaSuccess)
-      e = cudaFuncSetAttribute(k_group_mlem<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-    if (e == cudaSuccess)
-      e = cudaFuncSetAttribute(k_group_mlem<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-    if (e == cudaSuccess)
-      e = cudaFuncSetAttribute(k_group_mlem<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-    if (e == cudaSuccess)
-      e = cudaFuncSetAttribute(k_group_mlem_batch, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                               smem);
-    if (e == cudaSuccess)
-      e = cudaFuncSetAttribute(k_group_colsum<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-    if (e == cudaSuccess)
-      e = cudaFuncSetAttribute(k_group_colsum<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-    if (e == cudaSuccess)
-      e = cudaFuncSetAttribute(k_group_colsum<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-  }
-  if (e != cudaSuccess) return fail(cuda_status(e, "group tables"));
-  if (!hg.empty()) {
-    k_group_tables<<<(unsigned)hg.size(), kGroupThreads, nwords * 8, st>>>(A.row_ptr, A.col,
-                                                                            G->groups, nwords,
-                                                                            G->table, G->loc);
-    note_launch();
-    if (cudaGetLastError() != cudaSuccess) return fail(set_error(EPET_ERR_CUDA, "group tables"));
+    uint16_t* rank = nullptr;
+    int64_t *len = nullptr, *tmp = nullptr;
+    GALLOC(rank, (A.nnz + 1) * 2);
+    GALLOC(len, std::max<int64_t>(A.m, 1) * 8);
+    GALLOC(tmp, scan_tmp_elems(A.m) * 8);
+    epet_status rc = EPET_OK;
+    if (!hg.empty()) {
+      k_group_tables<<<(unsigned)hg.size(), kGroupThreads, nwords * 8, st>>>(A.row_ptr, A.col,
+                                                                              G->groups, nwords,
+                                                                              G->table, rank);
+      note_launch();
+      if (cudaGetLastError() != cudaSuccess) rc = set_error(EPET_ERR_CUDA, "group tables");
+    }
+    if (rc == EPET_OK && A.m > 0) {
+      k_padded_len<<<ceil_div(A.m, 256), 256, 0, st>>>(A.row_ptr, A.m, len);
+      note_launch();
+      rc = exclusive_scan_i64(len, G->row_ptr, A.m, tmp, st);
+    } else if (rc == EPET_OK) {
+      cudaMemsetAsync(G->row_ptr, 0, 8, st);
+    }
+    if (rc == EPET_OK) {
+      e = cudaMemcpyAsync(&G->npad, G->row_ptr + A.m, 8, cudaMemcpyDeviceToHost, st);
+      if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+      if (e != cudaSuccess) rc = cuda_status(e, "padded layout");
+    }
+    if (rc == EPET_OK) {
+      cudaError_t e1 = dev_alloc((void**)&G->val32, std::max<int64_t>(G->npad, 4) * 4, st);
+      cudaError_t e2 = dev_alloc((void**)&G->loc, std::max<int64_t>(G->npad, 4) * 2, st);
+      if (e1 != cudaSuccess || e2 != cudaSuccess)
+        rc = cuda_status(e1 != cudaSuccess ? e1 : e2, "grouped allocation of the padded layout");
+    }
+    if (rc == EPET_OK && A.m > 0) {
+      k_group_pad<<<ceil_div(A.m * 32, 256), 256, 0, st>>>(A.row_ptr, A.val, rank, G->row_ptr,
+                                                           A.m, G->val32, G->loc);
+      note_launch();
+      if (cudaGetLastError() != cudaSuccess) rc = set_error(EPET_ERR_CUDA, "padded layout");
+    }
+    dev_free(rank, st);
+    dev_free(len, st);
+    dev_free(tmp, st);
+    if (rc != EPET_OK) return fail(rc);
   }
   // the slots of each column in group order: the column-major copy of the
-  // (group x column) table, its values the slot indices
+  // (group x column) table, its values the slot indices (a wide group's
+  // padding slots sit in column 0 and hold zero corrections)
   {
     float* slot_bits = nullptr;
     int32_t* cg_group = nullptr;
+    int64_t* gptr = nullptr;
     GALLOC(slot_bits, ns * 4);
     GALLOC(cg_group, ns * 4);
     GALLOC(G->cg_slot, ns * 4);
-    int64_t* gptr = nullptr;
     GALLOC(gptr, (G->ngroups + 1) * 8);
     std::vector<int64_t> hp(G->ngroups + 1);
     for (int64_t i = 0; i < G->ngroups; i++) hp[i] = hg[i].tb;
@@ -608,15 +683,14 @@ epet_status grouped_build(const epet_csr& A, int value_format, GroupedMatrix* G,
     if (rc != EPET_OK) return fail(rc);
   }
   if (value_format != EPET_VALUES_FP32) {
-    GALLOC(G->val16, (A.nnz + 8) * 2);
+    GALLOC(G->val16, std::max<int64_t>(G->npad, 4) * 2);
     GALLOC(G->scale, std::max<int64_t>(A.m, 1) * 4);
-    cudaMemsetAsync(G->val16 + A.nnz, 0, 16, st);
     if (A.m > 0) {
       if (value_format == EPET_VALUES_BF16)
-        k_group_quantise<1><<<ceil_div(A.m * 32, 256), 256, 0, st>>>(A.row_ptr, A.val, A.m,
+        k_group_quantise<1><<<ceil_div(A.m * 32, 256), 256, 0, st>>>(G->row_ptr, G->val32, A.m,
                                                                      G->scale, G->val16);
       else
-        k_group_quantise<2><<<ceil_div(A.m * 32, 256), 256, 0, st>>>(A.row_ptr, A.val, A.m,
+        k_group_quantise<2><<<ceil_div(A.m * 32, 256), 256, 0, st>>>(G->row_ptr, G->val32, A.m,
                                                                      G->scale, G->val16);
       note_launch();
       if (cudaGetLastError() != cudaSuccess) return fail(set_error(EPET_ERR_CUDA, "quantise"));
@@ -627,69 +701,67 @@ epet_status grouped_build(const epet_csr& A, int value_format, GroupedMatrix* G,
   return EPET_OK;
 }
 
-static GroupIterArgs iter_args(const GroupedMatrix& G, const epet_csr& A, const float* x,
-                               const float* y, float* ybar) {
-  return GroupIterArgs{G.groups, G.ngroups, A.row_ptr,
-                       G.fmt == EPET_VALUES_FP32 ? (const void*)A.val : (const void*)G.val16,
+static GroupIterArgs iter_args(const GroupedMatrix& G, const float* x, const float* y,
+                               float* ybar) {
+  return GroupIterArgs{G.groups, G.ngroups, G.row_ptr,
+                       G.fmt == EPET_VALUES_FP32 ? (const void*)G.val32 : (const void*)G.val16,
                        G.scale, G.loc, G.table, x, y, ybar, G.partial};
 }
 
 size_t grouped_batch_desc_bytes() { return sizeof(GroupIterArgs); }
 
-void grouped_batch_desc(const GroupedMatrix& G, const epet_csr& A, const float* x,
-                        const float* y, float* ybar, void* out) {
-  *static_cast<GroupIterArgs*>(out) = iter_args(G, A, x, y, ybar);
+void grouped_batch_desc(const GroupedMatrix& G, const float* x, const float* y, float* ybar,
+                        void* out) {
+  *static_cast<GroupIterArgs*>(out) = iter_args(G, x, y, ybar);
+}
+
+static unsigned pass_grid(int64_t ngroups) {
+  return (unsigned)std::max<int64_t>(
+      1, std::min<int64_t>((ngroups + kGroupWarps - 1) / kGroupWarps, (int64_t)num_sms()));
 }
 
 epet_status grouped_pass_batch(const void* desc, const int64_t* gstart, int np,
                                int64_t total_groups, cudaStream_t st) {
   if (total_groups <= 0) return EPET_OK;
-  const size_t smem = (size_t)kGroupWarps * 2 * kGroupCap * 4;
-  const unsigned grid = (unsigned)std::min<int64_t>((total_groups + kGroupWarps - 1) / kGroupWarps,
-                                                    (int64_t)num_sms());
-  k_group_mlem_batch<<<grid, kGroupWarps * 32, smem, st>>>(
+  k_group_mlem_batch<<<pass_grid(total_groups), kGroupWarps * 32, kGroupSmem, st>>>(
       static_cast<const GroupIterArgs*>(desc), gstart, np);
   EPET_LAUNCHED();
   return EPET_OK;
 }
 
-epet_status grouped_column_sums(const GroupedMatrix& G, const epet_csr& A, bool quantised,
-                                float* out, cudaStream_t st) {
-  const int64_t V = A.n;
+epet_status grouped_column_sums(const GroupedMatrix& G, bool quantised, float* out,
+                                cudaStream_t st) {
   if (G.ngroups > 0) {
-    GroupIterArgs a = iter_args(G, A, nullptr, nullptr, nullptr);
+    GroupIterArgs a = iter_args(G, nullptr, nullptr, nullptr);
     int fmt = G.fmt;
     if (!quantised) {
-      a.val = A.val;
+      if (!G.val32) return set_error(EPET_ERR_INVALID, "internal: FP32 values released");
+      a.val = G.val32;
       fmt = EPET_VALUES_FP32;
     }
-    const size_t smem = (size_t)kGroupWarps * 2 * kGroupCap * 4;
-    const unsigned grid = (unsigned)std::min<int64_t>(
-        (G.ngroups + kGroupWarps - 1) / kGroupWarps, (int64_t)num_sms());
+    const unsigned grid = pass_grid(G.ngroups);
     switch (fmt) {
-      case EPET_VALUES_BF16: k_group_colsum<1><<<grid, kGroupWarps * 32, smem, st>>>(a); break;
-      case EPET_VALUES_FP16: k_group_colsum<2><<<grid, kGroupWarps * 32, smem, st>>>(a); break;
-      default: k_group_colsum<0><<<grid, kGroupWarps * 32, smem, st>>>(a);
+      case EPET_VALUES_BF16: k_group_colsum<1><<<grid, kGroupWarps * 32, kGroupSmem, st>>>(a); break;
+      case EPET_VALUES_FP16: k_group_colsum<2><<<grid, kGroupWarps * 32, kGroupSmem, st>>>(a); break;
+      default: k_group_colsum<0><<<grid, kGroupWarps * 32, kGroupSmem, st>>>(a);
     }
     EPET_LAUNCHED();
   }
-  return launch_rows(G.plan_cols, G.cg_ptr, G.cg_slot, G.ones, G.partial, V, EpiKeep{out},
+  return launch_rows(G.plan_cols, G.cg_ptr, G.cg_slot, G.ones, G.partial, G.n, EpiKeep{out},
                      nullptr, st);
 }
 
-epet_status grouped_pass(const GroupedMatrix& G, const epet_csr& A, const float* x, const float* y,
-                         float* ybar, cudaStream_t st) {
+epet_status grouped_pass(const GroupedMatrix& G, const float* x, const float* y, float* ybar,
+                         cudaStream_t st) {
   if (G.ngroups == 0) return EPET_OK;
-  GroupIterArgs a = iter_args(G, A, x, y, ybar);
-  const size_t smem = (size_t)kGroupWarps * 2 * kGroupCap * 4;
-  const unsigned grid = (unsigned)std::min<int64_t>(
-      (G.ngroups + kGroupWarps - 1) / kGroupWarps, (int64_t)num_sms());
+  const GroupIterArgs a = iter_args(G, x, y, ybar);
+  const unsigned grid = pass_grid(G.ngroups);
   // (the shared-memory size was allowed when the layout was built: this
   // launch may be captured in a graph)
   switch (G.fmt) {
-    case EPET_VALUES_BF16: k_group_mlem<1><<<grid, kGroupWarps * 32, smem, st>>>(a); break;
-    case EPET_VALUES_FP16: k_group_mlem<2><<<grid, kGroupWarps * 32, smem, st>>>(a); break;
-    default: k_group_mlem<0><<<grid, kGroupWarps * 32, smem, st>>>(a);
+    case EPET_VALUES_BF16: k_group_mlem<1><<<grid, kGroupWarps * 32, kGroupSmem, st>>>(a); break;
+    case EPET_VALUES_FP16: k_group_mlem<2><<<grid, kGroupWarps * 32, kGroupSmem, st>>>(a); break;
+    default: k_group_mlem<0><<<grid, kGroupWarps * 32, kGroupSmem, st>>>(a);
   }
   EPET_LAUNCHED();
   return EPET_OK;

@@ -75,7 +75,7 @@ static epet_status mlem_iteration_free(epet_mlem* h, cudaStream_t st) {
 // forward product keeps ybar and e as in the iteration).
 static epet_status mlem_correction(epet_mlem* h, float* c, cudaStream_t st) {
   if (h->grouped) {
-    EPET_CHECK(grouped_pass(h->G, h->A, h->x, h->y, h->ybar, st));
+    EPET_CHECK(grouped_pass(h->G, h->x, h->y, h->ybar, st));
     return launch_rows(h->G.plan_cols, h->G.cg_ptr, h->G.cg_slot, h->G.ones, h->G.partial, h->V,
                        EpiKeep{c}, nullptr, st);
   }
@@ -102,7 +102,7 @@ static epet_status mlem_correction(epet_mlem* h, float* c, cudaStream_t st) {
 // of A^T e), the fixed-order slot sums per column fused with x*c/s, the
 // image sum and the normalisation.
 static epet_status mlem_iteration_grouped(epet_mlem* h, cudaStream_t st) {
-  EPET_CHECK(grouped_pass(h->G, h->A, h->x, h->y, h->ybar, st));
+  EPET_CHECK(grouped_pass(h->G, h->x, h->y, h->ybar, st));
   EPET_CHECK(launch_rows(h->G.plan_cols, h->G.cg_ptr, h->G.cg_slot, h->G.ones, h->G.partial,
                          h->V, EpiMlemUpdate{h->x, h->s, h->xnew, nullptr}, nullptr, st));
   return launch_sum_normalise(h->xnew, h->V, h->part_x, h->x, st);
@@ -399,8 +399,7 @@ epet_status epet_mlem_create(const epet_problem* p, const int32_t* rows_d, const
   if (o.layout != EPET_LAYOUT_AUTO && o.layout != EPET_LAYOUT_GROUPED &&
       o.layout != EPET_LAYOUT_CSC)
     return fail(set_error(EPET_ERR_INVALID, "layout %d", o.layout));
-  const bool grouped_ok = grouped_supported(V, m) &&
-                          (reinterpret_cast<uintptr_t>(h->A.val) & 15) == 0;
+  const bool grouped_ok = grouped_supported(V, m);
   if (o.layout == EPET_LAYOUT_GROUPED && !grouped_ok)
     return fail(set_error(EPET_ERR_UNSUPPORTED, "grouped layout: %lld voxels (at most 819,200)",
                           (long long)V));
@@ -419,8 +418,8 @@ epet_status epet_mlem_create(const epet_problem* p, const int32_t* rows_d, const
       float *q = nullptr, *f = nullptr;
       ALLOC(q, V * 4);
       ALLOC(f, V * 4);
-      rc = grouped_column_sums(h->G, h->A, true, q, st);
-      if (rc == EPET_OK) rc = grouped_column_sums(h->G, h->A, false, f, st);
+      rc = grouped_column_sums(h->G, true, q, st);
+      if (rc == EPET_OK) rc = grouped_column_sums(h->G, false, f, st);
       if (rc == EPET_OK) {
         k_scale_by_ratio<<<ceil_div(V, 256), 256, 0, st>>>(h->s, q, f, V);
         note_launch();
@@ -430,13 +429,13 @@ epet_status epet_mlem_create(const epet_problem* p, const int32_t* rows_d, const
       dev_free(f, st);
       if (rc != EPET_OK) return fail(rc);
     }
+    grouped_drop_fp32(&h->G, st);
     EPET_CUDA(cudaStreamSynchronize(st));
     h->grouped = true;
-    dev_free(h->A.col, st);
-    h->A.col = nullptr;
-    if (o.value_format != EPET_VALUES_FP32) {
-      dev_free(h->A.val, st);
-      h->A.val = nullptr;
+    // the grouped layout holds the matrix: the CSR's arrays go (nnz stays)
+    for (void** q : {(void**)&h->A.row_ptr, (void**)&h->A.col, (void**)&h->A.val}) {
+      if (*q) dev_free(*q, st);
+      *q = nullptr;
     }
     h->plan_fwd = RowPlan{32, 1, num_sms(), false};  // reported: one warp per group
     h->plan_bwd = h->G.plan_cols;
@@ -445,7 +444,7 @@ epet_status epet_mlem_create(const epet_problem* p, const int32_t* rows_d, const
     if (o.autotune) {
       // the slot sums' launch shape: one pass fills the slots, then the
       // candidates run the real (idempotent) epilogue
-      rc = grouped_pass(h->G, h->A, h->x, h->y, h->ybar, st);
+      rc = grouped_pass(h->G, h->x, h->y, h->ybar, st);
       if (rc == EPET_OK)
         rc = tune_rows(
             4, V, h->G.nslots, h->G.ngroups, V ? (double)h->G.nslots / V : 0.0,
@@ -629,9 +628,9 @@ epet_status epet_mlem_stats(const epet_mlem* h, int64_t* nnz_h, int64_t* bytes_h
     // the correction written; slot sums: column pointers, per slot the slot
     // index, a one and the correction, x and s read, xnew written; image
     // sum and normalisation: xnew read twice, x written
-    const int64_t nnz = h->A.nnz, m = h->m, V = h->V, ns = h->G.nslots;
+    const int64_t np = h->G.npad, m = h->m, V = h->V, ns = h->G.nslots;  // (padded entries)
     const int64_t bv = h->G.fmt == EPET_VALUES_FP32 ? 4 : 2;
-    *bytes_h = (bv + 2) * nnz + 8 * (m + 1) + 8 * m + (bv == 2 ? 4 * m : 0) + 12 * ns +
+    *bytes_h = (bv + 2) * np + 8 * (m + 1) + 8 * m + (bv == 2 ? 4 * m : 0) + 12 * ns +
                8 * (V + 1) + 12 * ns + 8 * V + 4 * V + 8 * V + 4 * V;
   } else if (bytes_h && h->opt.matrix_free) {
     // no matrix: the pass writes and reads the rays (24 bytes each) and the

@@ -16,36 +16,43 @@ struct GroupDesc {
 };
 struct GroupedMatrix {
   int fmt = 0;  // EPET_VALUES_*
-  int64_t ngroups = 0, nslots = 0;
+  int64_t n = 0;                // columns (voxels)
+  int64_t ngroups = 0, nslots = 0, npad = 0;
   GroupDesc* groups = nullptr;
-  int32_t* table = nullptr;   // each group's distinct columns, ascending
-  uint16_t* loc = nullptr;    // per entry: rank of its column in its group's table
-  int64_t* cg_ptr = nullptr;  // per column: its slots (group order) at cg_slot[cg_ptr[v] ..]
-  int32_t* cg_slot = nullptr;
-  float* ones = nullptr;      // nslots ones (the slot sums run on the row kernel)
-  float* partial = nullptr;   // per slot: the group's share of c = A^T e
-  uint16_t* val16 = nullptr;  // 16-bit forms: values / row scale
+  int32_t* table = nullptr;     // each group's distinct columns, ascending
+  int64_t* row_ptr = nullptr;   // rows padded to whole 4-entry chunks
+  float* val32 = nullptr;       // values (FP32 form; 16-bit forms: until the sensitivity is fixed)
+  uint16_t* val16 = nullptr;    // 16-bit forms: values / row scale
   float* scale = nullptr;
+  uint16_t* loc = nullptr;      // per entry: rank of its column in its group's table
+  int64_t* cg_ptr = nullptr;    // per column: its slots (group order) at cg_slot[cg_ptr[v] ..]
+  int32_t* cg_slot = nullptr;
+  float* ones = nullptr;        // nslots ones (the slot sums run on the row kernel)
+  float* partial = nullptr;     // per slot: the group's share of c = A^T e
   RowPlan plan_cols;
 };
 bool grouped_supported(int64_t V, int64_t m);
+// Builds the grouped layout from a CSR (rows in the reconstruction's order);
+// A itself is left as it is (the caller may release it afterwards).
 epet_status grouped_build(const epet_csr& A, int value_format, GroupedMatrix* G, cudaStream_t st);
 // ybar = A x, e = y / ybar and the groups' shares of A^T e into G.partial.
-epet_status grouped_pass(const GroupedMatrix& G, const epet_csr& A, const float* x,
-                         const float* y, float* ybar, cudaStream_t st);
+epet_status grouped_pass(const GroupedMatrix& G, const float* x, const float* y, float* ybar,
+                         cudaStream_t st);
 void grouped_free(GroupedMatrix* G, cudaStream_t st);
+// Releases the FP32 values of a 16-bit form.
+void grouped_drop_fp32(GroupedMatrix* G, cudaStream_t st);
 // Column sums of the values over the matrix's rows into out[V]: the stored
-// 16-bit values dequantised (quantised) or the FP32 values A.val (while
-// they exist); fixed summation order.
-epet_status grouped_column_sums(const GroupedMatrix& G, const epet_csr& A, bool quantised,
-                                float* out, cudaStream_t st);
+// 16-bit values dequantised (quantised) or the FP32 values (while they
+// exist); fixed summation order.
+epet_status grouped_column_sums(const GroupedMatrix& G, bool quantised, float* out,
+                                cudaStream_t st);
 // Batched form: a descriptor per problem (grouped_batch_desc_bytes() each,
 // written by grouped_batch_desc into a host buffer and copied to the
 // device) and one pass over all problems' groups (gstart: device prefix of
 // the problems' group counts, np + 1 entries).
 size_t grouped_batch_desc_bytes();
-void grouped_batch_desc(const GroupedMatrix& G, const epet_csr& A, const float* x,
-                        const float* y, float* ybar, void* out);
+void grouped_batch_desc(const GroupedMatrix& G, const float* x, const float* y, float* ybar,
+                        void* out);
 epet_status grouped_pass_batch(const void* desc, const int64_t* gstart, int np,
                                int64_t total_groups, cudaStream_t st);
 }  // namespace epet
