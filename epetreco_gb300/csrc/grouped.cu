@@ -40,7 +40,12 @@ namespace epet {
 constexpr int kGroupFirstRows = 32;  // rows of a first-cut group (split while too wide)
 constexpr int kGroupThreads = 256;   // threads of the table-building kernels
 constexpr int kTrash = kGroupCap;    // rank of the padding entries
-constexpr int kGroupStride = kGroupCap + 4;  // floats per shared table (the trash slot included)
+// Shared tables are indexed by swizzled ranks, sw(r) = r + r / 32: the ranks
+// of a chunk's entries across a warp's lanes step by a few (a row's columns
+// ascend), and the added r / 32 breaks the regular bank pattern.  The
+// layout stores swizzled ranks, so the pass indexes with them directly.
+__host__ __device__ constexpr int sw_rank(int r) { return r + (r >> 5); }
+constexpr int kGroupStride = sw_rank(kGroupCap) + 4;  // floats per shared table (trash included)
 constexpr size_t kGroupSmem = (size_t)kGroupWarps * 2 * kGroupStride * 4;
 static_assert(kGroupSmem <= 227 * 1024, "grouped tables exceed shared memory");
 
@@ -135,7 +140,8 @@ k_group_tables(const int64_t* __restrict__ row_ptr, const int32_t* __restrict__ 
 
 // The padded layout, a warp per row: row r's entries at ptr[r] (a multiple
 // of 4) onwards, then zero values up to the next multiple of 4 with the
-// trash rank (a wide group's padding points past its row in its table).
+// trash rank (a wide group's padding points past its row in its table);
+// ranks stored swizzled.
 __global__ void k_group_pad(const int64_t* __restrict__ row_ptr, const float* __restrict__ val,
                             const uint16_t* __restrict__ rank, const int64_t* __restrict__ ptr,
                             int64_t m, float* __restrict__ pval, uint16_t* __restrict__ ploc) {
@@ -145,7 +151,7 @@ __global__ void k_group_pad(const int64_t* __restrict__ row_ptr, const float* __
   const int64_t b = row_ptr[r], n = row_ptr[r + 1] - b, d = ptr[r], pn = ptr[r + 1] - d;
   for (int64_t j = lane; j < pn; j += 32) {
     pval[d + j] = j < n ? val[b + j] : 0.f;
-    ploc[d + j] = j < n ? rank[b + j] : (uint16_t)kTrash;
+    ploc[d + j] = (uint16_t)sw_rank(j < n ? (int)rank[b + j] : kTrash);
   }
 }
 
@@ -273,9 +279,32 @@ __device__ __forceinline__ GroupHead group_head(const GroupIterArgs& a, const Gr
 // added, row after row, to the group's shared correction, written to
 // partial[slot] at the end.  The next row's entries are in flight while a
 // row is reduced and scattered.
+// L2 prefetch of [p, p + bytes) by one lane (a hint: 16-byte granules, the
+// range widened to them; the arrays it reads carry 64 bytes of slack).
+__device__ __forceinline__ void prefetch_l2(const void* p, int64_t bytes) {
+  const uintptr_t a0 = reinterpret_cast<uintptr_t>(p) & ~uintptr_t(15);
+  const uintptr_t a1 = (reinterpret_cast<uintptr_t>(p) + (uintptr_t)bytes + 15) & ~uintptr_t(15);
+  for (uintptr_t q = a0; q < a1; q += (uintptr_t)1 << 20) {
+    const uint32_t n = (uint32_t)min((uintptr_t)1 << 20, a1 - q);
+    asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(q), "r"(n) : "memory");
+  }
+}
+
+// The next group's table and entries into L2 (lane 0).
+template <int FMT>
+__device__ __forceinline__ void prefetch_group(const GroupIterArgs& a, const GroupHead& P) {
+  const int64_t b = P.rp_end > 0 ? __shfl_sync(0xffffffffu, P.rp, 0) : 0;
+  if ((threadIdx.x & 31) != 0 || P.gd.r1 <= P.gd.r0) return;
+  prefetch_l2(a.table + P.gd.tb, (int64_t)P.gd.nd * 4);
+  const int64_t n = P.rp_end - b;
+  prefetch_l2(static_cast<const char*>(a.val) + b * (FMT == 0 ? 4 : 2), n * (FMT == 0 ? 4 : 2));
+  prefetch_l2(a.loc + b, n * 2);
+}
+
 template <int FMT>
 __device__ __forceinline__ void group_pass(const GroupIterArgs& a, const GroupHead& H, float* xs,
-                                           float* cs, int lane) {
+                                           float* cs, int lane, bool has_next = false,
+                                           const GroupHead& next = GroupHead{}) {
   const GroupDesc& gd = H.gd;
   const int nr = gd.r1 - gd.r0;         // <= 32
   const bool wide = gd.nd > kGroupCap;  // one row, its own columns as table
@@ -286,11 +315,26 @@ __device__ __forceinline__ void group_pass(const GroupIterArgs& a, const GroupHe
     return i + 1 < 32 ? t : H.rp_end;
   };
   if (!wide) {
-    for (int j = lane; j < gd.nd; j += 32) {
-      xs[j] = __ldg(a.x + a.table[gd.tb + j]);
-      cs[j] = 0.f;
+    // x at the table: batches of 8 independent table loads, then their x
+    // gathers
+    for (int j0 = 0; j0 < gd.nd; j0 += 8 * 32) {
+      int col[8];
+#pragma unroll
+      for (int k = 0; k < 8; k++) {
+        const int j = j0 + 32 * k + lane;
+        col[k] = j < gd.nd ? __ldg(a.table + gd.tb + j) : 0;
+      }
+#pragma unroll
+      for (int k = 0; k < 8; k++) {
+        const int j = j0 + 32 * k + lane;
+        const float xv = __ldg(a.x + col[k]);
+        if (j < gd.nd) {
+          xs[sw_rank(j)] = xv;
+          cs[sw_rank(j)] = 0.f;
+        }
+      }
     }
-    if (lane == 0) xs[kTrash] = 0.f;
+    if (lane == 0) xs[sw_rank(kTrash)] = 0.f;
     __syncwarp();
   }
   auto load_row = [&](int i, RowBuf<FMT>& B) {
@@ -370,6 +414,7 @@ __device__ __forceinline__ void group_pass(const GroupIterArgs& a, const GroupHe
   for (int i = 0; i < nr; i += 2) {
     if (i + 1 < nr) load_row(i + 1, b1);
     process_row(i, b0);
+    if (i == 0 && has_next) prefetch_group<FMT>(a, next);  // (its head has arrived by now)
     if (i + 1 < nr) {
       if (i + 2 < nr) load_row(i + 2, b0);
       process_row(i + 1, b1);
@@ -377,7 +422,7 @@ __device__ __forceinline__ void group_pass(const GroupIterArgs& a, const GroupHe
   }
   if (lane < nr) a.ybar[gd.r0 + lane] = yb_l;
   if (!wide) {
-    for (int j = lane; j < gd.nd; j += 32) a.partial[gd.tb + j] = cs[j];
+    for (int j = lane; j < gd.nd; j += 32) a.partial[gd.tb + j] = cs[sw_rank(j)];
     __syncwarp();
   }
 }
@@ -402,8 +447,9 @@ k_group_mlem(GroupIterArgs a) {
     const GroupDesc nn =
         g + 2 * step < a.ngroups ? a.groups[g + 2 * step] : GroupDesc{0, 0, 0, 0};
     GroupHead head_next{};
-    if (g + step < a.ngroups) head_next = group_head<FMT>(a, nxt, lane);
-    group_pass<FMT>(a, cur, xs, cs, lane);
+    const bool more = g + step < a.ngroups;
+    if (more) head_next = group_head<FMT>(a, nxt, lane);
+    group_pass<FMT>(a, cur, xs, cs, lane, more, head_next);
     cur = head_next;
     nxt = nn;
   }
@@ -447,7 +493,7 @@ k_group_colsum(GroupIterArgs a) {
     const GroupDesc gd = a.groups[g];
     const bool wide = gd.nd > kGroupCap;
     if (!wide) {
-      for (int j = lane; j < gd.nd; j += 32) cs[j] = 0.f;
+      for (int j = lane; j < gd.nd; j += 32) cs[sw_rank(j)] = 0.f;
       __syncwarp();
     }
     for (int r = gd.r0; r < gd.r1; r++) {
@@ -463,7 +509,7 @@ k_group_colsum(GroupIterArgs a) {
       __syncwarp();
     }
     if (!wide) {
-      for (int j = lane; j < gd.nd; j += 32) a.partial[gd.tb + j] = cs[j];
+      for (int j = lane; j < gd.nd; j += 32) a.partial[gd.tb + j] = cs[sw_rank(j)];
       __syncwarp();
     }
   }
@@ -584,7 +630,7 @@ epet_status grouped_build(const epet_csr& A, int value_format, GroupedMatrix* G,
     if (e_ != cudaSuccess) return fail(cuda_status(e_, "grouped allocation " #ptr)); \
   } while (0)
   GALLOC(G->groups, hg.size() * sizeof(GroupDesc));
-  GALLOC(G->table, ns * 4);
+  GALLOC(G->table, ns * 4 + 64);  // (slack: the L2 prefetch widens ranges to 16 bytes)
   GALLOC(G->partial, ns * 4);
   GALLOC(G->ones, ns * 4);
   GALLOC(G->cg_ptr, (A.n + 1) * 8);
@@ -632,8 +678,8 @@ epet_status grouped_build(const epet_csr& A, int value_format, GroupedMatrix* G,
       if (e != cudaSuccess) rc = cuda_status(e, "padded layout");
     }
     if (rc == EPET_OK) {
-      cudaError_t e1 = dev_alloc((void**)&G->val32, std::max<int64_t>(G->npad, 4) * 4, st);
-      cudaError_t e2 = dev_alloc((void**)&G->loc, std::max<int64_t>(G->npad, 4) * 2, st);
+      cudaError_t e1 = dev_alloc((void**)&G->val32, std::max<int64_t>(G->npad, 4) * 4 + 64, st);
+      cudaError_t e2 = dev_alloc((void**)&G->loc, std::max<int64_t>(G->npad, 4) * 2 + 64, st);
       if (e1 != cudaSuccess || e2 != cudaSuccess)
         rc = cuda_status(e1 != cudaSuccess ? e1 : e2, "grouped allocation of the padded layout");
     }
@@ -683,7 +729,7 @@ epet_status grouped_build(const epet_csr& A, int value_format, GroupedMatrix* G,
     if (rc != EPET_OK) return fail(rc);
   }
   if (value_format != EPET_VALUES_FP32) {
-    GALLOC(G->val16, std::max<int64_t>(G->npad, 4) * 2);
+    GALLOC(G->val16, std::max<int64_t>(G->npad, 4) * 2 + 64);
     GALLOC(G->scale, std::max<int64_t>(A.m, 1) * 4);
     if (A.m > 0) {
       if (value_format == EPET_VALUES_BF16)
