@@ -279,32 +279,9 @@ __device__ __forceinline__ GroupHead group_head(const GroupIterArgs& a, const Gr
 // added, row after row, to the group's shared correction, written to
 // partial[slot] at the end.  The next row's entries are in flight while a
 // row is reduced and scattered.
-// L2 prefetch of [p, p + bytes) by one lane (a hint: 16-byte granules, the
-// range widened to them; the arrays it reads carry 64 bytes of slack).
-__device__ __forceinline__ void prefetch_l2(const void* p, int64_t bytes) {
-  const uintptr_t a0 = reinterpret_cast<uintptr_t>(p) & ~uintptr_t(15);
-  const uintptr_t a1 = (reinterpret_cast<uintptr_t>(p) + (uintptr_t)bytes + 15) & ~uintptr_t(15);
-  for (uintptr_t q = a0; q < a1; q += (uintptr_t)1 << 20) {
-    const uint32_t n = (uint32_t)min((uintptr_t)1 << 20, a1 - q);
-    asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(q), "r"(n) : "memory");
-  }
-}
-
-// The next group's table and entries into L2 (lane 0).
-template <int FMT>
-__device__ __forceinline__ void prefetch_group(const GroupIterArgs& a, const GroupHead& P) {
-  const int64_t b = P.rp_end > 0 ? __shfl_sync(0xffffffffu, P.rp, 0) : 0;
-  if ((threadIdx.x & 31) != 0 || P.gd.r1 <= P.gd.r0) return;
-  prefetch_l2(a.table + P.gd.tb, (int64_t)P.gd.nd * 4);
-  const int64_t n = P.rp_end - b;
-  prefetch_l2(static_cast<const char*>(a.val) + b * (FMT == 0 ? 4 : 2), n * (FMT == 0 ? 4 : 2));
-  prefetch_l2(a.loc + b, n * 2);
-}
-
 template <int FMT>
 __device__ __forceinline__ void group_pass(const GroupIterArgs& a, const GroupHead& H, float* xs,
-                                           float* cs, int lane, bool has_next = false,
-                                           const GroupHead& next = GroupHead{}) {
+                                           float* cs, int lane) {
   const GroupDesc& gd = H.gd;
   const int nr = gd.r1 - gd.r0;         // <= 32
   const bool wide = gd.nd > kGroupCap;  // one row, its own columns as table
@@ -414,7 +391,6 @@ __device__ __forceinline__ void group_pass(const GroupIterArgs& a, const GroupHe
   for (int i = 0; i < nr; i += 2) {
     if (i + 1 < nr) load_row(i + 1, b1);
     process_row(i, b0);
-    if (i == 0 && has_next) prefetch_group<FMT>(a, next);  // (its head has arrived by now)
     if (i + 1 < nr) {
       if (i + 2 < nr) load_row(i + 2, b0);
       process_row(i + 1, b1);
@@ -447,9 +423,8 @@ k_group_mlem(GroupIterArgs a) {
     const GroupDesc nn =
         g + 2 * step < a.ngroups ? a.groups[g + 2 * step] : GroupDesc{0, 0, 0, 0};
     GroupHead head_next{};
-    const bool more = g + step < a.ngroups;
-    if (more) head_next = group_head<FMT>(a, nxt, lane);
-    group_pass<FMT>(a, cur, xs, cs, lane, more, head_next);
+    if (g + step < a.ngroups) head_next = group_head<FMT>(a, nxt, lane);
+    group_pass<FMT>(a, cur, xs, cs, lane);
     cur = head_next;
     nxt = nn;
   }
@@ -630,7 +605,7 @@ epet_status grouped_build(const epet_csr& A, int value_format, GroupedMatrix* G,
     if (e_ != cudaSuccess) return fail(cuda_status(e_, "grouped allocation " #ptr)); \
   } while (0)
   GALLOC(G->groups, hg.size() * sizeof(GroupDesc));
-  GALLOC(G->table, ns * 4 + 64);  // (slack: the L2 prefetch widens ranges to 16 bytes)
+  GALLOC(G->table, ns * 4);
   GALLOC(G->partial, ns * 4);
   GALLOC(G->ones, ns * 4);
   GALLOC(G->cg_ptr, (A.n + 1) * 8);
@@ -678,8 +653,8 @@ epet_status grouped_build(const epet_csr& A, int value_format, GroupedMatrix* G,
       if (e != cudaSuccess) rc = cuda_status(e, "padded layout");
     }
     if (rc == EPET_OK) {
-      cudaError_t e1 = dev_alloc((void**)&G->val32, std::max<int64_t>(G->npad, 4) * 4 + 64, st);
-      cudaError_t e2 = dev_alloc((void**)&G->loc, std::max<int64_t>(G->npad, 4) * 2 + 64, st);
+      cudaError_t e1 = dev_alloc((void**)&G->val32, std::max<int64_t>(G->npad, 4) * 4, st);
+      cudaError_t e2 = dev_alloc((void**)&G->loc, std::max<int64_t>(G->npad, 4) * 2, st);
       if (e1 != cudaSuccess || e2 != cudaSuccess)
         rc = cuda_status(e1 != cudaSuccess ? e1 : e2, "grouped allocation of the padded layout");
     }
@@ -729,7 +704,7 @@ epet_status grouped_build(const epet_csr& A, int value_format, GroupedMatrix* G,
     if (rc != EPET_OK) return fail(rc);
   }
   if (value_format != EPET_VALUES_FP32) {
-    GALLOC(G->val16, std::max<int64_t>(G->npad, 4) * 2 + 64);
+    GALLOC(G->val16, std::max<int64_t>(G->npad, 4) * 2);
     GALLOC(G->scale, std::max<int64_t>(A.m, 1) * 4);
     if (A.m > 0) {
       if (value_format == EPET_VALUES_BF16)
