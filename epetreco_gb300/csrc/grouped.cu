@@ -440,16 +440,37 @@ k_group_mlem_batch(const GroupIterArgs* __restrict__ desc, const int64_t* __rest
   float* xs = gsm + (size_t)w * 2 * kGroupStride;
   float* cs = xs + kGroupStride;
   const int64_t total = gstart[np];
-  for (int64_t g = (int64_t)blockIdx.x * kGroupWarps + w; g < total;
-       g += (int64_t)gridDim.x * kGroupWarps) {
-    int lo = 0, hi = np;  // gstart[lo] <= g < gstart[hi]
+  const int64_t step = (int64_t)gridDim.x * kGroupWarps;
+  auto locate = [&](int64_t g) {  // gstart[lo] <= g < gstart[lo + 1]
+    int lo = 0, hi = np;
     while (hi - lo > 1) {
       const int mid = (lo + hi) >> 1;
       if (__ldg(gstart + mid) <= g) lo = mid;
       else hi = mid;
     }
-    const GroupIterArgs& a = desc[lo];
-    group_pass<0>(a, group_head<0>(a, a.groups[g - gstart[lo]], lane), xs, cs, lane);
+    return lo;
+  };
+  int64_t g = (int64_t)blockIdx.x * kGroupWarps + w;
+  if (g >= total) return;
+  // the problem's descriptor held by value; the next group's problem and
+  // head loaded one group ahead
+  int p = locate(g);
+  GroupIterArgs a = desc[p];
+  GroupHead cur = group_head<0>(a, a.groups[g - gstart[p]], lane);
+  for (; g < total; g += step) {
+    int pn = p;
+    GroupHead hn{};
+    if (g + step < total) {
+      pn = locate(g + step);
+      const GroupIterArgs& an = desc[pn];
+      hn = group_head<0>(an, an.groups[g + step - gstart[pn]], lane);
+    }
+    group_pass<0>(a, cur, xs, cs, lane);
+    if (pn != p) {
+      p = pn;
+      a = desc[p];
+    }
+    cur = hn;
   }
 }
 

@@ -303,6 +303,11 @@ __global__ void k_scale_by_ratio(float* __restrict__ s, const float* __restrict_
   if (i < n && den[i] > 0.f) s[i] = __fmul_rn(s[i], __fdiv_rn(num[i], den[i]));
 }
 
+__global__ void k_fill_u16(uint16_t* x, int64_t n, uint16_t v) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) x[i] = v;
+}
+
 __global__ void k_fill(float* x, int64_t n, float v) {
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i < n) x[i] = v;
@@ -403,7 +408,12 @@ epet_status epet_mlem_create(const epet_problem* p, const int32_t* rows_d, const
   if (o.layout == EPET_LAYOUT_GROUPED && !grouped_ok)
     return fail(set_error(EPET_ERR_UNSUPPORTED, "grouped layout: %lld voxels (at most 819,200)",
                           (long long)V));
-  if (o.layout != EPET_LAYOUT_CSC && grouped_ok) {
+  // AUTO: the grouped layout for FP32 values; the 16-bit forms keep the
+  // CSR and the column-major copy (their grouped pass is bound by shared
+  // memory, not by the bytes it saves, and runs slower)
+  const bool want_grouped = o.layout == EPET_LAYOUT_GROUPED ||
+                            (o.layout == EPET_LAYOUT_AUTO && o.value_format == EPET_VALUES_FP32);
+  if (want_grouped && grouped_ok) {
     // the grouped layout replaces the column indices (and, for the 16-bit
     // forms, the FP32 values): the CSR's row pointers stay
     rc = grouped_build(h->A, o.value_format, &h->G, st);
@@ -489,6 +499,34 @@ epet_status epet_mlem_create(const epet_problem* p, const int32_t* rows_d, const
       ALLOC(j.dst->q, csr16_capacity(n16) * 2);
       j.dst->nnz = csr16_capacity(n16);
       rc = epet_csr_compress(j.src, o.value_format, j.dst, stream);
+      if (rc != EPET_OK) return fail(rc);
+    }
+    // The transpose product uses the 16-bit column-major values; scale s by
+    // the ratio of their column sums to the FP32 ones over the measured
+    // rows, so the update x*c/s does not drift by the rounding of the values
+    // (see the grouped layout above).
+    if (V > 0 && m > 0) {
+      float *ones = nullptr, *q = nullptr, *f = nullptr;
+      uint16_t* ones16 = nullptr;
+      ALLOC(ones, m * 4);
+      ALLOC(ones16, m * 2);
+      ALLOC(q, V * 4);
+      ALLOC(f, V * 4);
+      k_fill<<<ceil_div(m, 256), 256, 0, st>>>(ones, m, 1.f);
+      note_launch();
+      k_fill_u16<<<ceil_div(m, 256), 256, 0, st>>>(ones16, m, (uint16_t)0x3f80u);  // BF16 1.0
+      note_launch();
+      rc = launch_rows(default_plan((double)nnz / V), h->At.col_ptr, h->At.row, h->At.val, ones, V,
+                       EpiKeep{f}, nullptr, st);
+      if (rc == EPET_OK)
+        rc = launch_rows16<EpiKeep, uint16_t>(&h->At16, ones16, EpiKeep{q}, nullptr, st);
+      if (rc == EPET_OK) {
+        k_scale_by_ratio<<<ceil_div(V, 256), 256, 0, st>>>(h->s, q, f, V);
+        note_launch();
+        if (cudaGetLastError() != cudaSuccess) rc = set_error(EPET_ERR_CUDA, "sensitivity ratio");
+      }
+      EPET_CUDA(cudaStreamSynchronize(st));
+      for (void* b : {(void*)ones, (void*)ones16, (void*)q, (void*)f}) dev_free(b, st);
       if (rc != EPET_OK) return fail(rc);
     }
     EPET_CUDA(cudaStreamSynchronize(st));

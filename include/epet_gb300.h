@@ -399,8 +399,13 @@ typedef struct {
  * BF16/FP16); one pass over the entries per iteration gives A x, the ratio
  * and A^T e, the latter summed per column in a fixed order; supported up to
  * 819,200 voxels.  CSC: the CSR and its column-major copy (16 bytes per entry
- * in FP32), the transpose product over the copy.  AUTO: GROUPED where
- * supported, else CSC.  Both are deterministic. */
+ * in FP32), the transpose product over the copy.  AUTO: GROUPED for FP32
+ * values where supported, else CSC (the 16-bit forms run faster in CSC: their
+ * grouped pass is bound by shared memory).  Both are deterministic.  The
+ * 16-bit forms scale the sensitivity per column by the ratio of the column
+ * sums of the values their transpose product uses to the FP32 column sums
+ * (over the measured rows), so the iterations do not drift by the rounding
+ * of the values. */
 enum { EPET_LAYOUT_AUTO = 0, EPET_LAYOUT_GROUPED = 1, EPET_LAYOUT_CSC = 2 };
 
 /* Builds the system matrix for the measured rows (rows_d channel ids, in
