@@ -128,6 +128,14 @@ SIGNATURES = {
     "epet_mlem_batch_get_image": [VP, I32, VP, VP],
     "epet_mlem_batch_member": [VP, I32],
     "epet_mlem_batch_stats": [VP, C.POINTER(C.c_int64), C.POINTER(C.c_int64), VP],
+    "epet_h5_dataset_shape": [C.c_char_p, C.c_char_p, C.POINTER(C.c_int32),
+                              C.POINTER(C.c_int64)],
+    "epet_h5_read_f32": [C.c_char_p, C.c_char_p, VP, I64],
+    "epet_h5_read_measurement": [C.c_char_p, VP, VP, I64, C.POINTER(C.c_int64),
+                                 C.POINTER(C.c_int64)],
+    "epet_h5_write_measurement": [C.c_char_p, VP, I64],
+    "epet_h5_write_density": [C.c_char_p, VP, C.POINTER(Grid)],
+    "epet_h5_read_density": [C.c_char_p, VP, I64, C.POINTER(Grid)],
 }
 _RESTYPES = {
     "epet_last_error": C.c_char_p,

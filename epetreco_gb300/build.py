@@ -20,7 +20,7 @@ LIB = os.path.join(PKG, "libepet_gb300.so")
 RECO = os.path.join(PKG, "epet_reco")  # C++ driver over the drop-in header
 SOURCES = ["runtime.cu", "geometry.cu", "workqueue.cu", "sm_build.cu", "sort.cu",
            "spmv.cu", "mlem.cu", "compat.cu", "compress.cu", "tune.cu", "batch.cu",
-           "grouped.cu"]
+           "grouped.cu", "hdf5_io.cpp"]
 HEADERS = ["common.cuh", "internal.h", "spmv.cuh", "rows.cuh", "mlem_internal.h"]
 
 

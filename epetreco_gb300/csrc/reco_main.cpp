@@ -1,16 +1,20 @@
 // reco_main.cpp -- the reference's MLEM driver flow (reco.cu:32-332) written
 // against the drop-in header include/epet_gb300_shim.hpp, single process,
-// no MPI, raw float32 files instead of HDF5.
+// no MPI.
 //
-//   epet_reco <measurement.f32> <out> <nrays> <sensitivity.f32> <nIt>
-//             <guess.f32|-> <geometry>
+//   epet_reco <measurement> <out> <nrays> <sensitivity> <nIt> <guess|-> <geometry>
 //             [--matrix-once | --matrix-free | --csc-transpose]
 //
-// measurement: dense float[NCHANNELS] (the reference's "messung" dataset);
-// sensitivity, guess, output: float[V] in voxel-id order.  <geometry> is 20
-// comma-separated numbers: pos0x,pos1x,na,n0z,n0y,n1z,n1y,da,segx,segy,segz,
-// ox,oy,oz,dx,dy,dz,nx,ny,nz.  Writes "<it>_<out>" after every iteration as
-// reco.cu does (reco.cu:284-291).
+// Files named *.h5 / *.hdf5 are HDF5 as the reference's (read and written by
+// the library's own HDF5 code): the measurement is the dataset "messung"
+// (readHDF5_MeasVct, wrappers.hpp:311), sensitivity and guess the dataset
+// "density" (readHDF5_Density, wrappers.hpp:452), and the output the
+// "density" file of writeHDF5_Density (wrappers.hpp:398).  Other names are
+// raw float32 files: the measurement dense float[NCHANNELS], the images
+// float[V] in voxel-id order.  <geometry> is 20 comma-separated numbers:
+// pos0x,pos1x,na,n0z,n0y,n1z,n1y,da,segx,segy,segz, ox,oy,oz,dx,dy,dz,
+// nx,ny,nz.  Writes "<it>_<out>" after every iteration as reco.cu does
+// (reco.cu:284-291).
 //
 // Default: the reference's loop -- the system matrix of each row chunk is
 // rebuilt in every iteration (reco.cu:216-254).  --matrix-once: the library's
@@ -21,6 +25,7 @@
 // column-major copy (epetBuildTranspose) instead of atomics.
 #include <cstdio>
 #include <cstdlib>
+#include <cstring>
 #include <sstream>
 #include <string>
 #include <vector>
@@ -60,8 +65,28 @@ struct Setup {
 };
 struct RandRayGen {};  // the per-channel-seeded generator of the library
 
-std::vector<float> read_f32(const std::string& fn) {
+bool is_h5(const std::string& fn) {
+  for (const char* ext : {".h5", ".hdf5"}) {
+    const size_t n = strlen(ext);
+    if (fn.size() >= n && fn.compare(fn.size() - n, n, ext) == 0) return true;
+  }
+  return false;
+}
+
+// The whole dataset `name` of an HDF5 file, or a raw float32 file; empty if
+// the file cannot be read.
+std::vector<float> read_f32(const std::string& fn, const char* name) {
   std::vector<float> v;
+  if (is_h5(fn)) {
+    int32_t nd = 0;
+    int64_t dims[8];
+    if (epet_h5_dataset_shape(fn.c_str(), name, &nd, dims) != EPET_OK) return v;
+    int64_t n = 1;
+    for (int i = 0; i < nd; i++) n *= dims[i];
+    v.resize(n);
+    if (epet_h5_read_f32(fn.c_str(), name, v.data(), n) != EPET_OK) v.clear();
+    return v;
+  }
   FILE* f = fopen(fn.c_str(), "rb");
   if (!f) return v;
   fseek(f, 0, SEEK_END);
@@ -73,7 +98,8 @@ std::vector<float> read_f32(const std::string& fn) {
   return v;
 }
 
-bool write_f32(const std::string& fn, const std::vector<float>& v) {
+bool write_f32(const std::string& fn, const std::vector<float>& v, const epet_grid& g) {
+  if (is_h5(fn)) return epet_h5_write_density(fn.c_str(), v.data(), &g) == EPET_OK;
   FILE* f = fopen(fn.c_str(), "wb");
   if (!f) return false;
   bool ok = fwrite(v.data(), 4, v.size(), f) == v.size();
@@ -116,12 +142,15 @@ int main(int argc, char** argv) {
             {(float)g[14], (float)g[15], (float)g[16]},
             {(int)g[17], (int)g[18], (int)g[19]}};
   const int V = grid.n[0] * grid.n[1] * grid.n[2];
+  const epet_grid egrid{{grid.o[0], grid.o[1], grid.o[2]},
+                        {grid.d[0], grid.d[1], grid.d[2]},
+                        {grid.n[0], grid.n[1], grid.n[2]}};
   const long NCH = (long)setup.na_ * setup.n0z_ * setup.n0y_ * setup.n1z_ * setup.n1y_;
   try {
     epetSetConstantGeometry(grid, setup, nrays);
 
     // measurement -> (row ids ascending, values), zero channels dropped
-    std::vector<float> meas = read_f32(fn);
+    std::vector<float> meas = read_f32(fn, "messung");
     if ((long)meas.size() != NCH) {
       fprintf(stderr, "measurement must hold %ld floats\n", NCH);
       return EXIT_FAILURE;
@@ -142,7 +171,7 @@ int main(int argc, char** argv) {
     CK(cudaMemcpy(yVal_devi, yVal.data(), sizeof(float) * effM, cudaMemcpyHostToDevice));
 
     // density guess or homogeneous, normalised (reco.cu:113-137)
-    std::vector<float> x_host = read_f32(xfn);
+    std::vector<float> x_host = read_f32(xfn, "density");
     const bool xgood = (int)x_host.size() == V;
     if (!xgood) x_host.assign(V, 1.f);
     float* x_devi = nullptr;
@@ -153,7 +182,7 @@ int main(int argc, char** argv) {
       scales<float>(x_devi, (float)(1. / norm), V);
     }
     // sensitivity, normalised (reco.cu:150-183)
-    std::vector<float> s_host = read_f32(sfn);
+    std::vector<float> s_host = read_f32(sfn, "density");
     if ((int)s_host.size() != V) {
       fprintf(stderr, "sensitivity must hold %d floats\n", V);
       return EXIT_FAILURE;
@@ -181,7 +210,7 @@ int main(int argc, char** argv) {
         CK(cudaMemcpy(x_host.data(), x_devi, sizeof(float) * V, cudaMemcpyDeviceToHost));
         std::stringstream ss;
         ss << it;
-        write_f32(ss.str() + "_" + on, x_host);
+        write_f32(ss.str() + "_" + on, x_host, egrid);
         printf("it %d loglik %.9g\n", it, ll);
       }
       epet_mlem_destroy(h);
@@ -240,7 +269,7 @@ int main(int argc, char** argv) {
       CK(cudaMemcpy(x_host.data(), x_devi, sizeof(float) * V, cudaMemcpyDeviceToHost));
       std::stringstream ss;
       ss << it;
-      write_f32(ss.str() + "_" + on, x_host);
+      write_f32(ss.str() + "_" + on, x_host, egrid);
       printf("it %d norm %.9g\n", it, (double)sum<float>(x_devi, V));
     }
     return 0;

@@ -374,7 +374,8 @@ epet_status epet_trim_memory(size_t keep_bytes);
 
 /* ---------------------------------------------------------- MLEM driver */
 /* One reconstruction (reco.cu:209-281) held on the device: measured rows,
- * their counts, the system matrix (CSR + CSC), sensitivity and image. */
+ * their counts, the system matrix (in the layout of opt->layout, or none
+ * with opt->matrix_free), sensitivity and image. */
 typedef struct epet_mlem epet_mlem;
 
 typedef struct {
@@ -481,6 +482,42 @@ epet_mlem* epet_mlem_batch_member(epet_mlem_batch* h, int32_t i);
 /* Totals over the problems; plan_h as epet_mlem_plan (may be NULL). */
 epet_status epet_mlem_batch_stats(const epet_mlem_batch* h, int64_t* nnz_h,
                                   int64_t* bytes_per_iter_h, int32_t plan_h[6]);
+
+/* ---------------------------------------------------------------- HDF5 files
+ * The reference's file formats without libhdf5 (host code, host buffers).
+ * Reading: superblocks of version 0-3, groups as symbol tables or compact
+ * links, datasets with contiguous or compact storage of IEEE floats or
+ * integers of either byte order (converted to float); other files return
+ * EPET_ERR_UNSUPPORTED.  Writing: superblock 0, the root group as a symbol
+ * table, one contiguous little-endian float dataset, as libhdf5 writes it. */
+
+/* Shape of dataset `name` ("a/b" for nested groups): *ndims_h and up to 8
+ * entries of dims_h (either may be NULL). */
+epet_status epet_h5_dataset_shape(const char* path, const char* name, int32_t* ndims_h,
+                                  int64_t* dims_h);
+/* All n elements of dataset `name` as float, in the file's (row-major)
+ * order; EPET_ERR_CAPACITY if n is not its element count.  H5Reader::read
+ * (H5Reader.hpp:39-70) reads the measurement "messung" this way. */
+epet_status epet_h5_read_f32(const char* path, const char* name, float* out_h, int64_t n);
+/* readHDF5_MeasVct (wrappers.hpp:311-333): the channels of "messung" whose
+ * value is not zero, ascending, as row ids rows_h and values y_h (up to
+ * `capacity` of each); *m_h = their number, *nchannels_h = the dataset's
+ * element count (either may be NULL).  With rows_h or y_h NULL only the
+ * counts are returned; EPET_ERR_CAPACITY when m > capacity. */
+epet_status epet_h5_read_measurement(const char* path, int32_t* rows_h, float* y_h,
+                                     int64_t capacity, int64_t* m_h, int64_t* nchannels_h);
+/* A measurement file: the 1-D float dataset "messung" of n counts (the
+ * reference reads it through H5Reader.hpp:16; it has no writer for it). */
+epet_status epet_h5_write_measurement(const char* path, const float* y_h, int64_t n);
+/* H5DensityWriter::write (H5DensityWriter.hpp:140-199): the 3-D float
+ * dataset "density" [n0][n1][n2] of the image x_h (voxel (i,j,k) at
+ * i*n1*n2 + j*n2 + k, the library's order) with float attributes xmin, ymin,
+ * zmin (= grid->o) and xmax, ymax, zmax (= o + n * d), int attributes xnbin,
+ * ynbin, znbin. */
+epet_status epet_h5_write_density(const char* path, const float* x_h, const epet_grid* grid);
+/* Reads a "density" file: the image (n elements; x_h may be NULL) and the
+ * grid from its attributes (pitch = (max - min) / nbin; grid_h may be NULL). */
+epet_status epet_h5_read_density(const char* path, float* x_h, int64_t n, epet_grid* grid_h);
 
 #ifdef __cplusplus
 }

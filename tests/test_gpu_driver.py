@@ -75,3 +75,26 @@ def test_driver_other_schedules_match_library(inputs, mode):
     R.iterate(2)
     x = R.image().cpu().numpy()
     assert np.linalg.norm(x_drv - x) / np.linalg.norm(x) < 1e-5
+
+
+def test_driver_hdf5_files_match_raw_files(inputs):
+    """The reference's file formats: the measurement as "messung", the
+    sensitivity as a "density" file, each iteration's image written as a
+    "density" file with the grid's attributes; the images equal the raw-file
+    run's bit for bit."""
+    from epetreco_gb300 import h5
+    p, rows, y, s, d, exe = inputs
+    dense = np.fromfile(d / "meas.f32", np.float32)
+    h5.write_measurement(d / "meas.h5", dense)
+    h5.writeHDF5_Density(s.cpu().numpy(), d / "sens.h5", p.grid)
+    nit = 2
+    cmd = [exe, str(d / "meas.h5"), "img.h5", str(p.nrays), str(d / "sens.h5"), str(nit), "-",
+           geometry_arg(p), "--matrix-once"]
+    r = subprocess.run(cmd, cwd=d, capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stderr
+    x_raw = run_driver(exe, d, p, nit, ["--matrix-once"])
+    for it in range(nit):
+        x, g = h5.read_density(d / f"{it}_img.h5")
+        assert x.shape == tuple(p.grid.n) and g.n == tuple(p.grid.n)
+        assert np.array_equal(np.float32(g.origin), np.float32(p.grid.origin))
+    assert np.array_equal(x.ravel(), x_raw)
