@@ -40,11 +40,16 @@ namespace epet {
 constexpr int kGroupFirstRows = 32;  // rows of a first-cut group (split while too wide)
 constexpr int kGroupThreads = 256;   // threads of the table-building kernels
 constexpr int kTrash = kGroupCap;    // rank of the padding entries
-// Shared tables are indexed by swizzled ranks, sw(r) = r + r / 32: the ranks
-// of a chunk's entries across a warp's lanes step by a few (a row's columns
-// ascend), and the added r / 32 breaks the regular bank pattern.  The
-// layout stores swizzled ranks, so the pass indexes with them directly.
-__host__ __device__ constexpr int sw_rank(int r) { return r + (r >> 5); }
+// Shared tables are indexed by rank (the word of rank r sits in bank r % 32).
+// A row's entries are stored so that each warp-wide shared access of the
+// pass takes 32 consecutive entries of the row (group_slot): their ranks
+// ascend by a few, which spreads them over the banks better than the fixed
+// swizzles of the ranks tried: 2.05 distinct-address wavefronts per 32
+// entries on rows of the full workload, against 2.94 with a lane taking 4
+// consecutive entries and the ranks swizzled as r + r / 32 (the pass 7 %
+// faster).  A layout balancing each row over the banks (1.27 wavefronts)
+// was no faster: the pass is bound by the latency of its entry stream.
+__host__ __device__ constexpr int sw_rank(int r) { return r; }
 constexpr int kGroupStride = sw_rank(kGroupCap) + 4;  // floats per shared table (trash included)
 constexpr size_t kGroupSmem = (size_t)kGroupWarps * 2 * kGroupStride * 4;
 static_assert(kGroupSmem <= 227 * 1024, "grouped tables exceed shared memory");
@@ -138,10 +143,24 @@ k_group_tables(const int64_t* __restrict__ row_ptr, const int32_t* __restrict__ 
   }
 }
 
+// Storage position of a row's j-th entry (its CSR order, then padding) in a
+// row of nq 4-entry chunks.  The pass hands chunk 32 u + l to lane l in
+// round u and reads position t of every lane's chunk with one shared access:
+// the entries are placed so that this access takes consecutive entries,
+// i.e. round u (cq = min(32, nq - 32 u) chunks) holds its entries o =
+// t * cq + l at chunk l, position t.
+__host__ __device__ inline int group_slot(int j, int nq) {
+  const int u = j >> 7, o = j & 127;
+  const int cq = nq - 32 * u < 32 ? nq - 32 * u : 32;
+  const int t = (o >= cq) + (o >= 2 * cq) + (o >= 3 * cq);  // o < 4 cq
+  return 128 * u + 4 * (o - t * cq) + t;
+}
+
 // The padded layout, a warp per row: row r's entries at ptr[r] (a multiple
 // of 4) onwards, then zero values up to the next multiple of 4 with the
-// trash rank (a wide group's padding points past its row in its table);
-// ranks stored swizzled.
+// trash rank, in the order of group_slot.  A row wider than the shared
+// tables (its own group, its own columns as the table) keeps the CSR order:
+// its padding points past its row in its table.
 __global__ void k_group_pad(const int64_t* __restrict__ row_ptr, const float* __restrict__ val,
                             const uint16_t* __restrict__ rank, const int64_t* __restrict__ ptr,
                             int64_t m, float* __restrict__ pval, uint16_t* __restrict__ ploc) {
@@ -149,9 +168,11 @@ __global__ void k_group_pad(const int64_t* __restrict__ row_ptr, const float* __
   const int lane = threadIdx.x & 31;
   if (r >= m) return;
   const int64_t b = row_ptr[r], n = row_ptr[r + 1] - b, d = ptr[r], pn = ptr[r + 1] - d;
+  const bool wide = n > kGroupCap;
   for (int64_t j = lane; j < pn; j += 32) {
-    pval[d + j] = j < n ? val[b + j] : 0.f;
-    ploc[d + j] = (uint16_t)sw_rank(j < n ? (int)rank[b + j] : kTrash);
+    const int64_t k = wide ? j : group_slot((int)j, (int)(pn >> 2));  // (pn <= kGroupCap + 3)
+    pval[d + k] = j < n ? val[b + j] : 0.f;
+    ploc[d + k] = (uint16_t)sw_rank(j < n ? (int)rank[b + j] : kTrash);
   }
 }
 
