@@ -87,14 +87,16 @@ struct WalkArgs {
 // window cell and of the two trash cells (8 bytes per cell): a channel needs
 // columns + cells + 2 <= cap_cells.
 struct WalkLayout {
-  size_t planes, ztab, pool, pext, slabs, total;
+  size_t planes, ztab, pool, pext, lines, slabs, total;
 };
+constexpr int kHullLines = 64;  // crystal-corner pair lines of the hull
 // nplanes: grid planes of all three axes (n0 + n1 + n2 + 3); nz: z cells.
-// The pool holds the column table and the cells.  Two arrays that die early
-// share it: the hull extents at the slab planes (pext, at its start) are
-// read only while the slab windows are built, and the slab windows (slabs,
-// at its end) only until the column table is built, so the table must end
-// before them and the cells, written afterwards, may run over them.
+// The pool holds the column table and the cells.  Three arrays that die
+// early share it: the hull extents at the slab planes (pext, at its start)
+// and the hull lines' parameters after them are read only while the slab
+// windows are built, and the slab windows (slabs, at its end) only until the
+// column table is built, so the table must end before them and the cells,
+// written afterwards, may run over them.
 __host__ __device__ inline WalkLayout walk_layout(int nslab, int nplanes, int nz, int cap_cells) {
   WalkLayout L;
   L.planes = 0;
@@ -102,10 +104,12 @@ __host__ __device__ inline WalkLayout walk_layout(int nslab, int nplanes, int nz
   L.pool = L.ztab + align256((size_t)nz * 8);
   const size_t pext_b = ((size_t)(nslab + 1) * 16 + 15) & ~size_t(15);
   const size_t slab_b = ((size_t)20 * nslab + 15) & ~size_t(15);
+  const size_t line_b = (size_t)6 * kHullLines * 4;
   size_t pool_b = (size_t)cap_cells * 8;
-  if (pool_b < pext_b + slab_b) pool_b = pext_b + slab_b;
+  if (pool_b < pext_b + line_b + slab_b) pool_b = pext_b + line_b + slab_b;
   pool_b = (pool_b + 15) & ~size_t(15);
   L.pext = L.pool;
+  L.lines = L.pool + pext_b;
   L.slabs = L.pool + pool_b - slab_b;
   L.total = L.pool + align256(pool_b);
   return L;
@@ -495,60 +499,77 @@ k_walk(WalkArgs args) {
   const int pa = sa == 0 ? 1 : 0, qa = sa == 0 ? 2 : 1;
   const int ns = g.n[sa];  // slabs
 
-  // ---- hull cross-section at every x plane: warp per plane, lanes over
-  // the 64 crystal-corner pair lines
+  // ---- hull cross-section at every slab plane: the 64 crystal-corner pair
+  // lines' parameters in shared memory (a thread per line), then two threads
+  // per plane, each taking the extremes over 32 of the lines, combined with
+  // one shuffle
   int4* pext = reinterpret_cast<int4*>(smem + lay.pext);
   {
-    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    float ax[2], ay[2], az[2], inv[2], dy[2], dz[2];
-    bool ok[2];
-    // per lane two pair lines, in (slab axis, p axis, q axis) coordinates
-    for (int q = 0; q < 2; q++) {
-      const int pidx = lane + 32 * q, a = pidx >> 3, b = pidx & 7;
-      ax[q] = c0[a][sa]; ay[q] = c0[a][pa]; az[q] = c0[a][qa];
-      const float dx = c1[b][sa] - ax[q];
-      ok[q] = dx != 0.f;
-      inv[q] = ok[q] ? __frcp_rn(dx) : 0.f;
-      dy[q] = c1[b][pa] - ay[q];
-      dz[q] = c1[b][qa] - az[q];
-    }
-    // t is monotone in the plane position: when every line meets the first
-    // and the last plane within its segment it meets all of them (the usual
-    // case, the grid lying between the heads), and the per-plane tests drop
-    bool span = true;
-    {
+    constexpr int kLines = kHullLines;
+    // ax, ay, az, inv (0: parallel to the planes), dy, dz of each line
+    float(*s_line)[kLines] = reinterpret_cast<float(*)[kLines]>(smem + lay.lines);
+    __shared__ int s_nospan;
+    if (threadIdx.x == 0) s_nospan = 0;
+    __syncthreads();
+    if (threadIdx.x < kLines) {
+      const int a = threadIdx.x >> 3, b = threadIdx.x & 7;
+      const float ax = c0[a][sa], ay = c0[a][pa], az = c0[a][qa];
+      const float dx = c1[b][sa] - ax;
+      const bool ok = dx != 0.f;
+      const float inv = ok ? __frcp_rn(dx) : 0.f;
+      s_line[0][threadIdx.x] = ax;
+      s_line[1][threadIdx.x] = ay;
+      s_line[2][threadIdx.x] = az;
+      s_line[3][threadIdx.x] = inv;
+      s_line[4][threadIdx.x] = c1[b][pa] - ay;
+      s_line[5][threadIdx.x] = c1[b][qa] - az;
+      // t is monotone in the plane position: when every line meets the
+      // first and the last plane within its segment it meets all of them
+      // (the usual case, the grid lying between the heads), and the
+      // per-plane tests drop
       const float X0 = voxel_plane(g, sa, 0), X1 = voxel_plane(g, sa, ns);
-      for (int q = 0; q < 2; q++) {
-        const float t0 = (X0 - ax[q]) * inv[q], t1 = (X1 - ax[q]) * inv[q];
-        span = span && ok[q] && t0 >= 0.f && t0 <= 1.f && t1 >= 0.f && t1 <= 1.f;
-      }
+      const float t0 = (X0 - ax) * inv, t1 = (X1 - ax) * inv;
+      if (!(ok && t0 >= 0.f && t0 <= 1.f && t1 >= 0.f && t1 <= 1.f)) s_nospan = 1;
     }
-    const bool all_span = __all_sync(0xffffffffu, span);
-    for (int k = w; k <= ns; k += kWalkThreads / 32) {
-      const float X = voxel_plane(g, sa, k);
-      int ylo = INT_MAX, yhi = INT_MIN, zlo = INT_MAX, zhi = INT_MIN;
+    __syncthreads();
+    const bool all_span = s_nospan == 0;
+    const int half = threadIdx.x & 1, l0 = half * (kLines / 2);
+    for (int k0 = 0; k0 <= ns; k0 += kWalkThreads / 2) {
+      const int k = k0 + (threadIdx.x >> 1);
+      const float X = voxel_plane(g, sa, min(k, ns));
+      float ylo = INFINITY, yhi = -INFINITY, zlo = INFINITY, zhi = -INFINITY;
+      bool any = false;
       if (all_span) {
-        for (int q = 0; q < 2; q++) {
-          const float t = (X - ax[q]) * inv[q];
-          const int ky = fkey(ay[q] + t * dy[q]), kz = fkey(az[q] + t * dz[q]);
-          ylo = min(ylo, ky); yhi = max(yhi, ky);
-          zlo = min(zlo, kz); zhi = max(zhi, kz);
+#pragma unroll 8
+        for (int l = l0; l < l0 + kLines / 2; l++) {
+          const float t = (X - s_line[0][l]) * s_line[3][l];
+          const float y = s_line[1][l] + t * s_line[4][l], z = s_line[2][l] + t * s_line[5][l];
+          ylo = fminf(ylo, y); yhi = fmaxf(yhi, y);
+          zlo = fminf(zlo, z); zhi = fmaxf(zhi, z);
         }
+        any = true;
       } else {
-        for (int q = 0; q < 2; q++) {
-          const float t = (X - ax[q]) * inv[q];
-          if (ok[q] && t >= 0.f && t <= 1.f) {
-            const int ky = fkey(ay[q] + t * dy[q]), kz = fkey(az[q] + t * dz[q]);
-            ylo = min(ylo, ky); yhi = max(yhi, ky);
-            zlo = min(zlo, kz); zhi = max(zhi, kz);
+        for (int l = l0; l < l0 + kLines / 2; l++) {
+          const float inv = s_line[3][l];
+          const float t = (X - s_line[0][l]) * inv;
+          if (inv != 0.f && t >= 0.f && t <= 1.f) {
+            const float y = s_line[1][l] + t * s_line[4][l], z = s_line[2][l] + t * s_line[5][l];
+            ylo = fminf(ylo, y); yhi = fmaxf(yhi, y);
+            zlo = fminf(zlo, z); zhi = fmaxf(zhi, z);
+            any = true;
           }
         }
       }
-      ylo = __reduce_min_sync(0xffffffffu, ylo);
-      yhi = __reduce_max_sync(0xffffffffu, yhi);
-      zlo = __reduce_min_sync(0xffffffffu, zlo);
-      zhi = __reduce_max_sync(0xffffffffu, zhi);
-      if (lane == 0) pext[k] = make_int4(ylo, yhi, zlo, zhi);
+      ylo = fminf(ylo, __shfl_xor_sync(0xffffffffu, ylo, 1));
+      yhi = fmaxf(yhi, __shfl_xor_sync(0xffffffffu, yhi, 1));
+      zlo = fminf(zlo, __shfl_xor_sync(0xffffffffu, zlo, 1));
+      zhi = fmaxf(zhi, __shfl_xor_sync(0xffffffffu, zhi, 1));
+      // (every lane takes part in the shuffle: no short-circuit around it)
+      const int any_pair = __shfl_xor_sync(0xffffffffu, (int)any, 1);
+      any = any || any_pair != 0;
+      if (half == 0 && k <= ns)
+        pext[k] = any ? make_int4(fkey(ylo), fkey(yhi), fkey(zlo), fkey(zhi))
+                      : make_int4(INT_MAX, INT_MIN, INT_MAX, INT_MIN);
     }
   }
   __syncthreads();
