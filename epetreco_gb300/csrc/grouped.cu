@@ -54,20 +54,66 @@ constexpr int kGroupStride = sw_rank(kGroupCap) + 4;  // floats per shared table
 constexpr size_t kGroupSmem = (size_t)kGroupWarps * 2 * kGroupStride * 4;
 static_assert(kGroupSmem <= 227 * 1024, "grouped tables exceed shared memory");
 
+// Row r of the source: its columns and values, and its length.
+struct RowSpan {
+  const int32_t* col;
+  const float* val;
+  int64_t n;
+};
+__device__ __forceinline__ RowSpan row_span(const RowSource& A, int64_t r) {
+  if (A.segs) {
+    const int64_t q = A.idx[r];
+    const SegDev sg = A.segs[q / A.ch];
+    const int64_t b = A.rp[q] - sg.e0;
+    return RowSpan{sg.col + b, sg.val + b, A.rp[q + 1] - A.rp[q]};
+  }
+  const int64_t b = A.rp[r];
+  return RowSpan{A.col + b, A.val + b, A.rp[r + 1] - b};
+}
+
+// The spans of rows r0 .. r1 - 1 (at most kGroupFirstRows) in shared memory,
+// with their exclusive prefix off[] (off[nr] = the group's entries); the
+// loads run in parallel, a thread per row.  Ends with a block barrier.
+struct GroupSpans {
+  const int32_t* col[kGroupFirstRows];
+  const float* val[kGroupFirstRows];
+  int off[kGroupFirstRows + 1];
+};
+__device__ __forceinline__ void load_spans(const RowSource& A, int r0, int r1, GroupSpans* S) {
+  const int nr = r1 - r0;
+  int n = 0;
+  if ((int)threadIdx.x < nr) {
+    const RowSpan rs = row_span(A, r0 + threadIdx.x);
+    S->col[threadIdx.x] = rs.col;
+    S->val[threadIdx.x] = rs.val;
+    n = (int)rs.n;
+  }
+  if (threadIdx.x < 32) {  // nr <= 32: one warp's scan
+    const int inc = warp_incl_scan(n);
+    if ((int)threadIdx.x < nr) S->off[threadIdx.x + 1] = inc;
+    if (threadIdx.x == 0) S->off[0] = 0;
+  }
+  __syncthreads();
+}
+
 // Distinct columns of the candidate groups cand[g] = {r0, r1}: a bitmap over
 // the columns in shared memory (nwords 32-bit words).
 __global__ void __launch_bounds__(kGroupThreads)
-k_group_distinct(const int64_t* __restrict__ row_ptr, const int32_t* __restrict__ col,
-                 const int2* __restrict__ cand, int nwords, int32_t* __restrict__ nd) {
+k_group_distinct(RowSource A, const int2* __restrict__ cand, int nwords,
+                 int32_t* __restrict__ nd) {
   extern __shared__ unsigned gbm[];
   __shared__ int wsum[kGroupThreads / 32];
+  __shared__ GroupSpans S;
   for (int i = threadIdx.x; i < nwords; i += kGroupThreads) gbm[i] = 0u;
-  __syncthreads();
   const int2 c = cand[blockIdx.x];
-  const int64_t b = row_ptr[c.x], e = row_ptr[c.y];
-  for (int64_t k = b + threadIdx.x; k < e; k += kGroupThreads) {
-    const unsigned v = (unsigned)col[k];
-    atomicOr(&gbm[v >> 5], 1u << (v & 31));
+  load_spans(A, c.x, c.y, &S);
+  {
+    int r = 0;
+    for (int k = threadIdx.x; k < S.off[c.y - c.x]; k += kGroupThreads) {
+      while (S.off[r + 1] <= k) r++;  // k ascends per thread: the row only moves forward
+      const unsigned v = (unsigned)S.col[r][k - S.off[r]];
+      atomicOr(&gbm[v >> 5], 1u << (v & 31));
+    }
   }
   __syncthreads();
   int n = 0;
@@ -82,31 +128,59 @@ k_group_distinct(const int64_t* __restrict__ row_ptr, const int32_t* __restrict_
   }
 }
 
-// Tables of the final groups (one block per group): the group's distinct
-// columns, ascending, at table[tb ..], and each entry's rank among them
-// (rank[k] for the CSR's entry k).  A single row wider than the shared
-// tables (a "wide" group) keeps its own columns as its table, padded like
-// the row with column 0 (the padding values are zero).
+// Storage position of a row's j-th entry (its CSR order, then padding) in a
+// row of nq 4-entry chunks.  The pass hands chunk 32 u + l to lane l in
+// round u and reads position t of every lane's chunk with one shared access:
+// the entries are placed so that this access takes consecutive entries,
+// i.e. round u (cq = min(32, nq - 32 u) chunks) holds its entries o =
+// t * cq + l at chunk l, position t.
+__host__ __device__ inline int group_slot(int j, int nq) {
+  const int u = j >> 7, o = j & 127;
+  const int cq = nq - 32 * u < 32 ? nq - 32 * u : 32;
+  const int t = (o >= cq) + (o >= 2 * cq) + (o >= 3 * cq);  // o < 4 cq
+  return 128 * u + 4 * (o - t * cq) + t;
+}
+
+// Tables and the padded layout of the final groups (one block per group):
+// the group's distinct columns, ascending, at table[tb ..]; every row r's
+// entries at ptr[r] (a multiple of 4) onwards in the order of group_slot,
+// each as its value and its column's rank among the group's columns, then
+// zero values on the trash rank up to the next multiple of 4.  A single row
+// wider than the shared tables (a "wide" group) keeps its own columns as its
+// table (padded like the row with column 0) and the CSR order; its padding
+// points past the row in that table.
 __global__ void __launch_bounds__(kGroupThreads)
-k_group_tables(const int64_t* __restrict__ row_ptr, const int32_t* __restrict__ col,
-               const GroupDesc* __restrict__ groups, int nwords, int32_t* __restrict__ table,
-               uint16_t* __restrict__ rank) {
+k_group_tables(RowSource A, const GroupDesc* __restrict__ groups, int nwords,
+               const int64_t* __restrict__ ptr, int32_t* __restrict__ table,
+               float* __restrict__ pval, uint16_t* __restrict__ ploc) {
   extern __shared__ unsigned gsh[];
   unsigned* bm = gsh;
   int* pre = reinterpret_cast<int*>(gsh + nwords);
   __shared__ int wtot[kGroupThreads / 32];
   const GroupDesc gd = groups[blockIdx.x];
-  const int64_t b = row_ptr[gd.r0], e = row_ptr[gd.r1];
-  if (gd.nd > kGroupCap) {
+  if (gd.nd > kGroupCap) {  // wide: one row
+    const RowSpan rs = row_span(A, gd.r0);
+    const int64_t d = ptr[gd.r0], pn = ptr[gd.r0 + 1] - d;
     for (int64_t j = threadIdx.x; j < gd.nd; j += kGroupThreads)
-      table[gd.tb + j] = b + j < e ? col[b + j] : 0;
+      table[gd.tb + j] = j < rs.n ? rs.col[j] : 0;
+    for (int64_t j = threadIdx.x; j < pn; j += kGroupThreads) {
+      pval[d + j] = j < rs.n ? rs.val[j] : 0.f;
+      ploc[d + j] = 0;  // (unused: a wide row reads its table by position)
+    }
     return;
   }
+  __shared__ GroupSpans S;
+  const int nr = gd.r1 - gd.r0;
   for (int i = threadIdx.x; i < nwords; i += kGroupThreads) bm[i] = 0u;
-  __syncthreads();
-  for (int64_t k = b + threadIdx.x; k < e; k += kGroupThreads) {
-    const unsigned v = (unsigned)col[k];
-    atomicOr(&bm[v >> 5], 1u << (v & 31));
+  load_spans(A, gd.r0, gd.r1, &S);
+  const int ntot = S.off[nr];
+  {
+    int r = 0;
+    for (int k = threadIdx.x; k < ntot; k += kGroupThreads) {
+      while (S.off[r + 1] <= k) r++;
+      const unsigned v = (unsigned)S.col[r][k - S.off[r]];
+      atomicOr(&bm[v >> 5], 1u << (v & 31));
+    }
   }
   __syncthreads();
   // exclusive prefix of the words' popcounts: thread t owns a contiguous
@@ -137,49 +211,40 @@ k_group_tables(const int64_t* __restrict__ row_ptr, const int32_t* __restrict__ 
     }
   }
   __syncthreads();
-  for (int64_t k = b + threadIdx.x; k < e; k += kGroupThreads) {
-    const unsigned v = (unsigned)col[k];
-    rank[k] = (uint16_t)(pre[v >> 5] + __popc(bm[v >> 5] & ((1u << (v & 31)) - 1u)));
+  // the entries (thread-strided over the group's entries, each finding its
+  // row), then the rows' padding (at most 3 entries a row)
+  {
+    int r = 0;
+    for (int k = threadIdx.x; k < ntot; k += kGroupThreads) {
+      while (S.off[r + 1] <= k) r++;
+      const int j = k - S.off[r];
+      const int64_t d = ptr[gd.r0 + r];
+      const int nq = (int)((ptr[gd.r0 + r + 1] - d) >> 2);
+      const unsigned v = (unsigned)S.col[r][j];
+      const int64_t o = d + group_slot(j, nq);
+      pval[o] = S.val[r][j];
+      ploc[o] = (uint16_t)sw_rank(pre[v >> 5] + __popc(bm[v >> 5] & ((1u << (v & 31)) - 1u)));
+    }
+  }
+  for (int t = threadIdx.x; t < 4 * nr; t += kGroupThreads) {
+    const int rr = t >> 2;
+    const int n = S.off[rr + 1] - S.off[rr];
+    const int64_t d = ptr[gd.r0 + rr];
+    const int pn = (int)(ptr[gd.r0 + rr + 1] - d);
+    const int j = n + (t & 3);
+    if (j < pn) {
+      const int64_t o = d + group_slot(j, pn >> 2);
+      pval[o] = 0.f;
+      ploc[o] = (uint16_t)sw_rank(kTrash);
+    }
   }
 }
 
-// Storage position of a row's j-th entry (its CSR order, then padding) in a
-// row of nq 4-entry chunks.  The pass hands chunk 32 u + l to lane l in
-// round u and reads position t of every lane's chunk with one shared access:
-// the entries are placed so that this access takes consecutive entries,
-// i.e. round u (cq = min(32, nq - 32 u) chunks) holds its entries o =
-// t * cq + l at chunk l, position t.
-__host__ __device__ inline int group_slot(int j, int nq) {
-  const int u = j >> 7, o = j & 127;
-  const int cq = nq - 32 * u < 32 ? nq - 32 * u : 32;
-  const int t = (o >= cq) + (o >= 2 * cq) + (o >= 3 * cq);  // o < 4 cq
-  return 128 * u + 4 * (o - t * cq) + t;
-}
-
-// The padded layout, a warp per row: row r's entries at ptr[r] (a multiple
-// of 4) onwards, then zero values up to the next multiple of 4 with the
-// trash rank, in the order of group_slot.  A row wider than the shared
-// tables (its own group, its own columns as the table) keeps the CSR order:
-// its padding points past its row in its table.
-__global__ void k_group_pad(const int64_t* __restrict__ row_ptr, const float* __restrict__ val,
-                            const uint16_t* __restrict__ rank, const int64_t* __restrict__ ptr,
-                            int64_t m, float* __restrict__ pval, uint16_t* __restrict__ ploc) {
-  const int64_t r = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  const int lane = threadIdx.x & 31;
-  if (r >= m) return;
-  const int64_t b = row_ptr[r], n = row_ptr[r + 1] - b, d = ptr[r], pn = ptr[r + 1] - d;
-  const bool wide = n > kGroupCap;
-  for (int64_t j = lane; j < pn; j += 32) {
-    const int64_t k = wide ? j : group_slot((int)j, (int)(pn >> 2));  // (pn <= kGroupCap + 3)
-    pval[d + k] = j < n ? val[b + j] : 0.f;
-    ploc[d + k] = (uint16_t)sw_rank(j < n ? (int)rank[b + j] : kTrash);
-  }
-}
-
-__global__ void k_padded_len(const int64_t* __restrict__ row_ptr, int64_t m,
-                             int64_t* __restrict__ len) {
+__global__ void k_padded_len(RowSource A, int64_t m, int64_t* __restrict__ len) {
   const int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (r < m) len[r] = (row_ptr[r + 1] - row_ptr[r] + 3) & ~int64_t(3);
+  if (r >= m) return;
+  const int64_t q = A.segs ? A.idx[r] : r;
+  len[r] = (A.rp[q + 1] - A.rp[q] + 3) & ~int64_t(3);
 }
 
 __global__ void k_slot_ids(int64_t n, float* __restrict__ out) {  // slot index bits
@@ -560,9 +625,9 @@ void grouped_drop_fp32(GroupedMatrix* G, cudaStream_t st) {
 // distinct columns fit kGroupCap: first cuts of kGroupFirstRows rows, halved
 // while too wide; a single row wider than that is a group of its own, its
 // table the row's columns padded to whole 4-entry chunks.
-static epet_status form_groups(const epet_csr& A, std::vector<GroupDesc>* out, cudaStream_t st) {
-  const int64_t m = A.m;
-  const int nwords = bitmap_words(A.n);
+static epet_status form_groups(const RowSource& A, int64_t m, int64_t ncols,
+                               std::vector<GroupDesc>* out, cudaStream_t st) {
+  const int nwords = bitmap_words(ncols);
   struct Piece {
     int32_t r0, r1, nd;  // nd < 0: not measured yet
   };
@@ -587,8 +652,7 @@ static epet_status form_groups(const epet_csr& A, std::vector<GroupDesc>* out, c
     if (e == cudaSuccess)
       e = cudaMemcpyAsync(cand, hc.data(), n * sizeof(int2), cudaMemcpyHostToDevice, st);
     if (e == cudaSuccess) {
-      k_group_distinct<<<(unsigned)n, kGroupThreads, nwords * 4, st>>>(A.row_ptr, A.col, cand,
-                                                                       nwords, nd);
+      k_group_distinct<<<(unsigned)n, kGroupThreads, nwords * 4, st>>>(A, cand, nwords, nd);
       note_launch();
       e = cudaGetLastError();
     }
@@ -625,15 +689,16 @@ static epet_status form_groups(const epet_csr& A, std::vector<GroupDesc>* out, c
   return EPET_OK;
 }
 
-epet_status grouped_build(const epet_csr& A, int value_format, GroupedMatrix* G,
-                          cudaStream_t st) {
+epet_status grouped_build(const RowSource& A, int64_t m, int64_t ncols, int64_t nnz,
+                          int value_format, GroupedMatrix* G, cudaStream_t st) {
+  (void)nnz;
   *G = GroupedMatrix{};
   G->fmt = value_format;
-  G->n = A.n;
-  if (!grouped_supported(A.n, A.m))
-    return set_error(EPET_ERR_UNSUPPORTED, "grouped layout: %lld columns", (long long)A.n);
+  G->n = ncols;
+  if (!grouped_supported(ncols, m))
+    return set_error(EPET_ERR_UNSUPPORTED, "grouped layout: %lld columns", (long long)ncols);
   std::vector<GroupDesc> hg;
-  EPET_CHECK(form_groups(A, &hg, st));
+  EPET_CHECK(form_groups(A, m, ncols, &hg, st));
   G->ngroups = (int64_t)hg.size();
   G->nslots = hg.empty() ? 0 : (int64_t)hg.back().tb + hg.back().nd;
   const int64_t ns = std::max<int64_t>(G->nslots, 1);
@@ -650,14 +715,14 @@ epet_status grouped_build(const epet_csr& A, int value_format, GroupedMatrix* G,
   GALLOC(G->table, ns * 4);
   GALLOC(G->partial, ns * 4);
   GALLOC(G->ones, ns * 4);
-  GALLOC(G->cg_ptr, (A.n + 1) * 8);
-  GALLOC(G->row_ptr, (A.m + 1) * 8);
+  GALLOC(G->cg_ptr, (ncols + 1) * 8);
+  GALLOC(G->row_ptr, (m + 1) * 8);
   if (!hg.empty()) {
     cudaError_t e = cudaMemcpyAsync(G->groups, hg.data(), hg.size() * sizeof(GroupDesc),
                                     cudaMemcpyHostToDevice, st);
     if (e != cudaSuccess) return fail(cuda_status(e, "group table"));
   }
-  const int nwords = bitmap_words(A.n);
+  const int nwords = bitmap_words(ncols);
   cudaError_t e = cudaFuncSetAttribute(k_group_tables, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                        nwords * 8);
   for (const void* k : {(const void*)k_group_mlem<0>, (const void*)k_group_mlem<1>,
@@ -667,30 +732,21 @@ epet_status grouped_build(const epet_csr& A, int value_format, GroupedMatrix* G,
     if (e == cudaSuccess)
       e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kGroupSmem);
   if (e != cudaSuccess) return fail(cuda_status(e, "grouped kernels"));
-  // ranks in the CSR's entry order, then the padded layout
+  // the padded row pointers, then the tables and the padded layout
   {
-    uint16_t* rank = nullptr;
     int64_t *len = nullptr, *tmp = nullptr;
-    GALLOC(rank, (A.nnz + 1) * 2);
-    GALLOC(len, std::max<int64_t>(A.m, 1) * 8);
-    GALLOC(tmp, scan_tmp_elems(A.m) * 8);
+    GALLOC(len, std::max<int64_t>(m, 1) * 8);
+    GALLOC(tmp, scan_tmp_elems(m) * 8);
     epet_status rc = EPET_OK;
-    if (!hg.empty()) {
-      k_group_tables<<<(unsigned)hg.size(), kGroupThreads, nwords * 8, st>>>(A.row_ptr, A.col,
-                                                                              G->groups, nwords,
-                                                                              G->table, rank);
+    if (m > 0) {
+      k_padded_len<<<ceil_div(m, 256), 256, 0, st>>>(A, m, len);
       note_launch();
-      if (cudaGetLastError() != cudaSuccess) rc = set_error(EPET_ERR_CUDA, "group tables");
-    }
-    if (rc == EPET_OK && A.m > 0) {
-      k_padded_len<<<ceil_div(A.m, 256), 256, 0, st>>>(A.row_ptr, A.m, len);
-      note_launch();
-      rc = exclusive_scan_i64(len, G->row_ptr, A.m, tmp, st);
-    } else if (rc == EPET_OK) {
+      rc = exclusive_scan_i64(len, G->row_ptr, m, tmp, st);
+    } else {
       cudaMemsetAsync(G->row_ptr, 0, 8, st);
     }
     if (rc == EPET_OK) {
-      e = cudaMemcpyAsync(&G->npad, G->row_ptr + A.m, 8, cudaMemcpyDeviceToHost, st);
+      e = cudaMemcpyAsync(&G->npad, G->row_ptr + m, 8, cudaMemcpyDeviceToHost, st);
       if (e == cudaSuccess) e = cudaStreamSynchronize(st);
       if (e != cudaSuccess) rc = cuda_status(e, "padded layout");
     }
@@ -700,13 +756,12 @@ epet_status grouped_build(const epet_csr& A, int value_format, GroupedMatrix* G,
       if (e1 != cudaSuccess || e2 != cudaSuccess)
         rc = cuda_status(e1 != cudaSuccess ? e1 : e2, "grouped allocation of the padded layout");
     }
-    if (rc == EPET_OK && A.m > 0) {
-      k_group_pad<<<ceil_div(A.m * 32, 256), 256, 0, st>>>(A.row_ptr, A.val, rank, G->row_ptr,
-                                                           A.m, G->val32, G->loc);
+    if (rc == EPET_OK && !hg.empty()) {
+      k_group_tables<<<(unsigned)hg.size(), kGroupThreads, nwords * 8, st>>>(
+          A, G->groups, nwords, G->row_ptr, G->table, G->val32, G->loc);
       note_launch();
-      if (cudaGetLastError() != cudaSuccess) rc = set_error(EPET_ERR_CUDA, "padded layout");
+      if (cudaGetLastError() != cudaSuccess) rc = set_error(EPET_ERR_CUDA, "group tables");
     }
-    dev_free(rank, st);
     dev_free(len, st);
     dev_free(tmp, st);
     if (rc != EPET_OK) return fail(rc);
@@ -733,12 +788,12 @@ epet_status grouped_build(const epet_csr& A, int value_format, GroupedMatrix* G,
       note_launch();
       k_fill_f32<<<ceil_div(G->nslots, 256), 256, 0, st>>>(G->ones, G->nslots, 1.f);
       note_launch();
-      epet_csr T{G->ngroups, A.n, G->nslots, gptr, G->table, slot_bits};
-      epet_csc C{G->ngroups, A.n, G->nslots, G->cg_ptr, cg_group,
+      epet_csr T{G->ngroups, ncols, G->nslots, gptr, G->table, slot_bits};
+      epet_csc C{G->ngroups, ncols, G->nslots, G->cg_ptr, cg_group,
                  reinterpret_cast<float*>(G->cg_slot)};
       rc = epet_csr_to_csc(&T, &C, nullptr, 0, st);
     } else if (rc == EPET_OK) {
-      cudaMemsetAsync(G->cg_ptr, 0, (A.n + 1) * 8, st);
+      cudaMemsetAsync(G->cg_ptr, 0, (ncols + 1) * 8, st);
     }
     dev_free(slot_bits, st);
     dev_free(cg_group, st);
@@ -747,20 +802,20 @@ epet_status grouped_build(const epet_csr& A, int value_format, GroupedMatrix* G,
   }
   if (value_format != EPET_VALUES_FP32) {
     GALLOC(G->val16, std::max<int64_t>(G->npad, 4) * 2);
-    GALLOC(G->scale, std::max<int64_t>(A.m, 1) * 4);
-    if (A.m > 0) {
+    GALLOC(G->scale, std::max<int64_t>(m, 1) * 4);
+    if (m > 0) {
       if (value_format == EPET_VALUES_BF16)
-        k_group_quantise<1><<<ceil_div(A.m * 32, 256), 256, 0, st>>>(G->row_ptr, G->val32, A.m,
+        k_group_quantise<1><<<ceil_div(m * 32, 256), 256, 0, st>>>(G->row_ptr, G->val32, m,
                                                                      G->scale, G->val16);
       else
-        k_group_quantise<2><<<ceil_div(A.m * 32, 256), 256, 0, st>>>(G->row_ptr, G->val32, A.m,
+        k_group_quantise<2><<<ceil_div(m * 32, 256), 256, 0, st>>>(G->row_ptr, G->val32, m,
                                                                      G->scale, G->val16);
       note_launch();
       if (cudaGetLastError() != cudaSuccess) return fail(set_error(EPET_ERR_CUDA, "quantise"));
     }
   }
 #undef GALLOC
-  G->plan_cols = default_plan(A.n ? (double)G->nslots / A.n : 0.0);
+  G->plan_cols = default_plan(ncols ? (double)G->nslots / ncols : 0.0);
   return EPET_OK;
 }
 

@@ -198,12 +198,6 @@ static epet_status order_rows(const epet_problem* p, const int32_t* rows_d, int6
   return rc;
 }
 
-struct SegDev {
-  const int32_t* col;
-  const float* val;
-  int64_t e0;
-};
-
 __global__ void k_perm_len(const int64_t* __restrict__ rp0, const int32_t* __restrict__ idx,
                            int64_t m, int64_t* __restrict__ len) {
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -230,60 +224,77 @@ __global__ void k_perm_rows(const int64_t* __restrict__ rp0, const SegDev* __res
 
 // The system matrix of the rows h->rows (the crystal-pair order), built
 // over the rows in list order (rows_d: neighbouring rows are near-parallel
-// lines, which the walk handles faster) into one allocation per chunk, then
-// moved row by row into h->A (exact size; no growth copies).
-static epet_status build_in_pair_order(const epet_problem* p, const int32_t* rows_d,
-                                       const int32_t* idx, int32_t max_row_nnz, epet_mlem* h,
-                                       cudaStream_t st) {
-  const int64_t m = h->m;
+// lines, which the walk handles faster) into one allocation per chunk
+// (chunks of a uniform row count).  rp0 (m + 1, list order) gets the row
+// pointers; segd (device) the chunk table.
+struct ListBuild {
   std::vector<CsrSegment> segs;
-  int64_t *rp0 = nullptr, *len = nullptr, *tmp = nullptr;
+  int64_t* rp0 = nullptr;
   SegDev* segd = nullptr;
-  int64_t nnz = 0;
+  int64_t ch = 1, nnz = 0;
+  void release(cudaStream_t st) {
+    for (const CsrSegment& sg : segs) {
+      dev_free(sg.col, st);
+      dev_free(sg.val, st);
+    }
+    segs.clear();
+    for (void* q : {(void*)rp0, (void*)segd})
+      if (q) dev_free(q, st);
+    rp0 = nullptr;
+    segd = nullptr;
+  }
+};
+
+static epet_status build_list_order(const epet_problem* p, const int32_t* rows_d, int64_t m,
+                                    int32_t max_row_nnz, ListBuild* b, cudaStream_t st) {
+  EPET_CUDA(dev_alloc((void**)&b->rp0, (m + 1) * 8, st));
+  EPET_CHECK(build_csr_segments(p, rows_d, m, b->rp0, &b->segs, &b->nnz, max_row_nnz, st));
+  b->ch = b->segs.empty() ? 1 : b->segs[0].nr;
+  for (size_t k = 0; k < b->segs.size(); k++)
+    if (b->segs[k].r0 != (int64_t)k * b->ch || (k + 1 < b->segs.size() && b->segs[k].nr != b->ch))
+      return set_error(EPET_ERR_INVALID, "internal: uneven build chunks");
+  std::vector<SegDev> hs;
+  for (const CsrSegment& sg : b->segs) hs.push_back({sg.col, sg.val, sg.e0});
+  EPET_CUDA(dev_alloc((void**)&b->segd, std::max<size_t>(hs.size(), 1) * sizeof(SegDev), st));
+  if (!hs.empty())
+    EPET_CUDA(cudaMemcpyAsync(b->segd, hs.data(), hs.size() * sizeof(SegDev),
+                              cudaMemcpyHostToDevice, st));
+  return EPET_OK;
+}
+
+// The list-order build moved row by row into h->A in the crystal-pair order
+// (exact size; no growth copies).
+static epet_status move_to_pair_order(const ListBuild& lb, const int32_t* idx, epet_mlem* h,
+                                      cudaStream_t st) {
+  const int64_t m = h->m;
+  const int64_t nnz = lb.nnz;
+  int64_t *len = nullptr, *tmp = nullptr;
   epet_csr B{m, h->V, 0, nullptr, nullptr, nullptr};
   epet_status rc = EPET_OK;
   auto cu = [&](cudaError_t e, const char* what) {
     if (rc == EPET_OK && e != cudaSuccess) rc = cuda_status(e, what);
   };
-  cu(dev_alloc((void**)&rp0, (m + 1) * 8, st), "allocation of the row pointers");
-  if (rc == EPET_OK) rc = build_csr_segments(p, rows_d, m, rp0, &segs, &nnz, max_row_nnz, st);
-  const int64_t ch = segs.empty() ? 1 : segs[0].nr;
-  for (size_t k = 0; rc == EPET_OK && k < segs.size(); k++)
-    if (segs[k].r0 != (int64_t)k * ch || (k + 1 < segs.size() && segs[k].nr != ch))
-      rc = set_error(EPET_ERR_INVALID, "internal: uneven build chunks");
+  cu(dev_alloc((void**)&B.row_ptr, (m + 1) * 8, st), "allocation of A");
+  cu(dev_alloc((void**)&B.col, (nnz + 4) * 4, st), "allocation of A");
+  cu(dev_alloc((void**)&B.val, (nnz + 4) * 4, st), "allocation of A");
+  cu(dev_alloc((void**)&len, std::max<int64_t>(m, 1) * 8, st), "allocation of the row move");
+  cu(dev_alloc((void**)&tmp, scan_tmp_elems(m) * 8, st), "allocation of the row move");
   if (rc == EPET_OK && m > 0) {
-    std::vector<SegDev> hs;
-    for (const CsrSegment& sg : segs) hs.push_back({sg.col, sg.val, sg.e0});
-    cu(dev_alloc((void**)&segd, std::max<size_t>(hs.size(), 1) * sizeof(SegDev), st),
-       "allocation of the chunk table");
-    if (rc == EPET_OK && !hs.empty())
-      cu(cudaMemcpyAsync(segd, hs.data(), hs.size() * sizeof(SegDev), cudaMemcpyHostToDevice, st),
-         "chunk table");
-    cu(dev_alloc((void**)&B.row_ptr, (m + 1) * 8, st), "allocation of A");
-    // (4 entries of padding: the grouped pass loads 4 entries at a time)
-    cu(dev_alloc((void**)&B.col, (nnz + 4) * 4, st), "allocation of A");
-    cu(dev_alloc((void**)&B.val, (nnz + 4) * 4, st), "allocation of A");
-    cu(dev_alloc((void**)&len, m * 8, st), "allocation of the row move");
-    cu(dev_alloc((void**)&tmp, scan_tmp_elems(m) * 8, st), "allocation of the row move");
+    k_perm_len<<<ceil_div(m, 256), 256, 0, st>>>(lb.rp0, idx, m, len);
+    note_launch();
+    rc = exclusive_scan_i64(len, B.row_ptr, m, tmp, st);
     if (rc == EPET_OK) {
-      k_perm_len<<<ceil_div(m, 256), 256, 0, st>>>(rp0, idx, m, len);
-      note_launch();
-      rc = exclusive_scan_i64(len, B.row_ptr, m, tmp, st);
-    }
-    if (rc == EPET_OK) {
-      k_perm_rows<<<ceil_div(m * 32, 256), 256, 0, st>>>(rp0, segd, ch, idx, m, B.row_ptr,
-                                                       B.col, B.val);
+      k_perm_rows<<<ceil_div(m * 32, 256), 256, 0, st>>>(lb.rp0, lb.segd, lb.ch, idx, m,
+                                                       B.row_ptr, B.col, B.val);
       note_launch();
       cu(cudaGetLastError(), "row move");
     }
-    // the copies above must finish before the segments are released
-    cu(cudaStreamSynchronize(st), "row move");
+  } else if (rc == EPET_OK) {
+    cu(cudaMemsetAsync(B.row_ptr, 0, 8, st), "row move");
   }
-  for (const CsrSegment& sg : segs) {
-    dev_free(sg.col, st);
-    dev_free(sg.val, st);
-  }
-  for (void* q : {(void*)rp0, (void*)len, (void*)tmp, (void*)segd})
+  // the copies must finish before the caller releases the segments
+  cu(cudaStreamSynchronize(st), "row move");
+  for (void* q : {(void*)len, (void*)tmp})
     if (q) dev_free(q, st);
   if (rc != EPET_OK) {
     for (void* q : {(void*)B.row_ptr, (void*)B.col, (void*)B.val})
@@ -395,29 +406,51 @@ epet_status epet_mlem_create(const epet_problem* p, const int32_t* rows_d, const
     epet_status rc = order_rows(p, rows_d, m, h, st, &idx);
     if (rc != EPET_OK) return fail(rc);
   }
-  // system matrix (rows in the crystal-pair order) and its column-major copy
-  epet_status rc = idx ? build_in_pair_order(p, rows_d, idx, o.max_row_nnz, h, st)
-                       : build_csr_growable(p, h->rows, m, &h->A, &h->capA, o.max_row_nnz, st);
-  if (idx) dev_free(idx, st);
-  if (rc != EPET_OK) return fail(rc);
-  const int64_t nnz = h->A.nnz;
   if (o.layout != EPET_LAYOUT_AUTO && o.layout != EPET_LAYOUT_GROUPED &&
-      o.layout != EPET_LAYOUT_CSC)
+      o.layout != EPET_LAYOUT_CSC) {
+    if (idx) dev_free(idx, st);
     return fail(set_error(EPET_ERR_INVALID, "layout %d", o.layout));
+  }
   const bool grouped_ok = grouped_supported(V, m);
-  if (o.layout == EPET_LAYOUT_GROUPED && !grouped_ok)
+  if (o.layout == EPET_LAYOUT_GROUPED && !grouped_ok) {
+    if (idx) dev_free(idx, st);
     return fail(set_error(EPET_ERR_UNSUPPORTED, "grouped layout: %lld voxels (at most 819,200)",
                           (long long)V));
+  }
   // AUTO: the grouped layout for FP32 values; the 16-bit forms keep the
   // CSR and the column-major copy (their grouped pass is bound by shared
   // memory, not by the bytes it saves, and runs slower)
   const bool want_grouped = o.layout == EPET_LAYOUT_GROUPED ||
                             (o.layout == EPET_LAYOUT_AUTO && o.value_format == EPET_VALUES_FP32);
+  // the system matrix (rows in the crystal-pair order): the grouped layout
+  // reads the list-order build's chunks directly; the CSC layout moves them
+  // into one CSR, then makes the column-major copy
+  epet_status rc = EPET_OK;
+  if (idx) {
+    ListBuild lb;
+    rc = build_list_order(p, rows_d, m, o.max_row_nnz, &lb, st);
+    if (rc == EPET_OK && want_grouped && grouped_ok) {
+      RowSource src{lb.rp0, nullptr, nullptr, lb.segd, lb.ch, idx};
+      rc = grouped_build(src, m, V, lb.nnz, o.value_format, &h->G, st);
+      if (rc == EPET_OK) {
+        cudaError_t e = cudaStreamSynchronize(st);  // before the chunks go
+        if (e != cudaSuccess) rc = cuda_status(e, "grouped layout");
+      }
+      h->A = epet_csr{m, V, lb.nnz, nullptr, nullptr, nullptr};
+    } else if (rc == EPET_OK) {
+      rc = move_to_pair_order(lb, idx, h, st);
+    }
+    lb.release(st);
+    dev_free(idx, st);
+  } else {
+    rc = build_csr_growable(p, h->rows, m, &h->A, &h->capA, o.max_row_nnz, st);
+    if (rc == EPET_OK && want_grouped && grouped_ok)
+      rc = grouped_build(RowSource{h->A.row_ptr, h->A.col, h->A.val, nullptr, 1, nullptr}, m, V,
+                         h->A.nnz, o.value_format, &h->G, st);
+  }
+  if (rc != EPET_OK) return fail(rc);
+  const int64_t nnz = h->A.nnz;
   if (want_grouped && grouped_ok) {
-    // the grouped layout replaces the column indices (and, for the 16-bit
-    // forms, the FP32 values): the CSR's row pointers stay
-    rc = grouped_build(h->A, o.value_format, &h->G, st);
-    if (rc != EPET_OK) return fail(rc);
     if (o.value_format != EPET_VALUES_FP32 && V > 0) {
       // The iterations run with the 16-bit values, whose column sums differ
       // from the FP32 ones by the rounding of the values; an MLEM update

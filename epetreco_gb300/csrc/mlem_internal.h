@@ -32,9 +32,28 @@ struct GroupedMatrix {
   RowPlan plan_cols;
 };
 bool grouped_supported(int64_t V, int64_t m);
-// Builds the grouped layout from a CSR (rows in the reconstruction's order);
-// A itself is left as it is (the caller may release it afterwards).
-epet_status grouped_build(const epet_csr& A, int value_format, GroupedMatrix* G, cudaStream_t st);
+// One chunk of a build held in its own allocation (entries e0 onwards).
+struct SegDev {
+  const int32_t* col;
+  const float* val;
+  int64_t e0;
+};
+// Where the grouped build reads row r of the matrix (rows in the
+// reconstruction's order): a CSR (segs null: entries rp[r] .. rp[r+1] of
+// col / val), or the chunks of a build over the rows in another order (row r
+// is built row q = idx[r], entries rp[q] .. rp[q+1] of the chunk q / ch).
+struct RowSource {
+  const int64_t* rp;
+  const int32_t* col;
+  const float* val;
+  const SegDev* segs;
+  int64_t ch;
+  const int32_t* idx;
+};
+// Builds the grouped layout of an m x n matrix with nnz entries; the source
+// is left as it is (the caller may release it afterwards).
+epet_status grouped_build(const RowSource& A, int64_t m, int64_t n, int64_t nnz,
+                          int value_format, GroupedMatrix* G, cudaStream_t st);
 // ybar = A x, e = y / ybar and the groups' shares of A^T e into G.partial.
 epet_status grouped_pass(const GroupedMatrix& G, const float* x, const float* y, float* ybar,
                          cudaStream_t st);

@@ -1023,8 +1023,8 @@ static epet_status launch_walk(WalkArgs a, size_t smem, cudaStream_t st) {
 // Rows processed per chunk (rays and staging are chunk-sized).
 static int64_t chunk_rows(const Geo& G, int cap_cells) {
   const int64_t per_row = (int64_t)G.p.nrays * 24 + (int64_t)cap_cells * 8 + 64;
-  int64_t c = ((int64_t)3 << 30) / per_row;  // ~3 GiB of chunk buffers
-  c = std::max<int64_t>(1024, std::min<int64_t>(c, 262144));
+  int64_t c = ((int64_t)8 << 30) / per_row;  // ~8 GiB of chunk buffers
+  c = std::max<int64_t>(1024, std::min<int64_t>(c, 4194304));
   return c;
 }
 
