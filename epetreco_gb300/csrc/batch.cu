@@ -5,7 +5,8 @@
 // device array of per-problem descriptors and tile tables, and runs every
 // step of an iteration as ONE launch over all problems: a tile of rows (or
 // voxels) finds its problem by binary search in the tile table, then works
-// on that problem's arrays.  The four launches of an iteration are captured
+// on that problem's arrays.  The four launches of an iteration (five with
+// wide row groups) are captured
 // in one CUDA graph.  Partial image sums are written per tile; a problem's
 // tiles are contiguous, so its image sum is a fixed-order sum over its own
 // tile range (deterministic, as in the single-problem driver).
@@ -127,6 +128,9 @@ struct epet_mlem_batch {
   void* gdesc = nullptr;      // device, nprob descriptors of the pass
   int64_t* gstart = nullptr;  // device, prefix of the problems' group counts
   int64_t total_groups = 0;
+  int32_t* gwide = nullptr;   // device, global ids of the wide groups
+  int64_t nwide = 0;
+  int graph_kernels = 0;      // kernels in the captured iteration
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t exec = nullptr;
 
@@ -146,7 +150,7 @@ void batch_free(epet_mlem_batch* h) {
   if (h->graph) cudaGraphDestroy(h->graph);
   for (epet_mlem* p : h->probs) epet_mlem_destroy(p);
   for (void* b : {(void*)h->desc, (void*)h->tiles, (void*)h->partial, (void*)h->sums,
-                  h->gdesc, (void*)h->gstart})
+                  h->gdesc, (void*)h->gstart, (void*)h->gwide})
     if (b) dev_free(b, 0);
   delete h;
 }
@@ -172,7 +176,8 @@ epet_status launch_batch_rows(const epet_mlem_batch* h, const RowPlan& plan, boo
 
 epet_status batch_iteration(const epet_mlem_batch* h, cudaStream_t st) {
   if (h->grouped)
-    EPET_CHECK(grouped_pass_batch(h->gdesc, h->gstart, h->np(), h->total_groups, st));
+    EPET_CHECK(grouped_pass_batch(h->gdesc, h->gstart, h->np(), h->total_groups, h->gwide,
+                                  h->nwide, st));
   else
     EPET_CHECK(launch_batch_rows(h, h->plan_fwd, true, st));
   EPET_CHECK(launch_batch_rows(h, h->plan_bwd, false, st));
@@ -241,6 +246,7 @@ epet_status epet_mlem_batch_create(int32_t nprob, const epet_problem* problems,
   h->grouped = all_grouped;
   std::vector<unsigned char> gd_h(all_grouped ? np * grouped_batch_desc_bytes() : 0);
   std::vector<int64_t> gs_h(np + 1, 0);
+  std::vector<int32_t> gw_h;  // global ids of the wide groups
   for (int i = 0; i < np; i++) {
     const epet_mlem* p = h->probs[i];
     if (all_grouped) {
@@ -249,6 +255,7 @@ epet_status epet_mlem_batch_create(int32_t nprob, const epet_problem* problems,
       dh[i] = BatchDesc{nullptr, nullptr, nullptr, p->G.cg_ptr, p->G.cg_slot, p->G.ones,
                         p->y, p->G.partial, p->ybar, p->s, p->x, p->xnew, p->m, p->V};
       grouped_batch_desc(p->G, p->x, p->y, p->ybar, gd_h.data() + i * grouped_batch_desc_bytes());
+      for (int32_t w : p->G.wide_h) gw_h.push_back((int32_t)(gs_h[i] + w));
       gs_h[i + 1] = gs_h[i] + p->G.ngroups;
       if (!aligned16(p->G.cg_slot, p->G.ones))
         return fail(set_error(EPET_ERR_UNSUPPORTED, "batch: slot streams not 16-byte aligned"));
@@ -281,6 +288,10 @@ epet_status epet_mlem_batch_create(int32_t nprob, const epet_problem* problems,
     ALLOC(h->gdesc, gd_h.size());
     ALLOC(h->gstart, (np + 1) * 8);
     h->total_groups = gs_h[np];
+    if (h->total_groups > INT32_MAX)
+      return fail(set_error(EPET_ERR_UNSUPPORTED, "batch: more than 2^31 row groups"));
+    h->nwide = (int64_t)gw_h.size();
+    if (h->nwide > 0) ALLOC(h->gwide, h->nwide * 4);
   }
 #undef ALLOC
   cudaError_t e = cudaMemcpyAsync(h->desc, dh.data(), np * sizeof(BatchDesc),
@@ -292,6 +303,8 @@ epet_status epet_mlem_batch_create(int32_t nprob, const epet_problem* problems,
     e = cudaMemcpyAsync(h->gdesc, gd_h.data(), gd_h.size(), cudaMemcpyHostToDevice, st);
   if (e == cudaSuccess && all_grouped)
     e = cudaMemcpyAsync(h->gstart, gs_h.data(), (np + 1) * 8, cudaMemcpyHostToDevice, st);
+  if (e == cudaSuccess && h->nwide > 0)
+    e = cudaMemcpyAsync(h->gwide, gw_h.data(), h->nwide * 4, cudaMemcpyHostToDevice, st);
   if (e == cudaSuccess) e = cudaStreamSynchronize(st);
   if (e != cudaSuccess) return fail(cuda_status(e, "batch descriptors"));
 
@@ -307,7 +320,7 @@ epet_status epet_mlem_batch_create(int32_t nprob, const epet_problem* problems,
     if (all_grouped) {
       // one pass fills the slots; the slot sums' candidates rerun the
       // (idempotent) update epilogue
-      rc = grouped_pass_batch(h->gdesc, h->gstart, np, h->total_groups, st);
+      rc = grouped_pass_batch(h->gdesc, h->gstart, np, h->total_groups, h->gwide, h->nwide, st);
       if (rc == EPET_OK)
         rc = tune_rows(
             7, h->voxels, nslots, np, avg_col,
@@ -346,7 +359,11 @@ epet_status epet_mlem_batch_iterate(epet_mlem_batch* h, int32_t nit, double* log
       EPET_CUDA(cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking));
       epet_status rc = EPET_OK;
       cudaError_t e = cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal);
+      const long long k0 = epet_launch_count();
       if (e == cudaSuccess) rc = batch_iteration(h, cap);
+      // (capturing counted the kernels; the replays below count them again)
+      h->graph_kernels = (int)(epet_launch_count() - k0);
+      note_launch(-h->graph_kernels);
       cudaError_t e2 = cudaStreamEndCapture(cap, &h->graph);
       cudaStreamDestroy(cap);
       if (e != cudaSuccess) return cuda_status(e, "begin capture");
@@ -354,13 +371,9 @@ epet_status epet_mlem_batch_iterate(epet_mlem_batch* h, int32_t nit, double* log
       if (e2 != cudaSuccess) return cuda_status(e2, "end capture");
       EPET_CUDA(cudaGraphInstantiate(&h->exec, h->graph, 0));
     }
-    const bool fwd = h->grouped ? h->total_groups > 0
-                                : h->host_total(0 + rpt_index(h->plan_fwd.G)) > 0;
-    const int per_iter = 1 + (fwd ? 1 : 0) + (h->host_total(8) > 0 ? 1 : 0) +
-                         (h->host_total(4 + rpt_index(h->plan_bwd.G)) > 0 ? 1 : 0);
     for (int it = 0; it < nit; it++) {
       EPET_CUDA(cudaGraphLaunch(h->exec, st));
-      note_launch(per_iter);
+      note_launch(h->graph_kernels);  // the kernels of the captured iteration
     }
   } else {
     for (int it = 0; it < nit; it++) EPET_CHECK(batch_iteration(h, st));

@@ -615,7 +615,11 @@ epet_status epet_mlem_iterate(epet_mlem* h, int32_t nit, double* loglik_h,
       EPET_CUDA(cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking));
       epet_status rc = EPET_OK;
       cudaError_t e = cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal);
+      const long long k0 = epet_launch_count();
       if (e == cudaSuccess) rc = mlem_iteration(h, cap);
+      // (capturing counted the kernels; the replays below count them again)
+      h->graph_kernels = (int)(epet_launch_count() - k0);
+      note_launch(-h->graph_kernels);
       cudaError_t e2 = cudaStreamEndCapture(cap, &h->graph);
       cudaStreamDestroy(cap);
       if (e != cudaSuccess) return cuda_status(e, "begin capture");
@@ -625,7 +629,7 @@ epet_status epet_mlem_iterate(epet_mlem* h, int32_t nit, double* loglik_h,
     }
     for (int it = 0; it < nit; it++) {
       EPET_CUDA(cudaGraphLaunch(h->exec, st));
-      note_launch(4);  // the captured iteration holds four kernels
+      note_launch(h->graph_kernels);  // the kernels of the captured iteration
     }
   } else {
     for (int it = 0; it < nit; it++) EPET_CHECK(mlem_iteration(h, st));

@@ -29,6 +29,9 @@ struct GroupedMatrix {
   int32_t* cg_slot = nullptr;
   float* ones = nullptr;        // nslots ones (the slot sums run on the row kernel)
   float* partial = nullptr;     // per slot: the group's share of c = A^T e
+  int32_t* wide = nullptr;      // ids of the groups of one row wider than the shared tables
+  int64_t nwide = 0;
+  std::vector<int32_t> wide_h;  // the same on the host
   RowPlan plan_cols;
 };
 bool grouped_supported(int64_t V, int64_t m);
@@ -54,7 +57,9 @@ struct RowSource {
 // is left as it is (the caller may release it afterwards).
 epet_status grouped_build(const RowSource& A, int64_t m, int64_t n, int64_t nnz,
                           int value_format, GroupedMatrix* G, cudaStream_t st);
-// ybar = A x, e = y / ybar and the groups' shares of A^T e into G.partial.
+// ybar = A x, e = y / ybar and the groups' shares of A^T e into G.partial
+// (one kernel, two when the matrix has wide groups: grouped_pass_kernels).
+int grouped_pass_kernels(const GroupedMatrix& G);
 epet_status grouped_pass(const GroupedMatrix& G, const float* x, const float* y, float* ybar,
                          cudaStream_t st);
 void grouped_free(GroupedMatrix* G, cudaStream_t st);
@@ -68,12 +73,14 @@ epet_status grouped_column_sums(const GroupedMatrix& G, bool quantised, float* o
 // Batched form: a descriptor per problem (grouped_batch_desc_bytes() each,
 // written by grouped_batch_desc into a host buffer and copied to the
 // device) and one pass over all problems' groups (gstart: device prefix of
-// the problems' group counts, np + 1 entries).
+// the problems' group counts, np + 1 entries; wide: the global ids of the
+// wide groups, nwide of them, passed by a second kernel).
 size_t grouped_batch_desc_bytes();
 void grouped_batch_desc(const GroupedMatrix& G, const float* x, const float* y, float* ybar,
                         void* out);
 epet_status grouped_pass_batch(const void* desc, const int64_t* gstart, int np,
-                               int64_t total_groups, cudaStream_t st);
+                               int64_t total_groups, const int32_t* wide, int64_t nwide,
+                               cudaStream_t st);
 }  // namespace epet
 
 struct epet_mlem {
@@ -95,6 +102,7 @@ struct epet_mlem {
   epet::RowPlan plan_fwd, plan_bwd;
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t exec = nullptr;
+  int graph_kernels = 0;  // kernels in the captured iteration
 };
 
 namespace epet {

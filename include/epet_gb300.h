@@ -456,7 +456,8 @@ epet_status epet_mlem_plan(const epet_mlem* h, int32_t plan_h[6]);
  * measured rows and sensitivity) iterated together: every step of an
  * iteration is ONE kernel launch over all problems' rows or voxels, and the
  * iteration (forward product + e = y/(Ax), transpose product + x*c/s,
- * per-problem fp64 image sums, normalisation: four launches) is captured in
+ * per-problem fp64 image sums, normalisation: four launches, five when a
+ * grouped-layout problem has a row wider than the shared tables) is captured in
  * one CUDA graph.  Launch shapes come from the autotuner unless
  * opt->autotune == 0.  The reference runs one reconstruction per process
  * (reco.cu:209-281); there is no batched counterpart.  FP32 values. */
