@@ -582,23 +582,27 @@ def gb300_arm(args):
         forms = {"fp32": {"iteration_ms": 1000 * t_iter, "it_per_s": 1.0 / t_iter,
                           "layout": "grouped (value + 2-byte group-local column rank)"},
                  "iterations": nit}
+        labels = {api.LAYOUT_CSC: "CSR + column-major copy (16-bit chunks)",
+                  api.LAYOUT_GROUPED: "grouped (16-bit value + 2-byte group-local column rank)"}
         for name, fmt in (("bf16", 1), ("fp16", 2)):
-            # the library's default layout for 16-bit values (CSR + column-major
-            # copy); the grouped layout's iteration timed beside it
+            # the library's default layout for 16-bit values; the other
+            # layout's iteration timed beside it
             R16 = api.Mlem(p, rows, y, s, use_graph=True, value_format=fmt)
             t16 = timeit(lambda: R16.iterate(1), reps=5)
             traces[name] = trace(R16)
             st16 = R16.stats()
+            lay = R16.layout
             R16.close()
-            G16 = api.Mlem(p, rows, y, s, use_graph=True, value_format=fmt,
-                           layout=api.LAYOUT_GROUPED)
-            t16g = timeit(lambda: G16.iterate(1), reps=5)
-            G16.close()
+            other = api.LAYOUT_CSC if lay == api.LAYOUT_GROUPED else api.LAYOUT_GROUPED
+            O16 = api.Mlem(p, rows, y, s, use_graph=True, value_format=fmt, layout=other)
+            t16o = timeit(lambda: O16.iterate(1), reps=5)
+            O16.close()
             forms[name] = {"iteration_ms": 1000 * t16, "it_per_s": 1.0 / t16,
-                           "layout": "CSR + column-major copy (16-bit chunks)",
+                           "layout": labels[lay],
                            "speedup_vs_fp32": t_iter / t16,
                            "bytes_per_iteration": st16["bytes_per_iteration"],
-                           "grouped_layout_iteration_ms": 1000 * t16g,
+                           ("grouped_layout_iteration_ms" if other == api.LAYOUT_GROUPED else
+                            "csc_layout_iteration_ms"): 1000 * t16o,
                            "image_rel_l2_vs_fp32": float(
                                np.linalg.norm(traces[name][-1] - traces["fp32"][-1]) /
                                np.linalg.norm(traces["fp32"][-1]))}

@@ -114,6 +114,7 @@ SIGNATURES = {
     "epet_mlem_set_image": [VP, VP, VP],
     "epet_mlem_stats": [VP, C.POINTER(C.c_int64), C.POINTER(C.c_int64)],
     "epet_mlem_plan": [VP, C.POINTER(C.c_int32)],
+    "epet_mlem_layout": [VP, C.POINTER(C.c_int32)],
     "epet_mlem_correction": [VP, VP, VP],
     "epet_mlem_update": [VP, VP, VP],
     "epet_mlem_loglik": [VP, C.POINTER(C.c_double), VP],

@@ -478,6 +478,13 @@ class Mlem:
         check(lib().epet_mlem_plan(self._h, pl))
         return {"forward": tuple(pl[0:3]), "transpose": tuple(pl[3:6])}
 
+    @property
+    def layout(self) -> int:
+        """LAYOUT_GROUPED or LAYOUT_CSC (-1 for a matrix-free object)."""
+        v = C.c_int32(0)
+        check(lib().epet_mlem_layout(self._h, C.byref(v)))
+        return v.value
+
     def close(self):
         if self._h and getattr(self, "_owner", None) is None:
             lib().epet_mlem_destroy(self._h)

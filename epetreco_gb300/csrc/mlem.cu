@@ -745,6 +745,12 @@ epet_status epet_mlem_plan(const epet_mlem* h, int32_t plan_h[6]) {
   return EPET_OK;
 }
 
+epet_status epet_mlem_layout(const epet_mlem* h, int32_t* layout_h) {
+  if (!h || !layout_h) return set_error(EPET_ERR_INVALID, "bad arguments");
+  *layout_h = h->opt.matrix_free ? -1 : (h->grouped ? EPET_LAYOUT_GROUPED : EPET_LAYOUT_CSC);
+  return EPET_OK;
+}
+
 epet_status epet_trim_memory(size_t keep_bytes) { return trim_memory(keep_bytes); }
 
 epet_status epet_sensitivity(const epet_problem* p, const int32_t* rows_d, int64_t m,

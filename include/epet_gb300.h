@@ -450,6 +450,9 @@ epet_status epet_mlem_stats(const epet_mlem* h, int64_t* nnz_h,
  * persistent grid (0 = one block per tile); plan_h[3..5] the same for the
  * transpose. */
 epet_status epet_mlem_plan(const epet_mlem* h, int32_t plan_h[6]);
+/* The layout the matrix is held in (EPET_LAYOUT_GROUPED or EPET_LAYOUT_CSC;
+ * -1 with matrix_free). */
+epet_status epet_mlem_layout(const epet_mlem* h, int32_t* layout_h);
 
 /* ---------------------------------------------- batched reconstructions */
 /* Many independent reconstructions (each its own geometry, grid, rays,
