@@ -42,6 +42,7 @@ namespace epet {
 constexpr int kWalkThreads = 128;
 constexpr int kGeomFloats = 56;  // per-channel geometry record (k_channel_geom)
 constexpr int kMaxSlabs = 1024;  // nx limit of the walk kernel
+constexpr float kWinPad = 1e-3f;  // window padding margin, in voxels (slab_window)
 
 enum WalkMode { kModeCsr = 0, kModeForward = 1, kModeBack = 2, kModeColSum = 3,
                 kModeWindow = 4, kModeMlem = 5 };
@@ -159,7 +160,13 @@ __device__ __forceinline__ float fval(int k) {
 
 // Index window of slab i along axis sa from the hull's cross-sections at its
 // two planes (pext[k] = {pmin, pmax, qmin, qmax} keys at plane k) and the
-// hull vertices (crystal corners) inside the slab; padded by one index.
+// hull vertices (crystal corners) inside the slab.  An index range is
+// widened by one only on a side whose extreme lies within kWinPad (in
+// voxels) of a grid plane, where the rounding of the hull's or a ray's
+// arithmetic could put a hit in the neighbouring cell (both are ~1e-6 voxel
+// here); the window then holds about 1.7x a row's non-zeros instead of 3.9x
+// with a voxel of padding on every side (channels of the full workload).
+// A hit outside the window is still counted and reported (hit_outside).
 __device__ void slab_window(const Geo& G, const float (*c0)[3], const float (*c1)[3],
                             const int4* pext, int sa, int i, Slab* out) {
   const epet_grid& g = G.p.grid;
@@ -182,10 +189,18 @@ __device__ void slab_window(const Geo& G, const float (*c0)[3], const float (*c1
   if (plo > phi) return;  // the bundle does not reach this slab
   const float pmin = fval(plo), pmax = fval(phi), qmin = fval(qlo), qmax = fval(qhi);
   const int np = g.n[pa], nq = g.n[qa];
-  int a0 = (int)floorf((pmin - g.o[pa]) / g.d[pa]) - 1;
-  int a1 = (int)floorf((pmax - g.o[pa]) / g.d[pa]) + 1;
-  int b0 = (int)floorf((qmin - g.o[qa]) / g.d[qa]) - 1;
-  int b1 = (int)floorf((qmax - g.o[qa]) / g.d[qa]) + 1;
+  auto lo_index = [](float f) {
+    const float fl = floorf(f);
+    return (int)fl - (f - fl < kWinPad ? 1 : 0);
+  };
+  auto hi_index = [](float f) {
+    const float fl = floorf(f);
+    return (int)fl + (f - fl > 1.f - kWinPad ? 1 : 0);
+  };
+  int a0 = lo_index((pmin - g.o[pa]) / g.d[pa]);
+  int a1 = hi_index((pmax - g.o[pa]) / g.d[pa]);
+  int b0 = lo_index((qmin - g.o[qa]) / g.d[qa]);
+  int b1 = hi_index((qmax - g.o[qa]) / g.d[qa]);
   if (a1 < 0 || a0 > np - 1 || b1 < 0 || b0 > nq - 1) return;
   a0 = clampi(a0, 0, np - 1); a1 = clampi(a1, 0, np - 1);
   b0 = clampi(b0, 0, nq - 1); b1 = clampi(b1, 0, nq - 1);
