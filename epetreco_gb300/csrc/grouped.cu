@@ -927,7 +927,7 @@ epet_status grouped_column_sums(const GroupedMatrix& G, bool quantised, float* o
     }
     EPET_LAUNCHED();
   }
-  return launch_rows(G.plan_cols, G.cg_ptr, G.cg_slot, G.ones, G.partial, G.n, EpiKeep{out},
+  return launch_sums(G.plan_cols, G.cg_ptr, G.cg_slot, G.partial, G.n, EpiKeep{out},
                      nullptr, st);
 }
 

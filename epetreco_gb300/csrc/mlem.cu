@@ -76,7 +76,7 @@ static epet_status mlem_iteration_free(epet_mlem* h, cudaStream_t st) {
 static epet_status mlem_correction(epet_mlem* h, float* c, cudaStream_t st) {
   if (h->grouped) {
     EPET_CHECK(grouped_pass(h->G, h->x, h->y, h->ybar, st));
-    return launch_rows(h->G.plan_cols, h->G.cg_ptr, h->G.cg_slot, h->G.ones, h->G.partial, h->V,
+    return launch_sums(h->G.plan_cols, h->G.cg_ptr, h->G.cg_slot, h->G.partial, h->V,
                        EpiKeep{c}, nullptr, st);
   }
   if (h->opt.matrix_free) {
@@ -103,7 +103,7 @@ static epet_status mlem_correction(epet_mlem* h, float* c, cudaStream_t st) {
 // image sum and the normalisation.
 static epet_status mlem_iteration_grouped(epet_mlem* h, cudaStream_t st) {
   EPET_CHECK(grouped_pass(h->G, h->x, h->y, h->ybar, st));
-  EPET_CHECK(launch_rows(h->G.plan_cols, h->G.cg_ptr, h->G.cg_slot, h->G.ones, h->G.partial,
+  EPET_CHECK(launch_sums(h->G.plan_cols, h->G.cg_ptr, h->G.cg_slot, h->G.partial,
                          h->V, EpiMlemUpdate{h->x, h->s, h->xnew, nullptr}, nullptr, st));
   return launch_sum_normalise(h->xnew, h->V, h->part_x, h->x, st);
 }
@@ -492,7 +492,7 @@ epet_status epet_mlem_create(const epet_problem* p, const int32_t* rows_d, const
         rc = tune_rows(
             4, V, h->G.nslots, h->G.ngroups, V ? (double)h->G.nslots / V : 0.0,
             [&](const RowPlan& pl) {
-              return launch_rows(pl, h->G.cg_ptr, h->G.cg_slot, h->G.ones, h->G.partial, h->V,
+              return launch_sums(pl, h->G.cg_ptr, h->G.cg_slot, h->G.partial, h->V,
                                  EpiMlemUpdate{h->x, h->s, h->xnew, nullptr}, nullptr, st);
             },
             st, &h->G.plan_cols);

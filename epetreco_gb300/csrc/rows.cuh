@@ -119,6 +119,75 @@ __device__ __forceinline__ float group_dot_vec(const int32_t* __restrict__ idx,
   return a;
 }
 
+// The same sums with every value 1 (no value stream): sum of x over the
+// row's indices, in the same order as the dot products above (a product by
+// 1 is exact, so the results equal theirs).
+template <int G>
+__device__ __forceinline__ float group_sum_scalar(const int32_t* __restrict__ idx,
+                                                  const float* __restrict__ x, int64_t beg,
+                                                  int64_t end, int lg) {
+  float a0 = 0.f, a1 = 0.f, a2 = 0.f, a3 = 0.f;
+  int64_t k = beg + lg;
+  for (; k + 3 * G < end; k += 4 * G) {
+    const int c0 = ld_stream(idx + k), c1 = ld_stream(idx + k + G);
+    const int c2 = ld_stream(idx + k + 2 * G), c3 = ld_stream(idx + k + 3 * G);
+    a0 += __ldg(x + c0);
+    a1 += __ldg(x + c1);
+    a2 += __ldg(x + c2);
+    a3 += __ldg(x + c3);
+  }
+  for (; k < end; k += G) a0 += __ldg(x + ld_stream(idx + k));
+  float a = (a0 + a1) + (a2 + a3);
+#pragma unroll
+  for (int o = G / 2; o > 0; o >>= 1) a += __shfl_xor_sync(0xffffffffu, a, o, G);
+  return a;
+}
+
+template <int G, int U>
+__device__ __forceinline__ float group_sum_vec(const int32_t* __restrict__ idx,
+                                               const float* __restrict__ x, int64_t beg,
+                                               int64_t end, int lg) {
+  const int64_t h = min(end, (beg + 3) & ~int64_t(3));
+  const int64_t t = max(h, end & ~int64_t(3));
+  float acc[U];
+#pragma unroll
+  for (int u = 0; u < U; u++) acc[u] = 0.f;
+  if (lg < h - beg) acc[0] = 1.f * __ldg(x + ld_stream(idx + beg + lg));
+  if (lg < end - t) acc[U - 1] += __ldg(x + ld_stream(idx + t + lg));
+  const int4* __restrict__ c4 = reinterpret_cast<const int4*>(idx + h);
+  const int64_t nc = (t - h) >> 2;
+  int4 c[U];
+#pragma unroll
+  for (int u = 0; u < U; u++) {
+    const int64_t jj = lg + u * G;
+    if (jj < nc) c[u] = __ldcs(c4 + jj);
+  }
+  for (int64_t j = lg; j < nc; j += U * G) {
+    int4 cn[U];
+#pragma unroll
+    for (int u = 0; u < U; u++) {
+      const int64_t jj = j + (U + u) * G;
+      if (jj < nc) cn[u] = __ldcs(c4 + jj);
+    }
+#pragma unroll
+    for (int u = 0; u < U; u++) {
+      if (j + u * G < nc) {
+        acc[u] += __ldg(x + c[u].x);
+        acc[u] += __ldg(x + c[u].y);
+        acc[u] += __ldg(x + c[u].z);
+        acc[u] += __ldg(x + c[u].w);
+      }
+      c[u] = cn[u];
+    }
+  }
+  float a = acc[0];
+#pragma unroll
+  for (int u = 1; u < U; u++) a += acc[u];
+#pragma unroll
+  for (int o = G / 2; o > 0; o >>= 1) a += __shfl_xor_sync(0xffffffffu, a, o, G);
+  return a;
+}
+
 // Row dot product in the form the template arguments select.
 template <int G, int U, bool VEC>
 __device__ __forceinline__ float row_dot(const int32_t* __restrict__ idx,
@@ -127,6 +196,13 @@ __device__ __forceinline__ float row_dot(const int32_t* __restrict__ idx,
                                          int lg) {
   if constexpr (VEC) return group_dot_vec<G, U>(idx, val, x, beg, end, lg);
   else return group_dot_scalar<G>(idx, val, x, beg, end, lg);
+}
+template <int G, int U, bool VEC>
+__device__ __forceinline__ float row_sum(const int32_t* __restrict__ idx,
+                                         const float* __restrict__ x, int64_t beg, int64_t end,
+                                         int lg) {
+  if constexpr (VEC) return group_sum_vec<G, U>(idx, x, beg, end, lg);
+  else return group_sum_scalar<G>(idx, x, beg, end, lg);
 }
 
 // Fixed-order block sum of one double per thread into *out (thread 0);

@@ -44,6 +44,27 @@ k_rows(const int64_t* __restrict__ ptr, const int32_t* __restrict__ idx,
   }
 }
 
+// The same with every value 1 (out = Epi(row, sum of x over the row's
+// indices)): the grouped layout's per-column sums over its slots.
+template <int G, int U, bool VEC, class Epi>
+__global__ void __launch_bounds__(kSpmvThreads)
+k_sums(const int64_t* __restrict__ ptr, const int32_t* __restrict__ idx,
+       const float* __restrict__ x, int64_t nrows, Epi epi, double* __restrict__ partial) {
+  constexpr int RPT = kSpmvThreads / G;
+  __shared__ double red[kSpmvThreads / 32];
+  const int lg = threadIdx.x % G;
+  const int64_t ntiles = (nrows + RPT - 1) / RPT;
+  for (int64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+    const int64_t row = tile * RPT + threadIdx.x / G;
+    double part = 0.0;
+    if (row < nrows) {
+      const float d = row_sum<G, U, VEC>(idx, x, ptr[row], ptr[row + 1], lg);
+      if (lg == 0) part = epi(row, d);
+    }
+    if (partial) block_sum_to(part, red, partial + tile);
+  }
+}
+
 // Fixed-order sum of the block partials.
 __global__ void k_sum_partials(const double* __restrict__ p, int64_t n, double* out) {
   __shared__ double red[32];
@@ -99,6 +120,26 @@ epet_status launch_rows(const RowPlan& plan, const int64_t* ptr, const int32_t* 
   EPET_LAUNCHED();
   return EPET_OK;
 }
+
+template <class Epi>
+epet_status launch_sums(const RowPlan& plan, const int64_t* ptr, const int32_t* idx,
+                        const float* x, int64_t nrows, Epi epi, double* partial,
+                        cudaStream_t st) {
+  if (nrows <= 0) return EPET_OK;
+  const int64_t nt = plan_tiles(plan, nrows);
+  const unsigned grid = (unsigned)(plan.grid > 0 ? std::min<int64_t>(nt, plan.grid) : nt);
+  dispatch_plan(plan, aligned16(idx, idx), [&](auto g, auto u, auto v) {
+    k_sums<decltype(g)::value, decltype(u)::value, decltype(v)::value, Epi>
+        <<<grid, kSpmvThreads, 0, st>>>(ptr, idx, x, nrows, epi, partial);
+  });
+  EPET_LAUNCHED();
+  return EPET_OK;
+}
+template epet_status launch_sums<EpiMlemUpdate>(const RowPlan&, const int64_t*, const int32_t*,
+                                                const float*, int64_t, EpiMlemUpdate, double*,
+                                                cudaStream_t);
+template epet_status launch_sums<EpiKeep>(const RowPlan&, const int64_t*, const int32_t*,
+                                          const float*, int64_t, EpiKeep, double*, cudaStream_t);
 
 template epet_status launch_rows<EpiMlemForward>(const RowPlan&, const int64_t*, const int32_t*,
                                                  const float*, const float*, int64_t,

@@ -74,6 +74,13 @@ epet_status launch_rows(const RowPlan& plan, const int64_t* ptr, const int32_t* 
                         const float* val, const float* x, int64_t nrows, Epi epi,
                         double* partial, cudaStream_t st);
 
+// The same with every value 1 and no value stream: out = Epi(row, sum of
+// x over the row's indices), equal to launch_rows with values 1.
+template <class Epi>
+epet_status launch_sums(const RowPlan& plan, const int64_t* ptr, const int32_t* idx,
+                        const float* x, int64_t nrows, Epi epi, double* partial,
+                        cudaStream_t st);
+
 // Autotuner: times run(plan) over candidate plans around default_plan(avg)
 // (group sizes, unroll depths, persistent grids) and returns the fastest.
 // Results are cached per (device, kind, rows, nnz, cols) for the life of the
