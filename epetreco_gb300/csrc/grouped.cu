@@ -96,6 +96,34 @@ __device__ __forceinline__ void load_spans(const RowSource& A, int r0, int r1, G
   __syncthreads();
 }
 
+// Calls f(k, row, j, column) for every entry k of the group (row-major
+// order: entry j of row `row`), thread-strided, with the column loads of
+// kEntryBatch entries issued before any is used (the loop is otherwise
+// bound by each load's latency).
+constexpr int kEntryBatch = 4;
+template <class F>
+__device__ __forceinline__ void for_group_entries(const GroupSpans& S, int nr, F&& f) {
+  const int ntot = S.off[nr];
+  int r = 0;
+  for (int k0 = threadIdx.x; k0 < ntot; k0 += kEntryBatch * kGroupThreads) {
+    int rr[kEntryBatch], jj[kEntryBatch], cc[kEntryBatch];
+#pragma unroll
+    for (int u = 0; u < kEntryBatch; u++) {
+      const int k = k0 + u * kGroupThreads;
+      rr[u] = -1;
+      if (k < ntot) {
+        while (S.off[r + 1] <= k) r++;  // k ascends per thread: the row only moves forward
+        rr[u] = r;
+        jj[u] = k - S.off[r];
+        cc[u] = S.col[r][jj[u]];
+      }
+    }
+#pragma unroll
+    for (int u = 0; u < kEntryBatch; u++)
+      if (rr[u] >= 0) f(k0 + u * kGroupThreads, rr[u], jj[u], (unsigned)cc[u]);
+  }
+}
+
 // Distinct columns of the candidate groups cand[g] = {r0, r1}: a bitmap over
 // the columns in shared memory (nwords 32-bit words).
 __global__ void __launch_bounds__(kGroupThreads)
@@ -107,14 +135,9 @@ k_group_distinct(RowSource A, const int2* __restrict__ cand, int nwords,
   for (int i = threadIdx.x; i < nwords; i += kGroupThreads) gbm[i] = 0u;
   const int2 c = cand[blockIdx.x];
   load_spans(A, c.x, c.y, &S);
-  {
-    int r = 0;
-    for (int k = threadIdx.x; k < S.off[c.y - c.x]; k += kGroupThreads) {
-      while (S.off[r + 1] <= k) r++;  // k ascends per thread: the row only moves forward
-      const unsigned v = (unsigned)S.col[r][k - S.off[r]];
-      atomicOr(&gbm[v >> 5], 1u << (v & 31));
-    }
-  }
+  for_group_entries(S, c.y - c.x, [&](int, int, int, unsigned v) {
+    atomicOr(&gbm[v >> 5], 1u << (v & 31));
+  });
   __syncthreads();
   int n = 0;
   for (int i = threadIdx.x; i < nwords; i += kGroupThreads) n += __popc(gbm[i]);
@@ -173,15 +196,9 @@ k_group_tables(RowSource A, const GroupDesc* __restrict__ groups, int nwords,
   const int nr = gd.r1 - gd.r0;
   for (int i = threadIdx.x; i < nwords; i += kGroupThreads) bm[i] = 0u;
   load_spans(A, gd.r0, gd.r1, &S);
-  const int ntot = S.off[nr];
-  {
-    int r = 0;
-    for (int k = threadIdx.x; k < ntot; k += kGroupThreads) {
-      while (S.off[r + 1] <= k) r++;
-      const unsigned v = (unsigned)S.col[r][k - S.off[r]];
-      atomicOr(&bm[v >> 5], 1u << (v & 31));
-    }
-  }
+  for_group_entries(S, nr, [&](int, int, int, unsigned v) {
+    atomicOr(&bm[v >> 5], 1u << (v & 31));
+  });
   __syncthreads();
   // exclusive prefix of the words' popcounts: thread t owns a contiguous
   // range of words
@@ -213,19 +230,13 @@ k_group_tables(RowSource A, const GroupDesc* __restrict__ groups, int nwords,
   __syncthreads();
   // the entries (thread-strided over the group's entries, each finding its
   // row), then the rows' padding (at most 3 entries a row)
-  {
-    int r = 0;
-    for (int k = threadIdx.x; k < ntot; k += kGroupThreads) {
-      while (S.off[r + 1] <= k) r++;
-      const int j = k - S.off[r];
-      const int64_t d = ptr[gd.r0 + r];
-      const int nq = (int)((ptr[gd.r0 + r + 1] - d) >> 2);
-      const unsigned v = (unsigned)S.col[r][j];
-      const int64_t o = d + group_slot(j, nq);
-      pval[o] = S.val[r][j];
-      ploc[o] = (uint16_t)sw_rank(pre[v >> 5] + __popc(bm[v >> 5] & ((1u << (v & 31)) - 1u)));
-    }
-  }
+  for_group_entries(S, nr, [&](int, int r, int j, unsigned v) {
+    const int64_t d = ptr[gd.r0 + r];
+    const int nq = (int)((ptr[gd.r0 + r + 1] - d) >> 2);
+    const int64_t o = d + group_slot(j, nq);
+    pval[o] = S.val[r][j];
+    ploc[o] = (uint16_t)sw_rank(pre[v >> 5] + __popc(bm[v >> 5] & ((1u << (v & 31)) - 1u)));
+  });
   for (int t = threadIdx.x; t < 4 * nr; t += kGroupThreads) {
     const int rr = t >> 2;
     const int n = S.off[rr + 1] - S.off[rr];
