@@ -318,9 +318,11 @@ epet_status epet_mlem_batch_create(int32_t nprob, const epet_problem* problems,
     // kinds 5 / 6 / 7 keep batch plans apart from single-matrix plans
     epet_status rc = EPET_OK;
     if (all_grouped) {
-      // one pass fills the slots; the slot sums' candidates rerun the
-      // (idempotent) update epilogue
-      rc = grouped_pass_batch(h->gdesc, h->gstart, np, h->total_groups, h->gwide, h->nwide, st);
+      // one pass fills the slots (unless the plan is cached); the slot
+      // sums' candidates rerun the (idempotent) update epilogue
+      if (!tune_lookup(7, h->voxels, nslots, np, &h->plan_bwd))
+        rc = grouped_pass_batch(h->gdesc, h->gstart, np, h->total_groups, h->gwide, h->nwide,
+                                st);
       if (rc == EPET_OK)
         rc = tune_rows(
             7, h->voxels, nslots, np, avg_col,

@@ -485,12 +485,15 @@ epet_status epet_mlem_create(const epet_problem* p, const int32_t* rows_d, const
     ALLOC(h->part_ll, 1024 * 8);
     ALLOC(h->part_x, sum_blocks(V) * 8);
     if (o.autotune) {
-      // the slot sums' launch shape: one pass fills the slots, then the
-      // candidates run the real (idempotent) epilogue
-      rc = grouped_pass(h->G, h->x, h->y, h->ybar, st);
+      // the slot sums' launch shape (from the cache when this shape was
+      // tuned before; else one pass fills the slots, then the candidates
+      // run the real, idempotent, epilogue)
+      const double avg = V ? (double)h->G.nslots / V : 0.0;
+      if (!tune_lookup(4, V, h->G.nslots, h->G.ngroups, &h->G.plan_cols))
+        rc = grouped_pass(h->G, h->x, h->y, h->ybar, st);
       if (rc == EPET_OK)
         rc = tune_rows(
-            4, V, h->G.nslots, h->G.ngroups, V ? (double)h->G.nslots / V : 0.0,
+            4, V, h->G.nslots, h->G.ngroups, avg,
             [&](const RowPlan& pl) {
               return launch_sums(pl, h->G.cg_ptr, h->G.cg_slot, h->G.partial, h->V,
                                  EpiMlemUpdate{h->x, h->s, h->xnew, nullptr}, nullptr, st);
