@@ -69,6 +69,7 @@ SIGNATURES = {
     "epet_version": [],
     "epet_launch_count": [],
     "epet_device_allocations": [],
+    "epet_debug_fail_allocations": [C.c_longlong],
     "epet_problem_validate": [P],
     "epet_trig_table": [P, VP, VP],
     "epet_dump_uniforms": [P, VP, I64, VP, VP],
@@ -137,6 +138,8 @@ SIGNATURES = {
     "epet_h5_write_measurement": [C.c_char_p, VP, I64],
     "epet_h5_write_density": [C.c_char_p, VP, C.POINTER(Grid)],
     "epet_h5_read_density": [C.c_char_p, VP, I64, C.POINTER(Grid)],
+    "epet_h5_write_checkpoint": [C.c_char_p, VP, C.POINTER(Grid), I64],
+    "epet_h5_read_attribute": [C.c_char_p, C.c_char_p, C.c_char_p, C.POINTER(C.c_double)],
 }
 _RESTYPES = {
     "epet_last_error": C.c_char_p,

@@ -391,6 +391,12 @@ def trim_memory(keep_bytes: int = 0) -> None:
     check(lib().epet_trim_memory(int(keep_bytes)))
 
 
+def debug_fail_allocations(after: int) -> None:
+    """Fault injection for tests: after `after` more device allocations the
+    library's allocations fail (EPET_ERR_CUDA) until called with -1."""
+    check(lib().epet_debug_fail_allocations(int(after)))
+
+
 def build_counters() -> dict:
     """Rows of system-matrix builds since load that were redone with their
     exact window size, and rows on the per-candidate path."""
@@ -477,6 +483,22 @@ class Mlem:
         pl = (C.c_int32 * 6)()
         check(lib().epet_mlem_plan(self._h, pl))
         return {"forward": tuple(pl[0:3]), "transpose": tuple(pl[3:6])}
+
+    def checkpoint(self, path, iteration: int) -> None:
+        """The image as the reference's "density" file (its grid attributes)
+        plus an int attribute "iteration" (the iterations done), the restart
+        point that reco.cu's "<it>_<out>" files are (reco.cu:284-291)."""
+        from . import h5
+        h5.write_checkpoint(path, self.image().cpu().numpy(), self.p.grid, iteration)
+
+    def resume(self, path) -> int:
+        """Sets the image from a checkpoint file and returns its iteration
+        count (0 for a plain "density" file without one)."""
+        import torch
+        from . import h5
+        x, _, it = h5.read_checkpoint(path)
+        self.set_image(torch.from_numpy(x.ravel()).cuda())
+        return it
 
     @property
     def layout(self) -> int:

@@ -343,9 +343,10 @@ epet_status epet_csr_compress(const epet_csr* a, int32_t format, epet_csr16* out
     rc = set_error(EPET_ERR_INVALID, "delta/q buffers missing");
   if (rc == EPET_OK) {
     int64_t* tmp = nullptr;
-    dev_alloc((void**)&tmp, scan_tmp_elems(a->m + 1) * 8, st);
-    rc = exclusive_scan_i64(cnt, out->row_ptr, a->m, tmp, st);
-    dev_free(tmp, st);
+    cudaError_t e = dev_alloc((void**)&tmp, scan_tmp_elems(a->m + 1) * 8, st);
+    rc = e == cudaSuccess ? exclusive_scan_i64(cnt, out->row_ptr, a->m, tmp, st)
+                          : cuda_status(e, "allocation of the scan");
+    if (tmp) dev_free(tmp, st);
   }
   if (rc == EPET_OK) {
     const unsigned nb = (unsigned)ceil_div(a->m * 32, 256);

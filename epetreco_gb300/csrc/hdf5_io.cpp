@@ -22,6 +22,7 @@
 #include <stdint.h>
 
 #include <algorithm>
+#include <climits>
 #include <cstdio>
 #include <cstring>
 #include <string>
@@ -609,8 +610,10 @@ epet_status epet_h5_write_measurement(const char* path, const float* y_h, int64_
   return write_file(path, "messung", y_h, {(uint64_t)n}, {});
 }
 
-epet_status epet_h5_write_density(const char* path, const float* x_h, const epet_grid* g) {
+static epet_status write_density(const char* path, const float* x_h, const epet_grid* g,
+                                 int64_t iteration) {
   if (!g) return set_error(EPET_ERR_INVALID, "grid is NULL");
+  if (iteration > INT32_MAX) return set_error(EPET_ERR_INVALID, "iteration over 2^31");
   std::vector<AttrOut> at;
   const char* ax[3] = {"x", "y", "z"};
   float mx[3];
@@ -621,8 +624,33 @@ epet_status epet_h5_write_density(const char* path, const float* x_h, const epet
   for (int d = 0; d < 3; d++) at.push_back({std::string(ax[d]) + "min", true, fbits(g->o[d])});
   for (int d = 0; d < 3; d++) at.push_back({std::string(ax[d]) + "max", true, fbits(mx[d])});
   for (int d = 0; d < 3; d++) at.push_back({std::string(ax[d]) + "nbin", false, (uint32_t)g->n[d]});
+  if (iteration >= 0) at.push_back({"iteration", false, (uint32_t)iteration});
   return write_file(path, "density", x_h,
                     {(uint64_t)g->n[0], (uint64_t)g->n[1], (uint64_t)g->n[2]}, at);
+}
+
+epet_status epet_h5_write_density(const char* path, const float* x_h, const epet_grid* g) {
+  return write_density(path, x_h, g, -1);
+}
+
+epet_status epet_h5_write_checkpoint(const char* path, const float* x_h, const epet_grid* g,
+                                     int64_t iteration) {
+  if (iteration < 0) return set_error(EPET_ERR_INVALID, "iteration < 0");
+  return write_density(path, x_h, g, iteration);
+}
+
+epet_status epet_h5_read_attribute(const char* path, const char* name, const char* attr,
+                                   double* value_h) {
+  Reader R;
+  DatasetInfo di;
+  H5_CHECK(open_dataset(path, name, &R, &di));
+  if (!attr) return set_error(EPET_ERR_INVALID, "attribute name is NULL");
+  for (const DatasetInfo::Attr& a : di.attrs)
+    if (a.name == attr && (int)a.raw.size() >= a.size && (a.cls == 0 || a.cls == 1)) {
+      if (value_h) *value_h = element(a.raw.data(), a.cls, a.size, a.big, a.sgn);
+      return EPET_OK;
+    }
+  return set_error(EPET_ERR_INVALID, "%s: \"%s\" has no numeric attribute %s", path, name, attr);
 }
 
 epet_status epet_h5_read_density(const char* path, float* x_h, int64_t n, epet_grid* g_h) {

@@ -773,10 +773,11 @@ epet_status epet_sensitivity(const epet_problem* p, const int32_t* rows_d, int64
     // normalised to sum 1 as backprojection.cu:157-161
     const int nb = (int)std::max<int64_t>(1, std::min<int64_t>(ceil_div(V, 256), 1024));
     double* part = nullptr;
-    dev_alloc((void**)&part, (nb + 1) * 8, st);
-    rc = sum_f64(s_d, V, part, nb, part + nb, st);
+    cudaError_t e = dev_alloc((void**)&part, (nb + 1) * 8, st);
+    rc = e == cudaSuccess ? sum_f64(s_d, V, part, nb, part + nb, st)
+                          : cuda_status(e, "allocation of the sum");
     if (rc == EPET_OK) rc = launch_normalise(s_d, part + nb, V, s_d, st);
-    dev_free(part, st);
+    if (part) dev_free(part, st);
   }
   if (!s64_d) dev_free(s64, st);
   return rc;

@@ -14,7 +14,9 @@
 // float[V] in voxel-id order.  <geometry> is 20 comma-separated numbers:
 // pos0x,pos1x,na,n0z,n0y,n1z,n1y,da,segx,segy,segz, ox,oy,oz,dx,dy,dz,
 // nx,ny,nz.  Writes "<it>_<out>" after every iteration as reco.cu does
-// (reco.cu:284-291).
+// (reco.cu:284-291); HDF5 outputs also carry the iterations done (attribute
+// "iteration"), and a guess file that carries it resumes the count there:
+// iterations it .. nIt-1 run, named as in the uninterrupted run.
 //
 // Default: the reference's loop -- the system matrix of each row chunk is
 // rebuilt in every iteration (reco.cu:216-254).  --matrix-once: the library's
@@ -98,8 +100,10 @@ std::vector<float> read_f32(const std::string& fn, const char* name) {
   return v;
 }
 
-bool write_f32(const std::string& fn, const std::vector<float>& v, const epet_grid& g) {
-  if (is_h5(fn)) return epet_h5_write_density(fn.c_str(), v.data(), &g) == EPET_OK;
+// An image file; HDF5 ones record the iterations done.
+bool write_f32(const std::string& fn, const std::vector<float>& v, const epet_grid& g,
+               int iterations_done) {
+  if (is_h5(fn)) return epet_h5_write_checkpoint(fn.c_str(), v.data(), &g, iterations_done) == EPET_OK;
   FILE* f = fopen(fn.c_str(), "wb");
   if (!f) return false;
   bool ok = fwrite(v.data(), 4, v.size(), f) == v.size();
@@ -173,6 +177,12 @@ int main(int argc, char** argv) {
     // density guess or homogeneous, normalised (reco.cu:113-137)
     std::vector<float> x_host = read_f32(xfn, "density");
     const bool xgood = (int)x_host.size() == V;
+    int it0 = 0;  // iterations already done (a checkpoint guess)
+    if (xgood && is_h5(xfn)) {
+      double v = 0.0;
+      if (epet_h5_read_attribute(xfn.c_str(), "density", "iteration", &v) == EPET_OK && v > 0)
+        it0 = (int)v;
+    }
     if (!xgood) x_host.assign(V, 1.f);
     float* x_devi = nullptr;
     CK(cudaMalloc((void**)&x_devi, sizeof(float) * V));
@@ -203,14 +213,14 @@ int main(int argc, char** argv) {
       epet_shim::check(epet_mlem_create(&p, yRowId_devi, yVal_devi, effM, s_devi, &o, &h, 0),
                        "epet_mlem_create");
       if (xgood) epet_shim::check(epet_mlem_set_image(h, x_devi, 0), "set image");
-      for (int it = 0; it < nIt; it++) {
+      for (int it = it0; it < nIt; it++) {
         double ll = 0;
         epet_shim::check(epet_mlem_iterate(h, 1, &ll, 0), "iterate");
         epet_shim::check(epet_mlem_get_image(h, x_devi, 0), "image");
         CK(cudaMemcpy(x_host.data(), x_devi, sizeof(float) * V, cudaMemcpyDeviceToHost));
         std::stringstream ss;
         ss << it;
-        write_f32(ss.str() + "_" + on, x_host, egrid);
+        write_f32(ss.str() + "_" + on, x_host, egrid, it + 1);
         printf("it %d loglik %.9g\n", it, ll);
       }
       epet_mlem_destroy(h);
@@ -240,7 +250,7 @@ int main(int argc, char** argv) {
     const unsigned NChunks =
         nChunks<unsigned, unsigned long long>((unsigned long long)effM * V,
                                               (unsigned long long)LIMM * V);
-    for (int it = 0; it < nIt; it++) {
+    for (int it = it0; it < nIt; it++) {
       CK(cudaMemset(c, 0, sizeof(float) * V));
       for (unsigned chunkId = 0; chunkId < NChunks; chunkId++) {
         unsigned m = nInChunk<unsigned, unsigned>(chunkId, effM, LIMM);
@@ -269,7 +279,7 @@ int main(int argc, char** argv) {
       CK(cudaMemcpy(x_host.data(), x_devi, sizeof(float) * V, cudaMemcpyDeviceToHost));
       std::stringstream ss;
       ss << it;
-      write_f32(ss.str() + "_" + on, x_host, egrid);
+      write_f32(ss.str() + "_" + on, x_host, egrid, it + 1);
       printf("it %d norm %.9g\n", it, (double)sum<float>(x_devi, V));
     }
     return 0;

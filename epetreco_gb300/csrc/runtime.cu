@@ -41,7 +41,20 @@ static cudaMemPool_t lib_pool(cudaError_t* err) {
 
 static std::atomic<long long> g_allocs{0};
 
+// Host-side fault injection for tests of the error paths: after this many
+// more allocations (-1: never) every device allocation of the library fails
+// with cudaErrorMemoryAllocation.  Nothing reaches the device.
+static std::atomic<long long> g_fail_after{-1};
+
 cudaError_t dev_alloc(void** p, size_t bytes, cudaStream_t st) {
+  long long left = g_fail_after.load(std::memory_order_relaxed);
+  while (left >= 0) {
+    if (left == 0) {
+      *p = nullptr;
+      return cudaErrorMemoryAllocation;
+    }
+    if (g_fail_after.compare_exchange_weak(left, left - 1, std::memory_order_relaxed)) break;
+  }
   g_allocs.fetch_add(1, std::memory_order_relaxed);
   cudaError_t e = cudaSuccess;
   cudaMemPool_t pool = lib_pool(&e);
@@ -137,6 +150,11 @@ const char* epet_last_error(void) { return epet::g_err; }
 const char* epet_version(void) { return "epet_gb300 1.0 (sm_103a)"; }
 
 long long epet_launch_count(void) { return epet::launches(); }
+
+epet_status epet_debug_fail_allocations(long long after) {
+  epet::g_fail_after.store(after < 0 ? -1 : after, std::memory_order_relaxed);
+  return EPET_OK;
+}
 
 long long epet_device_allocations(void) { return epet::g_allocs.load(); }
 

@@ -97,3 +97,34 @@ def read_density(ifn):
     _lib.check(_lib.lib().epet_h5_read_density(_path(ifn), x.ctypes.data_as(C.c_void_p), x.size,
                                                C.byref(g)))
     return x, VoxelGrid(tuple(g.o), tuple(g.d), tuple(g.n))
+
+
+def write_checkpoint(path, density, grid: VoxelGrid, iteration: int) -> None:
+    """A "density" file with an int attribute "iteration" (a restart point)."""
+    x = np.ascontiguousarray(np.asarray(density, np.float32).ravel())
+    n = int(np.prod(grid.n))
+    if x.size != n:
+        raise ValueError(f"density holds {x.size} values, the grid {n}")
+    g = _grid_struct(grid)
+    _lib.check(_lib.lib().epet_h5_write_checkpoint(_path(path), x.ctypes.data_as(C.c_void_p),
+                                                   C.byref(g), int(iteration)))
+
+
+def read_attribute(path, name: str, attr: str) -> float:
+    """Numeric scalar attribute `attr` of dataset `name`."""
+    v = C.c_double()
+    _lib.check(_lib.lib().epet_h5_read_attribute(_path(path), name.encode(), attr.encode(),
+                                                 C.byref(v)))
+    return v.value
+
+
+def read_checkpoint(path):
+    """(image [nx, ny, nz], VoxelGrid, iterations done; 0 for a "density"
+    file without the "iteration" attribute)."""
+    x, g = read_density(path)
+    try:
+        it = int(read_attribute(path, "density", "iteration"))
+    except _lib.EpetError:
+        it = 0
+    return x, g, it
+

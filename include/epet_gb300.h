@@ -140,6 +140,11 @@ long long epet_launch_count(void);
  * (from its memory pool; caller workspaces are not counted).  For
  * accounting and tests; no counterpart in the reference. */
 long long epet_device_allocations(void);
+/* Fault injection for tests of the error paths (no counterpart in the
+ * reference): after `after` more device allocations every allocation the
+ * library makes fails with EPET_ERR_CUDA (out of memory), on the host side,
+ * without touching the device; after < 0 switches it off. */
+epet_status epet_debug_fail_allocations(long long after);
 /* Problem checks: index ranges fit int32, nrays >= 1, positive pitches,
  * ray_mode one of EPET_RAYS_*. */
 epet_status epet_problem_validate(const epet_problem* p);
@@ -519,6 +524,16 @@ epet_status epet_h5_write_measurement(const char* path, const float* y_h, int64_
  * zmin (= grid->o) and xmax, ymax, zmax (= o + n * d), int attributes xnbin,
  * ynbin, znbin. */
 epet_status epet_h5_write_density(const char* path, const float* x_h, const epet_grid* grid);
+/* A restart point: the "density" file of epet_h5_write_density plus an int
+ * attribute "iteration" (the iterations done).  The reference's per-iteration
+ * "<it>_<out>" files (reco.cu:284-291) are its restart points, fed back as the
+ * guess (reco.cu:114-137), without the count. */
+epet_status epet_h5_write_checkpoint(const char* path, const float* x_h, const epet_grid* grid,
+                                     int64_t iteration);
+/* A numeric scalar attribute attr of dataset name, as double;
+ * EPET_ERR_INVALID when the dataset has none of that name. */
+epet_status epet_h5_read_attribute(const char* path, const char* name, const char* attr,
+                                   double* value_h);
 /* Reads a "density" file: the image (n elements; x_h may be NULL) and the
  * grid from its attributes (pitch = (max - min) / nbin; grid_h may be NULL). */
 epet_status epet_h5_read_density(const char* path, float* x_h, int64_t n, epet_grid* grid_h);

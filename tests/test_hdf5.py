@@ -188,3 +188,23 @@ def test_errors(tmp_path):
     st = L.epet_h5_read_measurement(os.fsencode(fn), rows.ctypes.data, rows.ctypes.data, 0,
                                     None, None)
     assert st == 2  # 8 measured channels, capacity 0
+
+
+def test_checkpoint_carries_the_iteration(tmp_path):
+    g = VoxelGrid((-0.01, -0.01, -0.01), (0.002, 0.002, 0.002), (4, 5, 6))
+    x = np.random.default_rng(7).random(g.nvoxels).astype(np.float32)
+    fn = tmp_path / "3_img.h5"
+    h5().write_checkpoint(fn, x, g, 3)
+    xr, gr, it = h5().read_checkpoint(fn)
+    assert it == 3 and gr.n == g.n and np.array_equal(xr.ravel(), x)
+    assert h5().read_attribute(fn, "density", "iteration") == 3.0
+    assert h5().read_attribute(fn, "density", "znbin") == 6.0
+    # still the reference's density file: its nine attributes and dataset
+    assert np.array_equal(h5().readHDF5_Density(fn), x)
+    plain = tmp_path / "img.h5"
+    h5().writeHDF5_Density(x, plain, g)
+    assert h5().read_checkpoint(plain)[2] == 0
+    with pytest.raises(_lib.EpetError, match="no numeric attribute"):
+        h5().read_attribute(plain, "density", "iteration")
+    with pytest.raises(_lib.EpetError):
+        h5().write_checkpoint(tmp_path / "bad.h5", x, g, -1)
