@@ -248,10 +248,12 @@ epet_status epet_mlem_batch_create(int32_t nprob, const epet_problem* problems,
   std::vector<int64_t> gs_h(np + 1, 0);
   std::vector<int32_t> gw_h;  // global ids of the wide groups
   for (int i = 0; i < np; i++) {
-    const epet_mlem* p = h->probs[i];
+    epet_mlem* p = h->probs[i];
     if (all_grouped) {
       // the transpose launch sums the problem's slots: the slot lists as
       // "columns", the ones as values, the slots' corrections gathered
+      const epet_status rc = grouped_ones(&p->G, st);
+      if (rc != EPET_OK) return fail(rc);
       dh[i] = BatchDesc{nullptr, nullptr, nullptr, p->G.cg_ptr, p->G.cg_slot, p->G.ones,
                         p->y, p->G.partial, p->ybar, p->s, p->x, p->xnew, p->m, p->V};
       grouped_batch_desc(p->G, p->x, p->y, p->ybar, gd_h.data() + i * grouped_batch_desc_bytes());

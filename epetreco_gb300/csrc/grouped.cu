@@ -42,7 +42,7 @@ constexpr int kGroupThreads = 256;   // threads of the table-building kernels
 constexpr int kTrash = kGroupCap;    // rank of the padding entries
 // Shared tables are indexed by rank (the word of rank r sits in bank r % 32).
 // A row's entries are stored so that each warp-wide shared access of the
-// pass takes 32 consecutive entries of the row (group_slot): their ranks
+// pass takes 32 consecutive entries of the row (k_group_tables): their ranks
 // ascend by a few, which spreads them over the banks better than the fixed
 // swizzles of the ranks tried: 2.05 distinct-address wavefronts per 32
 // entries on rows of the full workload, against 2.94 with a lane taking 4
@@ -151,37 +151,55 @@ k_group_distinct(RowSource A, const int2* __restrict__ cand, int nwords,
   }
 }
 
-// Storage position of a row's j-th entry (its CSR order, then padding) in a
-// row of nq 4-entry chunks.  The pass hands chunk 32 u + l to lane l in
-// round u and reads position t of every lane's chunk with one shared access:
-// the entries are placed so that this access takes consecutive entries,
-// i.e. round u (cq = min(32, nq - 32 u) chunks) holds its entries o =
-// t * cq + l at chunk l, position t.
-__host__ __device__ inline int group_slot(int j, int nq) {
-  const int u = j >> 7, o = j & 127;
-  const int cq = nq - 32 * u < 32 ? nq - 32 * u : 32;
-  const int t = (o >= cq) + (o >= 2 * cq) + (o >= 3 * cq);  // o < 4 cq
-  return 128 * u + 4 * (o - t * cq) + t;
-}
+// Storage order of a row of nq 4-entry chunks (its entries j in CSR order,
+// then padding): the pass hands chunk 32 u + l to lane l in round u and
+// reads position t of every lane's chunk with one shared access, so the
+// entries are placed for this access to take consecutive entries: round u
+// (cq = min(32, nq - 32 u) chunks) holds entry j = 128 u + t cq + l at chunk
+// l, position t, i.e. at 128 u + 4 l + t.
 
 // Tables and the padded layout of the final groups (one block per group):
 // the group's distinct columns, ascending, at table[tb ..]; every row r's
-// entries at ptr[r] (a multiple of 4) onwards in the order of group_slot,
+// entries at ptr[r] (a multiple of 4) onwards in the storage order above,
 // each as its value and its column's rank among the group's columns, then
 // zero values on the trash rank up to the next multiple of 4.  A single row
 // wider than the shared tables (a "wide" group) keeps its own columns as its
 // table (padded like the row with column 0) and the CSR order; its padding
 // points past the row in that table.
+//
+// Two launches.  The first (nd_out set, groups null, table the scratch
+// ftab) takes the first cuts, block b the rows [32 b, min(m, 32 b + 32)): it
+// writes each cut's count of distinct columns to nd_out[b] and, for a cut
+// that fits the shared tables, its table at ftab + b * kGroupCap and its
+// entries.  The second takes the final groups: a first cut kept whole
+// copies its table from ftab to its slots; the groups made by splitting
+// wider cuts are laid out in full.
 __global__ void __launch_bounds__(kGroupThreads)
-k_group_tables(RowSource A, const GroupDesc* __restrict__ groups, int nwords,
+k_group_tables(RowSource A, const GroupDesc* __restrict__ groups, int64_t m, int nwords,
                const int64_t* __restrict__ ptr, int32_t* __restrict__ table,
+               const int32_t* __restrict__ ftab, int32_t* __restrict__ nd_out,
                float* __restrict__ pval, uint16_t* __restrict__ ploc) {
   extern __shared__ unsigned gsh[];
   unsigned* bm = gsh;
   int* pre = reinterpret_cast<int*>(gsh + nwords);
   __shared__ int wtot[kGroupThreads / 32];
-  const GroupDesc gd = groups[blockIdx.x];
-  if (gd.nd > kGroupCap) {  // wide: one row
+  __shared__ int s_nd;
+  const bool first = nd_out != nullptr;
+  GroupDesc gd;
+  if (first) {
+    const int64_t r0 = (int64_t)blockIdx.x * kGroupFirstRows;
+    gd = GroupDesc{(int32_t)r0, (int32_t)min(m, r0 + kGroupFirstRows), 0, 0};
+  } else {
+    gd = groups[blockIdx.x];
+    if (gd.nd <= kGroupCap && gd.r0 % kGroupFirstRows == 0 &&
+        gd.r1 == min(m, (int64_t)gd.r0 + kGroupFirstRows)) {
+      // a first cut kept whole: laid out by the first launch
+      const int32_t* src = ftab + (int64_t)(gd.r0 / kGroupFirstRows) * kGroupCap;
+      for (int j = threadIdx.x; j < gd.nd; j += kGroupThreads) table[gd.tb + j] = src[j];
+      return;
+    }
+  }
+  if (!first && gd.nd > kGroupCap) {  // wide: one row
     const RowSpan rs = row_span(A, gd.r0);
     const int64_t d = ptr[gd.r0], pn = ptr[gd.r0 + 1] - d;
     for (int64_t j = threadIdx.x; j < gd.nd; j += kGroupThreads)
@@ -214,40 +232,66 @@ k_group_tables(RowSource A, const GroupDesc* __restrict__ groups, int nwords,
     const int t = lane < kGroupThreads / 32 ? wtot[lane] : 0;
     const int ti = warp_incl_scan(t);
     if (lane < kGroupThreads / 32) wtot[lane] = ti - t;
+    if (lane == kGroupThreads / 32 - 1) s_nd = ti;
   }
   __syncthreads();
+  if (first) {  // (uniform across the block)
+    if (threadIdx.x == 0) nd_out[blockIdx.x] = s_nd;
+    if (s_nd > kGroupCap) return;  // split by the host, laid out by the second launch
+  }
+  // (the first launch's table is its cut's share of the scratch ftab)
+  int32_t* const tab = first ? table + (int64_t)blockIdx.x * kGroupCap : table + gd.tb;
   int run = wtot[wid] + inc - cnt;
   for (int w = wb; w < we; w++) {
     pre[w] = run;
     unsigned word = bm[w];
     while (word) {
       const int bit = __ffs(word) - 1;
-      table[gd.tb + run] = w * 32 + bit;
+      tab[run] = w * 32 + bit;
       run++;
       word &= word - 1u;
     }
   }
   __syncthreads();
-  // the entries (thread-strided over the group's entries, each finding its
-  // row), then the rows' padding (at most 3 entries a row)
-  for_group_entries(S, nr, [&](int, int r, int j, unsigned v) {
-    const int64_t d = ptr[gd.r0 + r];
-    const int nq = (int)((ptr[gd.r0 + r + 1] - d) >> 2);
-    const int64_t o = d + group_slot(j, nq);
-    pval[o] = S.val[r][j];
-    ploc[o] = (uint16_t)sw_rank(pre[v >> 5] + __popc(bm[v >> 5] & ((1u << (v & 31)) - 1u)));
-  });
-  for (int t = threadIdx.x; t < 4 * nr; t += kGroupThreads) {
-    const int rr = t >> 2;
-    const int n = S.off[rr + 1] - S.off[rr];
-    const int64_t d = ptr[gd.r0 + rr];
-    const int pn = (int)(ptr[gd.r0 + rr + 1] - d);
-    const int j = n + (t & 3);
-    if (j < pn) {
-      const int64_t o = d + group_slot(j, pn >> 2);
-      pval[o] = 0.f;
-      ploc[o] = (uint16_t)sw_rank(kTrash);
+  // the padded layout a 4-entry chunk at a time (thread-strided over the
+  // group's chunks, each finding its row): chunk l of round u of a row holds
+  // its entries j = 128 u + t cq + l (t = 0..3, the storage order above),
+  // padding (j past the row) as zero values on the trash rank; the chunk's
+  // values and ranks are written with one 16-byte and one 8-byte store
+  const int64_t gbase = ptr[gd.r0];
+  const int nch = (int)((ptr[gd.r1] - gbase) >> 2);
+  int r = 0;
+  int pr0 = 0, pr1 = (int)(ptr[gd.r0 + 1] - gbase);  // row r's padded range
+  for (int k = threadIdx.x; k < nch; k += kGroupThreads) {
+    const int p = 4 * k;
+    while (pr1 <= p) {  // k ascends per thread: the row only moves forward
+      r++;
+      pr0 = pr1;
+      pr1 = (int)(ptr[gd.r0 + r + 1] - gbase);
     }
+    const int n = S.off[r + 1] - S.off[r];
+    const int c = (p - pr0) >> 2;  // chunk of the row
+    const int u = c >> 5, l = c & 31;
+    const int cq = min(32, ((pr1 - pr0) >> 2) - 32 * u);
+    int cc[4];
+    float vv[4];
+#pragma unroll
+    for (int t = 0; t < 4; t++) {
+      const int j = 128 * u + t * cq + l;
+      cc[t] = j < n ? S.col[r][j] : -1;
+      vv[t] = j < n ? S.val[r][j] : 0.f;
+    }
+    unsigned rk[4];
+#pragma unroll
+    for (int t = 0; t < 4; t++) {
+      const unsigned v = (unsigned)cc[t];
+      rk[t] = cc[t] >= 0
+                  ? (unsigned)sw_rank(pre[v >> 5] + __popc(bm[v >> 5] & ((1u << (v & 31)) - 1u)))
+                  : (unsigned)sw_rank(kTrash);
+    }
+    *reinterpret_cast<float4*>(pval + gbase + p) = make_float4(vv[0], vv[1], vv[2], vv[3]);
+    *reinterpret_cast<uint2*>(ploc + gbase + p) = make_uint2(rk[0] | (rk[1] << 16),
+                                                             rk[2] | (rk[3] << 16));
   }
 }
 
@@ -258,14 +302,20 @@ __global__ void k_padded_len(RowSource A, int64_t m, int64_t* __restrict__ len) 
   len[r] = (A.rp[q + 1] - A.rp[q] + 3) & ~int64_t(3);
 }
 
-__global__ void k_slot_ids(int64_t n, float* __restrict__ out) {  // slot index bits
-  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i < n) out[i] = __int_as_float((int32_t)i);
-}
-
 __global__ void k_fill_f32(float* __restrict__ p, int64_t n, float v) {
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i < n) p[i] = v;
+}
+
+epet_status grouped_ones(GroupedMatrix* G, cudaStream_t st) {
+  if (G->ones) return EPET_OK;
+  const int64_t ns = std::max<int64_t>(G->nslots, 1);
+  EPET_CUDA(dev_alloc((void**)&G->ones, ns * 4, st));
+  if (G->nslots > 0) {
+    k_fill_f32<<<ceil_div(G->nslots, 256), 256, 0, st>>>(G->ones, G->nslots, 1.f);
+    EPET_LAUNCHED();
+  }
+  return EPET_OK;
 }
 
 // 16-bit values: q = the 16-bit float of value / scale, scale = the row's
@@ -674,17 +724,30 @@ void grouped_drop_fp32(GroupedMatrix* G, cudaStream_t st) {
   }
 }
 
+// Where the first round of form_groups lays out the first cuts that fit
+// (k_group_tables' first launch): the padded row pointers, the scratch
+// tables (kGroupCap per first cut) and the padded values and ranks.
+struct FirstCuts {
+  const int64_t* ptr;
+  int32_t* ftab;
+  float* pval;
+  uint16_t* ploc;
+};
+
 // Groups of consecutive rows of A (row pointers on the device) whose
 // distinct columns fit kGroupCap: first cuts of kGroupFirstRows rows, halved
 // while too wide; a single row wider than that is a group of its own, its
-// table the row's columns padded to whole 4-entry chunks.
-static epet_status form_groups(const RowSource& A, int64_t m, int64_t ncols,
+// table the row's columns padded to whole 4-entry chunks.  The first round
+// measures the first cuts and lays out those that fit (FirstCuts); the
+// halves are measured by k_group_distinct.
+static epet_status form_groups(const RowSource& A, int64_t m, int64_t ncols, const FirstCuts& fc,
                                std::vector<GroupDesc>* out, cudaStream_t st) {
   const int nwords = bitmap_words(ncols);
   struct Piece {
     int32_t r0, r1, nd;  // nd < 0: not measured yet
   };
   std::vector<Piece> ps;
+  ps.reserve((size_t)(m / kGroupFirstRows) + 64);
   for (int64_t r = 0; r < m; r += kGroupFirstRows)
     ps.push_back({(int32_t)r, (int32_t)std::min<int64_t>(m, r + kGroupFirstRows), -1});
   int2* cand = nullptr;
@@ -693,21 +756,32 @@ static epet_status form_groups(const RowSource& A, int64_t m, int64_t ncols,
                                  nwords * 4));
   for (int round = 0; round < 40; round++) {
     std::vector<int> todo;
+    todo.reserve(ps.size());
     for (int i = 0; i < (int)ps.size(); i++)
       if (ps[i].nd < 0) todo.push_back(i);
     if (todo.empty()) break;
-    std::vector<int2> hc(todo.size());
-    for (size_t k = 0; k < todo.size(); k++) hc[k] = make_int2(ps[todo[k]].r0, ps[todo[k]].r1);
-    std::vector<int32_t> hn(todo.size());
     const size_t n = todo.size();
-    cudaError_t e = dev_alloc((void**)&cand, n * sizeof(int2), st);
-    if (e == cudaSuccess) e = dev_alloc((void**)&nd, n * 4, st);
-    if (e == cudaSuccess)
-      e = cudaMemcpyAsync(cand, hc.data(), n * sizeof(int2), cudaMemcpyHostToDevice, st);
-    if (e == cudaSuccess) {
-      k_group_distinct<<<(unsigned)n, kGroupThreads, nwords * 4, st>>>(A, cand, nwords, nd);
-      note_launch();
-      e = cudaGetLastError();
+    std::vector<int32_t> hn(n);
+    std::vector<int2> hc(round > 0 ? n : 0);
+    cudaError_t e = dev_alloc((void**)&nd, n * 4, st);
+    if (round == 0) {
+      // the first cuts (all pieces, in order)
+      if (e == cudaSuccess) {
+        k_group_tables<<<(unsigned)n, kGroupThreads, nwords * 8, st>>>(
+            A, nullptr, m, nwords, fc.ptr, fc.ftab, nullptr, nd, fc.pval, fc.ploc);
+        note_launch();
+        e = cudaGetLastError();
+      }
+    } else {
+      for (size_t k = 0; k < n; k++) hc[k] = make_int2(ps[todo[k]].r0, ps[todo[k]].r1);
+      if (e == cudaSuccess) e = dev_alloc((void**)&cand, n * sizeof(int2), st);
+      if (e == cudaSuccess)
+        e = cudaMemcpyAsync(cand, hc.data(), n * sizeof(int2), cudaMemcpyHostToDevice, st);
+      if (e == cudaSuccess) {
+        k_group_distinct<<<(unsigned)n, kGroupThreads, nwords * 4, st>>>(A, cand, nwords, nd);
+        note_launch();
+        e = cudaGetLastError();
+      }
     }
     if (e == cudaSuccess) e = cudaMemcpyAsync(hn.data(), nd, n * 4, cudaMemcpyDeviceToHost, st);
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);
@@ -731,6 +805,7 @@ static epet_status form_groups(const RowSource& A, int64_t m, int64_t ncols,
     ps.swap(next);
   }
   out->clear();
+  out->reserve(ps.size());
   int64_t tb = 0;
   for (const Piece& p : ps) {
     if (p.nd < 0) return set_error(EPET_ERR_INVALID, "internal: row groups unmeasured");
@@ -750,12 +825,9 @@ epet_status grouped_build(const RowSource& A, int64_t m, int64_t ncols, int64_t 
   G->n = ncols;
   if (!grouped_supported(ncols, m))
     return set_error(EPET_ERR_UNSUPPORTED, "grouped layout: %lld columns", (long long)ncols);
-  std::vector<GroupDesc> hg;
-  EPET_CHECK(form_groups(A, m, ncols, &hg, st));
-  G->ngroups = (int64_t)hg.size();
-  G->nslots = hg.empty() ? 0 : (int64_t)hg.back().tb + hg.back().nd;
-  const int64_t ns = std::max<int64_t>(G->nslots, 1);
+  int32_t* ftab = nullptr;  // first cuts' tables (scratch)
   auto fail = [&](epet_status rc) {
+    if (ftab) dev_free(ftab, st);
     grouped_free(G, st);
     return rc;
   };
@@ -764,31 +836,6 @@ epet_status grouped_build(const RowSource& A, int64_t m, int64_t ncols, int64_t 
     cudaError_t e_ = dev_alloc((void**)&(ptr), std::max<size_t>((bytes), 16), st); \
     if (e_ != cudaSuccess) return fail(cuda_status(e_, "grouped allocation " #ptr)); \
   } while (0)
-  GALLOC(G->groups, hg.size() * sizeof(GroupDesc));
-  GALLOC(G->table, ns * 4);
-  GALLOC(G->partial, ns * 4);
-  GALLOC(G->ones, ns * 4);
-  GALLOC(G->cg_ptr, (ncols + 1) * 8);
-  GALLOC(G->row_ptr, (m + 1) * 8);
-  if (!hg.empty()) {
-    cudaError_t e = cudaMemcpyAsync(G->groups, hg.data(), hg.size() * sizeof(GroupDesc),
-                                    cudaMemcpyHostToDevice, st);
-    if (e != cudaSuccess) return fail(cuda_status(e, "group table"));
-  }
-  {
-    std::vector<int32_t> wide;
-    for (size_t i = 0; i < hg.size(); i++)
-      if (hg[i].nd > kGroupCap) wide.push_back((int32_t)i);
-    G->nwide = (int64_t)wide.size();
-    G->wide_h = wide;
-    if (!wide.empty()) {
-      GALLOC(G->wide, wide.size() * 4);
-      cudaError_t e = cudaMemcpyAsync(G->wide, wide.data(), wide.size() * 4,
-                                      cudaMemcpyHostToDevice, st);
-      if (e == cudaSuccess) e = cudaStreamSynchronize(st);  // (the host vector goes)
-      if (e != cudaSuccess) return fail(cuda_status(e, "wide groups"));
-    }
-  }
   const int nwords = bitmap_words(ncols);
   cudaError_t e = cudaFuncSetAttribute(k_group_tables, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                        nwords * 8);
@@ -799,7 +846,8 @@ epet_status grouped_build(const RowSource& A, int64_t m, int64_t ncols, int64_t 
     if (e == cudaSuccess)
       e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kGroupSmem);
   if (e != cudaSuccess) return fail(cuda_status(e, "grouped kernels"));
-  // the padded row pointers, then the tables and the padded layout
+  // the padded row pointers (rows padded to whole 4-entry chunks)
+  GALLOC(G->row_ptr, (m + 1) * 8);
   {
     int64_t *len = nullptr, *tmp = nullptr;
     GALLOC(len, std::max<int64_t>(m, 1) * 8);
@@ -817,30 +865,60 @@ epet_status grouped_build(const RowSource& A, int64_t m, int64_t ncols, int64_t 
       if (e == cudaSuccess) e = cudaStreamSynchronize(st);
       if (e != cudaSuccess) rc = cuda_status(e, "padded layout");
     }
-    if (rc == EPET_OK) {
-      cudaError_t e1 = dev_alloc((void**)&G->val32, std::max<int64_t>(G->npad, 4) * 4, st);
-      cudaError_t e2 = dev_alloc((void**)&G->loc, std::max<int64_t>(G->npad, 4) * 2, st);
-      if (e1 != cudaSuccess || e2 != cudaSuccess)
-        rc = cuda_status(e1 != cudaSuccess ? e1 : e2, "grouped allocation of the padded layout");
-    }
-    if (rc == EPET_OK && !hg.empty()) {
-      k_group_tables<<<(unsigned)hg.size(), kGroupThreads, nwords * 8, st>>>(
-          A, G->groups, nwords, G->row_ptr, G->table, G->val32, G->loc);
-      note_launch();
-      if (cudaGetLastError() != cudaSuccess) rc = set_error(EPET_ERR_CUDA, "group tables");
-    }
     dev_free(len, st);
     dev_free(tmp, st);
     if (rc != EPET_OK) return fail(rc);
   }
+  GALLOC(G->val32, std::max<int64_t>(G->npad, 4) * 4);
+  GALLOC(G->loc, std::max<int64_t>(G->npad, 4) * 2);
+  // the groups; the first cuts that fit are laid out on the way
+  GALLOC(ftab, ceil_div(std::max<int64_t>(m, 1), (int64_t)kGroupFirstRows) * kGroupCap * 4);
+  std::vector<GroupDesc> hg;
+  {
+    const epet_status rc = form_groups(A, m, ncols, FirstCuts{G->row_ptr, ftab, G->val32, G->loc},
+                                       &hg, st);
+    if (rc != EPET_OK) return fail(rc);
+  }
+  G->ngroups = (int64_t)hg.size();
+  G->nslots = hg.empty() ? 0 : (int64_t)hg.back().tb + hg.back().nd;
+  const int64_t ns = std::max<int64_t>(G->nslots, 1);
+  GALLOC(G->groups, hg.size() * sizeof(GroupDesc));
+  GALLOC(G->table, ns * 4);
+  GALLOC(G->partial, ns * 4);
+  GALLOC(G->cg_ptr, (ncols + 1) * 8);
+  if (!hg.empty()) {
+    e = cudaMemcpyAsync(G->groups, hg.data(), hg.size() * sizeof(GroupDesc),
+                        cudaMemcpyHostToDevice, st);
+    if (e != cudaSuccess) return fail(cuda_status(e, "group table"));
+  }
+  {
+    std::vector<int32_t> wide;
+    for (size_t i = 0; i < hg.size(); i++)
+      if (hg[i].nd > kGroupCap) wide.push_back((int32_t)i);
+    G->nwide = (int64_t)wide.size();
+    G->wide_h = wide;
+    if (!wide.empty()) {
+      GALLOC(G->wide, wide.size() * 4);
+      e = cudaMemcpyAsync(G->wide, wide.data(), wide.size() * 4, cudaMemcpyHostToDevice, st);
+      if (e == cudaSuccess) e = cudaStreamSynchronize(st);  // (the host vector goes)
+      if (e != cudaSuccess) return fail(cuda_status(e, "wide groups"));
+    }
+  }
+  // the tables at their slots and the layout of the groups split from wider cuts
+  if (!hg.empty()) {
+    k_group_tables<<<(unsigned)hg.size(), kGroupThreads, nwords * 8, st>>>(
+        A, G->groups, m, nwords, G->row_ptr, G->table, ftab, nullptr, G->val32, G->loc);
+    note_launch();
+    if (cudaGetLastError() != cudaSuccess) return fail(set_error(EPET_ERR_CUDA, "group tables"));
+  }
+  dev_free(ftab, st);
+  ftab = nullptr;
   // the slots of each column in group order: the column-major copy of the
   // (group x column) table, its values the slot indices (a wide group's
   // padding slots sit in column 0 and hold zero corrections)
   {
-    float* slot_bits = nullptr;
     int32_t* cg_group = nullptr;
     int64_t* gptr = nullptr;
-    GALLOC(slot_bits, ns * 4);
     GALLOC(cg_group, ns * 4);
     GALLOC(G->cg_slot, ns * 4);
     GALLOC(gptr, (G->ngroups + 1) * 8);
@@ -851,18 +929,14 @@ epet_status grouped_build(const RowSource& A, int64_t m, int64_t ncols, int64_t 
     e = cudaMemcpyAsync(gptr, hp.data(), hp.size() * 8, cudaMemcpyHostToDevice, st);
     if (e != cudaSuccess) rc = cuda_status(e, "slot lists");
     if (rc == EPET_OK && G->nslots > 0) {
-      k_slot_ids<<<ceil_div(G->nslots, 256), 256, 0, st>>>(G->nslots, slot_bits);
-      note_launch();
-      k_fill_f32<<<ceil_div(G->nslots, 256), 256, 0, st>>>(G->ones, G->nslots, 1.f);
-      note_launch();
-      epet_csr T{G->ngroups, ncols, G->nslots, gptr, G->table, slot_bits};
+      // the slots' positions in the table are the copy's values
+      epet_csr T{G->ngroups, ncols, G->nslots, gptr, G->table, nullptr};
       epet_csc C{G->ngroups, ncols, G->nslots, G->cg_ptr, cg_group,
                  reinterpret_cast<float*>(G->cg_slot)};
-      rc = epet_csr_to_csc(&T, &C, nullptr, 0, st);
+      rc = csr_to_csc_positions(&T, &C, st);
     } else if (rc == EPET_OK) {
       cudaMemsetAsync(G->cg_ptr, 0, (ncols + 1) * 8, st);
     }
-    dev_free(slot_bits, st);
     dev_free(cg_group, st);
     dev_free(gptr, st);
     if (rc != EPET_OK) return fail(rc);

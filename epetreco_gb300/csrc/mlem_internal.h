@@ -27,7 +27,7 @@ struct GroupedMatrix {
   uint16_t* loc = nullptr;      // per entry: rank of its column in its group's table
   int64_t* cg_ptr = nullptr;    // per column: its slots (group order) at cg_slot[cg_ptr[v] ..]
   int32_t* cg_slot = nullptr;
-  float* ones = nullptr;        // nslots ones (the slot sums run on the row kernel)
+  float* ones = nullptr;        // nslots ones (batched form: its slot sums run on the row kernel)
   float* partial = nullptr;     // per slot: the group's share of c = A^T e
   int32_t* wide = nullptr;      // ids of the groups of one row wider than the shared tables
   int64_t nwide = 0;
@@ -63,6 +63,8 @@ int grouped_pass_kernels(const GroupedMatrix& G);
 epet_status grouped_pass(const GroupedMatrix& G, const float* x, const float* y, float* ybar,
                          cudaStream_t st);
 void grouped_free(GroupedMatrix* G, cudaStream_t st);
+// Allocates and fills G->ones (the batched form's slot sums) if not yet there.
+epet_status grouped_ones(GroupedMatrix* G, cudaStream_t st);
 // Releases the FP32 values of a 16-bit form.
 void grouped_drop_fp32(GroupedMatrix* G, cudaStream_t st);
 // Column sums of the values over the matrix's rows into out[V]: the stored

@@ -200,16 +200,23 @@ struct ArrOut {
 };
 
 // CSR in, with the row of every entry precomputed (k_row_ids): key =
-// column, value = (row << 32) | value bits.
-struct CsrIn {
+// column, value = (row << 32) | value bits; with POS the entry's position in
+// the CSR stands for its value (vals is not read).  A compile-time choice: a
+// run-time test in val() slowed the scatter's staging loop by 15 %.
+template <bool POS>
+struct CsrInT {
   const int32_t* col;
   const int32_t* row;
   const float* vals;
   __device__ uint32_t key(int64_t i) const { return (uint32_t)col[i]; }
   __device__ uint64_t val(int64_t i) const {
-    return ((uint64_t)(uint32_t)row[i] << 32) | __float_as_uint(vals[i]);
+    return ((uint64_t)(uint32_t)row[i] << 32) | (POS ? (uint32_t)i : __float_as_uint(vals[i]));
   }
 };
+template <typename In>
+struct IsCsrIn : std::false_type {};
+template <bool POS>
+struct IsCsrIn<CsrInT<POS>> : std::true_type {};
 
 // Row id of every CSR entry (a warp per row).
 __global__ void k_row_ids(const int64_t* __restrict__ row_ptr, int64_t m,
@@ -280,7 +287,7 @@ k_radix_scatter(In in, Out out, int64_t n, int shift, int64_t tpc, int nchunks,
       const bool ok = i < n;
       const unsigned dig = ok ? ((unsigned)(kk[r] >> shift) & (BINS - 1)) : BINS + lane;
       unsigned peers;
-      if constexpr (std::is_same<In, CsrIn>::value) {
+      if constexpr (IsCsrIn<In>::value) {
         // rows of a CSR: consecutive columns, up to 32 distinct digits per
         // round, where one ballot per digit bit is cheaper than a match
         peers = __ballot_sync(0xffffffffu, ok);
@@ -616,10 +623,18 @@ size_t epet_csr_to_csc_workspace_size(int64_t m, int64_t n, int64_t nnz) {
          align256(scan_tmp_elems(hist) * 8) + 256;
 }
 
-epet_status epet_csr_to_csc(const epet_csr* a, epet_csc* out, void* ws, size_t ws_bytes,
-                            epet_stream_t stream) {
+}  // extern "C"
+
+namespace epet {
+// The column-major copy; with POS, a->val is not read and every CSC value
+// is the bit pattern of its entry's position in the CSR (int32).
+template <bool POS>
+static epet_status csr_to_csc_impl(const epet_csr* a, epet_csc* out, void* ws, size_t ws_bytes,
+                                   epet_stream_t stream) {
   if (!a || !out || !out->col_ptr || (a->nnz > 0 && (!out->row || !out->val)))
     return set_error(EPET_ERR_INVALID, "bad arguments");
+  if (POS && a->nnz > (int64_t)INT32_MAX)
+    return set_error(EPET_ERR_UNSUPPORTED, "entry positions beyond int32");
   if (a->n < 0 || a->n > (int64_t)INT32_MAX + 1)
     return set_error(EPET_ERR_INVALID, "column count %lld", (long long)a->n);
   cudaStream_t st = (cudaStream_t)stream;
@@ -647,7 +662,7 @@ epet_status epet_csr_to_csc(const epet_csr* a, epet_csc* out, void* ws, size_t w
   const int bits = std::max(1, bits_for(a->n - 1));
   k_row_ids<<<ceil_div(a->m * 32, 256), 256, 0, st>>>(a->row_ptr, a->m, rid);
   EPET_LAUNCHED();
-  CsrIn in{a->col, rid, a->val};
+  CsrInT<POS> in{a->col, rid, POS ? nullptr : a->val};
   CscOut co{out->row, out->val, out->col_ptr};
   k_fill_i64<<<ceil_div(a->n + 1, 256), 256, 0, st>>>(out->col_ptr, a->n + 1, nnz);
   EPET_LAUNCHED();
@@ -687,7 +702,15 @@ epet_status epet_csr_to_csc(const epet_csr* a, epet_csc* out, void* ws, size_t w
   return EPET_OK;
 }
 
-}  // extern "C"
+epet_status csr_to_csc_positions(const epet_csr* a, epet_csc* out, cudaStream_t st) {
+  return csr_to_csc_impl<true>(a, out, nullptr, 0, (epet_stream_t)st);
+}
+}  // namespace epet
+
+extern "C" epet_status epet_csr_to_csc(const epet_csr* a, epet_csc* out, void* ws,
+                                       size_t ws_bytes, epet_stream_t stream) {
+  return csr_to_csc_impl<false>(a, out, ws, ws_bytes, stream);
+}
 
 // ----------------------------------------------- allocation-free cooSort
 //
