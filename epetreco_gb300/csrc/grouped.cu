@@ -96,31 +96,21 @@ __device__ __forceinline__ void load_spans(const RowSource& A, int r0, int r1, G
   __syncthreads();
 }
 
-// Calls f(k, row, j, column) for every entry k of the group (row-major
-// order: entry j of row `row`), thread-strided, with the column loads of
-// kEntryBatch entries issued before any is used (the loop is otherwise
-// bound by each load's latency).
-constexpr int kEntryBatch = 4;
-template <class F>
-__device__ __forceinline__ void for_group_entries(const GroupSpans& S, int nr, F&& f) {
-  const int ntot = S.off[nr];
-  int r = 0;
-  for (int k0 = threadIdx.x; k0 < ntot; k0 += kEntryBatch * kGroupThreads) {
-    int rr[kEntryBatch], jj[kEntryBatch], cc[kEntryBatch];
+// Sets the group's columns in the bitmap bm: a warp per row, its lanes
+// along the row, four column loads issued before their atomics.
+__device__ __forceinline__ void set_group_columns(const GroupSpans& S, int nr, unsigned* bm) {
+  const int lane = threadIdx.x & 31;
+  for (int r = threadIdx.x >> 5; r < nr; r += kGroupThreads / 32) {
+    const int32_t* col = S.col[r];
+    const int n = S.off[r + 1] - S.off[r];
+    for (int j0 = lane; j0 < n; j0 += 128) {
+      int v[4];
 #pragma unroll
-    for (int u = 0; u < kEntryBatch; u++) {
-      const int k = k0 + u * kGroupThreads;
-      rr[u] = -1;
-      if (k < ntot) {
-        while (S.off[r + 1] <= k) r++;  // k ascends per thread: the row only moves forward
-        rr[u] = r;
-        jj[u] = k - S.off[r];
-        cc[u] = S.col[r][jj[u]];
-      }
+      for (int u = 0; u < 4; u++) v[u] = j0 + 32 * u < n ? col[j0 + 32 * u] : -1;
+#pragma unroll
+      for (int u = 0; u < 4; u++)
+        if (v[u] >= 0) atomicOr(&bm[v[u] >> 5], 1u << (v[u] & 31));
     }
-#pragma unroll
-    for (int u = 0; u < kEntryBatch; u++)
-      if (rr[u] >= 0) f(k0 + u * kGroupThreads, rr[u], jj[u], (unsigned)cc[u]);
   }
 }
 
@@ -135,9 +125,7 @@ k_group_distinct(RowSource A, const int2* __restrict__ cand, int nwords,
   for (int i = threadIdx.x; i < nwords; i += kGroupThreads) gbm[i] = 0u;
   const int2 c = cand[blockIdx.x];
   load_spans(A, c.x, c.y, &S);
-  for_group_entries(S, c.y - c.x, [&](int, int, int, unsigned v) {
-    atomicOr(&gbm[v >> 5], 1u << (v & 31));
-  });
+  set_group_columns(S, c.y - c.x, gbm);
   __syncthreads();
   int n = 0;
   for (int i = threadIdx.x; i < nwords; i += kGroupThreads) n += __popc(gbm[i]);
@@ -174,14 +162,16 @@ k_group_distinct(RowSource A, const int2* __restrict__ cand, int nwords,
 // entries.  The second takes the final groups: a first cut kept whole
 // copies its table from ftab to its slots; the groups made by splitting
 // wider cuts are laid out in full.
-__global__ void __launch_bounds__(kGroupThreads)
+__global__ void __launch_bounds__(kGroupThreads, 8)
 k_group_tables(RowSource A, const GroupDesc* __restrict__ groups, int64_t m, int nwords,
                const int64_t* __restrict__ ptr, int32_t* __restrict__ table,
                const int32_t* __restrict__ ftab, int32_t* __restrict__ nd_out,
                float* __restrict__ pval, uint16_t* __restrict__ ploc) {
   extern __shared__ unsigned gsh[];
   unsigned* bm = gsh;
-  int* pre = reinterpret_cast<int*>(gsh + nwords);
+  // per bitmap word the rank of its first column (< kGroupCap where read):
+  // 16 bits keep the block at 6 bytes per word (8 blocks per SM at 52^3)
+  uint16_t* pre = reinterpret_cast<uint16_t*>(gsh + nwords);
   __shared__ int wtot[kGroupThreads / 32];
   __shared__ int s_nd;
   const bool first = nd_out != nullptr;
@@ -214,9 +204,7 @@ k_group_tables(RowSource A, const GroupDesc* __restrict__ groups, int64_t m, int
   const int nr = gd.r1 - gd.r0;
   for (int i = threadIdx.x; i < nwords; i += kGroupThreads) bm[i] = 0u;
   load_spans(A, gd.r0, gd.r1, &S);
-  for_group_entries(S, nr, [&](int, int, int, unsigned v) {
-    atomicOr(&bm[v >> 5], 1u << (v & 31));
-  });
+  set_group_columns(S, nr, bm);
   __syncthreads();
   // exclusive prefix of the words' popcounts: thread t owns a contiguous
   // range of words
@@ -243,7 +231,7 @@ k_group_tables(RowSource A, const GroupDesc* __restrict__ groups, int64_t m, int
   int32_t* const tab = first ? table + (int64_t)blockIdx.x * kGroupCap : table + gd.tb;
   int run = wtot[wid] + inc - cnt;
   for (int w = wb; w < we; w++) {
-    pre[w] = run;
+    pre[w] = (uint16_t)run;
     unsigned word = bm[w];
     while (word) {
       const int bit = __ffs(word) - 1;
@@ -253,47 +241,45 @@ k_group_tables(RowSource A, const GroupDesc* __restrict__ groups, int64_t m, int
     }
   }
   __syncthreads();
-  // the padded layout a 4-entry chunk at a time (thread-strided over the
-  // group's chunks, each finding its row): chunk l of round u of a row holds
-  // its entries j = 128 u + t cq + l (t = 0..3, the storage order above),
-  // padding (j past the row) as zero values on the trash rank; the chunk's
-  // values and ranks are written with one 16-byte and one 8-byte store
-  const int64_t gbase = ptr[gd.r0];
-  const int nch = (int)((ptr[gd.r1] - gbase) >> 2);
-  int r = 0;
-  int pr0 = 0, pr1 = (int)(ptr[gd.r0 + 1] - gbase);  // row r's padded range
-  for (int k = threadIdx.x; k < nch; k += kGroupThreads) {
-    const int p = 4 * k;
-    while (pr1 <= p) {  // k ascends per thread: the row only moves forward
-      r++;
-      pr0 = pr1;
-      pr1 = (int)(ptr[gd.r0 + r + 1] - gbase);
-    }
+  // the padded layout a 4-entry chunk at a time, a warp per row: lane l
+  // takes chunk l of every round u, which holds the row's entries j = 128 u
+  // + t cq + l (t = 0..3, the storage order above), padding (j past the row)
+  // as zero values on the trash rank; a chunk's values and ranks are
+  // written with one 16-byte and one 8-byte store
+  for (int r = wid; r < nr; r += kGroupThreads / 32) {
+    const int32_t* col = S.col[r];
+    const float* val = S.val[r];
     const int n = S.off[r + 1] - S.off[r];
-    const int c = (p - pr0) >> 2;  // chunk of the row
-    const int u = c >> 5, l = c & 31;
-    const int cq = min(32, ((pr1 - pr0) >> 2) - 32 * u);
-    int cc[4];
-    float vv[4];
+    const int64_t d = ptr[gd.r0 + r];
+    const int nq = (int)((ptr[gd.r0 + r + 1] - d) >> 2);
+    for (int c = lane; c < nq; c += 32) {
+      const int u = c >> 5;
+      const int cq = min(32, nq - 32 * u);
+      int cc[4];
+      float vv[4];
 #pragma unroll
-    for (int t = 0; t < 4; t++) {
-      const int j = 128 * u + t * cq + l;
-      cc[t] = j < n ? S.col[r][j] : -1;
-      vv[t] = j < n ? S.val[r][j] : 0.f;
-    }
-    unsigned rk[4];
+      for (int t = 0; t < 4; t++) {
+        const int j = 128 * u + t * cq + lane;
+        cc[t] = j < n ? col[j] : -1;
+        vv[t] = j < n ? val[j] : 0.f;
+      }
+      unsigned rk[4];
 #pragma unroll
-    for (int t = 0; t < 4; t++) {
-      const unsigned v = (unsigned)cc[t];
-      rk[t] = cc[t] >= 0
-                  ? (unsigned)sw_rank(pre[v >> 5] + __popc(bm[v >> 5] & ((1u << (v & 31)) - 1u)))
-                  : (unsigned)sw_rank(kTrash);
+      for (int t = 0; t < 4; t++) {
+        const unsigned v = (unsigned)cc[t];
+        rk[t] = cc[t] >= 0
+                    ? (unsigned)sw_rank(pre[v >> 5] + __popc(bm[v >> 5] & ((1u << (v & 31)) - 1u)))
+                    : (unsigned)sw_rank(kTrash);
+      }
+      *reinterpret_cast<float4*>(pval + d + 4 * c) = make_float4(vv[0], vv[1], vv[2], vv[3]);
+      *reinterpret_cast<uint2*>(ploc + d + 4 * c) = make_uint2(rk[0] | (rk[1] << 16),
+                                                               rk[2] | (rk[3] << 16));
     }
-    *reinterpret_cast<float4*>(pval + gbase + p) = make_float4(vv[0], vv[1], vv[2], vv[3]);
-    *reinterpret_cast<uint2*>(ploc + gbase + p) = make_uint2(rk[0] | (rk[1] << 16),
-                                                             rk[2] | (rk[3] << 16));
   }
 }
+
+// Dynamic shared memory of k_group_tables: the bitmap and the word ranks.
+static size_t table_smem(int nwords) { return (size_t)nwords * 6; }
 
 __global__ void k_padded_len(RowSource A, int64_t m, int64_t* __restrict__ len) {
   const int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -754,20 +740,24 @@ static epet_status form_groups(const RowSource& A, int64_t m, int64_t ncols, con
   int32_t* nd = nullptr;
   EPET_CUDA(cudaFuncSetAttribute(k_group_distinct, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  nwords * 4));
+  // (the host vectors keep their storage from round to round)
+  std::vector<Piece> next;
+  std::vector<int> todo;
+  std::vector<int32_t> hn;
+  std::vector<int2> hc;
   for (int round = 0; round < 40; round++) {
-    std::vector<int> todo;
-    todo.reserve(ps.size());
+    todo.clear();
     for (int i = 0; i < (int)ps.size(); i++)
       if (ps[i].nd < 0) todo.push_back(i);
     if (todo.empty()) break;
     const size_t n = todo.size();
-    std::vector<int32_t> hn(n);
-    std::vector<int2> hc(round > 0 ? n : 0);
+    hn.resize(n);
+    hc.resize(round > 0 ? n : 0);
     cudaError_t e = dev_alloc((void**)&nd, n * 4, st);
     if (round == 0) {
       // the first cuts (all pieces, in order)
       if (e == cudaSuccess) {
-        k_group_tables<<<(unsigned)n, kGroupThreads, nwords * 8, st>>>(
+        k_group_tables<<<(unsigned)n, kGroupThreads, table_smem(nwords), st>>>(
             A, nullptr, m, nwords, fc.ptr, fc.ftab, nullptr, nd, fc.pval, fc.ploc);
         note_launch();
         e = cudaGetLastError();
@@ -790,9 +780,13 @@ static epet_status form_groups(const RowSource& A, int64_t m, int64_t ncols, con
     cand = nullptr;
     nd = nullptr;
     if (e != cudaSuccess) return cuda_status(e, "row groups");
-    for (size_t k = 0; k < n; k++) ps[todo[k]].nd = hn[k];
-    std::vector<Piece> next;
-    next.reserve(ps.size() + 64);
+    bool split = false;
+    for (size_t k = 0; k < n; k++) {
+      ps[todo[k]].nd = hn[k];
+      split = split || (hn[k] > kGroupCap && ps[todo[k]].r1 - ps[todo[k]].r0 > 1);
+    }
+    if (!split) break;  // every piece measured and kept
+    next.clear();
     for (const Piece& p : ps) {
       if (p.nd > kGroupCap && p.r1 - p.r0 > 1) {
         const int32_t mid = p.r0 + (p.r1 - p.r0) / 2;
@@ -838,7 +832,9 @@ epet_status grouped_build(const RowSource& A, int64_t m, int64_t ncols, int64_t 
   } while (0)
   const int nwords = bitmap_words(ncols);
   cudaError_t e = cudaFuncSetAttribute(k_group_tables, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                       nwords * 8);
+                                       (int)table_smem(nwords));
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(k_group_tables, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
   for (const void* k : {(const void*)k_group_mlem<0>, (const void*)k_group_mlem<1>,
                         (const void*)k_group_mlem<2>, (const void*)k_group_mlem_batch,
                         (const void*)k_group_colsum<0>, (const void*)k_group_colsum<1>,
@@ -906,39 +902,20 @@ epet_status grouped_build(const RowSource& A, int64_t m, int64_t ncols, int64_t 
   }
   // the tables at their slots and the layout of the groups split from wider cuts
   if (!hg.empty()) {
-    k_group_tables<<<(unsigned)hg.size(), kGroupThreads, nwords * 8, st>>>(
+    k_group_tables<<<(unsigned)hg.size(), kGroupThreads, table_smem(nwords), st>>>(
         A, G->groups, m, nwords, G->row_ptr, G->table, ftab, nullptr, G->val32, G->loc);
     note_launch();
     if (cudaGetLastError() != cudaSuccess) return fail(set_error(EPET_ERR_CUDA, "group tables"));
   }
   dev_free(ftab, st);
   ftab = nullptr;
-  // the slots of each column in group order: the column-major copy of the
-  // (group x column) table, its values the slot indices (a wide group's
+  // the slots of each column in group order: the column-major order of the
+  // (group x column) table's entries, i.e. their positions (a wide group's
   // padding slots sit in column 0 and hold zero corrections)
+  GALLOC(G->cg_slot, ns * 4);
   {
-    int32_t* cg_group = nullptr;
-    int64_t* gptr = nullptr;
-    GALLOC(cg_group, ns * 4);
-    GALLOC(G->cg_slot, ns * 4);
-    GALLOC(gptr, (G->ngroups + 1) * 8);
-    std::vector<int64_t> hp(G->ngroups + 1);
-    for (int64_t i = 0; i < G->ngroups; i++) hp[i] = hg[i].tb;
-    hp[G->ngroups] = G->nslots;
-    epet_status rc = EPET_OK;
-    e = cudaMemcpyAsync(gptr, hp.data(), hp.size() * 8, cudaMemcpyHostToDevice, st);
-    if (e != cudaSuccess) rc = cuda_status(e, "slot lists");
-    if (rc == EPET_OK && G->nslots > 0) {
-      // the slots' positions in the table are the copy's values
-      epet_csr T{G->ngroups, ncols, G->nslots, gptr, G->table, nullptr};
-      epet_csc C{G->ngroups, ncols, G->nslots, G->cg_ptr, cg_group,
-                 reinterpret_cast<float*>(G->cg_slot)};
-      rc = csr_to_csc_positions(&T, &C, st);
-    } else if (rc == EPET_OK) {
-      cudaMemsetAsync(G->cg_ptr, 0, (ncols + 1) * 8, st);
-    }
-    dev_free(cg_group, st);
-    dev_free(gptr, st);
+    const epet_status rc = csr_to_csc_positions(G->nslots, ncols, G->table, G->cg_ptr,
+                                                reinterpret_cast<uint32_t*>(G->cg_slot), st);
     if (rc != EPET_OK) return fail(rc);
   }
   if (value_format != EPET_VALUES_FP32) {

@@ -16,9 +16,12 @@ epet_status exclusive_scan_i64(const int64_t* in, int64_t* out, int64_t n,
 
 // Radix sort histogram size (int64 entries) for n items (sort.cu).
 size_t radix_hist_elems(int64_t n);
-// epet_csr_to_csc with the entries' CSR positions (int32 bits) as the CSC
-// values; a->val is not read (at most 2^31 - 1 entries).
-epet_status csr_to_csc_positions(const epet_csr* a, epet_csc* out, cudaStream_t st);
+// The column-major order of a CSR's entries (nnz entries, n columns, at
+// most 2^31 - 1 entries): each column's entries' positions, ascending, at
+// pos[col_ptr[v] ..]; col_ptr has n + 1 entries.  Neither rows nor values
+// are read.
+epet_status csr_to_csc_positions(int64_t nnz, int64_t n, const int32_t* col, int64_t* col_ptr,
+                                 uint32_t* pos, cudaStream_t st);
 
 // Row walk configuration chosen for a problem (per-row accumulator size).
 int auto_row_capacity(const epet_problem& p);

@@ -200,23 +200,30 @@ struct ArrOut {
 };
 
 // CSR in, with the row of every entry precomputed (k_row_ids): key =
-// column, value = (row << 32) | value bits; with POS the entry's position in
-// the CSR stands for its value (vals is not read).  A compile-time choice: a
-// run-time test in val() slowed the scatter's staging loop by 15 %.
-template <bool POS>
-struct CsrInT {
+// column, value = (row << 32) | value bits.
+struct CsrIn {
   const int32_t* col;
   const int32_t* row;
   const float* vals;
   __device__ uint32_t key(int64_t i) const { return (uint32_t)col[i]; }
   __device__ uint64_t val(int64_t i) const {
-    return ((uint64_t)(uint32_t)row[i] << 32) | (POS ? (uint32_t)i : __float_as_uint(vals[i]));
+    return ((uint64_t)(uint32_t)row[i] << 32) | __float_as_uint(vals[i]);
   }
 };
+// The columns of a CSR with each entry's position as its value (the
+// positions' column-major order: no rows, no values read).
+struct PosIn {
+  const int32_t* col;
+  __device__ uint32_t key(int64_t i) const { return (uint32_t)col[i]; }
+  __device__ uint32_t val(int64_t i) const { return (uint32_t)i; }
+};
+// CSR-ordered keys (runs of ascending columns): ranked by ballots.
 template <typename In>
 struct IsCsrIn : std::false_type {};
-template <bool POS>
-struct IsCsrIn<CsrInT<POS>> : std::true_type {};
+template <>
+struct IsCsrIn<CsrIn> : std::true_type {};
+template <>
+struct IsCsrIn<PosIn> : std::true_type {};
 
 // Row id of every CSR entry (a warp per row).
 __global__ void k_row_ids(const int64_t* __restrict__ row_ptr, int64_t m,
@@ -226,6 +233,17 @@ __global__ void k_row_ids(const int64_t* __restrict__ row_ptr, int64_t m,
   for (int64_t k = row_ptr[r] + (threadIdx.x & 31); k < row_ptr[r + 1]; k += 32)
     row[k] = (int32_t)r;
 }
+
+// Positions in column-major order out, with the column starts (as CscOut).
+struct PosCscOut {
+  uint32_t* pos;
+  int64_t* col_first;
+  __device__ void put(int64_t p, uint32_t k, uint32_t v, bool first) const {
+    pos[p] = v;
+    if (first) atomicMin(reinterpret_cast<unsigned long long*>(col_first + k),
+                         (unsigned long long)p);
+  }
+};
 
 // CSC out: row and value arrays; the first position of every column goes to
 // col_first (atomicMin, initialised to nnz; empty columns are filled in
@@ -626,15 +644,11 @@ size_t epet_csr_to_csc_workspace_size(int64_t m, int64_t n, int64_t nnz) {
 }  // extern "C"
 
 namespace epet {
-// The column-major copy; with POS, a->val is not read and every CSC value
-// is the bit pattern of its entry's position in the CSR (int32).
-template <bool POS>
+// The column-major copy of a CSR.
 static epet_status csr_to_csc_impl(const epet_csr* a, epet_csc* out, void* ws, size_t ws_bytes,
                                    epet_stream_t stream) {
   if (!a || !out || !out->col_ptr || (a->nnz > 0 && (!out->row || !out->val)))
     return set_error(EPET_ERR_INVALID, "bad arguments");
-  if (POS && a->nnz > (int64_t)INT32_MAX)
-    return set_error(EPET_ERR_UNSUPPORTED, "entry positions beyond int32");
   if (a->n < 0 || a->n > (int64_t)INT32_MAX + 1)
     return set_error(EPET_ERR_INVALID, "column count %lld", (long long)a->n);
   cudaStream_t st = (cudaStream_t)stream;
@@ -662,7 +676,7 @@ static epet_status csr_to_csc_impl(const epet_csr* a, epet_csc* out, void* ws, s
   const int bits = std::max(1, bits_for(a->n - 1));
   k_row_ids<<<ceil_div(a->m * 32, 256), 256, 0, st>>>(a->row_ptr, a->m, rid);
   EPET_LAUNCHED();
-  CsrInT<POS> in{a->col, rid, POS ? nullptr : a->val};
+  CsrIn in{a->col, rid, a->val};
   CscOut co{out->row, out->val, out->col_ptr};
   k_fill_i64<<<ceil_div(a->n + 1, 256), 256, 0, st>>>(out->col_ptr, a->n + 1, nnz);
   EPET_LAUNCHED();
@@ -702,14 +716,65 @@ static epet_status csr_to_csc_impl(const epet_csr* a, epet_csc* out, void* ws, s
   return EPET_OK;
 }
 
-epet_status csr_to_csc_positions(const epet_csr* a, epet_csc* out, cudaStream_t st) {
-  return csr_to_csc_impl<true>(a, out, nullptr, 0, (epet_stream_t)st);
+epet_status csr_to_csc_positions(int64_t nnz, int64_t n, const int32_t* col, int64_t* col_ptr,
+                                 uint32_t* pos, cudaStream_t st) {
+  if (n < 0 || n > (int64_t)INT32_MAX + 1 || nnz < 0 || nnz > (int64_t)INT32_MAX)
+    return set_error(EPET_ERR_INVALID, "positions: %lld entries, %lld columns", (long long)nnz,
+                     (long long)n);
+  if (nnz == 0) {
+    EPET_CUDA(cudaMemsetAsync(col_ptr, 0, (n + 1) * 8, st));
+    return EPET_OK;
+  }
+  const int passes = csc_passes(n);
+  const size_t hn = radix_hist_elems(nnz);
+  Scratch scr;
+  EPET_CHECK(scr.init(nullptr, 0,
+                      2 * (passes > 2 ? 2 : 1) * align256(nnz * 4) + align256(hn * 8) +
+                          align256((hn + 1) * 8) + align256(scan_tmp_elems(hn) * 8) + 256,
+                      st));
+  uint32_t* ks[2] = {scr.take<uint32_t>(nnz), passes > 2 ? scr.take<uint32_t>(nnz) : nullptr};
+  uint32_t* vs[2] = {scr.take<uint32_t>(nnz), passes > 2 ? scr.take<uint32_t>(nnz) : nullptr};
+  int64_t* hist = scr.take<int64_t>(hn);
+  int64_t* hist_scan = scr.take<int64_t>(hn + 1);
+  int64_t* tmp = scr.take<int64_t>(scan_tmp_elems(hn));
+  if (scr.overrun) return set_error(EPET_ERR_INVALID, "internal: workspace size");
+  const int bits = std::max(1, bits_for(n - 1));
+  PosIn in{col};
+  PosCscOut co{pos, col_ptr};
+  k_fill_i64<<<ceil_div(n + 1, 256), 256, 0, st>>>(col_ptr, n + 1, nnz);
+  EPET_LAUNCHED();
+  using K = uint32_t;
+  using V = uint32_t;
+  if (passes == 1) {
+    EPET_CHECK((radix_pass<9, K, V>(in, co, nnz, 0, hist, hist_scan, tmp, st)));
+  } else if (passes == 2) {
+    const int b0 = bits - 9;
+    ArrOut<K, V> mid{ks[0], vs[0]};
+    if (b0 <= 8) EPET_CHECK((radix_pass<8, K, V>(in, mid, nnz, 0, hist, hist_scan, tmp, st)));
+    else EPET_CHECK((radix_pass<9, K, V>(in, mid, nnz, 0, hist, hist_scan, tmp, st)));
+    EPET_CHECK((radix_pass<9, K, V>(ArrIn<K, V>{ks[0], vs[0]}, co, nnz, b0 <= 8 ? 8 : 9, hist,
+                                    hist_scan, tmp, st)));
+  } else {
+    EPET_CHECK((radix_pass<9, K, V>(in, ArrOut<K, V>{ks[0], vs[0]}, nnz, 0, hist, hist_scan, tmp,
+                                    st)));
+    for (int k = 1; k < passes; k++) {
+      ArrIn<K, V> src{ks[(k - 1) & 1], vs[(k - 1) & 1]};
+      if (k + 1 < passes)
+        EPET_CHECK((radix_pass<9, K, V>(src, ArrOut<K, V>{ks[k & 1], vs[k & 1]}, nnz, 9 * k,
+                                        hist, hist_scan, tmp, st)));
+      else
+        EPET_CHECK((radix_pass<9, K, V>(src, co, nnz, 9 * k, hist, hist_scan, tmp, st)));
+    }
+  }
+  k_suffix_min_i64<<<1, 1024, 0, st>>>(col_ptr, n + 1);
+  EPET_LAUNCHED();
+  return EPET_OK;
 }
 }  // namespace epet
 
 extern "C" epet_status epet_csr_to_csc(const epet_csr* a, epet_csc* out, void* ws,
                                        size_t ws_bytes, epet_stream_t stream) {
-  return csr_to_csc_impl<false>(a, out, ws, ws_bytes, stream);
+  return csr_to_csc_impl(a, out, ws, ws_bytes, stream);
 }
 
 // ----------------------------------------------- allocation-free cooSort
