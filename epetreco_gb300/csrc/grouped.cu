@@ -729,84 +729,102 @@ struct FirstCuts {
 static epet_status form_groups(const RowSource& A, int64_t m, int64_t ncols, const FirstCuts& fc,
                                std::vector<GroupDesc>* out, cudaStream_t st) {
   const int nwords = bitmap_words(ncols);
-  struct Piece {
-    int32_t r0, r1, nd;  // nd < 0: not measured yet
-  };
-  std::vector<Piece> ps;
-  ps.reserve((size_t)(m / kGroupFirstRows) + 64);
-  for (int64_t r = 0; r < m; r += kGroupFirstRows)
-    ps.push_back({(int32_t)r, (int32_t)std::min<int64_t>(m, r + kGroupFirstRows), -1});
-  int2* cand = nullptr;
-  int32_t* nd = nullptr;
+  const int64_t ncut = (m + kGroupFirstRows - 1) / kGroupFirstRows;
   EPET_CUDA(cudaFuncSetAttribute(k_group_distinct, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  nwords * 4));
-  // (the host vectors keep their storage from round to round)
-  std::vector<Piece> next;
-  std::vector<int> todo;
-  std::vector<int32_t> hn;
-  std::vector<int2> hc;
-  for (int round = 0; round < 40; round++) {
-    todo.clear();
-    for (int i = 0; i < (int)ps.size(); i++)
-      if (ps[i].nd < 0) todo.push_back(i);
-    if (todo.empty()) break;
-    const size_t n = todo.size();
-    hn.resize(n);
-    hc.resize(round > 0 ? n : 0);
-    cudaError_t e = dev_alloc((void**)&nd, n * 4, st);
-    if (round == 0) {
-      // the first cuts (all pieces, in order)
-      if (e == cudaSuccess) {
-        k_group_tables<<<(unsigned)n, kGroupThreads, table_smem(nwords), st>>>(
-            A, nullptr, m, nwords, fc.ptr, fc.ftab, nullptr, nd, fc.pval, fc.ploc);
-        note_launch();
-        e = cudaGetLastError();
-      }
-    } else {
-      for (size_t k = 0; k < n; k++) hc[k] = make_int2(ps[todo[k]].r0, ps[todo[k]].r1);
-      if (e == cudaSuccess) e = dev_alloc((void**)&cand, n * sizeof(int2), st);
+  // every first cut counted, those that fit laid out
+  std::vector<int32_t> cut_nd(ncut);
+  {
+    int32_t* nd = nullptr;
+    cudaError_t e = dev_alloc((void**)&nd, std::max<int64_t>(ncut, 1) * 4, st);
+    if (e == cudaSuccess && ncut > 0) {
+      k_group_tables<<<(unsigned)ncut, kGroupThreads, table_smem(nwords), st>>>(
+          A, nullptr, m, nwords, fc.ptr, fc.ftab, nullptr, nd, fc.pval, fc.ploc);
+      note_launch();
+      e = cudaGetLastError();
       if (e == cudaSuccess)
-        e = cudaMemcpyAsync(cand, hc.data(), n * sizeof(int2), cudaMemcpyHostToDevice, st);
-      if (e == cudaSuccess) {
-        k_group_distinct<<<(unsigned)n, kGroupThreads, nwords * 4, st>>>(A, cand, nwords, nd);
-        note_launch();
-        e = cudaGetLastError();
-      }
+        e = cudaMemcpyAsync(cut_nd.data(), nd, ncut * 4, cudaMemcpyDeviceToHost, st);
+    }
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (nd) dev_free(nd, st);
+    if (e != cudaSuccess) return cuda_status(e, "row groups");
+  }
+  // The wider cuts, halved until their pieces fit or are one row; only
+  // those pieces are counted again.  A split cut s keeps its pieces as bits
+  // of mask[s] (a piece starting at row j of the cut) and their counts at
+  // sub[32 s + j].
+  std::vector<int32_t> slot(ncut, -1);
+  std::vector<uint32_t> mask;
+  std::vector<int32_t> sub;
+  std::vector<int2> pend, nextp;
+  for (int64_t c = 0; c < ncut; c++) {
+    const int32_t r0 = (int32_t)(c * kGroupFirstRows);
+    const int32_t r1 = (int32_t)std::min<int64_t>(m, r0 + kGroupFirstRows);
+    if (cut_nd[c] > kGroupCap && r1 - r0 > 1) {
+      slot[c] = (int32_t)mask.size();
+      mask.push_back(0u);
+      const int32_t mid = r0 + (r1 - r0) / 2;
+      pend.push_back(make_int2(r0, mid));
+      pend.push_back(make_int2(mid, r1));
+    }
+  }
+  sub.assign(mask.size() * kGroupFirstRows, 0);
+  std::vector<int32_t> hn;
+  for (int round = 1; !pend.empty(); round++) {
+    if (round > 40) return set_error(EPET_ERR_INVALID, "internal: row groups unmeasured");
+    const size_t n = pend.size();
+    hn.resize(n);
+    int2* cand = nullptr;
+    int32_t* nd = nullptr;
+    cudaError_t e = dev_alloc((void**)&cand, n * sizeof(int2), st);
+    if (e == cudaSuccess) e = dev_alloc((void**)&nd, n * 4, st);
+    if (e == cudaSuccess)
+      e = cudaMemcpyAsync(cand, pend.data(), n * sizeof(int2), cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess) {
+      k_group_distinct<<<(unsigned)n, kGroupThreads, nwords * 4, st>>>(A, cand, nwords, nd);
+      note_launch();
+      e = cudaGetLastError();
     }
     if (e == cudaSuccess) e = cudaMemcpyAsync(hn.data(), nd, n * 4, cudaMemcpyDeviceToHost, st);
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);
     if (cand) dev_free(cand, st);
     if (nd) dev_free(nd, st);
-    cand = nullptr;
-    nd = nullptr;
     if (e != cudaSuccess) return cuda_status(e, "row groups");
-    bool split = false;
+    nextp.clear();
     for (size_t k = 0; k < n; k++) {
-      ps[todo[k]].nd = hn[k];
-      split = split || (hn[k] > kGroupCap && ps[todo[k]].r1 - ps[todo[k]].r0 > 1);
-    }
-    if (!split) break;  // every piece measured and kept
-    next.clear();
-    for (const Piece& p : ps) {
-      if (p.nd > kGroupCap && p.r1 - p.r0 > 1) {
-        const int32_t mid = p.r0 + (p.r1 - p.r0) / 2;
-        next.push_back({p.r0, mid, -1});
-        next.push_back({mid, p.r1, -1});
+      const int2 p = pend[k];
+      if (hn[k] > kGroupCap && p.y - p.x > 1) {
+        const int32_t mid = p.x + (p.y - p.x) / 2;
+        nextp.push_back(make_int2(p.x, mid));
+        nextp.push_back(make_int2(mid, p.y));
       } else {
-        next.push_back(p);
+        const int32_t s = slot[p.x / kGroupFirstRows], j = p.x % kGroupFirstRows;
+        mask[s] |= 1u << j;
+        sub[(size_t)s * kGroupFirstRows + j] = hn[k];
       }
     }
-    ps.swap(next);
+    pend.swap(nextp);
   }
+  // the groups in row order: the cuts kept whole, and a split cut's pieces
   out->clear();
-  out->reserve(ps.size());
+  out->reserve(ncut + sub.size() / 8);
   int64_t tb = 0;
-  for (const Piece& p : ps) {
-    if (p.nd < 0) return set_error(EPET_ERR_INVALID, "internal: row groups unmeasured");
-    const int32_t n = p.nd > kGroupCap ? (p.nd + 3) & ~3 : p.nd;  // wide: padded like its row
-    if (tb + n > INT32_MAX) return set_error(EPET_ERR_UNSUPPORTED, "row-group tables exceed int32");
-    out->push_back(GroupDesc{p.r0, p.r1, (int32_t)tb, n});
-    tb += n;
+  for (int64_t c = 0; c < ncut; c++) {
+    const int32_t r0 = (int32_t)(c * kGroupFirstRows);
+    const int32_t r1 = (int32_t)std::min<int64_t>(m, r0 + kGroupFirstRows);
+    uint32_t msk = slot[c] < 0 ? 1u : mask[slot[c]];
+    if (!(msk & 1u)) return set_error(EPET_ERR_INVALID, "internal: row groups unmeasured");
+    while (msk) {
+      const int j = __builtin_ctz(msk);
+      msk &= msk - 1u;
+      const int32_t e = msk ? r0 + __builtin_ctz(msk) : r1;
+      const int32_t ndv = slot[c] < 0 ? cut_nd[c] : sub[(size_t)slot[c] * kGroupFirstRows + j];
+      const int32_t n = ndv > kGroupCap ? (ndv + 3) & ~3 : ndv;  // wide: padded like its row
+      if (tb + n > INT32_MAX)
+        return set_error(EPET_ERR_UNSUPPORTED, "row-group tables exceed int32");
+      out->push_back(GroupDesc{r0 + j, e, (int32_t)tb, n});
+      tb += n;
+    }
   }
   return EPET_OK;
 }
