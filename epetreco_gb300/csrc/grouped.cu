@@ -20,9 +20,9 @@
 // the same word (padding goes to the trash slot, which is never read) and
 // each column's sum runs in row order.  The group's corrections go to one
 // slot per (group, column); the slots of each column, listed in group order
-// (built once, a column-major copy of the table), are summed in that order
-// by a row kernel whose epilogue applies x*c/s.  Every sum has an
-// input-determined order, so results are deterministic.
+// (built once: the column-major order of the table's entries), are summed in
+// that order by the slot-sum kernel (k_sums), whose epilogue applies x*c/s.
+// Every sum has an input-determined order, so results are deterministic.
 #include <cuda_bf16.h>
 #include <cuda_fp16.h>
 
@@ -651,7 +651,7 @@ k_group_mlem_batch_wide(const GroupIterArgs* __restrict__ desc, const int64_t* _
 // Column sums of the grouped matrix's values (the 16-bit forms dequantised)
 // over its rows, by the same group / slot structure as the pass: a warp per
 // group adds its rows' values, row after row, into the group's shared sums
-// (the slots); the slot sums per column then run on the row kernel.
+// (the slots); the slot sums per column then run on the slot-sum kernel.
 template <int FMT>
 __global__ void __launch_bounds__(kGroupWarps * 32, 1)
 k_group_colsum(GroupIterArgs a) {
