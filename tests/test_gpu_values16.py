@@ -171,7 +171,7 @@ def test_product_against_oracle(mat, oracle, fmt):
 
 @pytest.mark.parametrize("fmt", ["bf16", "fp16"])
 def test_mlem_16bit_within_1e3_of_fp64(gpu_lib, oracle, fmt):
-    """Spec bound: image error <= 1e-3 relative L2 vs the FP64 oracle."""
+    """The 16-bit forms' bound: image error <= 1e-3 relative L2 vs the FP64 oracle."""
     from epetreco_gb300.phantom import measurement
     p = config("small")["problem"]
     rows, y, _ = measurement(p, 1e6)
